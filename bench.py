@@ -1,0 +1,364 @@
+"""Benchmark of the H1 operator hot path on one GB300 (replicas for --gpus N).
+
+Workload (BASELINE config "mixed precision, matrix-free"): structured 64^3 hex
+mesh of the unit cube (MakeStructured3DMesh), H1 order 4, 16,974,593 DOFs,
+per-element kappa ~ lognormal(0, 0.5) (seed 4), f ~ U[-1,1] per element
+(seed 5), zero Dirichlet on the boundary.  Synthetic data of the configured
+shape; no dataset is involved.
+
+One step = one application of the sum-factorized matrix-free operator in FP32
+(the inner-CG operator) to a resident vector: `value` = DOFs / step time in
+GDOF/s (whole job: summed over replicas).  The CG part of the metric is
+measured in the same run: time to 1e-10 true relative residual of the
+mixed-precision solver (FP32 inner Jacobi-PCG + FP64 refinement) and of the
+plain FP64 GPU CG on the same problem.
+
+`--impl reference` times the reference algorithm on the host cores instead:
+the FP64 CPU restatement of NGSolve's element-by-element ApplyElementMatrix
+(NGSolve itself cannot be built here: its netgen/ngcore dependency is absent).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "C3: 64^3 hex, H1 p=4, kappa lognormal(0,0.5), matrix-free, FP32 apply in FP64-refined CG"
+NX, ORDER = 64, 4
+SEED_KAPPA, SEED_F = 4, 5
+METRIC = "GDOF/s operator apply & CG time-to-1e-10 residual, mixed-prec vs FP64, 1 GB300"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--order", type=int, default=ORDER)
+    ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    return ap.parse_args()
+
+
+def model_bytes_flops(ne, ndof, p, s_v, s_g):
+    """Algorithmic work of one hex matrix-free apply (n = q = p+1): DOF vector
+    read + write, and the per-point symmetric metric G (6 values per point)."""
+    q = p + 1
+    n = p + 1
+    B = 2 * ndof * s_v + ne * q ** 3 * 6 * s_g
+    F = ne * (4 * (q * n ** 3 + q ** 2 * n ** 2 + q ** 3 * n) + 12 * q ** 4 + 15 * q ** 3)
+    return B, F
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(name):
+    """dram read+write bytes per launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_apply_sample(nx, order, target_s=10.0, threads=None):
+    """Reference algorithm (oracle restatement of ApplyElementMatrix) on a
+    bounded sample of elements; returns GDOF/s scaled to the whole mesh."""
+    from oracle import oracle as O
+    from ngsolve_gb300.meshes import MakeStructured3DMesh
+    mesh = MakeStructured3DMesh(hexes=True, nx=nx)
+    kappa = np.exp(np.random.default_rng(SEED_KAPPA).normal(0, 0.5, mesh.ne))
+    S = O.OracleSpace(mesh.points, mesh.elements, order)
+    x = np.random.default_rng(1).uniform(-1, 1, S.ndof)
+    e1 = 64
+    while True:
+        t0 = time.perf_counter()
+        S.apply_mf(x, kappa=kappa, e0=0, e1=e1)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 8 or e1 >= mesh.ne:
+            break
+        e1 = min(mesh.ne, e1 * 4)
+    reps = max(1, int(target_s / max(dt, 1e-3)))
+    reps = min(reps, 8)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        S.apply_mf(x, kappa=kappa, e0=0, e1=e1)
+    dt = (time.perf_counter() - t0) / reps
+    frac = e1 / mesh.ne
+    gdofs = S.ndof * frac / dt / 1e9
+    return {"value": gdofs, "unit": "GDOF/s", "cores": O.max_threads(), "kind": "port",
+            "sample": "elements 0..%d of %d (fraction %.4f) per apply, %d applies; GDOF/s = ndof*fraction/time"
+                      % (e1, mesh.ne, frac, reps),
+            "seconds_per_sample_apply": dt}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import os as _os
+    res = []
+    for _ in range(args.warmup):
+        cpu_apply_sample(args.nx, args.order, target_s=2.0)
+    for _ in range(args.steps):
+        res.append(cpu_apply_sample(args.nx, args.order, target_s=4.0))
+    val = statistics.median(r["value"] for r in res)
+    r0 = res[0]
+    out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GDOF/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(r["seconds_per_sample_apply"] for r in res),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "nx": args.nx, "order": args.order, "l2": "inputs larger than L2"},
+           "cpu_baseline": {"value": val, "unit": "GDOF/s", "cores": r0["cores"], "kind": "port", "sample": r0["sample"]},
+           "e2e": {"value": val, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "NGSolve needs netgen/ngcore (absent, no network): the CPU restatement of its element-wise "
+                   "ApplyElementMatrix algorithm (oracle/gh1_oracle.cpp) on %d host threads stands in" % r0["cores"]}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import torch
+    import ngsolve_gb300 as ng
+    from ngsolve_gb300 import build
+    build.build()
+    dev = local
+    torch.cuda.set_device(dev)
+
+    mesh = ng.MakeStructured3DMesh(hexes=True, nx=args.nx)
+    kappa = np.exp(np.random.default_rng(SEED_KAPPA).normal(0, 0.5, mesh.ne))
+    fvals = np.random.default_rng(SEED_F).uniform(-1, 1, mesh.ne)
+    fes = ng.H1(ng.Mesh(mesh, device=dev), order=args.order, dirichlet=".*")
+    u, v = fes.TnT()
+    a = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+    a += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+    a.Assemble()
+    N, ne = fes.ndof, mesh.ne
+    x32 = ng.BaseVector(data=torch.rand(N, dtype=torch.float32, device="cuda"))
+    y32 = ng.BaseVector(data=torch.zeros(N, dtype=torch.float32, device="cuda"))
+    x64 = ng.BaseVector(data=x32.t.double())
+    y64 = ng.BaseVector(N)
+
+    # ---- timed region: K FP32 operator applications ---------------------------
+    for _ in range(max(3, args.warmup)):
+        a.mat.Mult(x32, y32)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        a.mat.Mult(x32, y32)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    barrier(ws)
+    t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    t_step = max_over_ranks(t_step, ws)
+    value = ws * N / t_step / 1e9
+
+    # FP64 apply (reference precision) for context
+    for _ in range(2):
+        a.mat.Mult(x64, y64)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    k64 = 5
+    for _ in range(k64):
+        a.mat.Mult(x64, y64)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3 / k64
+
+    # ---- e2e through the public API with host buffers -------------------------
+    xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
+    xh.copy_(x32.t.cpu())
+    yh = torch.empty(N, dtype=torch.float32, pin_memory=True)
+    for _ in range(3):
+        x32.t.copy_(xh, non_blocking=True)
+        a.mat.Mult(x32, y32)
+        yh.copy_(y32.t, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0.record(stream)
+    ke = max(5, args.steps // 2)
+    for _ in range(ke):
+        x32.t.copy_(xh, non_blocking=True)
+        a.mat.Mult(x32, y32)
+        yh.copy_(y32.t, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3 / ke, ws)
+    e2e = {"value": ws * N / t_e2e / 1e9, "unit": "GDOF/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N}
+
+    # ---- CG time to 1e-10 : mixed vs FP64 --------------------------------------
+    cg = None
+    if not args.no_cg:
+        f = ng.LinearForm(fes)
+        f += ng.CoefficientFunction(fvals) * v * ng.dx
+        f.Assemble()
+        pre = a.mat.CreateSmoother(fes.FreeDofs())
+        torch.cuda.synchronize()
+
+        def solve(mode):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sol = ng.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-10, maxsteps=100000, printrates=False,
+                                mode=mode, stop_rule="true")
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0, sol, ng.solvers.CG.last_solver.result
+
+        solve("mixed")  # warm-up (graph instantiation)
+        tm, solm, rm = solve("mixed")
+        xm = solm.NumPy().copy()
+        t6, sol6, r6 = solve("fp64")
+        x6 = sol6.NumPy()
+        err = float(np.abs(xm - x6).max() / np.abs(x6).max())
+        cg = {"mixed_s": tm, "fp64_s": t6, "speedup_mixed_vs_fp64": t6 / tm,
+              "mixed": {"inner_iterations": rm.iterations, "outer": rm.outer, "applies32": rm.applies32,
+                        "applies64": rm.applies64, "true_relres": rm.true_relres, "status": rm.status},
+              "fp64": {"iterations": r6.iterations, "applies64": r6.applies64, "true_relres": r6.true_relres,
+                       "status": r6.status},
+              "err_mixed_vs_fp64_gpu": err,
+              "stop": "||b-Ax||_free <= 1e-10 ||b||_free (FP64 true residual)"}
+
+    peak, peak_kind = load_peaks()
+    B32, F = model_bytes_flops(ne, N, args.order, 4, 4)
+    achieved = B32 / t_step / 1e9 * 1.0 if ws == 1 else B32 / t_step / 1e9
+    traffic = load_traffic("hex_apply_fp32_c3.md")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": B32, "kernel": "hex_apply_kernel<5,float>"}
+    B64, _ = model_bytes_flops(ne, N, args.order, 8, 8)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_apply_sample(args.nx, args.order, target_s=10.0)
+        cpu.pop("seconds_per_sample_apply", None)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "nx": args.nx, "order": args.order, "ndof": N, "ne": ne,
+                          "parallelism": "replicas" if ws > 1 else "single",
+                          "l2": "inputs larger than L2 (G tile stream %.0f MB per apply)" % (ne * (args.order + 1) ** 3 * 24 / 1e6)},
+               "e2e": e2e, "gpu_launches": args.steps, "clocks": ck, "roofline": roofline,
+               "fp64_apply": {"ms": t64 * 1e3, "gdofs": N / t64 / 1e9, "achieved_tflops_model": F / t64 / 1e12,
+                              "achieved_gbs_model": B64 / t64 / 1e9},
+               "cg": cg, "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/* gh1.h -- C ABI of the GB300-native high-order H1 operator library.
+ *
+ * This library replaces, on one GPU, the hot path of NGSolve's H1 Poisson
+ * stack: shape/gradient evaluation at integration points, element-matrix
+ * assembly into a CSR SparseMatrix, sum-factorized matrix-free Apply on hexes
+ * (element-wise B^T D B on tets), CSR SpMV, Jacobi-preconditioned CG (FP64 and
+ * FP32-inner/FP64-refined), the adjoint dJ/dkappa contraction and batched solves.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (GH1_OK = 0) and never throws;
+ *    gh1_last_error(ctx) gives the message of the last failure on a context.
+ *  - Vectors passed to apply / solve calls are DEVICE pointers of the
+ *    precision named in the call (double* for GH1_F64, float* for GH1_F32).
+ *    Setup arrays (coordinates, connectivity, coefficients) are HOST pointers
+ *    unless a `mem` argument says GH1_MEM_DEVICE.
+ *  - All device work is ordered on the context's stream (gh1_set_stream).
+ *    A context is not thread safe: use one per host thread.
+ *  - Element types: 4 = tetrahedron, 8 = hexahedron, vertex order as in
+ *    NGSolve's ET_trait<ET_TET>/<ET_HEX> (fem/elementtopology.cpp:74-119).
+ *  - DOF numbering follows H1HighOrderFESpace::UpdateDofTables/GetDofNrs
+ *    (comp/h1hofespace.cpp:823-950, :1389-1420): vertices, then edges, faces,
+ *    cells; edges and faces are numbered by their sorted global vertex tuples.
+ */
+#ifndef GH1_H
+#define GH1_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  GH1_OK = 0,
+  GH1_ERR_ARG = 1,          /* invalid argument (the message says which)       */
+  GH1_ERR_CUDA = 2,         /* a CUDA runtime call failed                       */
+  GH1_ERR_NOMEM = 3,        /* device allocation failed                         */
+  GH1_ERR_UNSUPPORTED = 4,  /* element type / order / precision not provided    */
+  GH1_ERR_ILLEGAL_DNUMS = 5,/* scatter met a column missing from the pattern    */
+  GH1_MAXITER = 6,          /* solver stopped at maxit without reaching tol     */
+  GH1_BREAKDOWN = 7         /* CG breakdown: s^T A s <= 0 or a NaN appeared     */
+};
+enum { GH1_F64 = 0, GH1_F32 = 1 };
+enum { GH1_MEM_HOST = 0, GH1_MEM_DEVICE = 1 };
+enum { GH1_OP_CSR = 0, GH1_OP_MATFREE = 1 };
+
+typedef struct gh1_ctx gh1_ctx;
+typedef struct gh1_mesh gh1_mesh;
+typedef struct gh1_space gh1_space;
+typedef struct gh1_form gh1_form;
+typedef struct gh1_op gh1_op;
+typedef struct gh1_pre gh1_pre;
+
+/* ---- lifetime ---------------------------------------------------------- */
+int gh1_create(gh1_ctx** ctx, int device);
+int gh1_destroy(gh1_ctx* ctx);
+/* stream: a cudaStream_t (NULL = legacy default stream) */
+int gh1_set_stream(gh1_ctx* ctx, void* stream);
+const char* gh1_last_error(gh1_ctx* ctx);
+int gh1_version(void);
+
+/* ---- mesh and space -----------------------------------------------------
+ * Replaces MeshAccess + H1HighOrderFESpace construction
+ * (comp/meshaccess.cpp:1670, comp/h1hofespace.cpp:564-950).            */
+int gh1_mesh_upload(gh1_ctx* ctx, int nv, const double* coords /*nv*3*/, int ne, int et,
+                    const int32_t* elem_vertices /*ne*et*/, gh1_mesh** mesh);
+int gh1_mesh_free(gh1_mesh* mesh);
+/* dirichlet: 1 = all boundary DOFs are Dirichlet (dirichlet=".*"), 0 = none */
+int gh1_space_h1(gh1_mesh* mesh, int order, int dirichlet, gh1_space** space);
+int gh1_space_free(gh1_space* space);
+/* info[0..5] = ndof, nloc, nedges, nfaces, nfree, ne */
+int gh1_space_info(gh1_space* space, int64_t* info);
+/* element DOF numbers in NGSolve's local order (GetDofNrs), host ne*nloc */
+int gh1_space_get_dofs(gh1_space* space, int32_t* elem_dofs);
+/* FreeDofs() as one byte per DOF, host ndof */
+int gh1_space_get_freedofs(gh1_space* space, uint8_t* freedofs);
+/* shape values and reference gradients at points, evaluated on the GPU with the
+ * element's vertex numbers (H1HighOrderFE::CalcShape/CalcDShape,
+ * fem/tscalarfe_impl.hpp:24-56); host out: val[npts*nloc], grad[npts*nloc*3] */
+int gh1_shape_eval(gh1_ctx* ctx, int et, int order, const int32_t* vnums, int npts,
+                   const double* pts, double* val, double* grad);
+
+/* ---- bilinear form  kappa_e grad u.grad v + mu_e u v --------------------
+ * Replaces BilinearForm + SymbolicBFI for the Laplace/mass slice
+ * (comp/bilinearform.cpp:832, fem/symbolicintegrator.cpp:1548-1830).
+ * kappa / mu: per-element coefficients (NULL: kappa = 1, mu = 0).        */
+int gh1_form_create(gh1_space* space, const double* kappa, const double* mu, int mem, gh1_form** form);
+int gh1_form_set_coefs(gh1_form* form, const double* kappa, const double* mu, int mem);
+int gh1_form_free(gh1_form* form);
+
+/* BilinearForm.Assemble() -> SparseMatrix (comp/bilinearform.cpp:832-1000,
+ * linalg/sparsematrix_impl.hpp:148-190): GPU element matrices scattered into
+ * the MatrixGraph pattern (full storage, sorted columns).               */
+int gh1_assemble_csr(gh1_form* form, gh1_op** csr);
+/* info[0..1] = nrows, nnz */
+int gh1_csr_info(gh1_op* csr, int64_t* info);
+int gh1_csr_export(gh1_op* csr, int64_t* rowptr, int32_t* colind, double* vals, int mem);
+/* Upload an externally built CSR matrix (e.g. NGSolve's own SparseMatrix) */
+int gh1_csr_import(gh1_ctx* ctx, int64_t nrows, int64_t nnz, const int64_t* rowptr, const int32_t* colind,
+                   const double* vals, int mem, gh1_op** csr);
+
+/* BilinearForm(nonassemble=True).mat -> BilinearFormApplication
+ * (comp/bilinearform.cpp:7549-7607): sum-factorized on hexes, element-wise
+ * B^T D B on tets.  precision_mask: bit0 = FP64 data, bit1 = FP32 data.  */
+int gh1_matfree_create(gh1_form* form, int precision_mask, gh1_op** op);
+
+/* BaseMatrix::Mult / MultAdd (linalg/basematrix.hpp:117-126):
+ * y = s*A*x (accumulate=0) or y += s*A*x (accumulate=1); device pointers. */
+int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, int accumulate);
+/* info[0..3] = kind (GH1_OP_*), nrows, ne, order */
+int gh1_op_info(gh1_op* op, int64_t* info);
+int gh1_op_free(gh1_op* op);
+
+/* ---- preconditioner -----------------------------------------------------
+ * a.mat.CreateSmoother(freedofs) / Preconditioner(a,"local")
+ * (linalg/jacobi.cpp:40-110): invdiag = 1/A_ii on free DOFs, 0 elsewhere.
+ * freedofs: NULL = the space's free DOFs.                                */
+int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** pre);
+int gh1_pre_apply(gh1_pre* pre, double s, const void* x, void* y, int precision, int accumulate);
+int gh1_pre_free(gh1_pre* pre);
+
+/* ---- right-hand side ------------------------------------------------------
+ * LinearForm(f*v*dx) with f piecewise constant per element, integration
+ * order 2p (fem/symbolicintegrator.cpp:1109).  b: device double[ndof].    */
+int gh1_rhs_elementwise(gh1_space* space, const double* f_elem, int mem, double* b);
+
+/* ---- CG --------------------------------------------------------------------
+ * solvers.CG / CGSolver._SolveImpl (python/krylovspace.py:263-337).
+ * mode GH1_CG_FP64: the reference algorithm on the GPU in FP64.
+ * mode GH1_CG_MIXED: FP32 inner Jacobi-PCG inside FP64 iterative refinement
+ *   (outer residual b - A x, dot products and updates in FP64).
+ * stop_rule GH1_STOP_PRECOND: sqrt|w.d| <= tol * first (the reference rule);
+ * GH1_STOP_TRUE: ||b - A x||_free <= tol * ||b||_free.                     */
+enum { GH1_CG_FP64 = 0, GH1_CG_MIXED = 1 };
+enum { GH1_STOP_PRECOND = 0, GH1_STOP_TRUE = 1 };
+typedef struct {
+  double tol;          /* relative tolerance                                   */
+  int maxit;           /* maximal iterations (inner iterations for MIXED)      */
+  int mode;            /* GH1_CG_FP64 / GH1_CG_MIXED                           */
+  int stop_rule;       /* GH1_STOP_PRECOND / GH1_STOP_TRUE                     */
+  int initialize;      /* 1: start from x = 0, 0: use x as initial guess       */
+  double inner_tol;    /* MIXED: relative reduction per inner solve (0=default)*/
+  int max_outer;       /* MIXED: maximal refinement steps (0 = default 30)      */
+  int check_every;     /* iterations per graph launch between host checks (0=auto) */
+  double* res_hist;    /* optional host buffer [maxit+1] of residuals (may be NULL) */
+} gh1_cg_opts;
+typedef struct {
+  int status;          /* GH1_OK, GH1_MAXITER or GH1_BREAKDOWN                  */
+  int iterations;      /* CheckResidual calls (FP64) / total inner iterations   */
+  int outer;           /* MIXED: refinement steps taken                         */
+  int applies64;       /* FP64 operator applications                            */
+  int applies32;       /* FP32 operator applications                            */
+  double first_res;    /* first residual of the stop rule                       */
+  double final_res;    /* last residual of the stop rule                        */
+  double true_relres;  /* ||b-Ax||_free/||b||_free at exit (FP64)               */
+} gh1_cg_result;
+/* b, x: device double[ndof].  pre may be NULL only for GH1_CG_FP64 (then no
+ * preconditioning and no Dirichlet projection).                            */
+int gh1_cg(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* opts, gh1_cg_result* res);
+
+/* ---- adjoint ---------------------------------------------------------------
+ * Element-wise integral of grad u . grad w (Integrate(..., element_wise=True),
+ * comp/python_comp.cpp:3703-3948): out[e] = int_e grad u.grad w (device ptrs). */
+int gh1_elem_grad_dot(gh1_space* space, const double* u, const double* w, double* out);
+/* J(kappa) = 1/2 int (u - u_target)^2 with A(kappa) u = f (zero Dirichlet);
+ * dJ/dkappa_e = -int_e grad u . grad lambda,  A lambda = M (u - u_target).
+ * f, u_target: device double[ndof] (f already assembled); kappa: the form's.
+ * Outputs (device): u[ndof], lambda[ndof], dJdkappa[ne]; J on the host.   */
+int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u_target, double tol,
+                     double* u, double* lambda, double* dJdkappa, double* J);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GH1_H */

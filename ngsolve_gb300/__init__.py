@@ -1,0 +1,17 @@
+"""ngsolve_gb300 -- GB300-native engine for NGSolve's high-order H1 operator path.
+
+The numerical work runs in libgh1.so (CUDA, sm_103a; C ABI in include/gh1.h).
+This package mirrors the reference's Python objects on that path.
+"""
+from . import _lib
+from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMesh
+from .comp import (Mesh, H1, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
+                   BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, JacobiPrecond, Preconditioner,
+                   Integrate_grad_dot, ShapeEval, context)
+from . import solvers
+from .adjoint import AdjointProblem, AdjointJ
+
+__all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "BilinearForm",
+           "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
+           "SparseMatrix", "BilinearFormApplication", "JacobiPrecond", "Preconditioner", "Integrate_grad_dot",
+           "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ"]

@@ -1,0 +1,625 @@
+"""Python front end mirroring the NGSolve objects on the H1 operator path.
+
+    mesh = Mesh(MakeStructured3DMesh(hexes=True, nx=16))
+    fes = H1(mesh, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+    a = BilinearForm(fes)
+    a += CoefficientFunction(kappa) * grad(u) * grad(v) * dx
+    a.Assemble()                           # a.mat: SparseMatrix on the GPU
+    f = LinearForm(fes); f += CoefficientFunction(fe) * v * dx; f.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    gfu = GridFunction(fes)
+    gfu.vec.data = solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-10, maxsteps=1000)
+
+Names, argument meanings and error behaviour follow comp/python_comp.cpp
+(BilinearForm :2800-3060, LinearForm, GridFunction), linalg/python_linalg.cpp
+(BaseMatrix.Mult/MultAdd :1072-1073, CreateSmoother :1220) and
+python/krylovspace.py (solvers.CG).  Coefficients are per-element constants
+(an order-0 L2 GridFunction in the reference's adjoint tutorial).  Every
+numerical call goes to libgh1.so on the GPU; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .meshes import Mesh as _RawMesh
+
+_contexts = {}
+
+
+class Context:
+    """One gh1 context per CUDA device; work runs on torch's current stream."""
+
+    def __init__(self, device=0):
+        if not torch.cuda.is_available():
+            raise _lib.GH1Error(2, "no CUDA device available (the H1 engine has no CPU fallback)")
+        self.lib = _lib.load()
+        self.device = device
+        h = ctypes.c_void_p()
+        rc = self.lib.gh1_create(ctypes.byref(h), device)
+        if rc != 0:
+            msg = self.lib.gh1_last_error(h) if h.value else b"gh1_create failed"
+            raise _lib.GH1Error(rc, msg.decode())
+        self.h = h
+
+    def sync_stream(self):
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        self.lib.gh1_set_stream(self.h, ctypes.c_void_p(s))
+        return self
+
+    def check(self, rc):
+        _lib.check(rc, self.h)
+
+
+def context(device=0):
+    if device not in _contexts:
+        _contexts[device] = Context(device)
+    return _contexts[device].sync_stream()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _np_ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+# ---------------------------------------------------------------------------
+class Mesh:
+    """Uploaded volume mesh (tets or hexes) -- ngsolve.Mesh for the H1 path."""
+
+    def __init__(self, mesh, device=0):
+        if not isinstance(mesh, _RawMesh):
+            raise TypeError("Mesh expects a meshes.Mesh (points + element vertex lists)")
+        self.raw = mesh
+        self.device = device
+        self.ctx = context(device)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gh1_mesh_upload(self.ctx.h, mesh.nv, _np_ptr(mesh.points), mesh.ne, mesh.et,
+                                                    _np_ptr(mesh.elements), ctypes.byref(h)))
+        self.h = h
+
+    @property
+    def ne(self):
+        return self.raw.ne
+
+    @property
+    def nv(self):
+        return self.raw.nv
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_mesh_free(self.h)
+        except Exception:
+            pass
+
+
+class BitArray(np.ndarray):
+    """Free-DOF mask (bool per DOF), the role of ngstd BitArray."""
+
+
+# ---------------------------------------------------------------------------
+# symbolic placeholders for the two integrators on the path
+class _Proxy:
+    def __init__(self, fes, test):
+        self.fes, self.test = fes, test
+
+    def __mul__(self, other):
+        return _Product.of(self, other)
+
+    __rmul__ = __mul__
+
+
+class _Grad:
+    def __init__(self, proxy):
+        self.proxy = proxy
+
+    def __mul__(self, other):
+        return _Product.of(self, other)
+
+    __rmul__ = __mul__
+
+
+def grad(u):
+    if not isinstance(u, _Proxy):
+        raise TypeError("grad() expects a trial or test function")
+    return _Grad(u)
+
+
+class CoefficientFunction:
+    """Piecewise-constant coefficient: one value per element (or a scalar)."""
+
+    def __init__(self, values):
+        self.values = values
+
+    def element_values(self, ne):
+        v = np.asarray(self.values, dtype=np.float64)
+        if v.ndim == 0:
+            return np.full(ne, float(v))
+        if v.shape != (ne,):
+            raise ValueError("element-wise coefficient needs %d values, got %s" % (ne, v.shape))
+        return np.ascontiguousarray(v)
+
+    def __mul__(self, other):
+        return _Product.of(self, other)
+
+    __rmul__ = __mul__
+
+
+class _Measure:
+    pass
+
+
+dx = _Measure()
+
+
+class _Product:
+    """kind in {'laplace', 'mass', 'source'} with an element-wise coefficient."""
+
+    def __init__(self, factors):
+        self.factors = factors
+
+    @staticmethod
+    def of(a, b):
+        fa = a.factors if isinstance(a, _Product) else [a]
+        fb = b.factors if isinstance(b, _Product) else [b]
+        return _Product(fa + fb)
+
+    def __mul__(self, other):
+        return _Product.of(self, other)
+
+    __rmul__ = __mul__
+
+    def classify(self, ne):
+        grads = [f for f in self.factors if isinstance(f, _Grad)]
+        proxies = [f for f in self.factors if isinstance(f, _Proxy)]
+        coef = np.ones(ne)
+        has_dx = False
+        for f in self.factors:
+            if isinstance(f, CoefficientFunction):
+                coef = coef * f.element_values(ne)
+            elif isinstance(f, (int, float, np.floating)):
+                coef = coef * float(f)
+            elif isinstance(f, _Measure):
+                has_dx = True
+        if not has_dx:
+            raise ValueError("integrand needs * dx")
+        if len(grads) == 2 and not proxies and grads[0].proxy.test != grads[1].proxy.test:
+            return "laplace", coef
+        if len(proxies) == 2 and not grads and proxies[0].test != proxies[1].test:
+            return "mass", coef
+        if len(proxies) == 1 and not grads and proxies[0].test:
+            return "source", coef
+        raise NotImplementedError("only kappa*grad(u)*grad(v)*dx, mu*u*v*dx and f*v*dx are on the H1 path")
+
+
+# ---------------------------------------------------------------------------
+class H1:
+    """H1HighOrderFESpace of uniform order (comp/h1hofespace.cpp)."""
+
+    def __init__(self, mesh, order=1, dirichlet=""):
+        if not isinstance(mesh, Mesh):
+            mesh = Mesh(mesh)
+        self.mesh = mesh
+        self.order = int(order)
+        self.ctx = mesh.ctx
+        dir_all = 1 if dirichlet not in ("", None, False) else 0
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gh1_space_h1(mesh.h, self.order, dir_all, ctypes.byref(h)))
+        self.h = h
+        info = np.zeros(6, dtype=np.int64)
+        self.ctx.check(self.ctx.lib.gh1_space_info(h, _np_ptr(info)))
+        self.ndof, self.nloc, self.nedges, self.nfaces, self.nfree, self.ne = (int(v) for v in info)
+        self._dofs = None
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_space_free(self.h)
+        except Exception:
+            pass
+
+    def TnT(self):
+        return _Proxy(self, False), _Proxy(self, True)
+
+    def TrialFunction(self):
+        return _Proxy(self, False)
+
+    def TestFunction(self):
+        return _Proxy(self, True)
+
+    def FreeDofs(self):
+        out = np.zeros(self.ndof, dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.gh1_space_get_freedofs(self.h, _np_ptr(out)))
+        return out.astype(bool).view(BitArray)
+
+    def ElementDofs(self):
+        if self._dofs is None:
+            out = np.zeros((self.ne, self.nloc), dtype=np.int32)
+            self.ctx.check(self.ctx.lib.gh1_space_get_dofs(self.h, _np_ptr(out)))
+            self._dofs = out
+        return self._dofs
+
+    def GetDofNrs(self, el):
+        return tuple(int(d) for d in self.ElementDofs()[int(el)])
+
+
+# ---------------------------------------------------------------------------
+class BaseVector:
+    """Device vector (FP64 unless stated) -- ngla BaseVector / UnifiedVector."""
+
+    def __init__(self, n=None, data=None, dtype=torch.float64, device=0):
+        if data is not None:
+            self.t = data
+        else:
+            self.t = torch.zeros(int(n), dtype=dtype, device="cuda:%d" % device)
+
+    def __len__(self):
+        return self.t.numel()
+
+    @property
+    def size(self):
+        return self.t.numel()
+
+    def CreateVector(self):
+        return BaseVector(data=torch.zeros_like(self.t))
+
+    def NumPy(self):
+        return self.t.detach().cpu().numpy()
+
+    def FV(self):
+        return self.t
+
+    @property
+    def data(self):
+        return self
+
+    @data.setter
+    def data(self, value):
+        if isinstance(value, _Expr):
+            value.eval_into(self)
+        elif isinstance(value, BaseVector):
+            self.t.copy_(value.t)
+        elif isinstance(value, torch.Tensor):
+            self.t.copy_(value.to(self.t.device, self.t.dtype))
+        else:
+            self.t.copy_(torch.as_tensor(np.asarray(value), dtype=self.t.dtype, device=self.t.device))
+
+    def __setitem__(self, key, value):
+        self.t[key] = value
+
+    def __getitem__(self, key):
+        return self.t[key]
+
+    def InnerProduct(self, other, conjugate=False):
+        return float(torch.dot(self.t, other.t))
+
+    def Norm(self):
+        return float(torch.linalg.vector_norm(self.t))
+
+    def __add__(self, other):
+        return _LinComb([(1.0, self), (1.0, other)])
+
+    def __sub__(self, other):
+        return _LinComb([(1.0, self), (-1.0, other)])
+
+    def __rmul__(self, s):
+        return _LinComb([(float(s), self)])
+
+    def __iadd__(self, other):
+        if isinstance(other, _Expr):
+            tmp = self.CreateVector()
+            other.eval_into(tmp)
+            self.t.add_(tmp.t)
+        else:
+            self.t.add_(other.t)
+        return self
+
+    def __isub__(self, other):
+        if isinstance(other, _Expr):
+            tmp = self.CreateVector()
+            other.eval_into(tmp)
+            self.t.sub_(tmp.t)
+        else:
+            self.t.sub_(other.t)
+        return self
+
+    def __imul__(self, s):
+        self.t.mul_(float(s))
+        return self
+
+
+class _Expr:
+    def eval_into(self, y):
+        raise NotImplementedError
+
+
+class _LinComb(_Expr):
+    def __init__(self, terms):
+        self.terms = terms
+
+    def __add__(self, other):
+        if isinstance(other, _LinComb):
+            return _LinComb(self.terms + other.terms)
+        return _LinComb(self.terms + [(1.0, other)])
+
+    def __sub__(self, other):
+        if isinstance(other, _LinComb):
+            return _LinComb(self.terms + [(-s, v) for s, v in other.terms])
+        return _LinComb(self.terms + [(-1.0, other)])
+
+    def eval_into(self, y):
+        acc = torch.zeros_like(y.t)
+        for s, v in self.terms:
+            if isinstance(v, _Expr):
+                tmp = y.CreateVector()
+                v.eval_into(tmp)
+                acc.add_(tmp.t, alpha=s)
+            else:
+                acc.add_(v.t, alpha=s)
+        y.t.copy_(acc)
+
+
+class _MatVec(_Expr):
+    def __init__(self, mat, x, s=1.0):
+        self.mat, self.x, self.s = mat, x, s
+
+    def __rmul__(self, s):
+        return _MatVec(self.mat, self.x, self.s * float(s))
+
+    def __add__(self, other):
+        return _LinComb([(1.0, self), (1.0, other)])
+
+    def __radd__(self, other):
+        return _LinComb([(1.0, other), (1.0, self)])
+
+    def __rsub__(self, other):
+        return _LinComb([(1.0, other), (-1.0, self)])
+
+    def eval_into(self, y):
+        self.mat.MultScale(self.s, self.x, y)
+
+
+def _as_vec(x):
+    return x if isinstance(x, BaseVector) else BaseVector(data=x)
+
+
+class BaseMatrix:
+    """BaseMatrix Mult / MultAdd (linalg/basematrix.hpp:117-126) on a gh1 operator."""
+
+    def __init__(self, ctx, h, height, fes=None):
+        self.ctx, self.h, self.height, self.width, self.fes = ctx, h, int(height), int(height), fes
+
+    def __mul__(self, x):
+        return _MatVec(self, _as_vec(x))
+
+    def CreateVector(self, colvector=False):
+        return BaseVector(self.height)
+
+    CreateRowVector = CreateVector
+    CreateColVector = CreateVector
+
+    def _apply(self, s, x, y, acc):
+        x, y = _as_vec(x), _as_vec(y)
+        if x.t.dtype != y.t.dtype:
+            raise TypeError("x and y must have the same precision")
+        prec = _lib.GH1_F64 if x.t.dtype == torch.float64 else _lib.GH1_F32
+        if not (x.t.is_cuda and y.t.is_cuda and x.t.is_contiguous() and y.t.is_contiguous()):
+            raise TypeError("vectors must be contiguous CUDA tensors")
+        if x.t.numel() != self.width or y.t.numel() != self.height:
+            raise ValueError("vector size does not match the matrix")
+        self.ctx.sync_stream()
+        self.ctx.check(self.ctx.lib.gh1_op_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
+
+    def Mult(self, x, y):
+        self._apply(1.0, x, y, 0)
+
+    def MultScale(self, s, x, y):
+        self._apply(s, x, y, 0)
+
+    def MultAdd(self, s, x, y):
+        self._apply(s, x, y, 1)
+
+    def CreateSmoother(self, freedofs=None):
+        return JacobiPrecond(self, freedofs)
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_op_free(self.h)
+        except Exception:
+            pass
+
+
+class SparseMatrix(BaseMatrix):
+    """Assembled CSR matrix on the GPU (SparseMatrix<double>)."""
+
+    def __init__(self, ctx, h, fes=None):
+        info = np.zeros(2, dtype=np.int64)
+        ctx.check(ctx.lib.gh1_csr_info(h, _np_ptr(info)))
+        super().__init__(ctx, h, info[0], fes)
+        self.nze = int(info[1])
+
+    def CSR(self):
+        """(rowptr int64, colind int32, vals float64) copied to the host."""
+        rp = np.zeros(self.height + 1, dtype=np.int64)
+        ci = np.zeros(self.nze, dtype=np.int32)
+        va = np.zeros(self.nze, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.gh1_csr_export(self.h, _np_ptr(rp), _np_ptr(ci), _np_ptr(va), _lib.GH1_MEM_HOST))
+        return rp, ci, va
+
+    def __getitem__(self, ij):
+        i, j = ij
+        rp, ci, va = self.CSR()
+        row = ci[rp[i]:rp[i + 1]]
+        k = np.searchsorted(row, j)
+        return float(va[rp[i] + k]) if k < len(row) and row[k] == j else 0.0
+
+    @staticmethod
+    def FromCSR(rowptr, colind, vals, device=0):
+        ctx = context(device)
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        colind = np.ascontiguousarray(colind, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_csr_import(ctx.h, len(rowptr) - 1, len(colind), _np_ptr(rowptr), _np_ptr(colind),
+                                         _np_ptr(vals), _lib.GH1_MEM_HOST, ctypes.byref(h)))
+        return SparseMatrix(ctx, h)
+
+
+class BilinearFormApplication(BaseMatrix):
+    """Matrix-free operator: sum-factorized on hexes, element-wise on tets."""
+
+
+class JacobiPrecond(BaseMatrix):
+    """JacobiPrecond (linalg/jacobi.cpp:40-110): invdiag on free DOFs, 0 elsewhere."""
+
+    def __init__(self, mat, freedofs=None):
+        self.mat = mat
+        h = ctypes.c_void_p()
+        fd = None
+        if freedofs is not None:
+            fd = np.ascontiguousarray(np.asarray(freedofs, dtype=bool).astype(np.uint8))
+            if fd.shape != (mat.height,):
+                raise ValueError("freedofs size does not match the matrix")
+        mat.ctx.sync_stream()
+        mat.ctx.check(mat.ctx.lib.gh1_jacobi_create(mat.h, None if fd is None else _np_ptr(fd), _lib.GH1_MEM_HOST,
+                                                     ctypes.byref(h)))
+        self.ctx, self.h, self.height, self.width, self.fes = mat.ctx, h, mat.height, mat.height, mat.fes
+        self._fd = fd
+
+    def _apply(self, s, x, y, acc):
+        x, y = _as_vec(x), _as_vec(y)
+        prec = _lib.GH1_F64 if x.t.dtype == torch.float64 else _lib.GH1_F32
+        self.ctx.sync_stream()
+        self.ctx.check(self.ctx.lib.gh1_pre_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_pre_free(self.h)
+        except Exception:
+            pass
+
+
+def Preconditioner(a, kind="local"):
+    """Preconditioner(a, "local") = Jacobi on the free DOFs (comp/preconditioner.cpp:684-760)."""
+    if kind not in ("local", "jacobi"):
+        raise NotImplementedError("only the 'local' (Jacobi) preconditioner is on the H1 path")
+    return JacobiPrecond(a.mat, a.fes.FreeDofs())
+
+
+# ---------------------------------------------------------------------------
+class BilinearForm:
+    """BilinearForm(fes, nonassemble=False) with kappa grad.grad and mu u.v terms.
+
+    nonassemble=True gives the matrix-free operator as .mat (BilinearFormApplication,
+    comp/bilinearform.cpp:7549-7607); precision='fp32' adds the FP32 data used by
+    the mixed-precision solver (the reference's fp32 flag, :7590-7607)."""
+
+    def __init__(self, fes, nonassemble=False, precision="fp64", symmetric=True, **kwargs):
+        self.fes = fes
+        self.nonassemble = bool(nonassemble)
+        self.precision = precision
+        self.kappa = np.zeros(fes.ne)
+        self.mu = None
+        self._has_laplace = False
+        self._form = None
+        self.mat = None
+
+    def __iadd__(self, term):
+        kind, coef = term.classify(self.fes.ne)
+        if kind == "laplace":
+            self.kappa = self.kappa + coef
+            self._has_laplace = True
+        elif kind == "mass":
+            self.mu = coef if self.mu is None else self.mu + coef
+        else:
+            raise ValueError("a source term belongs to a LinearForm")
+        self._form = None
+        return self
+
+    def _make_form(self):
+        ctx = self.fes.ctx
+        kappa = np.ascontiguousarray(self.kappa, dtype=np.float64)
+        mu = None if self.mu is None else np.ascontiguousarray(self.mu, dtype=np.float64)
+        if self._form is None:
+            h = ctypes.c_void_p()
+            ctx.check(ctx.lib.gh1_form_create(self.fes.h, _np_ptr(kappa), None if mu is None else _np_ptr(mu),
+                                              _lib.GH1_MEM_HOST, ctypes.byref(h)))
+            self._form = h
+        return self._form
+
+    def Assemble(self, reallocate=False):
+        ctx = self.fes.ctx.sync_stream()
+        form = self._make_form()
+        h = ctypes.c_void_p()
+        if self.nonassemble:
+            mask = 1 | (2 if self.precision in ("fp32", "mixed") else 0)
+            ctx.check(ctx.lib.gh1_matfree_create(form, mask, ctypes.byref(h)))
+            self.mat = BilinearFormApplication(ctx, h, self.fes.ndof, self.fes)
+        else:
+            ctx.check(ctx.lib.gh1_assemble_csr(form, ctypes.byref(h)))
+            self.mat = SparseMatrix(ctx, h, self.fes)
+        return self
+
+    def Apply(self, x, y):
+        if self.mat is None:
+            self.Assemble()
+        self.mat.Mult(x, y)
+
+    def __del__(self):
+        try:
+            if self._form is not None:
+                self.fes.ctx.lib.gh1_form_free(self._form)
+        except Exception:
+            pass
+
+
+class LinearForm:
+    """LinearForm(fes) += f * v * dx with f constant per element; order 2p."""
+
+    def __init__(self, fes):
+        self.fes = fes
+        self.f = np.zeros(fes.ne)
+        self.vec = BaseVector(fes.ndof)
+
+    def __iadd__(self, term):
+        kind, coef = term.classify(self.fes.ne)
+        if kind != "source":
+            raise ValueError("LinearForm takes f*v*dx")
+        self.f = self.f + coef
+        return self
+
+    def Assemble(self):
+        ctx = self.fes.ctx.sync_stream()
+        f = np.ascontiguousarray(self.f, dtype=np.float64)
+        ctx.check(ctx.lib.gh1_rhs_elementwise(self.fes.h, _np_ptr(f), _lib.GH1_MEM_HOST, _ptr(self.vec.t)))
+        return self
+
+
+class GridFunction:
+    def __init__(self, fes, name="gfu"):
+        self.fes = fes
+        self.vec = BaseVector(fes.ndof)
+
+
+def Integrate_grad_dot(fes, u, w):
+    """Element-wise int_e grad u . grad w (Integrate(..., element_wise=True))."""
+    ctx = fes.ctx.sync_stream()
+    u, w = _as_vec(u), _as_vec(w)
+    out = torch.zeros(fes.ne, dtype=torch.float64, device=u.t.device)
+    ctx.check(ctx.lib.gh1_elem_grad_dot(fes.h, _ptr(u.t), _ptr(w.t), _ptr(out)))
+    return out
+
+
+def ShapeEval(et, order, vnums, pts, device=0):
+    """Shape values and reference gradients evaluated on the GPU."""
+    ctx = context(device)
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    vn = np.ascontiguousarray(vnums, dtype=np.int32)
+    n = (order + 1) * (order + 2) * (order + 3) // 6 if et == 4 else (order + 1) ** 3
+    val = np.zeros((len(pts), n))
+    grd = np.zeros((len(pts), n, 3))
+    ctx.check(ctx.lib.gh1_shape_eval(ctx.h, et, order, _np_ptr(vn), len(pts), _np_ptr(pts), _np_ptr(val), _np_ptr(grd)))
+    return val, grd

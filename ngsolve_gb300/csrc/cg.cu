@@ -1,0 +1,587 @@
+// cg.cu -- Jacobi preconditioner, preconditioned CG (FP64 and FP32-inner with
+// FP64 iterative refinement) and the adjoint gradient driver.
+//
+// CG follows CGSolver._SolveImpl (python/krylovspace.py:263-291) step by step:
+//   d = b - A x; w = P d; s = w; wdn = w.d; check sqrt|wdn|
+//   loop: w = A s; wd = wdn; as_s = s.w; (as_s == 0 or wd == 0 -> stop)
+//         alpha = wd/as_s; x += alpha s; d -= alpha w; w = P d; wdn = w.d;
+//         check; beta = wdn/wd; s = w + beta s
+// with CheckResidual (:129-219): iterations counts checks, converged when
+// iterations >= maxiter or residual <= tol * first residual.
+// GPU layout of one iteration: [apply: y = A s, s.y as the sum of element
+// energies s_e^T A_e s_e] -> [update: alpha, x, d, w = P d, y = 0, w.d, |d|^2;
+// the last block forms beta and the convergence flag] -> [direction: s = w +
+// beta s].  All scalars stay on the device; a CUDA graph holds `chunk`
+// iterations and the host reads the flag once per graph launch (the role of
+// the reference's WHILE-conditional graph, ngscuda/cuda_krylov.cpp:19-203).
+// Every device loop is bounded by maxit; kernels after convergence return at
+// their first instruction.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+#include "common.cuh"
+
+namespace gh1 {
+
+struct CGState {
+  double wd, wdn, energy, alpha, beta, res0, stop, res, dd, bb;
+  int it, maxit, done, status, rule, pad;
+};
+
+// grid-wide reduction of K doubles per thread; returns true in the last block,
+// where tot[] holds the totals (all threads).  No block waits for another.
+template <int K>
+__device__ bool grid_reduce(double (&v)[K], double* partial, unsigned int* counter, double (&tot)[K]) {
+  __shared__ double red[K][32];
+  __shared__ bool last;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (l == 0) red[k][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < K; k++) {
+      double s = 0;
+      for (int i = 0; i < nw; i++) s += red[k][i];
+      partial[(size_t)k * gridDim.x + blockIdx.x] = s;
+    }
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double s = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double*)partial)[(size_t)k * gridDim.x + i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncthreads();
+    if (l == 0) red[k][w] = s;
+    __syncthreads();
+    double t = 0;
+    for (int i = 0; i < nw; i++) t += red[k][i];
+    tot[k] = t;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+constexpr int RED_BLOCK = 256;
+
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_init_kernel(int64_t n, const T* __restrict__ inv, T* __restrict__ d,
+                                                            T* __restrict__ w, T* __restrict__ s, CGState* st, double tol,
+                                                            double* hist, double* partial, unsigned int* counter) {
+  T a0 = 0, a1 = 0;  // thread-local sums in the working precision
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T di = d[i], iv = inv[i];
+    T wi = iv * di;
+    w[i] = wi;
+    s[i] = wi;
+    a0 += wi * di;
+    if (iv != (T)0) a1 += di * di;
+  }
+  double v[2] = {(double)a0, (double)a1}, tot[2];
+  if (grid_reduce<2>(v, partial, counter, tot) && threadIdx.x == 0) {
+    st->wdn = tot[0];
+    st->wd = tot[0];
+    st->dd = tot[1];
+    double r = st->rule == GH1_STOP_TRUE ? sqrt(tot[1]) : sqrt(fabs(tot[0]));
+    st->res0 = r;
+    st->res = r;
+    st->stop = st->rule == GH1_STOP_TRUE ? tol * sqrt(st->bb) : tol * r;
+    st->it = 1;
+    if (hist) hist[0] = r;
+    st->status = GH1_OK;
+    st->done = (r <= st->stop || st->maxit <= 1 || tot[0] == 0.0) ? 1 : 0;
+    if (st->done && !(r <= st->stop) && tot[0] != 0.0) st->status = GH1_MAXITER;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T* __restrict__ inv, T* __restrict__ x,
+                                                              T* __restrict__ d, T* __restrict__ w, const T* __restrict__ s,
+                                                              T* __restrict__ y, CGState* st, double* hist, double* partial,
+                                                              unsigned int* counter) {
+  if (*(volatile int*)&st->done) return;
+  const double wd = st->wd, en = st->energy;
+  if (!(en > 0.0) || wd == 0.0 || !isfinite(en)) {
+    // as_s == 0 or wd == 0 (krylovspace.py:276): stop; non-positive or NaN energy: breakdown
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->done = 1;
+      st->status = (en == 0.0 || wd == 0.0) ? GH1_OK : GH1_BREAKDOWN;
+    }
+    return;
+  }
+  const T alpha = (T)(wd / en);
+  T a0 = 0, a1 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T si = s[i], yi = y[i], iv = inv[i];
+    x[i] += alpha * si;
+    T di = d[i] - alpha * yi;
+    d[i] = di;
+    T wi = iv * di;
+    w[i] = wi;
+    y[i] = (T)0;
+    a0 += wi * di;
+    if (iv != (T)0) a1 += di * di;
+  }
+  double v[2] = {(double)a0, (double)a1}, tot[2];
+  if (grid_reduce<2>(v, partial, counter, tot) && threadIdx.x == 0) {
+    double wdn = tot[0];
+    double r = st->rule == GH1_STOP_TRUE ? sqrt(tot[1]) : sqrt(fabs(wdn));
+    st->alpha = wd / en;
+    st->dd = tot[1];
+    st->res = r;
+    if (hist) hist[st->it] = r;
+    st->it += 1;
+    st->beta = wdn / wd;
+    st->wdn = wdn;
+    st->wd = wdn;
+    if (!isfinite(r)) { st->done = 1; st->status = GH1_BREAKDOWN; }
+    else if (r <= st->stop) { st->done = 1; st->status = GH1_OK; }
+    else if (st->it >= st->maxit) { st->done = 1; st->status = GH1_MAXITER; }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_dir_kernel(int64_t n, const T* __restrict__ w, T* __restrict__ s,
+                                                           const CGState* st) {
+  if (*(volatile const int*)&st->done) return;
+  const T beta = (T)st->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s[i] = w[i] + beta * s[i];
+}
+
+// r = b - y (FP64), |r_free|^2 and |b_free|^2 ; free = mask
+__global__ void __launch_bounds__(RED_BLOCK) residual_kernel(int64_t n, const double* __restrict__ b, const double* __restrict__ y,
+                                                             const uint8_t* __restrict__ freedof, double* __restrict__ r,
+                                                             double* out2, double* partial, unsigned int* counter) {
+  double v[2] = {0, 0}, tot[2];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double ri = b[i] - y[i];
+    if (r) r[i] = ri;
+    if (freedof[i]) { v[0] += ri * ri; v[1] += b[i] * b[i]; }
+  }
+  if (grid_reduce<2>(v, partial, counter, tot) && threadIdx.x == 0) { out2[0] = tot[0]; out2[1] = tot[1]; }
+}
+
+template <class TA, class TB>
+__global__ void axpby_kernel(int64_t n, double a, const TA* __restrict__ x, double b, TB* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (TB)(a * (double)x[i] + (b == 0.0 ? 0.0 : b * (double)y[i]));
+}
+
+__global__ void scale_to_f32_kernel(int64_t n, const double* __restrict__ r, const double* __restrict__ norm2,
+                                    float* __restrict__ d32) {
+  const double sc = norm2[0] > 0 ? 1.0 / sqrt(norm2[0]) : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    d32[i] = (float)(r[i] * sc);
+}
+
+__global__ void correct_kernel(int64_t n, const float* __restrict__ c32, const double* __restrict__ norm2, double* __restrict__ x) {
+  const double sc = sqrt(norm2[0]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += sc * (double)c32[i];
+}
+
+__global__ void jacobi_invert_kernel(int64_t n, const double* diag, const uint8_t* freedof, double* inv64, float* inv32) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double v = (freedof[i] && diag[i] != 0.0) ? 1.0 / diag[i] : 0.0;
+    inv64[i] = v;
+    inv32[i] = (float)v;
+  }
+}
+
+template <class T>
+__global__ void jacobi_apply_kernel(int64_t n, double s, const T* __restrict__ inv, const T* __restrict__ x, T* __restrict__ y,
+                                    int acc) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T v = (T)s * inv[i] * x[i];
+    y[i] = acc ? y[i] + v : v;
+  }
+}
+
+void jacobi_invert(gh1_ctx* ctx, int64_t n, const double* diag, const uint8_t* freedof, double* inv64, float* inv32) {
+  jacobi_invert_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, diag, freedof, inv64, inv32);
+  check_kernel(ctx, "jacobi_invert_kernel");
+}
+
+void jacobi_apply(gh1_ctx* ctx, int64_t n, double s, const double* inv64, const float* inv32, const void* x, void* y, int prec,
+                  int acc) {
+  if (prec == GH1_F64)
+    jacobi_apply_kernel<double><<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, s, inv64, (const double*)x, (double*)y, acc);
+  else
+    jacobi_apply_kernel<float><<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, s, inv32, (const float*)x, (float*)y, acc);
+  check_kernel(ctx, "jacobi_apply_kernel");
+}
+
+void vec_axpby(gh1_ctx* ctx, int64_t n, double a, const void* x, double b, void* y, int prec) {
+  if (prec == GH1_F64)
+    axpby_kernel<double, double><<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, a, (const double*)x, b, (double*)y);
+  else
+    axpby_kernel<float, float><<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, a, (const float*)x, b, (float*)y);
+  check_kernel(ctx, "axpby_kernel");
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Scratch {
+  // reduction scratch: partial sums [2 * grid] per reduction site + counters
+  DBuf<double> partial;
+  DBuf<unsigned int> counters;
+  DBuf<CGState> state;
+  DBuf<double> hist;
+  DBuf<double> norm2;  // [2]
+};
+
+int red_grid(gh1_ctx* ctx, int64_t n) { return grid_for(ctx, n, RED_BLOCK, 4); }
+
+// operator apply with the device energy sink (y must be zero on entry)
+void op_apply_energy(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter, double* energy,
+                     const int* skip) {
+  if (op->kind == GH1_OP_MATFREE) {
+    matfree_apply_ex(op, x, y, prec, partial, counter, energy, skip);
+  } else {
+    throw Error(GH1_ERR_UNSUPPORTED, "internal: CSR energy path");
+  }
+}
+
+// s^T y for CSR operators (the apply has no element energies)
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) dot_energy_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
+                                                               double* out, double* partial, unsigned int* counter,
+                                                               const int* skip) {
+  if (*(volatile const int*)skip) return;
+  double v[1] = {0}, tot[1];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[0] += (double)a[i] * (double)b[i];
+  if (grid_reduce<1>(v, partial, counter, tot) && threadIdx.x == 0) *out = tot[0];
+}
+
+template <class T>
+__global__ void csr_spmv_skip_kernel(int64_t nrows, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                                     const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, const int* skip) {
+  if (*(volatile const int*)skip) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp; row < nrows; row += nw) {
+    T acc = 0;
+    for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) acc += vals[k] * __ldg(x + colind[k]);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[row] = acc;
+  }
+}
+
+// One PCG solve in precision T on vectors already on the device.
+// d holds the initial residual on entry; x the initial guess.
+template <class T>
+struct PCG {
+  gh1_op* op;
+  gh1_ctx* ctx;
+  int64_t n;
+  const T* inv;
+  T *x, *d, *w, *s, *y;
+  int prec;
+  CGState* st;
+  double* partial;       // [4 * grid_max]
+  unsigned int* counters;  // [4]
+  double* hist;
+  int chunk;
+  int applies = 0;
+
+  void launch_iteration(cudaStream_t cs) {
+    int g = red_grid(ctx, n);
+    if (op->kind == GH1_OP_MATFREE) {
+      op_apply_energy(op, s, y, prec, partial + 2 * ctx->nsm * 64, counters + 1, &st->energy, &st->done);
+    } else {
+      const T* vals = std::is_same<T, float>::value ? (const T*)op->d_vals32.p : (const T*)op->d_vals.p;
+      int gg = grid_for(ctx, n * 32, 256, 16);
+      csr_spmv_skip_kernel<T><<<gg, 256, 0, cs>>>(n, op->rowptr, op->colind, vals, s, y, &st->done);
+      check_kernel(ctx, "csr_spmv_skip_kernel");
+      dot_energy_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, s, y, &st->energy, partial + 2 * ctx->nsm * 64, counters + 1, &st->done);
+      check_kernel(ctx, "dot_energy_kernel");
+    }
+    cg_update_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, x, d, w, s, y, st, hist, partial, counters + 2);
+    check_kernel(ctx, "cg_update_kernel");
+    cg_dir_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, w, s, st);
+    check_kernel(ctx, "cg_dir_kernel");
+  }
+
+  // returns iterations (checks) and fills host state
+  CGState run(double tol, int maxit, int rule, double bb, cudaStream_t cs, cudaGraphExec_t* cache_exec, int* cache_chunk) {
+    CGState h{};
+    h.maxit = maxit;
+    h.rule = rule;
+    h.bb = bb;
+    GH1_CUDA(cudaMemcpyAsync(st, &h, sizeof(CGState), cudaMemcpyHostToDevice, cs));
+    GH1_CUDA(cudaMemsetAsync(y, 0, n * sizeof(T), cs));
+    int g = red_grid(ctx, n);
+    cg_init_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, d, w, s, st, tol, hist, partial, counters + 0);
+    check_kernel(ctx, "cg_init_kernel");
+    CGState* hs = (CGState*)ctx->h_pinned;
+    // graph of `chunk` iterations, built once per solve shape
+    cudaGraphExec_t exec = *cache_exec;
+    if (!exec || *cache_chunk != chunk) {
+      if (exec) cudaGraphExecDestroy(exec);
+      cudaGraph_t graph;
+      GH1_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < chunk; k++) launch_iteration(cs);
+      GH1_CUDA(cudaStreamEndCapture(cs, &graph));
+      GH1_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+      cudaGraphDestroy(graph);
+      *cache_exec = exec;
+      *cache_chunk = chunk;
+    }
+    int launches = 0;
+    const int max_launches = (maxit + chunk - 1) / chunk + 2;
+    while (true) {
+      GH1_CUDA(cudaMemcpyAsync(hs, st, sizeof(CGState), cudaMemcpyDeviceToHost, cs));
+      GH1_CUDA(cudaStreamSynchronize(cs));
+      if (hs->done || launches >= max_launches) break;
+      GH1_CUDA(cudaGraphLaunch(exec, cs));
+      launches++;
+    }
+    CGState out = *hs;
+    applies = out.it - 1;
+    return out;
+  }
+};
+
+struct Work {
+  DBuf<double> d64, w64, s64, y64, r64;
+  DBuf<float> x32, d32, w32, s32, y32;
+};
+
+}  // namespace
+
+// per-operator cached graphs would outlive changes of pointers; graphs are
+// rebuilt per solve (capture + instantiate cost a few hundred microseconds).
+int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* o, gh1_cg_result* r) {
+  gh1_ctx* ctx = op->ctx;
+  const int64_t n = op->nrows;
+  cudaStream_t user = ctx->stream;
+  cudaStream_t cs;
+  GH1_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaEvent_t ev;
+  GH1_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  GH1_CUDA(cudaEventRecord(ev, user));
+  GH1_CUDA(cudaStreamWaitEvent(cs, ev, 0));
+  ctx->stream = cs;  // kernels launched by the operator go to the solver stream
+  int status = GH1_OK;
+  std::vector<cudaGraphExec_t> execs;
+  try {
+    std::memset(r, 0, sizeof(*r));
+    const int grid_max = ctx->nsm * 64;
+    DBuf<double> partial((size_t)4 * grid_max + 8);
+    DBuf<unsigned int> counters(8);
+    counters.zero(cs);
+    DBuf<CGState> st(1);
+    DBuf<double> hist((size_t)o->maxit + 2);
+    DBuf<double> norm2(2);
+    DBuf<uint8_t> ones;
+    const uint8_t* freemask = pre ? pre->d_free.p : nullptr;
+    if (!freemask) {
+      ones.alloc(n);
+      GH1_CUDA(cudaMemsetAsync(ones.p, 1, n, cs));
+      freemask = ones.p;
+    }
+    DBuf<double> inv_ident;
+    const double* inv64 = pre ? pre->d_inv64.p : nullptr;
+    if (!inv64) {
+      std::vector<double> one(n, 1.0);
+      inv_ident.upload(one, cs);
+      inv64 = inv_ident.p;
+    }
+    int chunk = o->check_every > 0 ? o->check_every : 16;
+    auto bnorm2 = [&](const double* y, double* rr) {  // |b - y|^2, |b|^2 on free DOFs
+      int g = red_grid(ctx, n);
+      residual_kernel<<<g, RED_BLOCK, 0, cs>>>(n, b, y, freemask, rr, norm2.p, partial.p, counters.p + 3);
+      check_kernel(ctx, "residual_kernel");
+      double h[2];
+      GH1_CUDA(cudaMemcpyAsync(h, norm2.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, cs));
+      GH1_CUDA(cudaStreamSynchronize(cs));
+      return std::pair<double, double>(h[0], h[1]);
+    };
+    Work W;
+    W.d64.alloc(n); W.w64.alloc(n); W.s64.alloc(n); W.y64.alloc(n);
+    auto apply64 = [&](const double* in, double* out) {
+      GH1_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), cs));
+      if (op->kind == GH1_OP_MATFREE) matfree_apply_ex(op, in, out, GH1_F64, nullptr, nullptr, nullptr, nullptr);
+      else spmv(op, in, out, GH1_F64);
+      r->applies64++;
+    };
+    if (o->initialize) GH1_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), cs));
+    // d = b - A x  (|b_free| as the reference scale of the true-residual rule)
+    std::pair<double, double> rb;
+    if (o->initialize) {
+      GH1_CUDA(cudaMemcpyAsync(W.d64.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, cs));
+      GH1_CUDA(cudaMemsetAsync(W.y64.p, 0, n * sizeof(double), cs));
+      rb = bnorm2(W.y64.p, nullptr);
+    } else {
+      apply64(x, W.y64.p);
+      rb = bnorm2(W.y64.p, W.d64.p);
+    }
+    const double bb = rb.second;
+    cudaGraphExec_t exec64 = nullptr, exec32 = nullptr;
+    int ch64 = 0, ch32 = 0;
+    if (o->mode == GH1_CG_FP64) {
+      PCG<double> P{op, ctx, n, inv64, x, W.d64.p, W.w64.p, W.s64.p, W.y64.p, GH1_F64, st.p, partial.p, counters.p, hist.p, chunk};
+      GH1_CUDA(cudaMemsetAsync(W.y64.p, 0, n * sizeof(double), cs));
+      CGState res = P.run(o->tol, o->maxit, o->stop_rule, bb, cs, &exec64, &ch64);
+      execs.push_back(exec64);
+      r->iterations = res.it;
+      r->applies64 += P.applies;
+      r->first_res = res.res0;
+      r->final_res = res.res;
+      status = res.status;
+      if (o->res_hist && res.it > 0)
+        GH1_CUDA(cudaMemcpyAsync(o->res_hist, hist.p, sizeof(double) * std::min(res.it, o->maxit + 1), cudaMemcpyDeviceToHost, cs));
+    } else {
+      // FP32 inner PCG inside FP64 iterative refinement
+      W.x32.alloc(n); W.d32.alloc(n); W.w32.alloc(n); W.s32.alloc(n); W.y32.alloc(n); W.r64.alloc(n);
+      GH1_CHECK(op->kind == GH1_OP_CSR || (op->prec_mask & 2), GH1_ERR_UNSUPPORTED,
+                "mixed precision needs an operator set up with FP32 data (precision mask bit 1)");
+      if (op->kind == GH1_OP_CSR && op->d_vals32.n != (size_t)op->nnz) {
+        op->d_vals32.alloc(op->nnz);
+        axpby_kernel<double, float><<<grid_for(ctx, op->nnz, 256), 256, 0, cs>>>(op->nnz, 1.0, op->d_vals.p, 0.0, op->d_vals32.p);
+        check_kernel(ctx, "axpby_kernel(vals32)");
+      }
+      const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+      const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
+      const double target = o->tol * std::sqrt(bb);
+      double rr = o->initialize ? bb : rb.first;
+      std::vector<double> hh;
+      int total_inner = 0;
+      status = GH1_MAXITER;
+      r->first_res = std::sqrt(rr);
+      for (int outer = 0; outer <= max_outer; outer++) {
+        if (outer > 0) {
+          apply64(x, W.y64.p);
+          auto q = bnorm2(W.y64.p, W.r64.p);
+          rr = q.first;
+        } else if (o->initialize) {
+          GH1_CUDA(cudaMemcpyAsync(W.r64.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, cs));
+          double h2[2] = {rr, bb};
+          GH1_CUDA(cudaMemcpyAsync(norm2.p, h2, sizeof(h2), cudaMemcpyHostToDevice, cs));
+        } else {
+          GH1_CUDA(cudaMemcpyAsync(W.r64.p, W.d64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, cs));
+          double h2[2] = {rr, bb};
+          GH1_CUDA(cudaMemcpyAsync(norm2.p, h2, sizeof(h2), cudaMemcpyHostToDevice, cs));
+        }
+        hh.push_back(std::sqrt(rr));
+        r->final_res = std::sqrt(rr);
+        r->outer = outer;
+        if (std::sqrt(rr) <= target) { status = GH1_OK; break; }
+        if (outer == max_outer || total_inner >= o->maxit) break;
+        // inner: A c = r / |r|  in FP32, c0 = 0
+        scale_to_f32_kernel<<<grid_for(ctx, n, 256), 256, 0, cs>>>(n, W.r64.p, norm2.p, W.d32.p);
+        check_kernel(ctx, "scale_to_f32_kernel");
+        GH1_CUDA(cudaMemsetAsync(W.x32.p, 0, n * sizeof(float), cs));
+        PCG<float> P{op, ctx, n, pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32, st.p, partial.p,
+                     counters.p, nullptr, chunk};
+        CGState res = P.run(inner_tol, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
+        total_inner += res.it;
+        r->applies32 += P.applies;
+        if (res.status == GH1_BREAKDOWN) { status = GH1_BREAKDOWN; break; }
+        correct_kernel<<<grid_for(ctx, n, 256), 256, 0, cs>>>(n, W.x32.p, norm2.p, x);
+        check_kernel(ctx, "correct_kernel");
+      }
+      execs.push_back(exec32);
+      r->iterations = total_inner;
+      if (o->res_hist) for (size_t k = 0; k < hh.size() && (int)k <= o->maxit; k++) o->res_hist[k] = hh[k];
+    }
+    // true relative residual at exit
+    apply64(x, W.y64.p);
+    auto q = bnorm2(W.y64.p, nullptr);
+    r->true_relres = bb > 0 ? std::sqrt(q.first / bb) : std::sqrt(q.first);
+    r->status = status;
+    GH1_CUDA(cudaStreamSynchronize(cs));
+  } catch (...) {
+    for (auto e : execs) if (e) cudaGraphExecDestroy(e);
+    cudaStreamSynchronize(cs);
+    ctx->stream = user;
+    cudaEventDestroy(ev);
+    cudaStreamDestroy(cs);
+    throw;
+  }
+  for (auto e : execs) if (e) cudaGraphExecDestroy(e);
+  ctx->stream = user;
+  GH1_CUDA(cudaEventRecord(ev, cs));
+  GH1_CUDA(cudaStreamWaitEvent(user, ev, 0));
+  cudaEventDestroy(ev);
+  cudaStreamDestroy(cs);
+  return status;
+}
+
+}  // namespace gh1
+
+// ---------------------------------------------------------------------------
+// adjoint gradient
+extern "C" int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u_target, double tol, double* u, double* lam,
+                                double* dJdkappa, double* J) {
+  if (!form || !f || !u_target || !u || !lam || !dJdkappa || !J) return GH1_ERR_ARG;
+  gh1_ctx* ctx = form->sp->ctx;
+  try {
+    using namespace gh1;
+    gh1_space* sp = form->sp;
+    const int64_t n = sp->ndof;
+    cudaStream_t s = ctx->stream;
+    gh1_op* A = nullptr;
+    gh1_pre* P = nullptr;
+    int rc = gh1_matfree_create(form, 1, &A);
+    if (rc) return rc;
+    rc = gh1_jacobi_create(A, nullptr, 0, &P);
+    if (rc) { gh1_op_free(A); return rc; }
+    gh1_cg_opts o{};
+    o.tol = tol; o.maxit = 100000; o.mode = GH1_CG_FP64; o.stop_rule = GH1_STOP_TRUE; o.initialize = 1;
+    gh1_cg_result res{};
+    rc = gh1_cg(A, P, f, u, &o, &res);
+    if (rc != GH1_OK) { gh1_pre_free(P); gh1_op_free(A); return rc; }
+    // mass operator (unit coefficient) for J and the adjoint right-hand side
+    gh1_form mf;
+    mf.sp = sp;
+    std::vector<double> zeros(sp->mesh->ne, 0.0), ones(sp->mesh->ne, 1.0);
+    mf.d_kappa.upload(zeros, s);
+    mf.d_mu.upload(ones, s);
+    mf.has_mu = true;
+    gh1_op M;
+    M.ctx = ctx; M.kind = GH1_OP_MATFREE; M.form = &mf; M.sp = sp; M.nrows = n; M.prec_mask = 1;
+    matfree_setup(&M);
+    DBuf<double> e(n), Me(n), tmp(1);
+    axpby_kernel<double, double><<<grid_for(ctx, n, 256), 256, 0, s>>>(n, 1.0, u, 0.0, e.p);
+    axpby_kernel<double, double><<<grid_for(ctx, n, 256), 256, 0, s>>>(n, -1.0, u_target, 1.0, e.p);
+    GH1_CUDA(cudaMemsetAsync(Me.p, 0, n * sizeof(double), s));
+    DBuf<double> partial((size_t)ctx->nsm * 64 + 8);
+    DBuf<unsigned int> cnt(1);
+    cnt.zero(s);
+    DBuf<double> en(1);
+    matfree_apply_ex(&M, e.p, Me.p, GH1_F64, partial.p, cnt.p, en.p, nullptr);
+    double hJ = 0;
+    GH1_CUDA(cudaMemcpyAsync(&hJ, en.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GH1_CUDA(cudaStreamSynchronize(s));
+    *J = 0.5 * hJ;
+    rc = gh1_cg(A, P, Me.p, lam, &o, &res);
+    if (rc != GH1_OK) { gh1_pre_free(P); gh1_op_free(A); return rc; }
+    elem_grad_dot_with(A, u, lam, dJdkappa);
+    axpby_kernel<double, double><<<grid_for(ctx, sp->mesh->ne, 256), 256, 0, s>>>(sp->mesh->ne, -1.0, dJdkappa, 0.0, dJdkappa);
+    GH1_CUDA(cudaStreamSynchronize(s));
+    gh1_pre_free(P);
+    gh1_op_free(A);
+    return GH1_OK;
+  } catch (const gh1::Error& e) {
+    ctx->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->err = e.what();
+    return GH1_ERR_ARG;
+  }
+}

@@ -1,0 +1,194 @@
+// common.cuh -- internal structures and helpers of libgh1 (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <stdexcept>
+#include <cstdio>
+#include "../../include/gh1.h"
+
+namespace gh1 {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define GH1_CUDA(call)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      throw ::gh1::Error(e_ == cudaErrorMemoryAllocation ? GH1_ERR_NOMEM : GH1_ERR_CUDA, \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+#define GH1_CHECK(cond, code, msg) \
+  do { if (!(cond)) throw ::gh1::Error(code, msg); } while (0)
+#define GH1_LAUNCH_CHECK() GH1_CUDA(cudaGetLastError())
+
+constexpr int MAX_HEX_ORDER = 8;   // n = p+1 <= 9 per direction
+constexpr int MAX_TET_ORDER = 6;
+constexpr int N_TET_CLASSES = 24;  // permutations of 4 vertex ranks
+constexpr int TET_NQ_MAX = 24;     // symmetric rules of degree <= 6 (order p <= 4)
+
+// device buffer with RAII
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count) GH1_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr; n = 0;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    if (n != count) alloc(count);
+    if (count) GH1_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+  void zero(cudaStream_t s) { if (n) GH1_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s)); }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+}  // namespace gh1
+
+struct gh1_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int nsm = 0;
+  int cc_major = 0, cc_minor = 0;
+  // scratch for reductions
+  gh1::DBuf<double> red;        // partial sums
+  gh1::DBuf<unsigned int> cnt;  // completion counters
+  double* h_pinned = nullptr;   // small pinned host staging
+};
+
+struct gh1_mesh {
+  gh1_ctx* ctx = nullptr;
+  int nv = 0, ne = 0, et = 0;
+  std::vector<double> X;
+  std::vector<int32_t> el;
+  gh1::DBuf<double> d_X;
+  gh1::DBuf<int32_t> d_el;
+};
+
+struct gh1_space {
+  gh1_ctx* ctx = nullptr;
+  gh1_mesh* mesh = nullptr;
+  int et = 8, p = 1, nloc = 0, n1 = 2;  // n1 = p+1 (hex DOFs per direction)
+  int nvert = 8, nedge = 12, nface = 6;
+  int64_t ndof = 0, nfree = 0;
+  int ned = 0, nfa = 0;
+  int n_edge_dofs = 0, n_face_dofs = 0, n_cell_dofs = 0;
+  int64_t first_edge = 0, first_face = 0, first_cell = 0;
+  std::vector<int32_t> el_dofs;   // ne*nloc, reference local order
+  std::vector<uint8_t> freedof;   // ndof
+  gh1::DBuf<int32_t> d_eldofs;    // ne*nloc (reference local order)
+  gh1::DBuf<uint8_t> d_free;      // ndof
+  // hex: tensor-ordered signed DOF table  tdof[e][a][b][c] = dof | (sign<0 ? 1<<31 : 0)
+  gh1::DBuf<int32_t> d_tdof;
+  // hex: integration rule (Gauss, q = p+1 points) and 1D tables B[q][n], D[q][n]
+  int nq1 = 0;                    // points per direction
+  std::vector<double> gx, gw;     // Gauss points / weights on [0,1]
+  gh1::DBuf<double> d_gx, d_gw;
+  gh1::DBuf<double> d_B64, d_D64;
+  gh1::DBuf<float> d_B32, d_D32;
+  // tet: orientation class per element, rule, per-class tables
+  gh1::DBuf<uint8_t> d_class;     // ne
+  int tet_nq = 0, tet_nq_mass = 0;
+  gh1::DBuf<double> d_tq, d_tqm;  // rules: (x,y,z,w) * nq
+  gh1::DBuf<double> d_tab64;      // [class][q][i][4]  (value, dx, dy, dz) at stiffness rule
+  gh1::DBuf<float> d_tab32;
+  gh1::DBuf<double> d_tabm64;     // [class][q][i] values at mass/rhs rule
+  gh1::DBuf<double> d_S;          // [class][7][nloc][nloc] reference stiffness/mass blocks
+  // CSR pattern (built lazily)
+  bool have_graph = false;
+  int64_t nnz = 0;
+  gh1::DBuf<int64_t> d_rowptr;
+  gh1::DBuf<int32_t> d_colind;
+};
+
+struct gh1_form {
+  gh1_space* sp = nullptr;
+  gh1::DBuf<double> d_kappa;  // ne
+  gh1::DBuf<double> d_mu;     // ne (empty: mu = 0)
+  bool has_mu = false;
+  int version = 0;            // bumped on coefficient change
+};
+
+struct gh1_op {
+  gh1_ctx* ctx = nullptr;
+  int kind = GH1_OP_CSR;
+  gh1_form* form = nullptr;   // NULL for imported CSR
+  gh1_space* sp = nullptr;
+  int64_t nrows = 0;
+  // CSR data
+  int64_t nnz = 0;
+  gh1::DBuf<int64_t> d_rowptr_own;
+  gh1::DBuf<int32_t> d_colind_own;
+  const int64_t* rowptr = nullptr;
+  const int32_t* colind = nullptr;
+  gh1::DBuf<double> d_vals;
+  gh1::DBuf<float> d_vals32;
+  // matrix-free data
+  int prec_mask = 1;
+  int form_version = -1;
+  gh1::DBuf<double> d_G64;    // hex: [e][6][q] ; tet: [e][6] (geometry incl. kappa, w at qp for hex)
+  gh1::DBuf<float> d_G32;
+  gh1::DBuf<double> d_M64;    // mass coefficient: hex [e][q], tet [e]
+  gh1::DBuf<float> d_M32;
+  bool has_mass = false;
+  gh1::DBuf<double> d_diag;   // operator diagonal (FP64)
+  bool have_diag = false;
+  // scratch vectors for accumulate / scaling
+  gh1::DBuf<double> d_tmp64;
+  gh1::DBuf<float> d_tmp32;
+};
+
+struct gh1_pre {
+  gh1_op* op = nullptr;
+  int64_t n = 0;
+  gh1::DBuf<double> d_inv64;
+  gh1::DBuf<float> d_inv32;
+  gh1::DBuf<uint8_t> d_free;
+};
+
+namespace gh1 {
+// host helpers implemented in api.cu
+int grid_for(gh1_ctx* ctx, int64_t work, int block, int per_sm = 8);
+void check_kernel(gh1_ctx* ctx, const char* what);
+
+// kernels / drivers (implemented in the .cu files)
+void build_tables(gh1_space* sp);                                   // tables.cu
+void build_graph(gh1_space* sp);                                    // assemble.cu
+void assemble_csr(gh1_form* f, double* vals);                       // assemble.cu
+void rhs_elementwise(gh1_space* sp, const double* f, double* b);    // assemble.cu
+void matfree_setup(gh1_op* op);                                     // matfree.cu
+void matfree_apply(gh1_op* op, const void* x, void* y, int prec, double* energy_partials, unsigned int* counter,
+                   double* energy_out);                              // matfree.cu
+void matfree_diag(gh1_op* op, double* diag);                        // matfree.cu
+void elem_grad_dot(gh1_space* sp, const double* u, const double* w, double* out);  // matfree.cu
+void elem_grad_dot_with(gh1_op* op, const double* u, const double* w, double* out);  // matfree.cu
+void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter,
+                      double* energy, const int* skip);  // matfree.cu
+void mass_apply(gh1_op* op, const double* x, double* y);            // matfree.cu
+void spmv(gh1_op* op, const void* x, void* y, int prec);            // spmv.cu
+void csr_diag(gh1_op* op, double* diag);                            // spmv.cu
+int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* o, gh1_cg_result* r);  // cg.cu
+void vec_axpby(gh1_ctx* ctx, int64_t n, double a, const void* x, double b, void* y, int prec);  // cg.cu
+void jacobi_invert(gh1_ctx* ctx, int64_t n, const double* diag, const uint8_t* freedof, double* inv64, float* inv32);  // cg.cu
+void jacobi_apply(gh1_ctx* ctx, int64_t n, double s, const double* inv64, const float* inv32, const void* x, void* y,
+                  int prec, int accumulate);  // cg.cu
+void shape_eval_gpu(gh1_ctx* ctx, int et, int p, const int32_t* vnums, int npts, const double* pts, double* val,
+                    double* grad);  // tables.cu
+}  // namespace gh1

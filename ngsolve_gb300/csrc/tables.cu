@@ -1,0 +1,230 @@
+// tables.cu -- integration rules and GPU evaluation of shapes / reference
+// gradients at the integration points.
+//
+// Replaces the per-element shape recomputation of T_CalcElementMatrixAdd /
+// ApplyElementMatrix (fem/symbolicintegrator.cpp:1548-1830, :2959-3040, via
+// CalcMappedDShape fem/tscalarfe_impl.hpp:759-890) by tables computed once:
+//  - hex: the 1D factor tables B[q][a] = psi_a(x_q), D[q][a] = psi_a'(x_q)
+//    at the Gauss points of SelectIntegrationRule(ET_HEX, 2p)
+//    (fem/intrule.cpp:3118-3132, :3234-3263): q = p+1 points per direction;
+//  - tet: shape values and reference gradients per orientation class (the
+//    24 rank permutations of the element's vertex numbers; the shapes depend
+//    on vertex numbers only through comparisons, fem/elementtopology.hpp:
+//    1208-1236) at the rule of order 2p-2 (bilinear, :1433-1455) and of
+//    order 2p (mass / linear form, :1109), plus the six reference stiffness
+//    blocks S_ab = sum_q w_q d_a phi_i d_b phi_j and the reference mass block.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+#include "common.cuh"
+#include "basis.cuh"
+#include "tet_rules.inc"
+
+namespace gh1 {
+
+// Gauss-Legendre on (0,1), Newton on P_n (ComputeGaussRule, fem/intrule.cpp:700-740)
+void gauss01(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0);
+  w.assign(n, 0);
+  int m = (n + 1) / 2;
+  for (int i = 1; i <= m; i++) {
+    double z = std::cos(M_PI * (i - 0.25) / (n + 0.5)), z1, pp = 1, p1, p2, p3;
+    for (int it = 0; it < 100; it++) {
+      p1 = 1; p2 = 0;
+      for (int j = 1; j <= n; j++) { p3 = p2; p2 = p1; p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j; }
+      pp = n * (z * p1 - p2) / (z * z - 1);
+      z1 = z;
+      z = z1 - p1 / pp;
+      if (std::fabs(z - z1) < 1e-15) break;
+    }
+    p1 = 1; p2 = 0;
+    for (int j = 1; j <= n; j++) { p3 = p2; p2 = p1; p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j; }
+    pp = n * (z * p1 - p2) / (z * z - 1);
+    x[i - 1] = 0.5 * (1 - z);
+    x[n - i] = 0.5 * (1 + z);
+    w[i - 1] = w[n - i] = 1.0 / ((1 - z * z) * pp * pp);
+  }
+}
+
+// tet rule of a given order: tabulated symmetric rules up to degree 6 (the point
+// counts of fem/intrule.cpp:2596-2812), collapsed tensor Gauss rule above.
+void tet_rule(int order, std::vector<double>& r /* x,y,z,w per point */) {
+  r.clear();
+  auto add = [&](const double (*t)[4], int n) { for (int i = 0; i < n; i++) for (int k = 0; k < 4; k++) r.push_back(t[i][k]); };
+  if (order <= 1) add(TET_RULE_D1, 1);
+  else if (order == 2) add(TET_RULE_D2, 4);
+  else if (order <= 5) add(TET_RULE_D5, 14);
+  else if (order == 6) add(TET_RULE_D6, 24);
+  else {
+    int n = order / 2 + 2;
+    std::vector<double> g, gw;
+    gauss01(n, g, gw);
+    for (int k = 0; k < n; k++)
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          double xx = g[i], yy = g[j], zz = g[k];
+          r.push_back(xx);
+          r.push_back(yy * (1 - xx));
+          r.push_back(zz * (1 - xx) * (1 - yy));
+          r.push_back(gw[i] * gw[j] * gw[k] * (1 - xx) * (1 - xx) * (1 - yy));
+        }
+  }
+}
+
+__device__ void class_ranks(int c, int* vn) {
+  // inverse of the lexicographic permutation index used on the host
+  int avail[4] = {0, 1, 2, 3}, navail = 4;
+  const int fact[4] = {6, 2, 1, 1};
+  for (int i = 0; i < 4; i++) {
+    int k = c / fact[i];
+    c %= fact[i];
+    vn[i] = avail[k];
+    for (int j = k; j < navail - 1; j++) avail[j] = avail[j + 1];
+    navail--;
+  }
+}
+
+__global__ void hex_1d_tables(int p, int nq, const double* gx, double* B64, double* D64, float* B32, float* D32) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const int n = p + 1;
+  Dual3 psi[MAX_HEX_ORDER + 1];
+  hex_psi<Dual3>(p, Dual3(gx[q], 1.0, 0.0, 0.0), psi);
+  for (int a = 0; a < n; a++) {
+    B64[q * n + a] = psi[a].v;
+    D64[q * n + a] = psi[a].dx;
+    B32[q * n + a] = (float)psi[a].v;
+    D32[q * n + a] = (float)psi[a].dx;
+  }
+}
+
+// one thread per (class, point): values + reference gradients
+__global__ void tet_class_tables(int p, int nloc, int nq, const double* rule, double* tab64, float* tab32,
+                                 int values_only, Dual3* scratch) {
+  int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= N_TET_CLASSES * nq) return;
+  int c = id / nq, q = id % nq;
+  int vn[4];
+  class_ranks(c, vn);
+  Dual3* sh = scratch + (size_t)id * nloc;  // global scratch keeps local memory small
+  tet_shapes<Dual3>(p, vn, Dual3(rule[4 * q], 1, 0, 0), Dual3(rule[4 * q + 1], 0, 1, 0), Dual3(rule[4 * q + 2], 0, 0, 1), sh);
+  for (int i = 0; i < nloc; i++) {
+    size_t o = ((size_t)c * nq + q) * nloc + i;
+    if (values_only) {
+      tab64[o] = sh[i].v;
+    } else {
+      tab64[4 * o + 0] = sh[i].v;
+      tab64[4 * o + 1] = sh[i].dx;
+      tab64[4 * o + 2] = sh[i].dy;
+      tab64[4 * o + 3] = sh[i].dz;
+      if (tab32) {
+        tab32[4 * o + 0] = (float)sh[i].v;
+        tab32[4 * o + 1] = (float)sh[i].dx;
+        tab32[4 * o + 2] = (float)sh[i].dy;
+        tab32[4 * o + 3] = (float)sh[i].dz;
+      }
+    }
+  }
+}
+
+// S[c][blk][i][j]: blk 0..2 = S_aa, 3 = S_01+S_10, 4 = S_02+S_20, 5 = S_12+S_21, 6 = mass
+__global__ void tet_ref_blocks(int nloc, int nq, const double* rule, const double* tab, int nqm, const double* rulem,
+                               const double* tabm, double* S) {
+  int c = blockIdx.y, blk = blockIdx.z;
+  for (int ij = blockIdx.x * blockDim.x + threadIdx.x; ij < nloc * nloc; ij += gridDim.x * blockDim.x) {
+    int i = ij / nloc, j = ij % nloc;
+    double s = 0;
+    if (blk < 6) {
+      const int A[6] = {0, 1, 2, 0, 0, 1}, Bc[6] = {0, 1, 2, 1, 2, 2};
+      int a = A[blk] + 1, b = Bc[blk] + 1;
+      for (int q = 0; q < nq; q++) {
+        const double* ti = tab + 4 * (((size_t)c * nq + q) * nloc + i);
+        const double* tj = tab + 4 * (((size_t)c * nq + q) * nloc + j);
+        double v = ti[a] * tj[b];
+        if (blk >= 3) v += ti[b] * tj[a];
+        s += rule[4 * q + 3] * v;
+      }
+    } else {
+      for (int q = 0; q < nqm; q++)
+        s += rulem[4 * q + 3] * tabm[((size_t)c * nqm + q) * nloc + i] * tabm[((size_t)c * nqm + q) * nloc + j];
+    }
+    S[(((size_t)c * 7 + blk) * nloc + i) * nloc + j] = s;
+  }
+}
+
+void build_tables(gh1_space* sp) {
+  cudaStream_t s = sp->ctx->stream;
+  const int p = sp->p;
+  if (sp->et == 8) {
+    sp->nq1 = (2 * p) / 2 + 1;
+    gauss01(sp->nq1, sp->gx, sp->gw);
+    sp->d_gx.upload(sp->gx, s);
+    sp->d_gw.upload(sp->gw, s);
+    const int n = p + 1, nq = sp->nq1;
+    sp->d_B64.alloc(nq * n); sp->d_D64.alloc(nq * n);
+    sp->d_B32.alloc(nq * n); sp->d_D32.alloc(nq * n);
+    hex_1d_tables<<<1, 32, 0, s>>>(p, nq, sp->d_gx.p, sp->d_B64.p, sp->d_D64.p, sp->d_B32.p, sp->d_D32.p);
+    check_kernel(sp->ctx, "hex_1d_tables");
+  } else {
+    std::vector<double> r, rm;
+    tet_rule(2 * p - 2 > 0 ? 2 * p - 2 : 0, r);
+    tet_rule(2 * p, rm);
+    sp->tet_nq = (int)r.size() / 4;
+    sp->tet_nq_mass = (int)rm.size() / 4;
+    sp->d_tq.upload(r, s);
+    sp->d_tqm.upload(rm, s);
+    const int nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
+    sp->d_tab64.alloc((size_t)N_TET_CLASSES * nq * nloc * 4);
+    sp->d_tab32.alloc((size_t)N_TET_CLASSES * nq * nloc * 4);
+    sp->d_tabm64.alloc((size_t)N_TET_CLASSES * nqm * nloc);
+    int tot = N_TET_CLASSES * nq;
+    int totm = N_TET_CLASSES * nqm;
+    DBuf<Dual3> scratch((size_t)std::max(tot, totm) * nloc);
+    tet_class_tables<<<(tot + 63) / 64, 64, 0, s>>>(p, nloc, nq, sp->d_tq.p, sp->d_tab64.p, sp->d_tab32.p, 0, scratch.p);
+    check_kernel(sp->ctx, "tet_class_tables");
+    tet_class_tables<<<(totm + 63) / 64, 64, 0, s>>>(p, nloc, nqm, sp->d_tqm.p, sp->d_tabm64.p, nullptr, 1, scratch.p);
+    check_kernel(sp->ctx, "tet_class_tables(mass)");
+    sp->d_S.alloc((size_t)N_TET_CLASSES * 7 * nloc * nloc);
+    dim3 g((nloc * nloc + 127) / 128, N_TET_CLASSES, 7);
+    tet_ref_blocks<<<g, 128, 0, s>>>(nloc, nq, sp->d_tq.p, sp->d_tab64.p, nqm, sp->d_tqm.p, sp->d_tabm64.p, sp->d_S.p);
+    check_kernel(sp->ctx, "tet_ref_blocks");
+    GH1_CUDA(cudaStreamSynchronize(s));  // scratch is released on return
+  }
+}
+
+// ---- shape evaluation at arbitrary points (gh1_shape_eval) -------------------
+__global__ void shape_eval_kernel(int et, int p, int nloc, int v0, int v1, int v2, int v3, int v4, int v5, int v6, int v7,
+                                  int npts, const double* pts, double* val, double* grad, Dual3* scratch) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= npts) return;
+  int vn[8] = {v0, v1, v2, v3, v4, v5, v6, v7};
+  Dual3* sh = scratch + (size_t)q * nloc;
+  Dual3 X(pts[3 * q], 1, 0, 0), Y(pts[3 * q + 1], 0, 1, 0), Z(pts[3 * q + 2], 0, 0, 1);
+  if (et == 4) tet_shapes<Dual3>(p, vn, X, Y, Z, sh);
+  else hex_shapes<Dual3>(p, vn, X, Y, Z, sh);
+  for (int i = 0; i < nloc; i++) {
+    val[(size_t)q * nloc + i] = sh[i].v;
+    grad[((size_t)q * nloc + i) * 3 + 0] = sh[i].dx;
+    grad[((size_t)q * nloc + i) * 3 + 1] = sh[i].dy;
+    grad[((size_t)q * nloc + i) * 3 + 2] = sh[i].dz;
+  }
+}
+
+void shape_eval_gpu(gh1_ctx* ctx, int et, int p, const int32_t* vnums, int npts, const double* pts, double* val,
+                    double* grad) {
+  int nloc = et == 4 ? (p + 1) * (p + 2) * (p + 3) / 6 : (p + 1) * (p + 1) * (p + 1);
+  int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < et; i++) v[i] = vnums[i];
+  cudaStream_t s = ctx->stream;
+  DBuf<double> dp(3 * (size_t)npts), dv((size_t)npts * nloc), dg((size_t)npts * nloc * 3);
+  DBuf<Dual3> scratch((size_t)npts * nloc);
+  dp.upload(pts, 3 * (size_t)npts, s);
+  shape_eval_kernel<<<(npts + 31) / 32, 32, 0, s>>>(et, p, nloc, v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], npts,
+                                                     dp.p, dv.p, dg.p, scratch.p);
+  check_kernel(ctx, "shape_eval_kernel");
+  GH1_CUDA(cudaMemcpyAsync(val, dv.p, dv.bytes(), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaMemcpyAsync(grad, dg.p, dg.bytes(), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace gh1

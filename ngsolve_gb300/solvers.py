@@ -1,0 +1,97 @@
+"""solvers.CG / CGSolver on the GPU (python/krylovspace.py:222-337 of NGSolve).
+
+The whole iteration runs on the device (libgh1 gh1_cg): the same algorithm and
+stopping rule as CGSolver._SolveImpl, with `mode="mixed"` adding FP32 inner
+solves inside FP64 iterative refinement.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .comp import BaseVector, _as_vec, _ptr
+
+
+class CGSolver:
+    """CGSolver(mat, pre, tol, maxiter, ...) -- .Solve(rhs, sol), .iterations,
+    .residuals (residual history of the stop rule)."""
+    name = "CG"
+
+    def __init__(self, mat, pre=None, freedofs=None, tol=None, maxiter=100, atol=None, callback=None,
+                 printrates=False, mode="fp64", stop_rule="precond", inner_tol=0.0, max_outer=0,
+                 check_every=0, conjugate=False, maxsteps=None, **kwargs):
+        if atol is not None:
+            raise NotImplementedError("atol: the GPU solver supports the relative tolerance only")
+        if pre is None and freedofs is not None:
+            pre = mat.CreateSmoother(freedofs)
+        if maxsteps is not None:
+            maxiter = maxsteps
+        self.mat, self.pre = mat, pre
+        self.tol = 1e-12 if tol is None else float(tol)
+        self.maxiter = int(maxiter)
+        self.callback = callback
+        self.printrates = printrates
+        self.mode = mode
+        self.stop_rule = stop_rule
+        self.inner_tol = inner_tol
+        self.max_outer = max_outer
+        self.check_every = check_every
+        self.residuals = []
+        self.iterations = 0
+        self.result = None
+
+    @property
+    def errors(self):
+        return self.residuals
+
+    def Solve(self, rhs, sol=None, initialize=True):
+        rhs = _as_vec(rhs)
+        if sol is None:
+            sol = rhs.CreateVector()
+            initialize = True
+        sol = _as_vec(sol)
+        if rhs.t.dtype != torch.float64 or sol.t.dtype != torch.float64:
+            raise TypeError("CG works on FP64 vectors (mixed mode keeps FP32 internally)")
+        ctx = self.mat.ctx.sync_stream()
+        hist = np.zeros(self.maxiter + 2)
+        o = _lib.CGOpts()
+        o.tol = self.tol
+        o.maxit = self.maxiter
+        o.mode = _lib.GH1_CG_MIXED if self.mode == "mixed" else _lib.GH1_CG_FP64
+        o.stop_rule = _lib.GH1_STOP_TRUE if self.stop_rule == "true" else _lib.GH1_STOP_PRECOND
+        o.initialize = 1 if initialize else 0
+        o.inner_tol = float(self.inner_tol)
+        o.max_outer = int(self.max_outer)
+        o.check_every = int(self.check_every)
+        o.res_hist = hist.ctypes.data
+        r = _lib.CGResult()
+        rc = ctx.lib.gh1_cg(self.mat.h, None if self.pre is None else self.pre.h, _ptr(rhs.t), _ptr(sol.t),
+                            ctypes.byref(o), ctypes.byref(r))
+        if rc not in (_lib.GH1_OK, 6, 7):
+            ctx.check(rc)
+        self.result = r
+        self.iterations = r.iterations
+        n_hist = (r.outer + 1) if self.mode == "mixed" else r.iterations
+        self.residuals = list(hist[:max(0, min(n_hist, len(hist)))])
+        if self.printrates:
+            print("%s %sconverged in %d iterations to residual %g (true relative residual %g)" %
+                  (self.name, "" if r.status == 0 else "NOT ", r.iterations, r.final_res, r.true_relres))
+        if self.callback is not None:
+            for k, v in enumerate(self.residuals[1:], start=2):
+                self.callback(k, v)
+        self.sol = sol
+        return sol
+
+    def Mult(self, x, y):
+        self.Solve(rhs=x, sol=y, initialize=True)
+
+
+def CG(mat, rhs, pre=None, sol=None, tol=1e-12, maxsteps=100, printrates=True, plotrates=False, initialize=True,
+       conjugate=False, callback=None, **kwargs):
+    """preconditioned conjugate gradient method (signature of ngsolve.solvers.CG)."""
+    solver = CGSolver(mat=mat, pre=pre, tol=tol, maxiter=maxsteps, callback=callback, printrates=printrates,
+                      conjugate=conjugate, **kwargs)
+    solver.Solve(rhs=rhs, sol=sol, initialize=initialize)
+    CG.last_solver = solver
+    return solver.sol

@@ -1,0 +1,214 @@
+"""ctypes front end of the FP64 CPU oracle (``gh1_oracle.cpp``).
+
+TEST INFRASTRUCTURE ONLY.  The oracle restates NGSolve's H1 assemble / apply /
+CG algorithms on the CPU; it is the checker for the GPU library.  Only the
+tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+import this module, and only to compare against or time the reference
+algorithm -- never as a product code path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "libgh1_oracle.so")
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with g++ -O3 -fopenmp (portable flags: x86 and Arm)."""
+    src = os.path.join(_HERE, "gh1_oracle.cpp")
+    if not force and os.path.exists(_SO) and os.path.getmtime(_SO) >= os.path.getmtime(src):
+        return _SO
+    os.makedirs(os.path.dirname(_SO), exist_ok=True)
+    tmp = _SO + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c++17",
+                           src, "-o", tmp])
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_SO)
+        P = ctypes.c_void_p
+        i, l, d = ctypes.c_int, ctypes.c_long, ctypes.c_double
+        L.orc_space_create.restype = P
+        L.orc_space_create.argtypes = [i, i, P, i, P, i]
+        L.orc_space_destroy.argtypes = [P]
+        L.orc_space_info.argtypes = [P, P]
+        L.orc_space_dofs.argtypes = [P, P]
+        L.orc_space_freedofs.argtypes = [P, P]
+        L.orc_space_topology.argtypes = [P, P, P]
+        L.orc_graph.restype = l
+        L.orc_graph.argtypes = [P]
+        L.orc_graph_get.argtypes = [P, P, P]
+        L.orc_assemble.argtypes = [P, P, P, P]
+        L.orc_element_matrix.argtypes = [P, i, d, d, P]
+        L.orc_spmv.argtypes = [l, P, P, P, d, P, P, i]
+        L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
+        L.orc_rhs.argtypes = [P, P, P]
+        L.orc_elem_grad_dot.argtypes = [P, P, P, P]
+        L.orc_shapes.argtypes = [i, i, P, i, P, P, P]
+        L.orc_dubiner2d.argtypes = [i, d, d, P]
+        L.orc_dubiner3d.argtypes = [i, d, d, d, P]
+        L.orc_rule.argtypes = [i, i, P, P]
+        L.orc_cg.argtypes = [P, l, P, P, P, P, P, P, P, P, d, i, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleSpace:
+    """H1 space of uniform order p on a tet (et=4) or hex (et=8) mesh."""
+
+    def __init__(self, points, elements, order):
+        self.points = np.ascontiguousarray(points, dtype=np.float64)
+        self.elements = np.ascontiguousarray(elements, dtype=np.int32)
+        self.et = int(self.elements.shape[1])
+        self.order = int(order)
+        self.ne = int(self.elements.shape[0])
+        self.h = lib().orc_space_create(self.et, len(self.points), _p(self.points), self.ne,
+                                        _p(self.elements), self.order)
+        info = np.zeros(7, dtype=np.int64)
+        lib().orc_space_info(self.h, _p(info))
+        self.ndof, self.nloc, self.ned, self.nfa = (int(v) for v in info[:4])
+        self.first_edge, self.first_face, self.first_cell = (int(v) for v in info[4:])
+        self._csr = None
+
+    def __del__(self):
+        try:
+            lib().orc_space_destroy(self.h)
+        except Exception:
+            pass
+
+    def element_dofs(self):
+        out = np.zeros((self.ne, self.nloc), dtype=np.int32)
+        lib().orc_space_dofs(self.h, _p(out))
+        return out
+
+    def freedofs(self):
+        out = np.zeros(self.ndof, dtype=np.uint8)
+        lib().orc_space_freedofs(self.h, _p(out))
+        return out
+
+    def topology(self):
+        ned = 6 if self.et == 4 else 12
+        nfa = 4 if self.et == 4 else 6
+        ee = np.zeros((self.ne, ned), dtype=np.int32)
+        ff = np.zeros((self.ne, nfa), dtype=np.int32)
+        lib().orc_space_topology(self.h, _p(ee), _p(ff))
+        return ee, ff
+
+    def graph(self):
+        if self._csr is None:
+            nnz = lib().orc_graph(self.h)
+            rowptr = np.zeros(self.ndof + 1, dtype=np.int64)
+            colind = np.zeros(nnz, dtype=np.int32)
+            lib().orc_graph_get(self.h, _p(rowptr), _p(colind))
+            self._csr = (rowptr, colind)
+        return self._csr
+
+    def assemble(self, kappa=None, mu=None):
+        rowptr, colind = self.graph()
+        vals = np.zeros(len(colind), dtype=np.float64)
+        k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
+        rc = lib().orc_assemble(self.h, _p(k), _p(m), _p(vals))
+        if rc != 0:
+            raise RuntimeError("illegal dnums in AddElementMatrix")
+        return rowptr, colind, vals
+
+    def element_matrix(self, e, kappa=1.0, mu=0.0):
+        K = np.zeros((self.nloc, self.nloc))
+        lib().orc_element_matrix(self.h, int(e), float(kappa), float(mu), _p(K))
+        return K
+
+    def apply_mf(self, x, kappa=None, mu=None, e0=0, e1=-1):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.ndof)
+        k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
+        lib().orc_apply_mf(self.h, _p(k), _p(m), _p(x), _p(y), int(e0), int(e1))
+        return y
+
+    def rhs(self, f_elem):
+        f = np.ascontiguousarray(f_elem, dtype=np.float64)
+        b = np.zeros(self.ndof)
+        lib().orc_rhs(self.h, _p(f), _p(b))
+        return b
+
+    def elem_grad_dot(self, u, w):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out = np.zeros(self.ne)
+        lib().orc_elem_grad_dot(self.h, _p(u), _p(w), _p(out))
+        return out
+
+    def cg(self, b, invdiag, tol=1e-10, maxit=10000, csr=None, kappa=None, mu=None, x0=None):
+        """CGSolver._SolveImpl on CSR (csr=(rowptr,colind,vals)) or matrix-free."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.ndof) if x0 is None else np.array(x0, dtype=np.float64)
+        hist = np.zeros(maxit + 2)
+        its = np.zeros(1, dtype=np.int32)
+        invdiag = np.ascontiguousarray(invdiag, dtype=np.float64)
+        k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
+        if csr is not None:
+            rp, ci, va = csr
+            lib().orc_cg(self.h, self.ndof, _p(rp), _p(ci), _p(va), None, None, _p(invdiag),
+                         _p(b), _p(x), tol, maxit, _p(hist), _p(its))
+        else:
+            lib().orc_cg(self.h, self.ndof, None, None, None, _p(k), _p(m), _p(invdiag),
+                         _p(b), _p(x), tol, maxit, _p(hist), _p(its))
+        n = int(its[0])
+        return x, n, hist[:n].copy()
+
+
+def spmv(rowptr, colind, vals, x, s=1.0):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(len(rowptr) - 1)
+    lib().orc_spmv(len(rowptr) - 1, _p(rowptr), _p(colind), _p(vals), float(s), _p(x), _p(y), 0)
+    return y
+
+
+def shapes(et, order, vnums, pts):
+    vn = np.ascontiguousarray(vnums, dtype=np.int32)
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    n = (order + 1) * (order + 2) * (order + 3) // 6 if et == 4 else (order + 1) ** 3
+    val = np.zeros((len(pts), n))
+    grad = np.zeros((len(pts), n, 3))
+    rc = lib().orc_shapes(et, order, _p(vn), len(pts), _p(pts), _p(val), _p(grad))
+    assert rc == n
+    return val, grad
+
+
+def rule(et, order):
+    n = lib().orc_rule(et, order, None, None)
+    pts = np.zeros((n, 3))
+    w = np.zeros(n)
+    lib().orc_rule(et, order, _p(pts), _p(w))
+    return pts, w
+
+
+def dubiner2d(n, x, y):
+    out = np.zeros((n + 1) * (n + 2) // 2)
+    lib().orc_dubiner2d(n, x, y, _p(out))
+    return out
+
+
+def dubiner3d(n, x, y, z):
+    out = np.zeros((n + 1) * (n + 2) * (n + 3) // 6)
+    lib().orc_dubiner3d(n, x, y, z, _p(out))
+    return out
+
+
+def max_threads():
+    return int(lib().orc_max_threads())

@@ -1,0 +1,279 @@
+"""GPU parity tests: libgh1 kernels (through the C ABI) against the FP64 CPU oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior, Mesh as RawMesh
+from tests.util import lognormal, csr_rowscaled_close, permute_tets
+
+pytestmark = pytest.mark.gpu
+
+
+def _mesh(kind, n, jitter, seed=11, permute=False):
+    m = MakeStructured3DMesh(hexes=(kind == "hex"), nx=n)
+    if jitter:
+        m = JitterInterior(m, jitter / n, seed)
+    if permute:
+        m = RawMesh(m.points, permute_tets(m.elements, seed + 1))
+    return m
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
+def test_shapes_tet(gpu, p):
+    rng = np.random.default_rng(p)
+    pts = rng.dirichlet(np.ones(4), size=7)[:, :3]
+    for vn in ([0, 1, 2, 3], [3, 1, 0, 2], [7, 2, 9, 4]):
+        gv, gg = gpu.ShapeEval(4, p, vn, pts)
+        ov, og = O.shapes(4, p, vn, pts)
+        assert np.abs(gv - ov).max() < 1e-13 and np.abs(gg - og).max() < 1e-12
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7, 8])
+def test_shapes_hex(gpu, p):
+    pts = np.random.default_rng(p).uniform(0, 1, (5, 3))
+    for vn in (list(range(8)), [5, 3, 0, 7, 1, 6, 2, 4]):
+        gv, gg = gpu.ShapeEval(8, p, vn, pts)
+        ov, og = O.shapes(8, p, vn, pts)
+        assert np.abs(gv - ov).max() < 1e-13 and np.abs(gg - og).max() < 1e-12
+
+
+def test_p1_mass_golden(gpu, cube_vol, golden):
+    """GPU assembly reproduces a.mat[1,1] of tests/pytest/test_matrix.py:84-93."""
+    pts, tets = cube_vol
+    fes = gpu.H1(RawMesh(pts, tets), order=1)
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes)
+    a += u * v * gpu.dx
+    a.Assemble()
+    g = golden["p1_mass_cube_vertex1"]
+    assert abs(a.mat[1, 1] - g["value"]) < g["tolerance"]
+    assert abs(a.mat[1, 1] - g["value"]) < 1e-17
+
+
+@pytest.mark.parametrize("kind,p,jit,perm", [("hex", 1, 0.1, False), ("hex", 2, 0.1, False), ("hex", 3, 0.15, False),
+                                             ("hex", 4, 0.1, False), ("tet", 1, 0.2, True), ("tet", 2, 0.2, False),
+                                             ("tet", 3, 0.2, True), ("tet", 4, 0.2, True), ("tet", 5, 0.0, True)])
+def test_assemble_parity(gpu, kind, p, jit, perm):
+    """Pattern bit-exact and entries within 1e-12 (row-scaled) of the oracle's Assemble."""
+    m = _mesh(kind, 3, jit, permute=perm)
+    kappa = lognormal(m.ne, 1.0, 3)
+    mu = lognormal(m.ne, 0.5, 4)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes)
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a += gpu.CoefficientFunction(mu) * u * v * gpu.dx
+    a.Assemble()
+    S = O.OracleSpace(m.points, m.elements, p)
+    assert fes.ndof == S.ndof
+    assert np.array_equal(fes.ElementDofs(), S.element_dofs())
+    assert np.array_equal(fes.FreeDofs(), S.freedofs().astype(bool))
+    orp, oci, ova = S.assemble(kappa=kappa, mu=mu)
+    rp, ci, va = a.mat.CSR()
+    csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12)
+
+
+@pytest.mark.parametrize("kind,p,jit,mass", [("hex", 1, 0.1, False), ("hex", 2, 0.1, True), ("hex", 3, 0.15, False),
+                                             ("hex", 4, 0.1, True), ("hex", 6, 0.1, False), ("hex", 8, 0.0, False),
+                                             ("tet", 2, 0.2, True), ("tet", 3, 0.2, False), ("tet", 4, 0.2, False)])
+def test_matfree_apply_parity(gpu, kind, p, jit, mass):
+    m = _mesh(kind, 3, jit, permute=(kind == "tet"))
+    kappa = lognormal(m.ne, 1.0, 5)
+    mu = lognormal(m.ne, 0.5, 6) if mass else None
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, nonassemble=True, precision="fp32")
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    if mass:
+        a += gpu.CoefficientFunction(mu) * u * v * gpu.dx
+    a.Assemble()
+    S = O.OracleSpace(m.points, m.elements, p)
+    x = np.random.default_rng(7).normal(size=fes.ndof)
+    yo = S.apply_mf(x, kappa=kappa, mu=mu)
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    a.mat.Mult(xv, yv)
+    sc = np.abs(yo).max()
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * sc
+    # MultAdd semantics: y += s A x
+    a.mat.MultAdd(-0.5, xv, yv)
+    assert np.abs(yv.NumPy() - 0.5 * yo).max() <= 1e-12 * sc
+    # FP32 data path: tolerance 1e-5 of the scale (single precision G and vectors)
+    x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+    a.mat.Mult(x32, y32)
+    assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * sc
+
+
+@pytest.mark.parametrize("kind,p", [("hex", 3), ("tet", 4)])
+def test_spmv_parity(gpu, kind, p):
+    m = _mesh(kind, 4, 0.1)
+    kappa = lognormal(m.ne, 1.0, 8)
+    fes = gpu.H1(m, order=p)
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes)
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a.Assemble()
+    rp, ci, va = a.mat.CSR()
+    x = np.random.default_rng(9).normal(size=fes.ndof)
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    for _ in range(3):  # repeated SpMVs (the reference does 100 in the timing config)
+        yv.data = a.mat * xv
+    yo = O.spmv(rp, ci, va, x)
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-13 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("kind,p", [("hex", 2), ("hex", 3), ("tet", 3)])
+def test_rhs_parity(gpu, kind, p):
+    m = _mesh(kind, 3, 0.1)
+    f = np.random.default_rng(10).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=p)
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    S = O.OracleSpace(m.points, m.elements, p)
+    bo = S.rhs(f)
+    assert np.abs(lf.vec.NumPy() - bo).max() <= 1e-13 * np.abs(bo).max()
+
+
+def _jacobi_inv(rp, ci, va, free):
+    d = va[[rp[i] + np.searchsorted(ci[rp[i]:rp[i + 1]], i) for i in range(len(rp) - 1)]]
+    return np.where(free, 1.0 / d, 0.0)
+
+
+@pytest.mark.parametrize("kind,p,matfree", [("hex", 3, False), ("hex", 3, True), ("tet", 2, False), ("tet", 3, True)])
+def test_cg_fp64_iterates(gpu, kind, p, matfree):
+    """FP64 CG on the GPU follows krylovspace.py: same residual history and
+    iteration count as the oracle, solution within 1e-9."""
+    m = _mesh(kind, 4, 0.1)
+    kappa = lognormal(m.ne, 1.0, 12)
+    f = np.random.default_rng(13).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, nonassemble=matfree)
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a.Assemble()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    sol = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=3000, printrates=False)
+    solver = gpu.solvers.CG.last_solver
+    S = O.OracleSpace(m.points, m.elements, p)
+    orp, oci, ova = S.assemble(kappa=kappa)
+    inv = _jacobi_inv(orp, oci, ova, S.freedofs().astype(bool))
+    xo, its, hist = S.cg(S.rhs(f), inv, tol=1e-10, maxit=3000, csr=(orp, oci, ova))
+    assert abs(solver.iterations - its) <= 1
+    k = min(len(hist), len(solver.residuals)) - 2
+    assert np.allclose(solver.residuals[:k], hist[:k], rtol=1e-6)
+    assert np.abs(sol.NumPy() - xo).max() <= 1e-9 * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("kind,p", [("hex", 4), ("tet", 3)])
+def test_cg_mixed_precision(gpu, kind, p):
+    """FP32 inner CG + FP64 refinement reaches 1e-10 true relative residual; the
+    solution is within 1e-9 (relative) of the FP64 oracle solution."""
+    m = _mesh(kind, 4, 0.1)
+    kappa = lognormal(m.ne, 0.5, 14)
+    f = np.random.default_rng(15).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, nonassemble=True, precision="fp32")
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a.Assemble()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    sol = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=20000, printrates=False,
+                         mode="mixed", stop_rule="true")
+    r = gpu.solvers.CG.last_solver.result
+    assert r.status == 0 and r.true_relres <= 1e-10 and r.outer >= 1
+    S = O.OracleSpace(m.points, m.elements, p)
+    orp, oci, ova = S.assemble(kappa=kappa)
+    inv = _jacobi_inv(orp, oci, ova, S.freedofs().astype(bool))
+    xo, _, _ = S.cg(S.rhs(f), inv, tol=1e-13, maxit=20000, csr=(orp, oci, ova))
+    assert np.abs(sol.NumPy() - xo).max() <= 1e-9 * np.abs(xo).max()
+
+
+def test_hex_p_exactness_gpu(gpu):
+    """u = x(1-x)y(1-y)z(1-z) in Q_2: GPU CG reproduces the oracle's exact solution."""
+    m = _mesh("hex", 3, 0.0)
+    fes = gpu.H1(m, order=2, dirichlet=".*")
+    S = O.OracleSpace(m.points, m.elements, 2)
+    pts, w = O.rule(8, 8)
+    d = S.element_dofs()
+    fb = np.zeros(S.ndof)
+    for e in range(S.ne):
+        X = m.points[m.elements[e]]
+        lo, hi = X.min(0), X.max(0)
+        q = lo + (hi - lo) * pts[:, [2, 1, 0]]
+        q = q * (1 - q)
+        f = 2 * (q[:, 1] * q[:, 2] + q[:, 0] * q[:, 2] + q[:, 0] * q[:, 1])
+        val, _ = O.shapes(8, 2, m.elements[e], pts)
+        fb[d[e]] += (w * f * np.prod(hi - lo)) @ val
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, nonassemble=True)
+    a += gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a.Assemble()
+    b = gpu.BaseVector(fes.ndof)
+    b.data = fb
+    sol = gpu.solvers.CG(mat=a.mat, rhs=b, pre=a.mat.CreateSmoother(fes.FreeDofs()), tol=1e-14, maxsteps=2000,
+                         printrates=False)
+    # value at the vertices = u(vertex) (vertex DOFs interpolate, higher DOFs carry the bubble)
+    xs = sol.NumPy()[:m.nv]
+    P = m.points
+    exact = np.prod(P * (1 - P), axis=1)
+    assert np.abs(xs - exact).max() < 1e-12
+
+
+def test_adjoint_gradient(gpu):
+    """dJ/dkappa from the adjoint kernel vs central finite differences (h=1e-6)
+    and vs the oracle's adjoint recipe."""
+    m = _mesh("hex", 4, 0.0)
+    p = 2
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    rng = np.random.default_rng(21)
+    kappa = np.exp(rng.normal(0, 1, m.ne))
+    kstar = np.exp(rng.normal(0, 1, m.ne))
+    f = rng.uniform(-1, 1, m.ne)
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    target = gpu.AdjointProblem(fes, lf.vec, torch.zeros(fes.ndof, dtype=torch.float64, device="cuda"), tol=1e-14)
+    target.evaluate(kstar)
+    ut = target.u.clone()
+    prob = gpu.AdjointProblem(fes, lf.vec, ut, tol=1e-14)
+    kt = torch.tensor(kappa, dtype=torch.float64, requires_grad=True)
+    J = gpu.AdjointJ.apply(kt, prob)
+    J.backward()
+    g = kt.grad.numpy()
+    h = 1e-6
+    for e in rng.choice(m.ne, 6, replace=False):
+        kp, km = kappa.copy(), kappa.copy()
+        kp[e] *= 1 + h
+        km[e] *= 1 - h
+        fd = (prob.evaluate(kp)[0] - prob.evaluate(km)[0]) / (2 * h * kappa[e])
+        assert abs(fd - g[e]) <= 1e-6 * max(abs(g[e]), 1e-3 * np.abs(g).max())
+    # oracle recipe: u, lambda by direct solves, -int grad u . grad lambda
+    S = O.OracleSpace(m.points, m.elements, p)
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    free = S.freedofs().astype(bool)
+    rp, ci, va = S.assemble(kappa=kappa)
+    A = sp.csr_matrix((va, ci, rp), shape=(S.ndof, S.ndof))[free][:, free].tocsc()
+    mrp, mci, mva = S.assemble(kappa=np.zeros(m.ne), mu=np.ones(m.ne))
+    M = sp.csr_matrix((mva, mci, mrp), shape=(S.ndof, S.ndof))
+    uo = np.zeros(S.ndof)
+    uo[free] = spla.spsolve(A, S.rhs(f)[free])
+    ut_h = ut.cpu().numpy()
+    lam = np.zeros(S.ndof)
+    lam[free] = spla.spsolve(A, (M @ (uo - ut_h))[free])
+    go = -S.elem_grad_dot(uo, lam)
+    assert np.abs(g - go).max() <= 1e-8 * np.abs(go).max()
