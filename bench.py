@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"],
+                    help="c3 (default, the headline line); c1/c2/c4 print their own measurement records")
     return ap.parse_args()
 
 
@@ -215,6 +217,133 @@ def run_reference(args, ws, rank):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# other configurations (measurement records, not the headline line)
+def _timed(fn, reps=1):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        r = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps, r
+
+
+def workload_c1(args):
+    """16^3 hex, p=3, kappa=1, f ~ U[-1,1] per element (seed 1), zero Dirichlet:
+    GPU Assemble + Jacobi-PCG (FP64, reference stop rule) to 1e-10."""
+    import torch
+    import ngsolve_gb300 as ng
+    mesh = ng.MakeStructured3DMesh(hexes=True, nx=16)
+    f = np.random.default_rng(1).uniform(-1, 1, mesh.ne)
+    t_space, fes = _timed(lambda: ng.H1(mesh, order=3, dirichlet=".*"))
+    u, v = fes.TnT()
+    a = ng.BilinearForm(fes)
+    a += ng.grad(u) * ng.grad(v) * ng.dx
+    t_graph, _ = _timed(lambda: a.Assemble())       # first call builds the pattern
+    t_asm, _ = _timed(lambda: a.Assemble(), reps=3)  # element matrices + scatter only
+    lf = ng.LinearForm(fes)
+    lf += ng.CoefficientFunction(f) * v * ng.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    def solve():
+        return ng.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=10000, printrates=False)
+    solve()
+    t_cg, _ = _timed(solve, reps=3)
+    r = ng.solvers.CG.last_solver.result
+    return {"workload": "C1: 16^3 hex p=3 FP64 assemble + Jacobi-PCG to 1e-10", "ndof": fes.ndof, "nnz": a.mat.nze,
+            "space_s": t_space, "assemble_first_s": t_graph, "assemble_s": t_asm, "cg_s": t_cg,
+            "cg_iterations": r.iterations, "true_relres": r.true_relres}
+
+
+def workload_c2(args):
+    """32^3 Kuhn tets, interior vertices jittered U[-0.2h,0.2h] (seed 2), kappa
+    lognormal(0,1) (seed 3), p=2,3,4: Assemble, 100 SpMVs (vs cuSPARSE through
+    torch.sparse), matrix-free apply."""
+    import torch
+    import ngsolve_gb300 as ng
+    out = {"workload": "C2: 32^3 Kuhn tets (196,608), jitter 0.2h, kappa lognormal(0,1)", "orders": {}}
+    mesh = ng.JitterInterior(ng.MakeStructured3DMesh(hexes=False, nx=32), 0.2 / 32, 2)
+    kappa = np.exp(np.random.default_rng(3).normal(0, 1, mesh.ne))
+    for p in (2, 3, 4):
+        fes = ng.H1(mesh, order=p, dirichlet=".*")
+        u, v = fes.TnT()
+        a = ng.BilinearForm(fes)
+        a += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+        t_first, _ = _timed(lambda: a.Assemble())
+        t_asm, _ = _timed(lambda: a.Assemble(), reps=3)
+        N, nnz = fes.ndof, a.mat.nze
+        x = ng.BaseVector(data=torch.rand(N, dtype=torch.float64, device="cuda"))
+        y = ng.BaseVector(N)
+        for _ in range(5):
+            a.mat.Mult(x, y)
+        t_spmv, _ = _timed(lambda: a.mat.Mult(x, y), reps=100)
+        rp, ci, va = a.mat.CSR()
+        A = torch.sparse_csr_tensor(torch.tensor(rp, dtype=torch.int32), torch.tensor(ci, dtype=torch.int32),
+                                    torch.tensor(va), size=(N, N), device="cuda")
+        xt = x.t.view(-1, 1)
+        for _ in range(5):
+            A @ xt
+        t_cusp, _ = _timed(lambda: A @ xt, reps=100)
+        err = float((A @ xt).view(-1).sub(y.t).abs().max() / y.t.abs().max())
+        amf = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+        amf += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+        amf.Assemble()
+        for _ in range(3):
+            amf.mat.Mult(x, y)
+        t_mf64, _ = _timed(lambda: amf.mat.Mult(x, y), reps=20)
+        x32 = ng.BaseVector(data=x.t.float())
+        y32 = ng.BaseVector(data=torch.zeros(N, dtype=torch.float32, device="cuda"))
+        for _ in range(3):
+            amf.mat.Mult(x32, y32)
+        t_mf32, _ = _timed(lambda: amf.mat.Mult(x32, y32), reps=20)
+        B = nnz * 12 + 8 * (N + 1) + 2 * N * 8
+        out["orders"][p] = {"ndof": N, "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm,
+                            "spmv_ms": t_spmv * 1e3, "spmv_gbs": B / t_spmv / 1e9, "cusparse_ms": t_cusp * 1e3,
+                            "spmv_vs_cusparse": t_cusp / t_spmv, "spmv_err_vs_cusparse": err,
+                            "matfree_fp64_ms": t_mf64 * 1e3, "matfree_fp32_ms": t_mf32 * 1e3,
+                            "matfree_fp32_gdofs": N / t_mf32 / 1e9}
+        del A, a, amf
+        torch.cuda.empty_cache()
+    return out
+
+
+def workload_c4(args):
+    """32^3 hex, p=3, kappa lognormal(0,1) (seed 6), kappa* (seed 7): dJ/dkappa by
+    the adjoint kernel vs central finite differences (h=1e-6) on 32 elements (seed 8)."""
+    import torch
+    import ngsolve_gb300 as ng
+    mesh = ng.MakeStructured3DMesh(hexes=True, nx=32)
+    kappa = np.exp(np.random.default_rng(6).normal(0, 1, mesh.ne))
+    kstar = np.exp(np.random.default_rng(7).normal(0, 1, mesh.ne))
+    f = np.random.default_rng(5).uniform(-1, 1, mesh.ne)
+    fes = ng.H1(mesh, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+    lf = ng.LinearForm(fes)
+    lf += ng.CoefficientFunction(f) * v * ng.dx
+    lf.Assemble()
+    tgt = ng.AdjointProblem(fes, lf.vec, torch.zeros(fes.ndof, dtype=torch.float64, device="cuda"), tol=1e-14)
+    tgt.evaluate(kstar)
+    prob = ng.AdjointProblem(fes, lf.vec, tgt.u.clone(), tol=1e-14)
+    prob.evaluate(kappa)
+    t_grad, (J, g) = _timed(lambda: prob.evaluate(kappa))
+    g = g.cpu().numpy()
+    els = np.random.default_rng(8).choice(mesh.ne, 32, replace=False)
+    h = 1e-6
+    rel = []
+    t0 = time.perf_counter()
+    for e in els:
+        kp, km = kappa.copy(), kappa.copy()
+        kp[e] += h
+        km[e] -= h
+        fd = (prob.evaluate(kp)[0] - prob.evaluate(km)[0]) / (2 * h)
+        rel.append(abs(fd - g[e]) / max(abs(g[e]), 1e-30))
+    t_fd = time.perf_counter() - t0
+    return {"workload": "C4: 32^3 hex p=3 adjoint dJ/dkappa", "ndof": fes.ndof, "J": J, "gradient_s": t_grad,
+            "fd_elements": 32, "fd_h": h, "fd_max_rel_err": float(max(rel)), "fd_median_rel_err": float(np.median(rel)),
+            "fd_s": t_fd}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup(args.gpus)
@@ -227,6 +356,12 @@ def main():
     build.build()
     dev = local
     torch.cuda.set_device(dev)
+    if args.workload != "c3":
+        fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4}[args.workload]
+        rec = fn(args)
+        if rank == 0:
+            print(json.dumps({"record": args.workload, **rec}), flush=True)
+        return
 
     mesh = ng.MakeStructured3DMesh(hexes=True, nx=args.nx)
     kappa = np.exp(np.random.default_rng(SEED_KAPPA).normal(0, 0.5, mesh.ne))

@@ -22,8 +22,8 @@ class AdjointProblem:
 
     def __init__(self, fes, f_vec, u_target, tol=1e-12):
         self.fes = fes
-        self.f = f_vec.t if hasattr(f_vec, "t") else f_vec
-        self.u_target = u_target.t if hasattr(u_target, "t") else u_target
+        self.f = f_vec if isinstance(f_vec, torch.Tensor) else f_vec.t
+        self.u_target = u_target if isinstance(u_target, torch.Tensor) else u_target.t
         self.tol = float(tol)
         ctx = fes.ctx
         h = ctypes.c_void_p()

@@ -169,9 +169,13 @@ void build_space(gh1_space* sp) {
   if (!tet) {
     // tensor-ordered signed DOF table: every hex shape is sign * psi_a psi_b psi_c
     const int n = p + 1, n3 = n * n * n;
-    std::vector<int32_t> tdof((size_t)ne * n3, -1);
+    sp->tstride = (n3 + 3) / 4 * 4;
+    const int ts = sp->tstride;
+    std::vector<int32_t> tdof((size_t)ne * ts, 0);
+    for (int64_t e = 0; e < ne; e++)
+      for (int t = 0; t < n3; t++) tdof[(size_t)e * ts + t] = -1;
     host_parallel(ne, [&](int64_t e) {
-      int32_t* T = &tdof[(size_t)e * n3];
+      int32_t* T = &tdof[(size_t)e * ts];
       int vn[8];
       for (int i = 0; i < 8; i++) vn[i] = ev(e, i);
       auto put = [&](int a, int b, int c, int64_t dof, int sign) {

@@ -106,8 +106,8 @@ __global__ void tet_assemble_kernel(int ne, int nloc, const int* __restrict__ el
 }
 
 // hex: one thread per (element, t, t'), tensor indices with signs
-__global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof, const double* __restrict__ Gq,
-                                    const double* __restrict__ Mq, const double* __restrict__ B, const double* __restrict__ D,
+__global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ Gq,
+                                    int gstride, int mass, const double* __restrict__ B, const double* __restrict__ D,
                                     const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind, double* vals,
                                     int* bad) {
   const int N3 = N * N * N;
@@ -117,7 +117,7 @@ __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof,
     int e = (int)(id / per), tt = (int)(id % per), t = tt / N3, u = tt % N3;
     int a = t / (N * N), b = (t / N) % N, c = t % N;
     int a2 = u / (N * N), b2 = (u / N) % N, c2 = u % N;
-    const double* Ge = Gq + (size_t)e * 6 * N3;
+    const double* Ge = Gq + (size_t)e * gstride;
     double s = 0;
     for (int i = 0; i < N; i++) {
       double Ba = B[i * N + a], Da = D[i * N + a], Ba2 = B[i * N + a2], Da2 = D[i * N + a2];
@@ -131,11 +131,11 @@ __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof,
           double gxx = Ge[q], gyy = Ge[N3 + q], gzz = Ge[2 * N3 + q], gxy = Ge[3 * N3 + q], gxz = Ge[4 * N3 + q],
                  gyz = Ge[5 * N3 + q];
           s += x1 * (gxx * x2 + gxy * y2 + gxz * z2) + y1 * (gxy * x2 + gyy * y2 + gyz * z2) + z1 * (gxz * x2 + gyz * y2 + gzz * z2);
-          if (Mq) s += Mq[(size_t)e * N3 + q] * (Ba * Bb * Bc) * (Ba2 * Bb2 * Bc2);
+          if (mass) s += Ge[6 * N3 + q] * (Ba * Bb * Bc) * (Ba2 * Bb2 * Bc2);
         }
       }
     }
-    int dt = tdof[(size_t)e * N3 + t], du = tdof[(size_t)e * N3 + u];
+    int dt = tdof[(size_t)e * tstride + t], du = tdof[(size_t)e * tstride + u];
     if ((dt < 0) != (du < 0)) s = -s;
     int64_t pos = find_col(rowptr, colind, dt & 0x7fffffff, du & 0x7fffffff);
     if (pos < 0) { atomicExch(bad, 1); continue; }
@@ -166,8 +166,9 @@ void assemble_csr(gh1_form* f, double* vals) {
     const int N = sp->p + 1;
     int64_t tot = (int64_t)ne * N * N * N * N * N * N;
     int grid = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)ctx->nsm * 32);
-    hex_assemble_kernel<<<grid, 256, 0, s>>>(ne, N, sp->d_tdof.p, geo.d_G64.p, geo.has_mass ? geo.d_M64.p : nullptr,
-                                             sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p, sp->d_colind.p, vals, bad.p);
+    hex_assemble_kernel<<<grid, 256, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, geo.d_G64.p, geo.gstride64,
+                                             geo.has_mass ? 1 : 0, sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p, sp->d_colind.p,
+                                             vals, bad.p);
     check_kernel(ctx, "hex_assemble_kernel");
   }
   int hbad = 0;
@@ -200,7 +201,7 @@ __global__ void hex_wdet_kernel(int ne, int nq1, const double* __restrict__ X, c
   wdet[id] = gw[i] * gw[j] * gw[k] * fabs(det);
 }
 
-__global__ void hex_rhs_kernel(int ne, int N, const int* __restrict__ tdof, const double* __restrict__ wdet,
+__global__ void hex_rhs_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ wdet,
                                const double* __restrict__ B, const double* __restrict__ f, double* b) {
   const int N3 = N * N * N;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,7 +212,7 @@ __global__ void hex_rhs_kernel(int ne, int N, const int* __restrict__ tdof, cons
   for (int i = 0; i < N; i++)
     for (int j = 0; j < N; j++)
       for (int k = 0; k < N; k++) s += wdet[(size_t)e * N3 + (i * N + j) * N + k] * B[i * N + a] * B[j * N + bb] * B[k * N + c];
-  int d = tdof[id];
+  int d = tdof[(size_t)e * tstride + t];
   s *= f[e];
   atomicAdd(b + (d & 0x7fffffff), d < 0 ? -s : s);
 }
@@ -247,7 +248,7 @@ void rhs_elementwise(gh1_space* sp, const double* f, double* b) {
                                                                    sp->d_gw.p, wdet.p);
     check_kernel(ctx, "hex_wdet_kernel");
     tot = (int64_t)ne * N * N * N;
-    hex_rhs_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, N, sp->d_tdof.p, wdet.p, sp->d_B64.p, f, b);
+    hex_rhs_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, wdet.p, sp->d_B64.p, f, b);
     check_kernel(ctx, "hex_rhs_kernel");
     GH1_CUDA(cudaStreamSynchronize(s));
   } else {

@@ -482,13 +482,16 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
         r->outer = outer;
         if (std::sqrt(rr) <= target) { status = GH1_OK; break; }
         if (outer == max_outer || total_inner >= o->maxit) break;
-        // inner: A c = r / |r|  in FP32, c0 = 0
+        // inner: A c = r / |r|  in FP32, c0 = 0.  The last refinement step only
+        // needs the reduction that is still missing (with a safety factor 0.1).
+        const double missing = target / std::sqrt(rr);
+        const double tol_k = std::min(0.5, std::max(inner_tol, 0.1 * missing));
         scale_to_f32_kernel<<<grid_for(ctx, n, 256), 256, 0, cs>>>(n, W.r64.p, norm2.p, W.d32.p);
         check_kernel(ctx, "scale_to_f32_kernel");
         GH1_CUDA(cudaMemsetAsync(W.x32.p, 0, n * sizeof(float), cs));
         PCG<float> P{op, ctx, n, pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32, st.p, partial.p,
                      counters.p, nullptr, chunk};
-        CGState res = P.run(inner_tol, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
+        CGState res = P.run(tol_k, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
         total_inner += res.it;
         r->applies32 += P.applies;
         if (res.status == GH1_BREAKDOWN) { status = GH1_BREAKDOWN; break; }

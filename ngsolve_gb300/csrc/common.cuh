@@ -95,8 +95,10 @@ struct gh1_space {
   std::vector<uint8_t> freedof;   // ndof
   gh1::DBuf<int32_t> d_eldofs;    // ne*nloc (reference local order)
   gh1::DBuf<uint8_t> d_free;      // ndof
-  // hex: tensor-ordered signed DOF table  tdof[e][a][b][c] = dof | (sign<0 ? 1<<31 : 0)
+  // hex: tensor-ordered signed DOF table  tdof[e*tstride + (a*n+b)*n+c] = dof | (sign<0 ? 1<<31 : 0);
+  // the per-element stride is padded to 16 bytes so rows can be bulk-copied
   gh1::DBuf<int32_t> d_tdof;
+  int tstride = 0;
   // hex: integration rule (Gauss, q = p+1 points) and 1D tables B[q][n], D[q][n]
   int nq1 = 0;                    // points per direction
   std::vector<double> gx, gw;     // Gauss points / weights on [0,1]
@@ -143,10 +145,17 @@ struct gh1_op {
   // matrix-free data
   int prec_mask = 1;
   int form_version = -1;
-  gh1::DBuf<double> d_G64;    // hex: [e][6][q] ; tet: [e][6] (geometry incl. kappa, w at qp for hex)
+  // hex: G[e*gstride + c*nq + q], c = xx yy zz xy xz yz (+ mass coefficient as c = 6);
+  //      gstride padded to a multiple of 16 bytes (bulk-copy rows)
+  // tet: G[e*6 + c] and M[e]
+  gh1::DBuf<double> d_G64;
   gh1::DBuf<float> d_G32;
-  gh1::DBuf<double> d_M64;    // mass coefficient: hex [e][q], tet [e]
+  int ncomp = 6, gstride64 = 0, gstride32 = 0;
+  gh1::DBuf<double> d_M64;    // tet mass coefficient [e]
   gh1::DBuf<float> d_M32;
+  gh1::DBuf<int> d_err;       // device error flag of the pipelined apply (bounded waits)
+  int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
+  int hex_gmode[2] = {0, 0};                 // autotuned G staging per precision (0: TMA tile, 1: direct)
   bool has_mass = false;
   gh1::DBuf<double> d_diag;   // operator diagonal (FP64)
   bool have_diag = false;

@@ -10,9 +10,11 @@ Each rule is built from symmetry orbits in barycentric coordinates
   S211(a,b) (a,a,b,1-2a-b)     12 points
 and its orbit parameters and weights are found here by solving the moment
 equations  sum_q w_q x^i y^j z^k = i! j! k! / (i+j+k+3)!  for all monomials of
-total degree <= d with a multi-start least-squares solve (scipy).  Only rules
-with positive weights and interior points are accepted.  Run once; the output
-is committed.  Usage:  python gen_tet_rules.py
+total degree <= d with a multi-start least-squares solve (scipy); only rules
+with positive weights and interior points are accepted.  The double solution is
+then refined by Gauss-Newton in 40-digit arithmetic (mpmath), so every moment
+of the rounded rule is exact to double rounding relative to its own size.  Run
+once; the output is committed.  Usage:  python gen_tet_rules.py
 """
 import itertools
 import math
@@ -89,6 +91,95 @@ def solve(structure, degree, seed=0, tries=4000):
     raise RuntimeError("no rule found for %s degree %d" % (structure, degree))
 
 
+def refine_mp(structure, degree, v0, dps=40, iters=8):
+    """Gauss-Newton on the moment equations in mpmath (dps digits) from the
+    double-precision solution: the rounded rule then has moments exact to
+    double rounding relative to each moment (not only in absolute terms)."""
+    import mpmath as mp
+    mp.mp.dps = dps
+    mons = monomials(degree)
+    exact_mp = [mp.factorial(i) * mp.factorial(j) * mp.factorial(k) / mp.factorial(i + j + k + 3) for i, j, k in mons]
+
+    def orbit_mp(kind, par):
+        if kind == "S4":
+            base = (mp.mpf(1) / 4,) * 4
+        elif kind == "S31":
+            a = par[0]
+            base = (a, a, a, 1 - 3 * a)
+        elif kind == "S22":
+            a = par[0]
+            base = (a, a, mp.mpf(1) / 2 - a, mp.mpf(1) / 2 - a)
+        else:
+            a, b = par
+            base = (a, a, b, 1 - 2 * a - b)
+        perms = sorted(set(itertools.permutations(range(4))))
+        pts = {}
+        for pm in perms:
+            key = tuple(round(float(base[q]), 9) for q in pm)
+            if key not in pts:
+                pts[key] = tuple(base[q] for q in pm)
+        return [pts[k] for k in sorted(pts)]
+
+    def resid(v):
+        pos = 0
+        P, W = [], []
+        pars = []
+        for kind in structure:
+            pars.append(v[pos:pos + NPAR[kind]])
+            pos += NPAR[kind]
+        for o, kind in enumerate(structure):
+            pts = orbit_mp(kind, pars[o])
+            P += pts
+            W += [v[pos + o]] * len(pts)
+        return [sum(w * p[0] ** i * p[1] ** j * p[2] ** k for p, w in zip(P, W)) - ex
+                for (i, j, k), ex in zip(mons, exact_mp)], P, W
+
+    v = [mp.mpf(float(t)) for t in v0]
+    for _ in range(iters):
+        r, _, _ = resid(v)
+        h = mp.mpf(10) ** (-dps // 2)
+        J = mp.matrix(len(r), len(v))
+        for c in range(len(v)):
+            vp = list(v)
+            vp[c] += h
+            rp, _, _ = resid(vp)
+            for rr in range(len(r)):
+                J[rr, c] = (rp[rr] - r[rr]) / h
+        JT = J.T
+        delta = mp.lu_solve(JT * J, -(JT * mp.matrix(r)))
+        v = [v[c] + delta[c] for c in range(len(v))]
+    r, P, W = resid(v)
+    return np.array([[float(c) for c in p[:3]] for p in P]), np.array([float(w) for w in W]), max(abs(x) for x in r)
+
+
+def solve_refined(structure, degree):
+    P, W = solve(structure, degree)
+    # recover the orbit parameters from the double solution (one point per orbit)
+    v0 = []
+    idx = 0
+    for kind in structure:
+        n = ORBIT_SIZE[kind]
+        block = P[idx:idx + n]
+        bary = np.column_stack([block, 1 - block.sum(1)])
+        if kind == "S31":
+            vals, cnt = np.unique(np.round(bary[0], 12), return_counts=True)
+            v0.append(vals[np.argmax(cnt)])
+        elif kind == "S22":
+            v0.append(min(bary[0]))
+        elif kind == "S211":
+            vals, cnt = np.unique(np.round(bary[0], 12), return_counts=True)
+            a = vals[np.argmax(cnt)]
+            others = [x for x in bary[0] if abs(x - a) > 1e-9]
+            v0 += [a, others[0]]
+        idx += n
+    idx = 0
+    for kind in structure:
+        v0.append(W[idx])
+        idx += ORBIT_SIZE[kind]
+    Pm, Wm, res = refine_mp(structure, degree, v0)
+    return Pm, Wm, res
+
+
 RULES = [
     (1, ["S4"]),
     (2, ["S31"]),
@@ -101,10 +192,12 @@ def main():
     out = ["// generated by gen_tet_rules.py -- symmetric tet rules on the reference tet",
            "// {(1,0,0),(0,1,0),(0,0,1),(0,0,0)}: x,y,z = barycentric lambda_0..2, weights sum to 1/6"]
     for degree, structure in RULES:
-        P, W = solve(structure, degree)
+        P, W, res_mp = solve_refined(structure, degree)
         mons = monomials(degree)
-        err = max(abs(np.sum(W * P[:, 0] ** i * P[:, 1] ** j * P[:, 2] ** k) - exact(i, j, k)) for i, j, k in mons)
-        out.append("// degree %d, %d points, max moment error %.1e" % (degree, len(W), err))
+        err = max(abs(np.sum(W * P[:, 0] ** i * P[:, 1] ** j * P[:, 2] ** k) - exact(i, j, k)) / exact(i, j, k)
+                  for i, j, k in mons)
+        out.append("// degree %d, %d points, max relative moment error in double %.1e (40-digit residual %.1e)"
+                   % (degree, len(W), err, float(res_mp)))
         out.append("static const double TET_RULE_D%d[%d][4] = {" % (degree, len(W)))
         for p, w in zip(P, W):
             out.append("  {%.17g, %.17g, %.17g, %.17g}," % (p[0], p[1], p[2], w))

@@ -21,8 +21,11 @@
 // ngscuda/cuda_matrix_free_btdtb.cpp:60-310) and a per-element constant
 // G_e = kappa_e |det J| J^{-1} J^{-T} (affine map, comp/meshaccess.cpp:541-552).
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
+#include <vector>
 #include "common.cuh"
 #include "basis.cuh"
 
@@ -53,11 +56,12 @@ __device__ __forceinline__ void hex_jacobian(const double* X, const int* v, doub
   }
 }
 
-// G[e][c][q] (c: xx yy zz xy xz yz) and M[e][q] for hex elements, FP64 math
+// G[e*gs + c*nq + q] (c: xx yy zz xy xz yz, and mu w |det J| as c = 6 when mu
+// is given) for hex elements; FP64 arithmetic, stored in FP64 and/or FP32
 __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
                                 const double* __restrict__ gx, const double* __restrict__ gw,
-                                const double* __restrict__ kappa, const double* __restrict__ mu, double* G64,
-                                float* G32, double* M64, float* M32) {
+                                const double* __restrict__ kappa, const double* __restrict__ mu, double* G64, int gs64,
+                                float* G32, int gs32) {
   const int nq = nq1 * nq1 * nq1;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -70,22 +74,18 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
   inv3(J, Ji, det);
   double wdet = gw[i] * gw[j] * gw[k] * fabs(det);
   double f = kappa[e] * wdet;
-  double g[6];
+  double g[7];
   g[0] = f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
   g[1] = f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
   g[2] = f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
   g[3] = f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
   g[4] = f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
   g[5] = f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
-  for (int c = 0; c < 6; c++) {
-    size_t o = ((size_t)e * 6 + c) * nq + q;
-    if (G64) G64[o] = g[c];
-    if (G32) G32[o] = (float)g[c];
-  }
-  if (mu) {
-    double m = mu[e] * wdet;
-    if (M64) M64[(size_t)e * nq + q] = m;
-    if (M32) M32[(size_t)e * nq + q] = (float)m;
+  const int nc = mu ? 7 : 6;
+  if (mu) g[6] = mu[e] * wdet;
+  for (int c = 0; c < nc; c++) {
+    if (G64) G64[(size_t)e * gs64 + c * nq + q] = g[c];
+    if (G32) G32[(size_t)e * gs32 + c * nq + q] = (float)g[c];
   }
 }
 
@@ -120,6 +120,33 @@ __global__ void tet_geom_kernel(int ne, const double* __restrict__ X, const int*
     if (M64) M64[e] = m;
     if (M32) M32[e] = (float)m;
   }
+}
+
+// ---------------------------------------------------------------------------
+// 1D hex factor tables B[q][a] = psi_a(x_q), D[q][a] = psi_a'(x_q) of every order
+// in constant memory: with the contraction loops unrolled the FMAs take their
+// table operand straight from the constant bank (no shared-memory load per FMA).
+constexpr int tab_off(int N) { return N <= 2 ? 0 : tab_off(N - 1) + (N - 1) * (N - 1); }
+constexpr int TAB_TOTAL = tab_off(MAX_HEX_ORDER + 2);
+__constant__ float c_B32[TAB_TOTAL], c_D32[TAB_TOTAL];
+__constant__ double c_B64[TAB_TOTAL], c_D64[TAB_TOTAL];
+template <class T> struct CTab;
+template <> struct CTab<float> {
+  static __device__ __forceinline__ float B(int i) { return c_B32[i]; }
+  static __device__ __forceinline__ float D(int i) { return c_D32[i]; }
+};
+template <> struct CTab<double> {
+  static __device__ __forceinline__ double B(int i) { return c_B64[i]; }
+  static __device__ __forceinline__ double D(int i) { return c_D64[i]; }
+};
+
+void upload_const_tables(gh1_space* sp) {
+  const int N = sp->p + 1, off = tab_off(N);
+  cudaStream_t s = sp->ctx->stream;
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_B32, sp->d_B32.p, N * N * sizeof(float), off * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_D32, sp->d_D32.p, N * N * sizeof(float), off * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_B64, sp->d_B64.p, N * N * sizeof(double), off * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_D64, sp->d_D64.p, N * N * sizeof(double), off * sizeof(double), cudaMemcpyDeviceToDevice, s));
 }
 
 // ---------------------------------------------------------------------------
@@ -171,23 +198,81 @@ __device__ void block_reduce_finish(double v, double* partial, unsigned int* cou
 template <int N>
 struct HexCfg {
   static constexpr int N2 = N * N, N3 = N * N * N;
-  static constexpr int G = ((N2 + 31) / 32) * 32;  // threads per element
-  static constexpr int EPB = G == 32 ? 8 : (G == 64 ? 4 : 2);  // elements per block
+  static constexpr int G = ((N2 + 31) / 32) * 32;  // threads per element group
+  static constexpr int EPB = G == 32 ? 4 : 2;      // element groups per block
   static constexpr int BLOCK = G * EPB;
 };
 
+__host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
+
+// shared memory of the pipelined apply, per element group:
+//   [G tile (G mode 0 only)] | DOF-table tile x2 | 5 work arrays | 3 mbarriers
 template <int N, class T>
-constexpr size_t hex_smem_bytes() {
-  return (size_t)HexCfg<N>::EPB * (5 * HexCfg<N>::N3 * sizeof(T) + HexCfg<N>::N3 * sizeof(int)) + 2 * N * N * sizeof(T);
+struct HexSmem {
+  static constexpr size_t tables = 0;
+  static __host__ __device__ size_t gbytes(int gstride) { return round16((size_t)gstride * sizeof(T)); }
+  static __host__ __device__ size_t tbytes(int tstride) { return round16((size_t)tstride * sizeof(int)); }
+  static constexpr size_t work = round16(5 * (size_t)N * N * N * sizeof(T));
+  static __host__ __device__ size_t group(int gstride, int tstride, int gmode) {
+    return (gmode == 0 ? gbytes(gstride) : 0) + 2 * tbytes(tstride) + work + 32;
+  }
+  static __host__ __device__ size_t total(int gstride, int tstride, int gmode) {
+    return tables + (size_t)HexCfg<N>::EPB * group(gstride, tstride, gmode);
+  }
+};
+
+// ---- bulk-copy (TMA) and mbarrier helpers ------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// global -> shared bulk copy (size and both addresses multiples of 16 bytes)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok)
+               : "r"(smem_u32(bar)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+// bounded wait: false after ~2^22 polls (an error, never expected)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// all threads of the element group agree on a predicate
+template <int G>
+__device__ __forceinline__ bool group_all(int gid, bool v) {
+  if (G == 32) return __all_sync(0xffffffffu, v);
+  uint32_t r;
+  asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(r)
+               : "r"((uint32_t)v), "r"(gid + 1), "r"(G)
+               : "memory");
+  return r != 0;
 }
 
 // Forward chain: gathered coefficients in su[(a*N+b)*N+c] -> reference gradient
 // components at the qp of lane (j,k) for all i (registers gx[i], gy[i], gz[i]),
 // plus the interpolated value uq[i] when WANT_U.
 template <int N, class T, bool WANT_U>
-__device__ __forceinline__ void hex_forward(int lane, int gid, const T* sB, const T* sD, T* su, T* s1, T* s2, T* t2,
-                                            T* t3, T* gx, T* gy, T* gz, T* uq) {
-  constexpr int N2 = N * N, G = HexCfg<N>::G;
+__device__ __forceinline__ void hex_forward(int lane, int gid, T* su, T* s1, T* s2, T* t2, T* t3, T* gx, T* gy, T* gz,
+                                            T* uq) {
+  constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
+  using TB = CTab<T>;
   T* t1 = su;  // alias: u is consumed by stage 1 before t1 is written
   if (lane < N2) {
     const int a = lane / N, b = lane % N;
@@ -198,7 +283,7 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, const T* sB, cons
     for (int k = 0; k < N; k++) {
       T ub = 0, ud = 0;
 #pragma unroll
-      for (int c = 0; c < N; c++) { ub += sB[k * N + c] * u[c]; ud += sD[k * N + c] * u[c]; }
+      for (int c = 0; c < N; c++) { ub += TB::B(O + k * N + c) * u[c]; ud += TB::D(O + k * N + c) * u[c]; }
       s1[(a * N + b) * N + k] = ub;
       s2[(a * N + b) * N + k] = ud;
     }
@@ -214,9 +299,9 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, const T* sB, cons
       T bb = 0, db = 0, bd = 0;
 #pragma unroll
       for (int b = 0; b < N; b++) {
-        bb += sB[j * N + b] * v1[b];
-        db += sD[j * N + b] * v1[b];
-        bd += sB[j * N + b] * v2[b];
+        bb += TB::B(O + j * N + b) * v1[b];
+        db += TB::D(O + j * N + b) * v1[b];
+        bd += TB::B(O + j * N + b) * v2[b];
       }
       t1[(a * N + j) * N + k] = bb;
       t2[(a * N + j) * N + k] = db;
@@ -238,10 +323,10 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, const T* sB, cons
       T x = 0, y = 0, z = 0, uu = 0;
 #pragma unroll
       for (int a = 0; a < N; a++) {
-        x += sD[i * N + a] * w1[a];
-        y += sB[i * N + a] * w2[a];
-        z += sB[i * N + a] * w3[a];
-        if (WANT_U) uu += sB[i * N + a] * w1[a];
+        x += TB::D(O + i * N + a) * w1[a];
+        y += TB::B(O + i * N + a) * w2[a];
+        z += TB::B(O + i * N + a) * w3[a];
+        if (WANT_U) uu += TB::B(O + i * N + a) * w1[a];
       }
       gx[i] = x; gy[i] = y; gz[i] = z;
       if (WANT_U) uq[i] = uu;
@@ -253,9 +338,10 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, const T* sB, cons
 // Transposed chain: lane (j,k) holds vx,vy,vz (and vm) at its qp column ->
 // element residual in su[(a*N+b)*N+c].
 template <int N, class T, bool WANT_M>
-__device__ __forceinline__ void hex_backward(int lane, int gid, const T* sB, const T* sD, T* su, T* s1, T* s2, T* t2,
-                                             T* t3, const T* vx, const T* vy, const T* vz, const T* vm) {
-  constexpr int N2 = N * N, G = HexCfg<N>::G;
+__device__ __forceinline__ void hex_backward(int lane, int gid, T* su, T* s1, T* s2, T* t2, T* t3, const T* vx,
+                                             const T* vy, const T* vz, const T* vm) {
+  constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
+  using TB = CTab<T>;
   T* t1 = su;
   if (lane < N2) {
     const int j = lane / N, k = lane % N;
@@ -264,10 +350,10 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, const T* sB, con
       T w1 = 0, w2 = 0, w3 = 0;
 #pragma unroll
       for (int i = 0; i < N; i++) {
-        w1 += sD[i * N + a] * vx[i];
-        if (WANT_M) w1 += sB[i * N + a] * vm[i];
-        w2 += sB[i * N + a] * vy[i];
-        w3 += sB[i * N + a] * vz[i];
+        w1 += TB::D(O + i * N + a) * vx[i];
+        if (WANT_M) w1 += TB::B(O + i * N + a) * vm[i];
+        w2 += TB::B(O + i * N + a) * vy[i];
+        w3 += TB::B(O + i * N + a) * vz[i];
       }
       t1[(a * N + j) * N + k] = w1;
       t2[(a * N + j) * N + k] = w2;
@@ -289,8 +375,8 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, const T* sB, con
       T v1 = 0, v2 = 0;
 #pragma unroll
       for (int j = 0; j < N; j++) {
-        v1 += sB[j * N + b] * r1[j] + sD[j * N + b] * r2[j];
-        v2 += sB[j * N + b] * r3[j];
+        v1 += TB::B(O + j * N + b) * r1[j] + TB::D(O + j * N + b) * r2[j];
+        v2 += TB::B(O + j * N + b) * r3[j];
       }
       s1[(a * N + b) * N + k] = v1;
       s2[(a * N + b) * N + k] = v2;
@@ -306,7 +392,7 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, const T* sB, con
     for (int c = 0; c < N; c++) {
       T v = 0;
 #pragma unroll
-      for (int k = 0; k < N; k++) v += sB[k * N + c] * r1[k] + sD[k * N + c] * r2[k];
+      for (int k = 0; k < N; k++) v += TB::B(O + k * N + c) * r1[k] + TB::D(O + k * N + c) * r2[k];
       su[(a * N + b) * N + c] = v;
     }
   }
@@ -314,60 +400,167 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, const T* sB, con
 }
 
 // y += A x over all hex elements; optional energy sum_e x_e^T A_e x_e.
+// Persistent element groups; per element e of a group (DOF-row buffer b):
+//   lane 0 bulk-copies (TMA) the DOF-table row of the NEXT element into buffer
+//   b^1 (mbarrier T[b^1]);
+//   forward contractions of e;
+//   wait for T[b^1] and issue the x gather of the next element into registers
+//   (the loads complete under the remaining work of e);
+//   wait for the G tile of e (mbarrier Gb), quadrature-point transform, then
+//   lane 0 bulk-copies the G tile of the next element into the same buffer;
+//   transposed contractions and scatter (DOFs >= first_cell belong to e
+//   alone: plain stores, the rest atomic adds).
 // skip != NULL: the kernel returns immediately when *skip != 0 (CG finished).
-template <int N, class T, bool MASS>
+template <int N, class T, bool MASS, int GM>
 __global__ void __launch_bounds__(HexCfg<N>::BLOCK)
-hex_apply_kernel(int ne, const int* __restrict__ tdof, const T* __restrict__ Gq, const T* __restrict__ Mq,
-                 const T* __restrict__ x, T* __restrict__ y, const T* __restrict__ Bg, const T* __restrict__ Dg,
-                 double* partial, unsigned int* counter, double* energy, const int* skip) {
+hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __restrict__ Gq, int gstride,
+                 const T* __restrict__ x, T* __restrict__ y, int first_cell, double* partial, unsigned int* counter,
+                 double* energy, const int* skip, int* err) {
   using C = HexCfg<N>;
+  using SM = HexSmem<N, T>;
   constexpr int N2 = C::N2, N3 = C::N3, G = C::G;
+  constexpr int NG = (N3 + G - 1) / G;  // gathered values per lane
   if (skip && *(volatile const int*)skip) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sB = (T*)smem_raw;
-  T* sD = sB + N2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int gid = threadIdx.x / G, lane = threadIdx.x % G;
-  T* base = sD + N2 + (size_t)gid * 5 * N3;
-  T *su = base, *s1 = base + N3, *s2 = base + 2 * N3, *t2 = base + 3 * N3, *t3 = base + 4 * N3;
-  int* sidx = (int*)(sD + N2 + (size_t)C::EPB * 5 * N3) + gid * N3;
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) { sB[t] = Bg[t]; sD[t] = Dg[t]; }
+  const size_t gb = GM == 0 ? SM::gbytes(gstride) : 0, tb = SM::tbytes(tstride);
+  unsigned char* gp = smem_raw + SM::tables + (size_t)gid * SM::group(gstride, tstride, GM);
+  T* gbuf = (T*)gp;
+  auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };  // arithmetic keeps them out of local memory
+  T* work = (T*)(gp + gb + 2 * tb);
+  T *su = work, *s1 = work + N3, *s2 = work + 2 * N3, *t2 = work + 3 * N3, *t3 = work + 4 * N3;
+  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + SM::work);  // [0],[1]: DOF rows, [2]: G tile
+  if (lane == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    fence_mbar_init();
+  }
   __syncthreads();
+  const int stride = gridDim.x * C::EPB;
+  int e = blockIdx.x * C::EPB + gid;
+  auto issue_t = [&](int el, int b) {
+    mbar_expect_tx(&mbar[b], (uint32_t)tb);
+    bulk_g2s(tbuf(b), tdof + (size_t)el * tstride, (uint32_t)tb, &mbar[b]);
+  };
+  auto issue_g = [&](int el) {
+    mbar_expect_tx(&mbar[2], (uint32_t)gb);
+    bulk_g2s(gbuf, Gq + (size_t)el * gstride, (uint32_t)gb, &mbar[2]);
+  };
+  T xr[NG];   // gathered (signed) coefficients of the element about to be computed
   T acc = 0;  // per-lane energy in the working precision (FP64 throughput is scarce)
-  for (int e = blockIdx.x * C::EPB + gid; e < ne; e += gridDim.x * C::EPB) {
-    const int* td = tdof + (size_t)e * N3;
-    for (int t = lane; t < N3; t += G) {
-      int d = __ldg(td + t);
-      sidx[t] = d;
-      T v = __ldg(x + (d & 0x7fffffff));
-      su[t] = d < 0 ? -v : v;
+  int t_issued = 0, t_waited = 0, g_issued = 0, g_waited = 0;
+  bool ok = true;
+  if (e < ne) {
+    if (lane == 0) {
+      issue_t(e, 0);
+      if (GM == 0) issue_g(e);
     }
+    t_issued = 1;
+    g_issued = GM == 0 ? 1 : 0;
+    ok = group_all<G>(gid, mbar_wait_bounded(&mbar[0], 0));
+    t_waited = 1;
+    if (ok) {
+      const int* td = tbuf(0);
+#pragma unroll
+      for (int j = 0; j < NG; j++) {
+        const int t = lane + j * G;
+        if (t < N3) {
+          const int d = td[t];
+          const T v = __ldg(x + (d & 0x7fffffff));
+          xr[j] = d < 0 ? -v : v;
+        }
+      }
+    }
+  }
+  for (int k = 0; ok && e < ne; e += stride, k++) {
+    const int b = k & 1;
+    const bool has_next = e + stride < ne;
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int t = lane + j * G;
+      if (t < N3) su[t] = xr[j];
+    }
+    if (lane == 0 && has_next) {
+      fence_proxy_async();  // DOF-row buffer b^1 was last read through the generic proxy
+      issue_t(e + stride, b ^ 1);
+    }
+    if (has_next) t_issued++;
     group_sync<G>(gid);
     T gx[N], gy[N], gz[N], uq[N];
-    hex_forward<N, T, MASS>(lane, gid, sB, sD, su, s1, s2, t2, t3, gx, gy, gz, uq);
+    hex_forward<N, T, MASS>(lane, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
+    if (has_next) {
+      ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
+      t_waited++;
+      if (!ok) break;
+      const int* tn = tbuf(b ^ 1);
+#pragma unroll
+      for (int j = 0; j < NG; j++) {
+        const int t = lane + j * G;
+        if (t < N3) {
+          const int d = tn[t];
+          const T v = __ldg(x + (d & 0x7fffffff));
+          xr[j] = d < 0 ? -v : v;
+        }
+      }
+    }
+    if (GM == 0) {
+      ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
+      g_waited++;
+      if (!ok) break;
+    }
+    // G mode 0: the tile is in shared memory; mode 1: coalesced loads from HBM
+    const T* Gsrc = GM == 0 ? (const T*)gbuf : Gq + (size_t)e * gstride;
     T vx[N], vy[N], vz[N], vm[N];
     if (lane < N2) {
-      const T* Ge = Gq + (size_t)e * 6 * N3 + lane;
 #pragma unroll
       for (int i = 0; i < N; i++) {
-        const int o = i * N2;
-        T gxx = __ldg(Ge + o), gyy = __ldg(Ge + N3 + o), gzz = __ldg(Ge + 2 * N3 + o);
-        T gxy = __ldg(Ge + 3 * N3 + o), gxz = __ldg(Ge + 4 * N3 + o), gyz = __ldg(Ge + 5 * N3 + o);
+        const int o = i * N2 + lane;
+        T gxx, gyy, gzz, gxy, gxz, gyz;
+        if (GM == 0) {
+          gxx = Gsrc[o]; gyy = Gsrc[N3 + o]; gzz = Gsrc[2 * N3 + o];
+          gxy = Gsrc[3 * N3 + o]; gxz = Gsrc[4 * N3 + o]; gyz = Gsrc[5 * N3 + o];
+        } else {
+          gxx = __ldcs(Gsrc + o); gyy = __ldcs(Gsrc + N3 + o); gzz = __ldcs(Gsrc + 2 * N3 + o);
+          gxy = __ldcs(Gsrc + 3 * N3 + o); gxz = __ldcs(Gsrc + 4 * N3 + o); gyz = __ldcs(Gsrc + 5 * N3 + o);
+        }
         vx[i] = gxx * gx[i] + gxy * gy[i] + gxz * gz[i];
         vy[i] = gxy * gx[i] + gyy * gy[i] + gyz * gz[i];
         vz[i] = gxz * gx[i] + gyz * gy[i] + gzz * gz[i];
         T en = gx[i] * vx[i] + gy[i] * vy[i] + gz[i] * vz[i];
         if (MASS) {
-          vm[i] = __ldg(Mq + (size_t)e * N3 + o + lane) * uq[i];
+          vm[i] = (GM == 0 ? Gsrc[6 * N3 + o] : __ldcs(Gsrc + 6 * N3 + o)) * uq[i];
           en += uq[i] * vm[i];
         }
         acc += en;
       }
     }
-    hex_backward<N, T, MASS>(lane, gid, sB, sD, su, s1, s2, t2, t3, vx, vy, vz, vm);
+    if (GM == 0) {
+      group_sync<G>(gid);  // everyone is done with the G tile
+      if (lane == 0 && has_next) {
+        fence_proxy_async();
+        issue_g(e + stride);
+      }
+      if (has_next) g_issued++;
+    }
+    hex_backward<N, T, MASS>(lane, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
+    const int* td = tbuf(b);
     for (int t = lane; t < N3; t += G) {
-      int d = sidx[t];
-      T v = su[t];
-      atomic_add_t(y + (d & 0x7fffffff), d < 0 ? -v : v);
+      const int d = td[t];
+      const int dof = d & 0x7fffffff;
+      const T v = d < 0 ? -su[t] : su[t];
+      if (dof >= first_cell) y[dof] = v;  // element-interior DOF: single writer
+      else atomic_add_t(y + dof, v);
+    }
+    group_sync<G>(gid);
+  }
+  if (!ok) {
+    // record the failure, then give the copies still in flight a bounded chance
+    // to land before the block (and its shared memory) retires
+    if (lane == 0) {
+      atomicExch(err, 1);
+      for (int j = t_waited; j < t_issued; j++) mbar_wait_bounded(&mbar[j & 1], (j >> 1) & 1);
+      for (int j = g_waited; j < g_issued; j++) mbar_wait_bounded(&mbar[2], j & 1);
     }
     group_sync<G>(gid);
   }
@@ -377,42 +570,37 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, const T* __restrict__ Gq,
 // element-wise  int_e grad u . grad w  (geometry from G / kappa_e)
 template <int N>
 __global__ void __launch_bounds__(HexCfg<N>::BLOCK)
-hex_graddot_kernel(int ne, const int* __restrict__ tdof, const double* __restrict__ Gq, const double* __restrict__ kappa,
-                   const double* __restrict__ u, const double* __restrict__ w, const double* __restrict__ Bg,
-                   const double* __restrict__ Dg, double* out) {
+hex_graddot_kernel(int ne, const int* __restrict__ tdof, int tstride, const double* __restrict__ Gq, int gstride,
+                   const double* __restrict__ kappa, const double* __restrict__ u, const double* __restrict__ w, double* out) {
   using C = HexCfg<N>;
   using T = double;
   constexpr int N2 = C::N2, N3 = C::N3, G = C::G;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sB = (T*)smem_raw;
-  T* sD = sB + N2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int gid = threadIdx.x / G, lane = threadIdx.x % G;
-  T* base = sD + N2 + (size_t)gid * 5 * N3;
+  T* base = (T*)(smem_raw + HexSmem<N, T>::tables) + (size_t)gid * 5 * N3;
   T *su = base, *s1 = base + N3, *s2 = base + 2 * N3, *t2 = base + 3 * N3, *t3 = base + 4 * N3;
   __shared__ double red[C::EPB][(C::G + 31) / 32];
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) { sB[t] = Bg[t]; sD[t] = Dg[t]; }
-  __syncthreads();
   for (int e0 = blockIdx.x * C::EPB; e0 < ne; e0 += gridDim.x * C::EPB) {
     int e = e0 + gid;
     bool valid = e < ne;
     T ux[N], uy[N], uz[N], wx[N], wy[N], wz[N], dummy[N];
     for (int t = lane; t < N3; t += G) {
-      int d = valid ? tdof[(size_t)e * N3 + t] : 0;
+      int d = valid ? tdof[(size_t)e * tstride + t] : 0;
       T v = valid ? u[d & 0x7fffffff] : 0.0;
       su[t] = d < 0 ? -v : v;
     }
     group_sync<G>(gid);
-    hex_forward<N, T, false>(lane, gid, sB, sD, su, s1, s2, t2, t3, ux, uy, uz, dummy);
+    hex_forward<N, T, false>(lane, gid, su, s1, s2, t2, t3, ux, uy, uz, dummy);
     for (int t = lane; t < N3; t += G) {
-      int d = valid ? tdof[(size_t)e * N3 + t] : 0;
+      int d = valid ? tdof[(size_t)e * tstride + t] : 0;
       T v = valid ? w[d & 0x7fffffff] : 0.0;
       su[t] = d < 0 ? -v : v;
     }
     group_sync<G>(gid);
-    hex_forward<N, T, false>(lane, gid, sB, sD, su, s1, s2, t2, t3, wx, wy, wz, dummy);
+    hex_forward<N, T, false>(lane, gid, su, s1, s2, t2, t3, wx, wy, wz, dummy);
     double acc = 0;
     if (lane < N2 && valid) {
-      const T* Ge = Gq + (size_t)e * 6 * N3 + lane;
+      const T* Ge = Gq + (size_t)e * gstride + lane;
       double ik = 1.0 / kappa[e];
       for (int i = 0; i < N; i++) {
         const int o = i * N2;
@@ -434,15 +622,15 @@ hex_graddot_kernel(int ne, const int* __restrict__ tdof, const double* __restric
 }
 
 // diagonal of the hex operator: one thread per (element, tensor index)
-__global__ void hex_diag_kernel(int ne, int N, const int* __restrict__ tdof, const double* __restrict__ Gq,
-                                const double* __restrict__ Mq, const double* __restrict__ B, const double* __restrict__ D,
+__global__ void hex_diag_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ Gq,
+                                int gstride, int mass, const double* __restrict__ B, const double* __restrict__ D,
                                 double* diag) {
   const int N3 = N * N * N;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * N3) return;
   int e = (int)(id / N3), t = (int)(id % N3);
   int a = t / (N * N), b = (t / N) % N, c = t % N;
-  const double* Ge = Gq + (size_t)e * 6 * N3;
+  const double* Ge = Gq + (size_t)e * gstride;
   double s = 0;
   for (int i = 0; i < N; i++) {
     double Ba = B[i * N + a], Da = D[i * N + a];
@@ -454,11 +642,11 @@ __global__ void hex_diag_kernel(int ne, int N, const int* __restrict__ tdof, con
         double gx = Da * Bb * Bc, gy = Ba * Db * Bc, gz = Ba * Bb * Dc;
         s += Ge[q] * gx * gx + Ge[N3 + q] * gy * gy + Ge[2 * N3 + q] * gz * gz +
              2 * (Ge[3 * N3 + q] * gx * gy + Ge[4 * N3 + q] * gx * gz + Ge[5 * N3 + q] * gy * gz);
-        if (Mq) { double v = Ba * Bb * Bc; s += Mq[(size_t)e * N3 + q] * v * v; }
+        if (mass) { double v = Ba * Bb * Bc; s += Ge[6 * N3 + q] * v * v; }
       }
     }
   }
-  atomicAdd(diag + (tdof[id] & 0x7fffffff), s);
+  atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), s);
 }
 
 // ---------------------------------------------------------------------------
@@ -567,76 +755,136 @@ __global__ void tet_graddot_kernel(int ne, int nloc, int nq, const int* __restri
 
 // ---------------------------------------------------------------------------
 // host drivers
-// sets the dynamic shared-memory limit and returns resident blocks per SM;
-// done once per instantiation, outside any stream capture (called at setup)
-template <int N, class T, bool MASS>
-int hex_apply_prepare() {
-  static int per_sm = -1;
-  if (per_sm < 0) {
-    size_t smem = hex_smem_bytes<N, T>();
-    GH1_CUDA(cudaFuncSetAttribute(hex_apply_kernel<N, T, MASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int v = 0;
-    GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, hex_apply_kernel<N, T, MASS>, HexCfg<N>::BLOCK, smem));
-    per_sm = v < 1 ? 1 : v;
+// raises the dynamic shared-memory limit of one instantiation (once) and
+// returns its resident blocks per SM for a given shared-memory size; called at
+// setup, outside any stream capture, and cached in the operator
+template <int N, class T, bool MASS, int GM>
+int hex_apply_occupancy(size_t smem) {
+  static bool attr = false;
+  auto kern = hex_apply_kernel<N, T, MASS, GM>;
+  if (!attr) {
+    int dev = 0, optin = 0;
+    GH1_CUDA(cudaGetDevice(&dev));
+    GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+    GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    attr = true;
   }
-  return per_sm;
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, HexCfg<N>::BLOCK, smem));
+  GH1_CHECK(v >= 1, GH1_ERR_UNSUPPORTED, "hex apply does not fit on an SM (shared memory)");
+  return v;
 }
 
-void hex_prepare_all(int N) {
-#define GH1_PREP(NN)                                                                              \
-  case NN:                                                                                        \
-    hex_apply_prepare<NN, float, false>(); hex_apply_prepare<NN, float, true>();                  \
-    hex_apply_prepare<NN, double, false>(); hex_apply_prepare<NN, double, true>();                \
-    break;
-  switch (N) {
-    GH1_PREP(2) GH1_PREP(3) GH1_PREP(4) GH1_PREP(5) GH1_PREP(6) GH1_PREP(7) GH1_PREP(8) GH1_PREP(9)
-    default: break;
-  }
-#undef GH1_PREP
-}
-
-template <int N, class T, bool MASS>
-void launch_hex_apply(gh1_op* op, const T* x, T* y, const T* G, const T* M, double* partial, unsigned int* counter,
-                      double* energy, const int* skip, int nblocks_override = 0) {
+template <int N, class T, bool MASS, int GM>
+void launch_hex_apply(gh1_op* op, const T* x, T* y, const T* G, int gstride, double* partial, unsigned int* counter,
+                      double* energy, const int* skip) {
   using C = HexCfg<N>;
   gh1_space* sp = op->sp;
-  size_t smem = hex_smem_bytes<N, T>();
-  const int per_sm = hex_apply_prepare<N, T, MASS>();
-  int ne = sp->mesh->ne;
-  int blocks_needed = (ne + C::EPB - 1) / C::EPB;
-  int grid = std::min(blocks_needed, sp->ctx->nsm * per_sm);
-  if (nblocks_override > 0) grid = std::min(blocks_needed, nblocks_override);
-  const T* Bt = std::is_same<T, float>::value ? (const T*)sp->d_B32.p : (const T*)sp->d_B64.p;
-  const T* Dt = std::is_same<T, float>::value ? (const T*)sp->d_D32.p : (const T*)sp->d_D64.p;
-  hex_apply_kernel<N, T, MASS><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(ne, sp->d_tdof.p, G, M, x, y, Bt, Dt, partial,
-                                                                           counter, energy, skip);
+  const size_t smem = HexSmem<N, T>::total(gstride, sp->tstride, GM);
+  const int pi = std::is_same<T, float>::value ? 1 : 0;
+  const int per_sm = op->hex_per_sm[pi][GM];
+  GH1_CHECK(per_sm > 0, GH1_ERR_ARG, "internal: hex apply occupancy not prepared");
+  const int ne = sp->mesh->ne;
+  const int blocks_needed = (ne + C::EPB - 1) / C::EPB;
+  const int grid = std::min(blocks_needed, sp->ctx->nsm * per_sm);
+  hex_apply_kernel<N, T, MASS, GM><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(
+      ne, sp->d_tdof.p, sp->tstride, G, gstride, x, y, (int)sp->first_cell, partial, counter, energy, skip, op->d_err.p);
   check_kernel(sp->ctx, "hex_apply_kernel");
 }
 
-template <class T>
-void hex_apply_dispatch(gh1_op* op, const T* x, T* y, const T* G, const T* M, double* partial, unsigned int* counter,
-                        double* energy, const int* skip) {
-  const int N = op->sp->p + 1;
-  bool mass = M != nullptr;
-#define GH1_HEX_CASE(NN)                                                                                  \
-  case NN:                                                                                                \
-    if (mass) launch_hex_apply<NN, T, true>(op, x, y, G, M, partial, counter, energy, skip);             \
-    else launch_hex_apply<NN, T, false>(op, x, y, G, M, partial, counter, energy, skip);                 \
-    break;
-  switch (N) {
-    GH1_HEX_CASE(2) GH1_HEX_CASE(3) GH1_HEX_CASE(4) GH1_HEX_CASE(5) GH1_HEX_CASE(6) GH1_HEX_CASE(7)
-    GH1_HEX_CASE(8) GH1_HEX_CASE(9)
-    default: throw Error(GH1_ERR_UNSUPPORTED, "hex order out of range");
+#define GH1_HEX_SWITCH(N, CASE)                                                                        \
+  switch (N) {                                                                                         \
+    CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)                                   \
+    default: throw Error(GH1_ERR_UNSUPPORTED, "hex order out of range");                              \
   }
+
+template <class T, int GM>
+void hex_apply_dispatch_gm(gh1_op* op, const T* x, T* y, const T* G, int gstride, double* partial,
+                           unsigned int* counter, double* energy, const int* skip) {
+  const bool mass = op->has_mass;
+#define GH1_HEX_CASE(NN)                                                                                      \
+  case NN:                                                                                                    \
+    if (mass) launch_hex_apply<NN, T, true, GM>(op, x, y, G, gstride, partial, counter, energy, skip);       \
+    else launch_hex_apply<NN, T, false, GM>(op, x, y, G, gstride, partial, counter, energy, skip);           \
+    break;
+  GH1_HEX_SWITCH(op->sp->p + 1, GH1_HEX_CASE)
 #undef GH1_HEX_CASE
 }
 
-int matfree_grid_blocks(gh1_op* op) {
-  // number of blocks the apply launches (sizes the partial-sum buffer)
-  gh1_space* sp = op->sp;
-  int ne = sp->mesh->ne;
-  if (sp->et == 4) return std::max(1, std::min((ne + 7) / 8, sp->ctx->nsm * 8));
-  return std::max(1, std::min(ne, sp->ctx->nsm * 32));
+template <class T>
+void hex_apply_dispatch(gh1_op* op, const T* x, T* y, const T* G, int gstride, double* partial, unsigned int* counter,
+                        double* energy, const int* skip) {
+  const int pi = std::is_same<T, float>::value ? 1 : 0;
+  if (op->hex_gmode[pi] == 0) hex_apply_dispatch_gm<T, 0>(op, x, y, G, gstride, partial, counter, energy, skip);
+  else hex_apply_dispatch_gm<T, 1>(op, x, y, G, gstride, partial, counter, energy, skip);
+}
+
+template <class T, int GM>
+int hex_occupancy_dispatch(gh1_op* op, int gstride) {
+  const bool mass = op->has_mass;
+  const int tstride = op->sp->tstride;
+  int v = 0;
+#define GH1_OCC_CASE(NN)                                                                                        \
+  case NN:                                                                                                      \
+    v = mass ? hex_apply_occupancy<NN, T, true, GM>(HexSmem<NN, T>::total(gstride, tstride, GM))               \
+             : hex_apply_occupancy<NN, T, false, GM>(HexSmem<NN, T>::total(gstride, tstride, GM));             \
+    break;
+  GH1_HEX_SWITCH(op->sp->p + 1, GH1_OCC_CASE)
+#undef GH1_OCC_CASE
+  return v;
+}
+
+// Autotuner: times each G-staging variant (TMA tile in shared memory vs direct
+// coalesced loads) on this operator's own mesh and keeps the faster one.  The
+// choice is cached per (order, precision, element-count bucket) for the process.
+template <class T>
+void hex_autotune(gh1_op* op, const T* G, int gstride) {
+  const int pi = std::is_same<T, float>::value ? 1 : 0;
+  const char* env = getenv("GH1_HEX_GMODE");
+  if (env && (env[0] == '0' || env[0] == '1')) {
+    op->hex_gmode[pi] = env[0] - '0';
+    return;
+  }
+  static std::vector<std::array<int, 4>> cache;  // N, precision, log2(ne), choice
+  const int N = op->sp->p + 1, ne = op->sp->mesh->ne;
+  int lb = 0;
+  while ((1 << (lb + 1)) <= ne) lb++;
+  for (auto& c : cache)
+    if (c[0] == N && c[1] == pi && c[2] == lb + (op->has_mass ? 100 : 0)) { op->hex_gmode[pi] = c[3]; return; }
+  if (ne < 4096) {  // small meshes: no measurable difference, skip the timing
+    op->hex_gmode[pi] = 0;
+    return;
+  }
+  cudaStream_t s = op->sp->ctx->stream;
+  DBuf<T> xs(op->nrows), ys(op->nrows);
+  xs.zero(s);
+  cudaEvent_t a, b;
+  GH1_CUDA(cudaEventCreate(&a));
+  GH1_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  int choice = 0;
+  for (int gm = 0; gm < 2; gm++) {
+    op->hex_gmode[pi] = gm;
+    for (int r = 0; r < 2; r++) hex_apply_dispatch<T>(op, xs.p, ys.p, G, gstride, nullptr, nullptr, nullptr, nullptr);
+    GH1_CUDA(cudaEventRecord(a, s));
+    for (int r = 0; r < 3; r++) hex_apply_dispatch<T>(op, xs.p, ys.p, G, gstride, nullptr, nullptr, nullptr, nullptr);
+    GH1_CUDA(cudaEventRecord(b, s));
+    GH1_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    GH1_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (ms < best) { best = ms; choice = gm; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  op->hex_gmode[pi] = choice;
+  cache.push_back({N, pi, lb + (op->has_mass ? 100 : 0), choice});
+}
+
+static int pad16(int count, int elem_bytes) {
+  const int per = 16 / elem_bytes;
+  return (count + per - 1) / per * per;
 }
 
 void matfree_setup(gh1_op* op) {
@@ -644,24 +892,33 @@ void matfree_setup(gh1_op* op) {
   gh1_form* f = op->form;
   cudaStream_t s = sp->ctx->stream;
   const int ne = sp->mesh->ne;
-  const bool want64 = true;  // the FP64 copy also serves the diagonal and the adjoint contraction
-  const bool want32 = (op->prec_mask & 2) != 0;
+  const bool want32 = (op->prec_mask & 2) != 0;  // FP64 data always exists: diagonal, adjoint, refinement
   op->has_mass = f->has_mu;
+  if (op->d_err.n == 0) {
+    op->d_err.alloc(1);
+    op->d_err.zero(s);
+  }
   if (sp->et == 8) {
     const int nq = sp->nq1 * sp->nq1 * sp->nq1;
-    op->d_G64.alloc((size_t)ne * 6 * nq);
-    if (want32) op->d_G32.alloc((size_t)ne * 6 * nq); else op->d_G32.release();
-    if (op->has_mass) {
-      op->d_M64.alloc((size_t)ne * nq);
-      if (want32) op->d_M32.alloc((size_t)ne * nq);
-    }
+    op->ncomp = op->has_mass ? 7 : 6;
+    op->gstride64 = pad16(op->ncomp * nq, 8);
+    op->gstride32 = pad16(op->ncomp * nq, 4);
+    op->d_G64.alloc((size_t)ne * op->gstride64);
+    if (want32) op->d_G32.alloc((size_t)ne * op->gstride32); else op->d_G32.release();
     int64_t tot = (int64_t)ne * nq;
     hex_geom_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
         ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_kappa.p,
-        op->has_mass ? f->d_mu.p : nullptr, want64 ? op->d_G64.p : nullptr, want32 ? op->d_G32.p : nullptr,
-        op->has_mass ? op->d_M64.p : nullptr, (op->has_mass && want32) ? op->d_M32.p : nullptr);
+        op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
     check_kernel(sp->ctx, "hex_geom_kernel");
-    hex_prepare_all(sp->p + 1);
+    upload_const_tables(sp);
+    op->hex_per_sm[0][0] = hex_occupancy_dispatch<double, 0>(op, op->gstride64);
+    op->hex_per_sm[0][1] = hex_occupancy_dispatch<double, 1>(op, op->gstride64);
+    if (want32) {
+      op->hex_per_sm[1][0] = hex_occupancy_dispatch<float, 0>(op, op->gstride32);
+      op->hex_per_sm[1][1] = hex_occupancy_dispatch<float, 1>(op, op->gstride32);
+    }
+    hex_autotune<double>(op, op->d_G64.p, op->gstride64);
+    if (want32) hex_autotune<float>(op, op->d_G32.p, op->gstride32);
   } else {
     op->d_G64.alloc((size_t)ne * 6);
     if (want32) op->d_G32.alloc((size_t)ne * 6); else op->d_G32.release();
@@ -702,11 +959,11 @@ void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* part
   gh1_space* sp = op->sp;
   if (sp->et == 8) {
     if (prec == GH1_F64)
-      hex_apply_dispatch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->has_mass ? op->d_M64.p : nullptr,
-                                 partial, counter, energy, skip);
+      hex_apply_dispatch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->gstride64, partial, counter, energy,
+                                 skip);
     else
-      hex_apply_dispatch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->has_mass ? op->d_M32.p : nullptr,
-                                partial, counter, energy, skip);
+      hex_apply_dispatch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->gstride32, partial, counter, energy,
+                                skip);
   } else {
     GH1_CHECK(sp->tet_nq_mass <= 128 || !op->has_mass, GH1_ERR_UNSUPPORTED, "tet mass rule too large");
     if (prec == GH1_F64)
@@ -730,8 +987,8 @@ void matfree_diag(gh1_op* op, double* diag) {
   if (sp->et == 8) {
     const int N = sp->p + 1;
     int64_t tot = (int64_t)ne * N * N * N;
-    hex_diag_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(ne, N, sp->d_tdof.p, op->d_G64.p,
-                                                                   op->has_mass ? op->d_M64.p : nullptr, sp->d_B64.p,
+    hex_diag_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, op->d_G64.p,
+                                                                   op->gstride64, op->has_mass ? 1 : 0, sp->d_B64.p,
                                                                    sp->d_D64.p, diag);
     check_kernel(sp->ctx, "hex_diag_kernel");
   } else {
@@ -743,9 +1000,10 @@ void matfree_diag(gh1_op* op, double* diag) {
 }
 
 template <int N>
-void launch_hex_graddot(gh1_space* sp, const double* G, const double* kappa, const double* u, const double* w, double* out) {
+void launch_hex_graddot(gh1_op* op, const double* u, const double* w, double* out) {
   using C = HexCfg<N>;
-  size_t smem = hex_smem_bytes<N, double>();
+  gh1_space* sp = op->sp;
+  const size_t smem = HexSmem<N, double>::tables + (size_t)C::EPB * HexSmem<N, double>::work;
   static bool attr_set = false;
   if (!attr_set) {
     GH1_CUDA(cudaFuncSetAttribute(hex_graddot_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -753,8 +1011,8 @@ void launch_hex_graddot(gh1_space* sp, const double* G, const double* kappa, con
   }
   int ne = sp->mesh->ne;
   int grid = std::max(1, std::min((ne + C::EPB - 1) / C::EPB, sp->ctx->nsm * 16));
-  hex_graddot_kernel<N><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(ne, sp->d_tdof.p, G, kappa, u, w, sp->d_B64.p,
-                                                                    sp->d_D64.p, out);
+  hex_graddot_kernel<N><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(ne, sp->d_tdof.p, sp->tstride, op->d_G64.p,
+                                                                    op->gstride64, op->form->d_kappa.p, u, w, out);
   check_kernel(sp->ctx, "hex_graddot_kernel");
 }
 
@@ -775,17 +1033,12 @@ void elem_grad_dot_with(gh1_op* op, const double* u, const double* w, double* ou
   gh1_space* sp = op->sp;
   const double* kappa = op->form->d_kappa.p;
   if (sp->et == 8) {
-    switch (sp->p + 1) {
-      case 2: launch_hex_graddot<2>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 3: launch_hex_graddot<3>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 4: launch_hex_graddot<4>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 5: launch_hex_graddot<5>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 6: launch_hex_graddot<6>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 7: launch_hex_graddot<7>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 8: launch_hex_graddot<8>(sp, op->d_G64.p, kappa, u, w, out); break;
-      case 9: launch_hex_graddot<9>(sp, op->d_G64.p, kappa, u, w, out); break;
-      default: throw Error(GH1_ERR_UNSUPPORTED, "hex order out of range");
-    }
+#define GH1_GD_CASE(NN) \
+  case NN:              \
+    launch_hex_graddot<NN>(op, u, w, out); \
+    break;
+    GH1_HEX_SWITCH(sp->p + 1, GH1_GD_CASE)
+#undef GH1_GD_CASE
   } else {
     int ne = sp->mesh->ne;
     tet_graddot_kernel<<<(ne + 127) / 128, 128, 0, sp->ctx->stream>>>(ne, sp->nloc, sp->tet_nq, sp->d_eldofs.p,

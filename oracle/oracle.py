@@ -47,7 +47,7 @@ def lib():
         L.orc_graph.restype = l
         L.orc_graph.argtypes = [P]
         L.orc_graph_get.argtypes = [P, P, P]
-        L.orc_assemble.argtypes = [P, P, P, P]
+        L.orc_assemble.argtypes = [P, P, P, P, i]
         L.orc_element_matrix.argtypes = [P, i, d, d, P]
         L.orc_spmv.argtypes = [l, P, P, P, d, P, P, i]
         L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
@@ -116,12 +116,14 @@ class OracleSpace:
             self._csr = (rowptr, colind)
         return self._csr
 
-    def assemble(self, kappa=None, mu=None):
+    def assemble(self, kappa=None, mu=None, reverse=False):
+        """CSR of the assembled form; reverse=True sums quadrature points in the
+        opposite order (the rounding noise of the algorithm)."""
         rowptr, colind = self.graph()
         vals = np.zeros(len(colind), dtype=np.float64)
         k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
         m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
-        rc = lib().orc_assemble(self.h, _p(k), _p(m), _p(vals))
+        rc = lib().orc_assemble(self.h, _p(k), _p(m), _p(vals), 1 if reverse else 0)
         if rc != 0:
             raise RuntimeError("illegal dnums in AddElementMatrix")
         return rowptr, colind, vals

@@ -70,8 +70,9 @@ def test_assemble_parity(gpu, kind, p, jit, perm):
     assert np.array_equal(fes.ElementDofs(), S.element_dofs())
     assert np.array_equal(fes.FreeDofs(), S.freedofs().astype(bool))
     orp, oci, ova = S.assemble(kappa=kappa, mu=mu)
+    _, _, noise = S.assemble(kappa=kappa, mu=mu, reverse=True)
     rp, ci, va = a.mat.CSR()
-    csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12)
+    csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12, noise=noise)
 
 
 @pytest.mark.parametrize("kind,p,jit,mass", [("hex", 1, 0.1, False), ("hex", 2, 0.1, True), ("hex", 3, 0.15, False),
@@ -176,8 +177,10 @@ def test_cg_fp64_iterates(gpu, kind, p, matfree):
 
 @pytest.mark.parametrize("kind,p", [("hex", 4), ("tet", 3)])
 def test_cg_mixed_precision(gpu, kind, p):
-    """FP32 inner CG + FP64 refinement reaches 1e-10 true relative residual; the
-    solution is within 1e-9 (relative) of the FP64 oracle solution."""
+    """FP32 inner CG + FP64 refinement reaches 1e-10 true relative residual; run
+    to 1e-11 its solution is within 1e-9 (relative, max norm) of the FP64 oracle
+    solution (the hierarchical basis has cond(A) ~ 1e9 at p=4, so a 1e-10
+    residual alone bounds the error only to ~1e-8)."""
     m = _mesh(kind, 4, 0.1)
     kappa = lognormal(m.ne, 0.5, 14)
     f = np.random.default_rng(15).uniform(-1, 1, m.ne)
@@ -194,6 +197,9 @@ def test_cg_mixed_precision(gpu, kind, p):
                          mode="mixed", stop_rule="true")
     r = gpu.solvers.CG.last_solver.result
     assert r.status == 0 and r.true_relres <= 1e-10 and r.outer >= 1
+    sol = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-11, maxsteps=20000, printrates=False,
+                         mode="mixed", stop_rule="true")
+    assert gpu.solvers.CG.last_solver.result.true_relres <= 1e-11
     S = O.OracleSpace(m.points, m.elements, p)
     orp, oci, ova = S.assemble(kappa=kappa)
     inv = _jacobi_inv(orp, oci, ova, S.freedofs().astype(bool))

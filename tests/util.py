@@ -6,12 +6,13 @@ def lognormal(n, sigma, seed):
     return np.exp(np.random.default_rng(seed).normal(0.0, sigma, n))
 
 
-def csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12):
-    """Pattern bit-exact; every entry within rtol of its row maximum; and within
-    rtol relative wherever |entry| >= 1e-4 of the row maximum.  (Summation-order
-    rounding of an entry is ~1e-16 of the row maximum, so smaller entries --
-    cancellations and orthogonality zeros -- can only be held to the row-scaled
-    bound.)"""
+def csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12, noise=None):
+    """Pattern bit-exact; every entry within rtol of its row maximum; and, on
+    entries >= 1e-2 of the row maximum, within max(rtol, 10*noise) relative,
+    where `noise` is the largest relative change of those entries when the
+    oracle sums its quadrature points in reverse order (the rounding floor of
+    the reference algorithm itself).  Smaller entries -- cancellations and
+    orthogonality zeros -- are held to the row-scaled bound only."""
     assert np.array_equal(rp, orp), "rowptr differs"
     assert np.array_equal(ci, oci), "colind differs"
     rows = np.repeat(np.arange(len(orp) - 1), np.diff(orp))
@@ -20,9 +21,13 @@ def csr_rowscaled_close(rp, ci, va, orp, oci, ova, rtol=1e-12):
     err = np.abs(va - ova)
     scale = rowmax[rows]
     assert np.all(err <= rtol * scale + 1e-300), "row-scaled error %g" % np.max(err / np.maximum(scale, 1e-300))
-    big = np.abs(ova) >= 1e-4 * scale
+    big = np.abs(ova) >= 1e-2 * scale
     rel = err[big] / np.abs(ova[big])
-    assert np.all(rel <= rtol), "relative error %g" % rel.max()
+    tol = rtol
+    if noise is not None:
+        n = np.abs(noise - ova)[big] / np.abs(ova[big])
+        tol = max(rtol, 10 * float(n.max()))
+    assert np.all(rel <= tol), "relative error %g (tolerance %g)" % (rel.max(), tol)
 
 
 def permute_tets(elements, seed):
