@@ -201,20 +201,41 @@ __global__ void hex_wdet_kernel(int ne, int nq1, const double* __restrict__ X, c
   wdet[id] = gw[i] * gw[j] * gw[k] * fabs(det);
 }
 
-__global__ void hex_rhs_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ wdet,
-                               const double* __restrict__ B, const double* __restrict__ f, double* b) {
-  const int N3 = N * N * N;
-  int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= (int64_t)ne * N3) return;
-  int e = (int)(id / N3), t = (int)(id % N3);
-  int a = t / (N * N), bb = (t / N) % N, c = t % N;
-  double s = 0;
-  for (int i = 0; i < N; i++)
-    for (int j = 0; j < N; j++)
-      for (int k = 0; k < N; k++) s += wdet[(size_t)e * N3 + (i * N + j) * N + k] * B[i * N + a] * B[j * N + bb] * B[k * N + c];
-  int d = tdof[(size_t)e * tstride + t];
-  s *= f[e];
-  atomicAdd(b + (d & 0x7fffffff), d < 0 ? -s : s);
+// b(a,b,c) += f_e sum_i B(i,a) sum_j B(j,b) sum_k B(k,c) wdet(i,j,k): one block per element
+__global__ void __launch_bounds__(128) hex_rhs_kernel(int ne, int N, const int* __restrict__ tdof, int tstride,
+                                                       const double* __restrict__ wdet, const double* __restrict__ B,
+                                                       const double* __restrict__ f, double* b) {
+  extern __shared__ double rsm[];
+  const int N2 = N * N, N3 = N2 * N;
+  double* u = rsm;
+  double* v = rsm + N3;
+  for (int e = blockIdx.x; e < ne; e += gridDim.x) {
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) u[t] = wdet[(size_t)e * N3 + t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) {  // contract k -> c
+      const int ij = t / N, c = t % N;
+      double s = 0;
+      for (int k = 0; k < N; k++) s += B[k * N + c] * u[ij * N + k];
+      v[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) {  // contract j -> b
+      const int i = t / N2, bb = (t / N) % N, c = t % N;
+      double s = 0;
+      for (int j = 0; j < N; j++) s += B[j * N + bb] * v[(i * N + j) * N + c];
+      u[t] = s;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) {  // contract i -> a
+      const int a = t / N2, bc = t % N2;
+      double s = 0;
+      for (int i = 0; i < N; i++) s += B[i * N + a] * u[i * N2 + bc];
+      s *= f[e];
+      const int d = tdof[(size_t)e * tstride + t];
+      atomicAdd(b + (d & 0x7fffffff), d < 0 ? -s : s);
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void tet_rhs_kernel(int ne, int nloc, int nqm, const int* __restrict__ eldofs, const uint8_t* __restrict__ cls,
@@ -247,8 +268,8 @@ void rhs_elementwise(gh1_space* sp, const double* f, double* b) {
     hex_wdet_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p,
                                                                    sp->d_gw.p, wdet.p);
     check_kernel(ctx, "hex_wdet_kernel");
-    tot = (int64_t)ne * N * N * N;
-    hex_rhs_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, wdet.p, sp->d_B64.p, f, b);
+    hex_rhs_kernel<<<std::min(ne, ctx->nsm * 16), 128, 2 * (size_t)N * N * N * sizeof(double), s>>>(
+        ne, N, sp->d_tdof.p, sp->tstride, wdet.p, sp->d_B64.p, f, b);
     check_kernel(ctx, "hex_rhs_kernel");
     GH1_CUDA(cudaStreamSynchronize(s));
   } else {

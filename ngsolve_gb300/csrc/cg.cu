@@ -74,6 +74,21 @@ __device__ bool grid_reduce(double (&v)[K], double* partial, unsigned int* count
 
 constexpr int RED_BLOCK = 256;
 
+// 16-byte vector access for the bandwidth-bound CG updates
+template <class T> struct V16;
+template <> struct V16<float> {
+  using type = float4;
+  static constexpr int W = 4;
+  static __device__ __forceinline__ void get(const type& v, float* o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+  static __device__ __forceinline__ type make(const float* o) { return make_float4(o[0], o[1], o[2], o[3]); }
+};
+template <> struct V16<double> {
+  using type = double2;
+  static constexpr int W = 2;
+  static __device__ __forceinline__ void get(const type& v, double* o) { o[0] = v.x; o[1] = v.y; }
+  static __device__ __forceinline__ type make(const double* o) { return make_double2(o[0], o[1]); }
+};
+
 template <class T>
 __global__ void __launch_bounds__(RED_BLOCK) cg_init_kernel(int64_t n, const T* __restrict__ inv, T* __restrict__ d,
                                                             T* __restrict__ w, T* __restrict__ s, CGState* st, double tol,
@@ -104,6 +119,7 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_init_kernel(int64_t n, const T* 
   }
 }
 
+// x += alpha s; d -= alpha y; w = P d; y = 0; partial sums of w.d and |d_free|^2
 template <class T>
 __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T* __restrict__ inv, T* __restrict__ x,
                                                               T* __restrict__ d, T* __restrict__ w, const T* __restrict__ s,
@@ -119,9 +135,34 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T
     }
     return;
   }
+  using VT = V16<T>;
+  using V = typename VT::type;
+  constexpr int W = VT::W;
   const T alpha = (T)(wd / en);
   T a0 = 0, a1 = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t nv = n / W, tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < nv; i += nth) {
+    T sv[W], yv[W], iv[W], xv[W], dv[W], wv[W];
+    VT::get(((const V*)s)[i], sv);
+    VT::get(((const V*)y)[i], yv);
+    VT::get(((const V*)inv)[i], iv);
+    VT::get(((const V*)x)[i], xv);
+    VT::get(((const V*)d)[i], dv);
+#pragma unroll
+    for (int c = 0; c < W; c++) {
+      xv[c] += alpha * sv[c];
+      dv[c] -= alpha * yv[c];
+      wv[c] = iv[c] * dv[c];
+      a0 += wv[c] * dv[c];
+      if (iv[c] != (T)0) a1 += dv[c] * dv[c];
+      yv[c] = (T)0;
+    }
+    ((V*)x)[i] = VT::make(xv);
+    ((V*)d)[i] = VT::make(dv);
+    ((V*)w)[i] = VT::make(wv);
+    ((V*)y)[i] = VT::make(yv);
+  }
+  for (int64_t i = nv * W + tid; i < n; i += nth) {
     T si = s[i], yi = y[i], iv = inv[i];
     x[i] += alpha * si;
     T di = d[i] - alpha * yi;
@@ -150,13 +191,25 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T
   }
 }
 
+// s = w + beta s
 template <class T>
 __global__ void __launch_bounds__(RED_BLOCK) cg_dir_kernel(int64_t n, const T* __restrict__ w, T* __restrict__ s,
                                                            const CGState* st) {
   if (*(volatile const int*)&st->done) return;
+  using VT = V16<T>;
+  using V = typename VT::type;
+  constexpr int W = VT::W;
   const T beta = (T)st->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s[i] = w[i] + beta * s[i];
+  const int64_t nv = n / W, tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = tid; i < nv; i += nth) {
+    T wv[W], sv[W];
+    VT::get(((const V*)w)[i], wv);
+    VT::get(((const V*)s)[i], sv);
+#pragma unroll
+    for (int c = 0; c < W; c++) sv[c] = wv[c] + beta * sv[c];
+    ((V*)s)[i] = VT::make(sv);
+  }
+  for (int64_t i = nv * W + tid; i < n; i += nth) s[i] = w[i] + beta * s[i];
 }
 
 // r = b - y (FP64), |r_free|^2 and |b_free|^2 ; free = mask
@@ -242,7 +295,7 @@ struct Scratch {
   DBuf<double> norm2;  // [2]
 };
 
-int red_grid(gh1_ctx* ctx, int64_t n) { return grid_for(ctx, n, RED_BLOCK, 4); }
+int red_grid(gh1_ctx* ctx, int64_t n) { return grid_for(ctx, n, RED_BLOCK, 8); }
 
 // operator apply with the device energy sink (y must be zero on entry)
 void op_apply_energy(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter, double* energy,

@@ -199,6 +199,7 @@ template <int N>
 struct HexCfg {
   static constexpr int N2 = N * N, N3 = N * N * N;
   static constexpr int G = ((N2 + 31) / 32) * 32;  // threads per element group
+  static constexpr int EPW = N2 <= 32 ? 32 / N2 : 1;  // elements per group (low orders share a warp)
   static constexpr int EPB = G == 32 ? 4 : 2;      // element groups per block
   static constexpr int BLOCK = G * EPB;
 };
@@ -209,10 +210,11 @@ __host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 
 //   [G tile (G mode 0 only)] | DOF-table tile x2 | 5 work arrays | 3 mbarriers
 template <int N, class T>
 struct HexSmem {
+  static constexpr int W = HexCfg<N>::EPW;
   static constexpr size_t tables = 0;
-  static __host__ __device__ size_t gbytes(int gstride) { return round16((size_t)gstride * sizeof(T)); }
-  static __host__ __device__ size_t tbytes(int tstride) { return round16((size_t)tstride * sizeof(int)); }
-  static constexpr size_t work = round16(5 * (size_t)N * N * N * sizeof(T));
+  static __host__ __device__ size_t gbytes(int gstride) { return W * round16((size_t)gstride * sizeof(T)); }
+  static __host__ __device__ size_t tbytes(int tstride) { return W * round16((size_t)tstride * sizeof(int)); }
+  static constexpr size_t work = round16(5 * (size_t)W * N * N * N * sizeof(T));
   static __host__ __device__ size_t group(int gstride, int tstride, int gmode) {
     return (gmode == 0 ? gbytes(gstride) : 0) + 2 * tbytes(tstride) + work + 32;
   }
@@ -269,13 +271,13 @@ __device__ __forceinline__ bool group_all(int gid, bool v) {
 // components at the qp of lane (j,k) for all i (registers gx[i], gy[i], gz[i]),
 // plus the interpolated value uq[i] when WANT_U.
 template <int N, class T, bool WANT_U>
-__device__ __forceinline__ void hex_forward(int lane, int gid, T* su, T* s1, T* s2, T* t2, T* t3, T* gx, T* gy, T* gz,
-                                            T* uq) {
+__device__ __forceinline__ void hex_forward(int pl, bool active, int gid, T* su, T* s1, T* s2, T* t2, T* t3, T* gx, T* gy,
+                                            T* gz, T* uq) {
   constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
   using TB = CTab<T>;
   T* t1 = su;  // alias: u is consumed by stage 1 before t1 is written
-  if (lane < N2) {
-    const int a = lane / N, b = lane % N;
+  if (active) {
+    const int a = pl / N, b = pl % N;
     T u[N];
 #pragma unroll
     for (int c = 0; c < N; c++) u[c] = su[(a * N + b) * N + c];
@@ -289,8 +291,8 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, T* su, T* s1, T* 
     }
   }
   group_sync<G>(gid);
-  if (lane < N2) {
-    const int a = lane / N, k = lane % N;
+  if (active) {
+    const int a = pl / N, k = pl % N;
     T v1[N], v2[N];
 #pragma unroll
     for (int b = 0; b < N; b++) { v1[b] = s1[(a * N + b) * N + k]; v2[b] = s2[(a * N + b) * N + k]; }
@@ -309,8 +311,8 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, T* su, T* s1, T* 
     }
   }
   group_sync<G>(gid);
-  if (lane < N2) {
-    const int j = lane / N, k = lane % N;
+  if (active) {
+    const int j = pl / N, k = pl % N;
     T w1[N], w2[N], w3[N];
 #pragma unroll
     for (int a = 0; a < N; a++) {
@@ -338,13 +340,13 @@ __device__ __forceinline__ void hex_forward(int lane, int gid, T* su, T* s1, T* 
 // Transposed chain: lane (j,k) holds vx,vy,vz (and vm) at its qp column ->
 // element residual in su[(a*N+b)*N+c].
 template <int N, class T, bool WANT_M>
-__device__ __forceinline__ void hex_backward(int lane, int gid, T* su, T* s1, T* s2, T* t2, T* t3, const T* vx,
-                                             const T* vy, const T* vz, const T* vm) {
+__device__ __forceinline__ void hex_backward(int pl, bool active, int gid, T* su, T* s1, T* s2, T* t2, T* t3,
+                                             const T* vx, const T* vy, const T* vz, const T* vm) {
   constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
   using TB = CTab<T>;
   T* t1 = su;
-  if (lane < N2) {
-    const int j = lane / N, k = lane % N;
+  if (active) {
+    const int j = pl / N, k = pl % N;
 #pragma unroll
     for (int a = 0; a < N; a++) {
       T w1 = 0, w2 = 0, w3 = 0;
@@ -361,8 +363,8 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, T* su, T* s1, T*
     }
   }
   group_sync<G>(gid);
-  if (lane < N2) {
-    const int a = lane / N, k = lane % N;
+  if (active) {
+    const int a = pl / N, k = pl % N;
     T r1[N], r2[N], r3[N];
 #pragma unroll
     for (int j = 0; j < N; j++) {
@@ -383,8 +385,8 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, T* su, T* s1, T*
     }
   }
   group_sync<G>(gid);
-  if (lane < N2) {
-    const int a = lane / N, b = lane % N;
+  if (active) {
+    const int a = pl / N, b = pl % N;
     T r1[N], r2[N];
 #pragma unroll
     for (int k = 0; k < N; k++) { r1[k] = s1[(a * N + b) * N + k]; r2[k] = s2[(a * N + b) * N + k]; }
@@ -400,16 +402,18 @@ __device__ __forceinline__ void hex_backward(int lane, int gid, T* su, T* s1, T*
 }
 
 // y += A x over all hex elements; optional energy sum_e x_e^T A_e x_e.
-// Persistent element groups; per element e of a group (DOF-row buffer b):
-//   lane 0 bulk-copies (TMA) the DOF-table row of the NEXT element into buffer
+// Persistent element groups.  A group works on a chunk of EPW consecutive
+// elements at a time (EPW = 1 for p >= 4; low orders pack several elements into
+// one warp, N*N lanes each).  Per chunk (DOF-row buffer b):
+//   lane 0 bulk-copies (TMA) the DOF-table rows of the NEXT chunk into buffer
 //   b^1 (mbarrier T[b^1]);
-//   forward contractions of e;
-//   wait for T[b^1] and issue the x gather of the next element into registers
-//   (the loads complete under the remaining work of e);
-//   wait for the G tile of e (mbarrier Gb), quadrature-point transform, then
-//   lane 0 bulk-copies the G tile of the next element into the same buffer;
-//   transposed contractions and scatter (DOFs >= first_cell belong to e
-//   alone: plain stores, the rest atomic adds).
+//   forward contractions;
+//   wait for T[b^1] and issue the x gather of the next chunk into registers
+//   (the loads complete under the remaining work);
+//   [G mode 0: wait for the G tiles of this chunk (mbarrier Gb)] quadrature-
+//   point transform, then lane 0 bulk-copies the next chunk's G tiles;
+//   transposed contractions and scatter (DOFs >= first_cell belong to one
+//   element alone: plain stores, the rest atomic adds).
 // skip != NULL: the kernel returns immediately when *skip != 0 (CG finished).
 template <int N, class T, bool MASS, int GM>
 __global__ void __launch_bounds__(HexCfg<N>::BLOCK)
@@ -418,18 +422,22 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
                  double* energy, const int* skip, int* err) {
   using C = HexCfg<N>;
   using SM = HexSmem<N, T>;
-  constexpr int N2 = C::N2, N3 = C::N3, G = C::G;
-  constexpr int NG = (N3 + G - 1) / G;  // gathered values per lane
+  constexpr int N2 = C::N2, N3 = C::N3, G = C::G, EPW = C::EPW, CN3 = EPW * N3;
+  constexpr int NG = (CN3 + G - 1) / G;  // gathered values per lane
   if (skip && *(volatile const int*)skip) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int gid = threadIdx.x / G, lane = threadIdx.x % G;
+  const int slot = lane / N2, pl = lane % N2;  // element slot of this lane and its pencil
+  const size_t rowg = round16((size_t)gstride * sizeof(T)), rowt = round16((size_t)tstride * sizeof(int));
   const size_t gb = GM == 0 ? SM::gbytes(gstride) : 0, tb = SM::tbytes(tstride);
   unsigned char* gp = smem_raw + SM::tables + (size_t)gid * SM::group(gstride, tstride, GM);
   T* gbuf = (T*)gp;
   auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };  // arithmetic keeps them out of local memory
   T* work = (T*)(gp + gb + 2 * tb);
-  T *su = work, *s1 = work + N3, *s2 = work + 2 * N3, *t2 = work + 3 * N3, *t3 = work + 4 * N3;
-  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + SM::work);  // [0],[1]: DOF rows, [2]: G tile
+  const int so = slot < EPW ? slot * N3 : 0;  // this lane's slot offset in the work arrays
+  T *su = work + so, *s1 = work + CN3 + so, *s2 = work + 2 * CN3 + so, *t2 = work + 3 * CN3 + so,
+    *t3 = work + 4 * CN3 + so;
+  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + SM::work);  // [0],[1]: DOF rows, [2]: G tiles
   if (lane == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -437,85 +445,84 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
     fence_mbar_init();
   }
   __syncthreads();
+  const int nch = (ne + EPW - 1) / EPW;
   const int stride = gridDim.x * C::EPB;
-  int e = blockIdx.x * C::EPB + gid;
-  auto issue_t = [&](int el, int b) {
-    mbar_expect_tx(&mbar[b], (uint32_t)tb);
-    bulk_g2s(tbuf(b), tdof + (size_t)el * tstride, (uint32_t)tb, &mbar[b]);
+  int ch = blockIdx.x * C::EPB + gid;
+  auto rows_of = [&](int c) { return min(EPW, ne - c * EPW); };
+  auto issue_t = [&](int c, int b) {
+    const uint32_t bytes = (uint32_t)(rows_of(c) * rowt);
+    mbar_expect_tx(&mbar[b], bytes);
+    bulk_g2s(tbuf(b), tdof + (size_t)c * EPW * tstride, bytes, &mbar[b]);
   };
-  auto issue_g = [&](int el) {
-    mbar_expect_tx(&mbar[2], (uint32_t)gb);
-    bulk_g2s(gbuf, Gq + (size_t)el * gstride, (uint32_t)gb, &mbar[2]);
+  auto issue_g = [&](int c) {
+    const uint32_t bytes = (uint32_t)(rows_of(c) * rowg);
+    mbar_expect_tx(&mbar[2], bytes);
+    bulk_g2s(gbuf, Gq + (size_t)c * EPW * gstride, bytes, &mbar[2]);
   };
-  T xr[NG];   // gathered (signed) coefficients of the element about to be computed
+  auto gather = [&](int c, const int* tn, T* xr) {
+    const int nrow = rows_of(c);
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int t = lane + j * G;
+      xr[j] = 0;
+      if (t < CN3 && t / N3 < nrow) {
+        const int d = tn[(t / N3) * (int)(rowt / sizeof(int)) + t % N3];
+        const T v = __ldg(x + (d & 0x7fffffff));
+        xr[j] = d < 0 ? -v : v;
+      }
+    }
+  };
+  T xr[NG];   // gathered (signed) coefficients of the chunk about to be computed
   T acc = 0;  // per-lane energy in the working precision (FP64 throughput is scarce)
   int t_issued = 0, t_waited = 0, g_issued = 0, g_waited = 0;
   bool ok = true;
-  if (e < ne) {
+  if (ch < nch) {
     if (lane == 0) {
-      issue_t(e, 0);
-      if (GM == 0) issue_g(e);
+      issue_t(ch, 0);
+      if (GM == 0) issue_g(ch);
     }
     t_issued = 1;
     g_issued = GM == 0 ? 1 : 0;
     ok = group_all<G>(gid, mbar_wait_bounded(&mbar[0], 0));
     t_waited = 1;
-    if (ok) {
-      const int* td = tbuf(0);
-#pragma unroll
-      for (int j = 0; j < NG; j++) {
-        const int t = lane + j * G;
-        if (t < N3) {
-          const int d = td[t];
-          const T v = __ldg(x + (d & 0x7fffffff));
-          xr[j] = d < 0 ? -v : v;
-        }
-      }
-    }
+    if (ok) gather(ch, tbuf(0), xr);
   }
-  for (int k = 0; ok && e < ne; e += stride, k++) {
+  for (int k = 0; ok && ch < nch; ch += stride, k++) {
     const int b = k & 1;
-    const bool has_next = e + stride < ne;
+    const bool has_next = ch + stride < nch;
+    const bool active = slot < EPW && ch * EPW + slot < ne;
 #pragma unroll
     for (int j = 0; j < NG; j++) {
       const int t = lane + j * G;
-      if (t < N3) su[t] = xr[j];
+      if (t < CN3) work[t] = xr[j];  // su of every slot
     }
     if (lane == 0 && has_next) {
       fence_proxy_async();  // DOF-row buffer b^1 was last read through the generic proxy
-      issue_t(e + stride, b ^ 1);
+      issue_t(ch + stride, b ^ 1);
     }
     if (has_next) t_issued++;
     group_sync<G>(gid);
     T gx[N], gy[N], gz[N], uq[N];
-    hex_forward<N, T, MASS>(lane, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
+    hex_forward<N, T, MASS>(pl, active, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
     if (has_next) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
       t_waited++;
       if (!ok) break;
-      const int* tn = tbuf(b ^ 1);
-#pragma unroll
-      for (int j = 0; j < NG; j++) {
-        const int t = lane + j * G;
-        if (t < N3) {
-          const int d = tn[t];
-          const T v = __ldg(x + (d & 0x7fffffff));
-          xr[j] = d < 0 ? -v : v;
-        }
-      }
+      gather(ch + stride, tbuf(b ^ 1), xr);
     }
     if (GM == 0) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
       g_waited++;
       if (!ok) break;
     }
-    // G mode 0: the tile is in shared memory; mode 1: coalesced loads from HBM
-    const T* Gsrc = GM == 0 ? (const T*)gbuf : Gq + (size_t)e * gstride;
+    // G mode 0: the tiles are in shared memory; mode 1: coalesced loads from HBM
+    const T* Gsrc = GM == 0 ? (const T*)((const unsigned char*)gbuf + (slot < EPW ? slot : 0) * rowg)
+                            : Gq + ((size_t)ch * EPW + (slot < EPW ? slot : 0)) * gstride;
     T vx[N], vy[N], vz[N], vm[N];
-    if (lane < N2) {
+    if (active) {
 #pragma unroll
       for (int i = 0; i < N; i++) {
-        const int o = i * N2 + lane;
+        const int o = i * N2 + pl;
         T gxx, gyy, gzz, gxy, gxz, gyz;
         if (GM == 0) {
           gxx = Gsrc[o]; gyy = Gsrc[N3 + o]; gzz = Gsrc[2 * N3 + o];
@@ -536,19 +543,21 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
       }
     }
     if (GM == 0) {
-      group_sync<G>(gid);  // everyone is done with the G tile
+      group_sync<G>(gid);  // everyone is done with the G tiles
       if (lane == 0 && has_next) {
         fence_proxy_async();
-        issue_g(e + stride);
+        issue_g(ch + stride);
       }
       if (has_next) g_issued++;
     }
-    hex_backward<N, T, MASS>(lane, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
+    hex_backward<N, T, MASS>(pl, active, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
     const int* td = tbuf(b);
-    for (int t = lane; t < N3; t += G) {
-      const int d = td[t];
+    const int nrow = rows_of(ch);
+    for (int t = lane; t < CN3; t += G) {
+      if (t / N3 >= nrow) continue;
+      const int d = td[(t / N3) * (int)(rowt / sizeof(int)) + t % N3];
       const int dof = d & 0x7fffffff;
-      const T v = d < 0 ? -su[t] : su[t];
+      const T v = d < 0 ? -work[t] : work[t];
       if (dof >= first_cell) y[dof] = v;  // element-interior DOF: single writer
       else atomic_add_t(y + dof, v);
     }
@@ -565,6 +574,162 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
     group_sync<G>(gid);
   }
   if (partial) block_reduce_finish((double)acc, partial, counter, energy);
+}
+
+// Multi-right-hand-side apply for batched solves: Y_r += A X_r for the right-hand
+// sides r < R whose flag active[r] is set (vectors stored rhs-major, stride n).
+// The G tiles and DOF rows of a chunk are bulk-copied once (TMA, mbarriers) and
+// reused for every active right-hand side, so the dominant G stream is read once
+// per R applications.  Per-rhs energies x_r^T A x_r go to energy[r].
+template <int N, class T, bool MASS>
+__global__ void __launch_bounds__(HexCfg<N>::BLOCK)
+hex_apply_multi_kernel(int ne, int64_t n, int R, const int* __restrict__ active, const int* __restrict__ tdof, int tstride,
+                       const T* __restrict__ Gq, int gstride, const T* __restrict__ x, T* __restrict__ y, int first_cell,
+                       double* partial, unsigned int* counter, double* energy, int* err) {
+  using C = HexCfg<N>;
+  using SM = HexSmem<N, T>;
+  constexpr int N2 = C::N2, N3 = C::N3, G = C::G, EPW = C::EPW, CN3 = EPW * N3;
+  constexpr int RMAX = 16;
+  __shared__ float sacc[C::EPB][RMAX];
+  __shared__ int sact[RMAX];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int gid = threadIdx.x / G, lane = threadIdx.x % G;
+  const int slot = lane / N2, pl = lane % N2;
+  const size_t rowg = round16((size_t)gstride * sizeof(T)), rowt = round16((size_t)tstride * sizeof(int));
+  const size_t gb = SM::gbytes(gstride), tb = SM::tbytes(tstride);
+  unsigned char* gp = smem_raw + SM::tables + (size_t)gid * SM::group(gstride, tstride, 0);
+  T* gbuf = (T*)gp;
+  auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };
+  T* work = (T*)(gp + gb + 2 * tb);
+  const int so = slot < EPW ? slot * N3 : 0;
+  T *su = work + so, *s1 = work + CN3 + so, *s2 = work + 2 * CN3 + so, *t2 = work + 3 * CN3 + so,
+    *t3 = work + 4 * CN3 + so;
+  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + SM::work);
+  for (int r = threadIdx.x; r < RMAX; r += blockDim.x) sact[r] = (r < R) ? active[r] : 0;
+  for (int t = threadIdx.x; t < C::EPB * RMAX; t += blockDim.x) (&sacc[0][0])[t] = 0.f;
+  if (lane == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  int any = 0;
+  for (int r = 0; r < R; r++) any |= sact[r];
+  const int nch = (ne + EPW - 1) / EPW;
+  const int stride = gridDim.x * C::EPB;
+  int ch = blockIdx.x * C::EPB + gid;
+  auto rows_of = [&](int c) { return min(EPW, ne - c * EPW); };
+  auto issue = [&](int c, int b) {
+    const uint32_t bt = (uint32_t)(rows_of(c) * rowt), bg = (uint32_t)(rows_of(c) * rowg);
+    mbar_expect_tx(&mbar[b], bt);
+    bulk_g2s(tbuf(b), tdof + (size_t)c * EPW * tstride, bt, &mbar[b]);
+    mbar_expect_tx(&mbar[2], bg);
+    bulk_g2s(gbuf, Gq + (size_t)c * EPW * gstride, bg, &mbar[2]);
+  };
+  int issued = 0, waited = 0;
+  bool ok = true;
+  if (any && ch < nch && lane == 0) issue(ch, 0);
+  if (any && ch < nch) issued = 1;
+  for (int k = 0; any && ok && ch < nch; ch += stride, k++) {
+    const int b = k & 1;
+    ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b], (k >> 1) & 1) && mbar_wait_bounded(&mbar[2], k & 1));
+    waited++;
+    if (!ok) break;
+    const int* td = tbuf(b);
+    const int nrow = rows_of(ch);
+    const bool act_el = slot < EPW && ch * EPW + slot < ne;
+    const T* Ge = (const T*)((const unsigned char*)gbuf + (slot < EPW ? slot : 0) * rowg);
+    for (int r = 0; r < R; r++) {
+      if (!sact[r]) continue;
+      const T* xr = x + (size_t)r * n;
+      T* yr = y + (size_t)r * n;
+      for (int t = lane; t < CN3; t += G) {
+        T v = 0;
+        if (t / N3 < nrow) {
+          const int d = td[(t / N3) * (int)(rowt / sizeof(int)) + t % N3];
+          v = __ldg(xr + (d & 0x7fffffff));
+          if (d < 0) v = -v;
+        }
+        work[t] = v;
+      }
+      group_sync<G>(gid);
+      T gx[N], gy[N], gz[N], uq[N];
+      hex_forward<N, T, MASS>(pl, act_el, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
+      T vx[N], vy[N], vz[N], vm[N];
+      T en = 0;
+      if (act_el) {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+          const int o = i * N2 + pl;
+          T gxx = Ge[o], gyy = Ge[N3 + o], gzz = Ge[2 * N3 + o], gxy = Ge[3 * N3 + o], gxz = Ge[4 * N3 + o],
+            gyz = Ge[5 * N3 + o];
+          vx[i] = gxx * gx[i] + gxy * gy[i] + gxz * gz[i];
+          vy[i] = gxy * gx[i] + gyy * gy[i] + gyz * gz[i];
+          vz[i] = gxz * gx[i] + gyz * gy[i] + gzz * gz[i];
+          en += gx[i] * vx[i] + gy[i] * vy[i] + gz[i] * vz[i];
+          if (MASS) {
+            vm[i] = Ge[6 * N3 + o] * uq[i];
+            en += uq[i] * vm[i];
+          }
+        }
+      }
+      // per-rhs energy: warp sum, one shared-memory add per warp
+      float ef = (float)en;
+      for (int o = 16; o > 0; o >>= 1) ef += __shfl_xor_sync(0xffffffffu, ef, o);
+      if ((lane & 31) == 0) atomicAdd(&sacc[gid][r], ef);
+      hex_backward<N, T, MASS>(pl, act_el, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
+      for (int t = lane; t < CN3; t += G) {
+        if (t / N3 >= nrow) continue;
+        const int d = td[(t / N3) * (int)(rowt / sizeof(int)) + t % N3];
+        const int dof = d & 0x7fffffff;
+        const T v = d < 0 ? -work[t] : work[t];
+        if (dof >= first_cell) yr[dof] = v;
+        else atomic_add_t(yr + dof, v);
+      }
+      group_sync<G>(gid);
+    }
+    // all right-hand sides of this chunk are done: refill both buffers for the next chunk
+    group_sync<G>(gid);
+    if (lane == 0 && ch + stride < nch) {
+      fence_proxy_async();
+      issue(ch + stride, b ^ 1);
+    }
+    if (ch + stride < nch) issued++;
+  }
+  if (!ok) {
+    if (lane == 0) {
+      atomicExch(err, 1);
+      for (int j = waited; j < issued; j++) {
+        mbar_wait_bounded(&mbar[j & 1], (j >> 1) & 1);
+        mbar_wait_bounded(&mbar[2], j & 1);
+      }
+    }
+    group_sync<G>(gid);
+  }
+  // block sums per rhs -> partial[r][block]; the last block totals into energy[r]
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x < RMAX) {
+    float s = 0;
+    for (int g = 0; g < C::EPB; g++) s += sacc[g][threadIdx.x];
+    if (threadIdx.x < R) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = (double)s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    if (threadIdx.x < R && sact[threadIdx.x]) {
+      double s = 0;
+      for (int i = 0; i < (int)gridDim.x; i++) s += ((volatile double*)partial)[(size_t)threadIdx.x * gridDim.x + i];
+      energy[threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+  }
 }
 
 // element-wise  int_e grad u . grad w  (geometry from G / kappa_e)
@@ -590,14 +755,14 @@ hex_graddot_kernel(int ne, const int* __restrict__ tdof, int tstride, const doub
       su[t] = d < 0 ? -v : v;
     }
     group_sync<G>(gid);
-    hex_forward<N, T, false>(lane, gid, su, s1, s2, t2, t3, ux, uy, uz, dummy);
+    hex_forward<N, T, false>(lane, lane < N2, gid, su, s1, s2, t2, t3, ux, uy, uz, dummy);
     for (int t = lane; t < N3; t += G) {
       int d = valid ? tdof[(size_t)e * tstride + t] : 0;
       T v = valid ? w[d & 0x7fffffff] : 0.0;
       su[t] = d < 0 ? -v : v;
     }
     group_sync<G>(gid);
-    hex_forward<N, T, false>(lane, gid, su, s1, s2, t2, t3, wx, wy, wz, dummy);
+    hex_forward<N, T, false>(lane, lane < N2, gid, su, s1, s2, t2, t3, wx, wy, wz, dummy);
     double acc = 0;
     if (lane < N2 && valid) {
       const T* Ge = Gq + (size_t)e * gstride + lane;
@@ -621,32 +786,57 @@ hex_graddot_kernel(int ne, const int* __restrict__ tdof, int tstride, const doub
   }
 }
 
-// diagonal of the hex operator: one thread per (element, tensor index)
-__global__ void hex_diag_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ Gq,
-                                int gstride, int mass, const double* __restrict__ B, const double* __restrict__ D,
-                                double* diag) {
-  const int N3 = N * N * N;
-  int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= (int64_t)ne * N3) return;
-  int e = (int)(id / N3), t = (int)(id % N3);
-  int a = t / (N * N), b = (t / N) % N, c = t % N;
-  const double* Ge = Gq + (size_t)e * gstride;
-  double s = 0;
-  for (int i = 0; i < N; i++) {
-    double Ba = B[i * N + a], Da = D[i * N + a];
-    for (int j = 0; j < N; j++) {
-      double Bb = B[j * N + b], Db = D[j * N + b];
-      for (int k = 0; k < N; k++) {
-        double Bc = B[k * N + c], Dc = D[k * N + c];
-        int q = (i * N + j) * N + k;
-        double gx = Da * Bb * Bc, gy = Ba * Db * Bc, gz = Ba * Bb * Dc;
-        s += Ge[q] * gx * gx + Ge[N3 + q] * gy * gy + Ge[2 * N3 + q] * gz * gz +
-             2 * (Ge[3 * N3 + q] * gx * gy + Ge[4 * N3 + q] * gx * gz + Ge[5 * N3 + q] * gy * gz);
-        if (mass) { double v = Ba * Bb * Bc; s += Ge[6 * N3 + q] * v * v; }
-      }
+// diagonal of the hex operator, sum-factorized: one block per element,
+//   d(a,b,c) = sum_m sum_i h_m(i,a) sum_j g_m(j,b) sum_k f_m(k,c) G_m(i,j,k)
+// with the per-component factor pairs (D D, B B, ...) of grad phi_t . G grad phi_t.
+__global__ void __launch_bounds__(256) hex_diag_kernel(int ne, int N, const int* __restrict__ tdof, int tstride,
+                                                        const double* __restrict__ Gq, int gstride, int mass,
+                                                        const double* __restrict__ B, const double* __restrict__ D,
+                                                        double* diag) {
+  extern __shared__ double dsm[];
+  const int N2 = N * N, N3 = N2 * N, nc = mass ? 7 : 6;
+  double* g = dsm;             // nc * N3: G, then H, then K (in place per stage via ping-pong)
+  double* h = dsm + 7 * N3;    // nc * N3
+  // factor selectors per component m: 0 = B*B, 1 = D*D, 2 = B*D ; weights of the i-stage
+  // m:        xx   yy   zz   xy   xz   yz   mass
+  const int fk[7] = {0, 0, 1, 0, 2, 2, 0};  // k-factor (c index)
+  const int fj[7] = {0, 1, 0, 2, 0, 2, 0};  // j-factor (b index)
+  const int fi[7] = {1, 0, 0, 2, 2, 0, 0};  // i-factor (a index)
+  const double wi[7] = {1, 1, 1, 2, 2, 2, 1};
+  auto fac = [&](int sel, int q, int a) {
+    const double b = B[q * N + a], d = D[q * N + a];
+    return sel == 0 ? b * b : (sel == 1 ? d * d : b * d);
+  };
+  for (int e = blockIdx.x; e < ne; e += gridDim.x) {
+    const double* Ge = Gq + (size_t)e * gstride;
+    for (int t = threadIdx.x; t < nc * N3; t += blockDim.x) g[t] = Ge[t];
+    __syncthreads();
+    // contract k: h[m][i][j][c] = sum_k f_m(k,c) g[m][i][j][k]
+    for (int t = threadIdx.x; t < nc * N3; t += blockDim.x) {
+      const int m = t / N3, r = t % N3, ij = r / N, c = r % N;
+      double v = 0;
+      for (int k = 0; k < N; k++) v += fac(fk[m], k, c) * g[m * N3 + ij * N + k];
+      h[t] = v;
     }
+    __syncthreads();
+    // contract j: g[m][i][b][c] = sum_j g_m(j,b) h[m][i][j][c]
+    for (int t = threadIdx.x; t < nc * N3; t += blockDim.x) {
+      const int m = t / N3, r = t % N3, i = r / N2, b = (r / N) % N, c = r % N;
+      double v = 0;
+      for (int j = 0; j < N; j++) v += fac(fj[m], j, b) * h[m * N3 + (i * N + j) * N + c];
+      g[t] = v;
+    }
+    __syncthreads();
+    // contract i and sum the components
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) {
+      const int a = t / N2, bc = t % N2;
+      double v = 0;
+      for (int m = 0; m < nc; m++)
+        for (int i = 0; i < N; i++) v += wi[m] * fac(fi[m], i, a) * g[m * N3 + i * N2 + bc];
+      atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
+    }
+    __syncthreads();
   }
-  atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), s);
 }
 
 // ---------------------------------------------------------------------------
@@ -787,7 +977,8 @@ void launch_hex_apply(gh1_op* op, const T* x, T* y, const T* G, int gstride, dou
   const int per_sm = op->hex_per_sm[pi][GM];
   GH1_CHECK(per_sm > 0, GH1_ERR_ARG, "internal: hex apply occupancy not prepared");
   const int ne = sp->mesh->ne;
-  const int blocks_needed = (ne + C::EPB - 1) / C::EPB;
+  const int nch = (ne + C::EPW - 1) / C::EPW;
+  const int blocks_needed = (nch + C::EPB - 1) / C::EPB;
   const int grid = std::min(blocks_needed, sp->ctx->nsm * per_sm);
   hex_apply_kernel<N, T, MASS, GM><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(
       ne, sp->d_tdof.p, sp->tstride, G, gstride, x, y, (int)sp->first_cell, partial, counter, energy, skip, op->d_err.p);
@@ -986,10 +1177,12 @@ void matfree_diag(gh1_op* op, double* diag) {
   const int ne = sp->mesh->ne;
   if (sp->et == 8) {
     const int N = sp->p + 1;
-    int64_t tot = (int64_t)ne * N * N * N;
-    hex_diag_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, op->d_G64.p,
-                                                                   op->gstride64, op->has_mass ? 1 : 0, sp->d_B64.p,
-                                                                   sp->d_D64.p, diag);
+    const size_t smem = (size_t)14 * N * N * N * sizeof(double);
+    if (smem > 48 * 1024)
+      GH1_CUDA(cudaFuncSetAttribute(hex_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = std::min(ne, sp->ctx->nsm * 8);
+    hex_diag_kernel<<<grid, 256, smem, s>>>(ne, N, sp->d_tdof.p, sp->tstride, op->d_G64.p, op->gstride64,
+                                            op->has_mass ? 1 : 0, sp->d_B64.p, sp->d_D64.p, diag);
     check_kernel(sp->ctx, "hex_diag_kernel");
   } else {
     int64_t tot = (int64_t)ne * sp->nloc;
