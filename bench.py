@@ -47,8 +47,9 @@ def parse():
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"],
-                    help="c3 (default, the headline line); c1/c2/c4 print their own measurement records")
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
+    ap.add_argument("--c5-problems", type=int, default=256)
     return ap.parse_args()
 
 
@@ -344,6 +345,79 @@ def workload_c4(args):
             "fd_s": t_fd}
 
 
+def workload_c5(args):
+    """256 independent problems on structured hex meshes, side n ~ U{8..40},
+    order p ~ U{1..6}, kappa ~ lognormal(0,1) per element, 16 seeded f ~ U[-1,1]
+    right-hand sides each (4,096 solves), seed 9; FP32 inner / FP64 refined to
+    1e-10.  Problems run in waves that fit the device; each wave is one batched
+    solve (one CUDA graph re-launched until every system converged)."""
+    import torch
+    import ngsolve_gb300 as ng
+    rng = np.random.default_rng(9)
+    nprob = args.c5_problems
+    sides = rng.integers(8, 41, nprob)
+    orders = rng.integers(1, 7, nprob)
+    R = 16
+    budget = 100e9
+    waves, cur, cur_b = [], [], 0.0
+    for i in range(nprob):
+        n, p = int(sides[i]), int(orders[i])
+        ndof = (n * p + 1) ** 3
+        ne = n ** 3
+        est = ndof * R * 60 + ne * (p + 1) ** 3 * 7 * 12 + ndof * 64
+        if cur and cur_b + est > budget:
+            waves.append(cur)
+            cur, cur_b = [], 0.0
+        cur.append(i)
+        cur_b += est
+    if cur:
+        waves.append(cur)
+    t_solve, t_setup = 0.0, 0.0
+    dof_solves, dof_iters, iters, outers, worst = 0, 0.0, [], [], 0.0
+    for w in waves:
+        t0 = time.perf_counter()
+        forms, rhs = [], []
+        for i in w:
+            n, p = int(sides[i]), int(orders[i])
+            mesh = ng.MakeStructured3DMesh(hexes=True, nx=n)
+            kappa = np.exp(rng.normal(0, 1, mesh.ne))
+            fes = ng.H1(mesh, order=p, dirichlet=".*")
+            u, v = fes.TnT()
+            a = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+            a += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+            B = torch.zeros((R, fes.ndof), dtype=torch.float64, device="cuda")
+            for r in range(R):
+                lf = ng.LinearForm(fes)
+                lf += ng.CoefficientFunction(rng.uniform(-1, 1, mesh.ne)) * v * ng.dx
+                lf.Assemble()
+                B[r].copy_(lf.vec.t)
+            forms.append(a)
+            rhs.append(B)
+        solver = ng.solvers.BatchCG(forms, [R] * len(w))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        t_setup += t1 - t0
+        X = solver.Solve(rhs, tol=1e-10)
+        torch.cuda.synchronize()
+        t_solve += time.perf_counter() - t1
+        for k, i in enumerate(w):
+            ndof = forms[k].fes.ndof
+            for r in range(R):
+                res = solver.results[k * R + r]
+                dof_solves += ndof
+                dof_iters += ndof * res.iterations
+                iters.append(res.iterations)
+                outers.append(res.outer)
+                worst = max(worst, res.true_relres if res.status == 0 else float("inf"))
+        del solver, forms, rhs, X
+        torch.cuda.empty_cache()
+    return {"workload": "C5: %d problems x 16 rhs, n~U{8..40}, p~U{1..6}, mixed to 1e-10" % nprob,
+            "waves": len(waves), "solves": nprob * R, "total_dofs_x_rhs": dof_solves,
+            "solve_s": t_solve, "setup_s": t_setup, "max_true_relres": worst,
+            "inner_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters))},
+            "outer_max": int(max(outers)), "gdof_iterations_per_s": dof_iters / t_solve / 1e9}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup(args.gpus)
@@ -357,7 +431,7 @@ def main():
     dev = local
     torch.cuda.set_device(dev)
     if args.workload != "c3":
-        fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4}[args.workload]
+        fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4, "c5": workload_c5}[args.workload]
         rec = fn(args)
         if rank == 0:
             print(json.dumps({"record": args.workload, **rec}), flush=True)

@@ -170,6 +170,25 @@ int gh1_elem_grad_dot(gh1_space* space, const double* u, const double* w, double
 int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u_target, double tol,
                      double* u, double* lambda, double* dJdkappa, double* J);
 
+/* ---- batched solves ----------------------------------------------------------
+ * Many independent hex problems (forms), 1..16 right-hand sides each (config
+ * "256 problems x 16 rhs"), solved by the mixed-precision method of gh1_cg:
+ * every (problem, rhs) pair is a device-side state machine (FP64 residual ->
+ * FP32 inner Jacobi-PCG -> FP64 correction) and all problems advance together
+ * through ONE CUDA graph (one branch per problem) launched until all pairs
+ * converged.  The multi-rhs apply reads each element's G tile once for all
+ * right-hand sides.  No counterpart in the reference, which solves one system
+ * per CGSolver call (python/krylovspace.py:263-291).
+ * rhs[p], x[p]: device double[nrhs[p]*ndof_p], right-hand side r at offset
+ * r*ndof_p.  opts: tol, maxit (per inner solve), inner_tol, max_outer,
+ * check_every (inner iterations per graph round), initialize.
+ * res: sum(nrhs) results, problem-major.                                      */
+typedef struct gh1_batch gh1_batch;
+int gh1_batch_create(gh1_ctx* ctx, int nprob, gh1_form* const* forms, const int* nrhs, gh1_batch** batch);
+int gh1_batch_solve(gh1_batch* batch, const double* const* rhs, double* const* x, const gh1_cg_opts* opts,
+                    gh1_cg_result* res);
+int gh1_batch_free(gh1_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

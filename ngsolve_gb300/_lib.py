@@ -72,6 +72,9 @@ SIGNATURES = {
     "gh1_cg": [_P, _P, _P, _P, ctypes.POINTER(CGOpts), ctypes.POINTER(CGResult)],
     "gh1_elem_grad_dot": [_P, _P, _P, _P],
     "gh1_adjoint_grad": [_P, _P, _P, _D, _P, _P, _P, _P],
+    "gh1_batch_create": [_P, _I, _P, _P, _PP],
+    "gh1_batch_solve": [_P, _P, _P, ctypes.POINTER(CGOpts), _P],
+    "gh1_batch_free": [_P],
 }
 
 _lib = None

@@ -22,6 +22,7 @@
 #include <type_traits>
 #include <vector>
 #include "common.cuh"
+#include "reduce.cuh"
 
 namespace gh1 {
 
@@ -29,48 +30,6 @@ struct CGState {
   double wd, wdn, energy, alpha, beta, res0, stop, res, dd, bb;
   int it, maxit, done, status, rule, pad;
 };
-
-// grid-wide reduction of K doubles per thread; returns true in the last block,
-// where tot[] holds the totals (all threads).  No block waits for another.
-template <int K>
-__device__ bool grid_reduce(double (&v)[K], double* partial, unsigned int* counter, double (&tot)[K]) {
-  __shared__ double red[K][32];
-  __shared__ bool last;
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    double x = v[k];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (l == 0) red[k][w] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < K; k++) {
-      double s = 0;
-      for (int i = 0; i < nw; i++) s += red[k][i];
-      partial[(size_t)k * gridDim.x + blockIdx.x] = s;
-    }
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    double s = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double*)partial)[(size_t)k * gridDim.x + i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    __syncthreads();
-    if (l == 0) red[k][w] = s;
-    __syncthreads();
-    double t = 0;
-    for (int i = 0; i < nw; i++) t += red[k][i];
-    tot[k] = t;
-  }
-  if (threadIdx.x == 0) *counter = 0u;
-  return true;
-}
 
 constexpr int RED_BLOCK = 256;
 
@@ -319,21 +278,6 @@ __global__ void __launch_bounds__(RED_BLOCK) dot_energy_kernel(int64_t n, const 
   if (grid_reduce<1>(v, partial, counter, tot) && threadIdx.x == 0) *out = tot[0];
 }
 
-template <class T>
-__global__ void csr_spmv_skip_kernel(int64_t nrows, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
-                                     const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, const int* skip) {
-  if (*(volatile const int*)skip) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t row = warp; row < nrows; row += nw) {
-    T acc = 0;
-    for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) acc += vals[k] * __ldg(x + colind[k]);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[row] = acc;
-  }
-}
-
 // One PCG solve in precision T on vectors already on the device.
 // d holds the initial residual on entry; x the initial guess.
 template <class T>
@@ -356,10 +300,7 @@ struct PCG {
     if (op->kind == GH1_OP_MATFREE) {
       op_apply_energy(op, s, y, prec, partial + 2 * ctx->nsm * 64, counters + 1, &st->energy, &st->done);
     } else {
-      const T* vals = std::is_same<T, float>::value ? (const T*)op->d_vals32.p : (const T*)op->d_vals.p;
-      int gg = grid_for(ctx, n * 32, 256, 16);
-      csr_spmv_skip_kernel<T><<<gg, 256, 0, cs>>>(n, op->rowptr, op->colind, vals, s, y, &st->done);
-      check_kernel(ctx, "csr_spmv_skip_kernel");
+      spmv_skip(op, s, y, prec, &st->done);
       dot_energy_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, s, y, &st->energy, partial + 2 * ctx->nsm * 64, counters + 1, &st->done);
       check_kernel(ctx, "dot_energy_kernel");
     }
@@ -385,6 +326,7 @@ struct PCG {
     cudaGraphExec_t exec = *cache_exec;
     if (!exec || *cache_chunk != chunk) {
       if (exec) cudaGraphExecDestroy(exec);
+      if (op->kind == GH1_OP_CSR) spmv_prepare(op, prec);
       cudaGraph_t graph;
       GH1_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < chunk; k++) launch_iteration(cs);
@@ -503,11 +445,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
       W.x32.alloc(n); W.d32.alloc(n); W.w32.alloc(n); W.s32.alloc(n); W.y32.alloc(n); W.r64.alloc(n);
       GH1_CHECK(op->kind == GH1_OP_CSR || (op->prec_mask & 2), GH1_ERR_UNSUPPORTED,
                 "mixed precision needs an operator set up with FP32 data (precision mask bit 1)");
-      if (op->kind == GH1_OP_CSR && op->d_vals32.n != (size_t)op->nnz) {
-        op->d_vals32.alloc(op->nnz);
-        axpby_kernel<double, float><<<grid_for(ctx, op->nnz, 256), 256, 0, cs>>>(op->nnz, 1.0, op->d_vals.p, 0.0, op->d_vals32.p);
-        check_kernel(ctx, "axpby_kernel(vals32)");
-      }
+      if (op->kind == GH1_OP_CSR) spmv_prepare(op, GH1_F32);
       const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
       const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
       const double target = o->tol * std::sqrt(bb);

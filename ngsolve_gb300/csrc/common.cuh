@@ -156,6 +156,8 @@ struct gh1_op {
   gh1::DBuf<int> d_err;       // device error flag of the pipelined apply (bounded waits)
   int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
   int hex_gmode[2] = {0, 0};                 // autotuned G staging per precision (0: TMA tile, 1: direct)
+  int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
+  int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
   gh1::DBuf<double> d_diag;   // operator diagonal (FP64)
   bool have_diag = false;
@@ -188,10 +190,14 @@ void matfree_apply(gh1_op* op, const void* x, void* y, int prec, double* energy_
 void matfree_diag(gh1_op* op, double* diag);                        // matfree.cu
 void elem_grad_dot(gh1_space* sp, const double* u, const double* w, double* out);  // matfree.cu
 void elem_grad_dot_with(gh1_op* op, const double* u, const double* w, double* out);  // matfree.cu
+int matfree_apply_multi(gh1_op* op, int R, const int* phase, int want, const void* x, void* y, int prec, double* partial,
+                        unsigned int* counter, double* energy, bool prepare_only);  // matfree.cu
 void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter,
                       double* energy, const int* skip);  // matfree.cu
 void mass_apply(gh1_op* op, const double* x, double* y);            // matfree.cu
 void spmv(gh1_op* op, const void* x, void* y, int prec);            // spmv.cu
+void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
+void spmv_skip(gh1_op* op, const void* x, void* y, int prec, const int* skip);  // spmv.cu
 void csr_diag(gh1_op* op, double* diag);                            // spmv.cu
 int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* o, gh1_cg_result* r);  // cg.cu
 void vec_axpby(gh1_ctx* ctx, int64_t n, double a, const void* x, double b, void* y, int prec);  // cg.cu

@@ -577,13 +577,14 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
 }
 
 // Multi-right-hand-side apply for batched solves: Y_r += A X_r for the right-hand
-// sides r < R whose flag active[r] is set (vectors stored rhs-major, stride n).
+// sides r < R with phase[r] == want (vectors stored rhs-major, stride n).
 // The G tiles and DOF rows of a chunk are bulk-copied once (TMA, mbarriers) and
 // reused for every active right-hand side, so the dominant G stream is read once
 // per R applications.  Per-rhs energies x_r^T A x_r go to energy[r].
 template <int N, class T, bool MASS>
 __global__ void __launch_bounds__(HexCfg<N>::BLOCK)
-hex_apply_multi_kernel(int ne, int64_t n, int R, const int* __restrict__ active, const int* __restrict__ tdof, int tstride,
+hex_apply_multi_kernel(int ne, int64_t n, int R, const int* __restrict__ phase, int want, const int* __restrict__ tdof,
+                       int tstride,
                        const T* __restrict__ Gq, int gstride, const T* __restrict__ x, T* __restrict__ y, int first_cell,
                        double* partial, unsigned int* counter, double* energy, int* err) {
   using C = HexCfg<N>;
@@ -605,7 +606,7 @@ hex_apply_multi_kernel(int ne, int64_t n, int R, const int* __restrict__ active,
   T *su = work + so, *s1 = work + CN3 + so, *s2 = work + 2 * CN3 + so, *t2 = work + 3 * CN3 + so,
     *t3 = work + 4 * CN3 + so;
   uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + SM::work);
-  for (int r = threadIdx.x; r < RMAX; r += blockDim.x) sact[r] = (r < R) ? active[r] : 0;
+  for (int r = threadIdx.x; r < RMAX; r += blockDim.x) sact[r] = (r < R) ? (phase[r] == want) : 0;
   for (int t = threadIdx.x; t < C::EPB * RMAX; t += blockDim.x) (&sacc[0][0])[t] = 0.f;
   if (lane == 0) {
     mbar_init(&mbar[0], 1);
@@ -1071,6 +1072,73 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   cudaEventDestroy(b);
   op->hex_gmode[pi] = choice;
   cache.push_back({N, pi, lb + (op->has_mass ? 100 : 0), choice});
+}
+
+// ---- multi-right-hand-side apply (batched solves) ----------------------------
+template <int N, class T, bool MASS>
+int hex_multi_occupancy(size_t smem) {
+  static bool attr = false;
+  auto kern = hex_apply_multi_kernel<N, T, MASS>;
+  if (!attr) {
+    int dev = 0, optin = 0;
+    GH1_CUDA(cudaGetDevice(&dev));
+    GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+    GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    attr = true;
+  }
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, HexCfg<N>::BLOCK, smem));
+  GH1_CHECK(v >= 1, GH1_ERR_UNSUPPORTED, "multi-rhs hex apply does not fit on an SM");
+  return v;
+}
+
+template <int N, class T, bool MASS>
+int hex_multi_launch(gh1_op* op, int R, const int* phase, int want, const T* x, T* y, double* partial,
+                     unsigned int* counter, double* energy, bool prepare_only) {
+  using C = HexCfg<N>;
+  gh1_space* sp = op->sp;
+  const int gs = std::is_same<T, float>::value ? op->gstride32 : op->gstride64;
+  const T* G = std::is_same<T, float>::value ? (const T*)op->d_G32.p : (const T*)op->d_G64.p;
+  const size_t smem = HexSmem<N, T>::total(gs, sp->tstride, 0);
+  const int pi = std::is_same<T, float>::value ? 1 : 0;
+  if (prepare_only || op->multi_per_sm[pi] <= 0) op->multi_per_sm[pi] = hex_multi_occupancy<N, T, MASS>(smem);
+  const int ne = sp->mesh->ne, nch = (ne + C::EPW - 1) / C::EPW;
+  const int grid = std::min((nch + C::EPB - 1) / C::EPB, sp->ctx->nsm * op->multi_per_sm[pi]);
+  if (prepare_only) return grid;
+  hex_apply_multi_kernel<N, T, MASS><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(
+      ne, op->nrows, R, phase, want, sp->d_tdof.p, sp->tstride, G, gs, x, y, (int)sp->first_cell, partial, counter, energy,
+      op->d_err.p);
+  check_kernel(sp->ctx, "hex_apply_multi_kernel");
+  return grid;
+}
+
+// y_r += A x_r for rhs with phase[r] == want; energies into energy[r].  Returns the
+// grid size (partial must hold R * grid doubles).  prepare_only: set up occupancy
+// (call before any stream capture) and return the grid without launching.
+int matfree_apply_multi(gh1_op* op, int R, const int* phase, int want, const void* x, void* y, int prec, double* partial,
+                        unsigned int* counter, double* energy, bool prepare_only) {
+  GH1_CHECK(op->sp->et == 8, GH1_ERR_UNSUPPORTED, "batched solves need hex meshes");
+  GH1_CHECK(R >= 1 && R <= 16, GH1_ERR_UNSUPPORTED, "batched solves take 1..16 right-hand sides per problem");
+  const bool mass = op->has_mass;
+  int g = 0;
+#define GH1_MULTI_CASE(NN)                                                                                          \
+  case NN:                                                                                                          \
+    if (prec == GH1_F64)                                                                                            \
+      g = mass ? hex_multi_launch<NN, double, true>(op, R, phase, want, (const double*)x, (double*)y, partial,      \
+                                                    counter, energy, prepare_only)                                  \
+               : hex_multi_launch<NN, double, false>(op, R, phase, want, (const double*)x, (double*)y, partial,     \
+                                                     counter, energy, prepare_only);                                \
+    else                                                                                                            \
+      g = mass ? hex_multi_launch<NN, float, true>(op, R, phase, want, (const float*)x, (float*)y, partial, counter, \
+                                                   energy, prepare_only)                                            \
+               : hex_multi_launch<NN, float, false>(op, R, phase, want, (const float*)x, (float*)y, partial, counter, \
+                                                    energy, prepare_only);                                          \
+    break;
+  GH1_HEX_SWITCH(op->sp->p + 1, GH1_MULTI_CASE)
+#undef GH1_MULTI_CASE
+  return g;
 }
 
 static int pad16(int count, int elem_bytes) {

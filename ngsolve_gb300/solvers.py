@@ -95,3 +95,53 @@ def CG(mat, rhs, pre=None, sol=None, tol=1e-12, maxsteps=100, printrates=True, p
     solver.Solve(rhs=rhs, sol=sol, initialize=initialize)
     CG.last_solver = solver
     return solver.sol
+
+
+class BatchCG:
+    """Batched mixed-precision CG over many independent hex problems.
+
+    forms: list of BilinearForm (hex meshes, kappa/mu per element); nrhs: right-hand
+    sides per problem (<= 16).  Solve(rhs_list, tol) takes per problem a (nrhs, ndof)
+    FP64 CUDA tensor and returns the solutions in the same layout; `results` holds
+    one CGResult per (problem, rhs)."""
+
+    def __init__(self, forms, nrhs):
+        if len(forms) != len(nrhs):
+            raise ValueError("one rhs count per form")
+        self.forms = list(forms)
+        self.nrhs = [int(r) for r in nrhs]
+        ctx = self.forms[0].fes.ctx.sync_stream()
+        self.ctx = ctx
+        handles = (ctypes.c_void_p * len(forms))(*[f._make_form().value for f in self.forms])
+        counts = (ctypes.c_int * len(forms))(*self.nrhs)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_batch_create(ctx.h, len(forms), handles, counts, ctypes.byref(h)))
+        self.h = h
+        self.results = []
+
+    def Solve(self, rhs, tol=1e-10, maxit=5000, inner_tol=0.0, max_outer=0, check_every=0, sol=None):
+        ctx = self.ctx.sync_stream()
+        if len(rhs) != len(self.forms):
+            raise ValueError("one rhs tensor per problem")
+        xs = sol if sol is not None else [torch.zeros_like(b) for b in rhs]
+        for b, x, f, r in zip(rhs, xs, self.forms, self.nrhs):
+            if b.shape != (r, f.fes.ndof) or b.dtype != torch.float64 or not b.is_cuda or not b.is_contiguous():
+                raise ValueError("rhs of a problem must be a contiguous (nrhs, ndof) float64 CUDA tensor")
+        bp = (ctypes.c_void_p * len(rhs))(*[b.data_ptr() for b in rhs])
+        xp = (ctypes.c_void_p * len(xs))(*[x.data_ptr() for x in xs])
+        o = _lib.CGOpts()
+        o.tol, o.maxit, o.mode, o.stop_rule, o.initialize = float(tol), int(maxit), _lib.GH1_CG_MIXED, _lib.GH1_STOP_TRUE, 1
+        o.inner_tol, o.max_outer, o.check_every = float(inner_tol), int(max_outer), int(check_every)
+        res = (_lib.CGResult * sum(self.nrhs))()
+        rc = ctx.lib.gh1_batch_solve(self.h, bp, xp, ctypes.byref(o), res)
+        if rc not in (_lib.GH1_OK, 6, 7):
+            ctx.check(rc)
+        self.status = rc
+        self.results = list(res)
+        return xs
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_batch_free(self.h)
+        except Exception:
+            pass
