@@ -189,6 +189,35 @@ int gh1_batch_solve(gh1_batch* batch, const double* const* rhs, double* const* x
                     gh1_cg_result* res);
 int gh1_batch_free(gh1_batch* batch);
 
+/* ---- shape evaluation without device allocation ------------------------------
+ * No counterpart in the reference.  gh1_shape_eval allocates device buffers on
+ * every call (copies of the points and outputs, and per-point scratch); some
+ * callers cannot let a library allocate at that point: hosts that hand all
+ * device memory out of their own fixed pool or budget, and loops that must not
+ * stall on cudaMalloc/cudaFree (which can synchronise the device).  This
+ * variant computes the same values with the same kernel, from DEVICE inputs
+ * into DEVICE outputs, and takes its scratch from one fixed array compiled into
+ * the library (GH1_SHAPE_NOALLOC_MAX_ENTRIES entries of 32 bytes = 8 MiB),
+ * which every GPU that loads the library holds until the process exits.
+ *  - npts * nloc must not exceed GH1_SHAPE_NOALLOC_MAX_ENTRIES
+ *    (nloc = (p+1)(p+2)(p+3)/6 on tets, (p+1)^3 on hexes); larger requests are
+ *    rejected with GH1_ERR_ARG before any device work.
+ *  - vnums: host int32[et]; pts: device double[npts*3]; val: device
+ *    double[npts*nloc]; grad: device double[npts*nloc*3] (device or managed
+ *    memory of the context's device).
+ *  - Asynchronous: the work is queued on the context's stream and the call
+ *    returns without waiting for it.
+ *  - The first call on each device looks up the scratch array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the one scratch array, which keeps the last call's
+ *    contents (nothing in it has to start at zero: every entry a thread reads
+ *    it has written first in the same call).  Calls whose work overlaps on the
+ *    GPU (two streams, or two contexts on one device) race on it.            */
+#define GH1_SHAPE_NOALLOC_MAX_ENTRIES 262144
+int gh1_shape_eval_noalloc(gh1_ctx* ctx, int et, int order, const int32_t* vnums, int npts,
+                           const double* pts, double* val, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

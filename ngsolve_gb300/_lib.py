@@ -75,6 +75,7 @@ SIGNATURES = {
     "gh1_batch_create": [_P, _I, _P, _P, _PP],
     "gh1_batch_solve": [_P, _P, _P, ctypes.POINTER(CGOpts), _P],
     "gh1_batch_free": [_P],
+    "gh1_shape_eval_noalloc": [_P, _I, _I, _P, _I, _P, _P, _P],
 }
 
 _lib = None

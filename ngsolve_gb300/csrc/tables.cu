@@ -15,6 +15,7 @@
 //    blocks S_ab = sum_q w_q d_a phi_i d_b phi_j and the reference mass block.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 #include "common.cuh"
 #include "basis.cuh"
@@ -227,4 +228,93 @@ void shape_eval_gpu(gh1_ctx* ctx, int et, int p, const int32_t* vnums, int npts,
   GH1_CUDA(cudaStreamSynchronize(s));
 }
 
+// ---- shape evaluation into caller-owned device memory, no allocation -----------
+// For callers that cannot let the library allocate device memory (their own
+// fixed pool, or a loop that must not stall on cudaMalloc / cudaFree): the
+// per-(point, shape) scratch of shape_eval_kernel lives in this fixed module
+// array, GH1_SHAPE_NOALLOC_MAX_ENTRIES Dual3 values (8 MiB), which every device
+// that loads the library holds until the process exits.  The array name is only
+// a host-side handle; kernels get its device address from cudaGetSymbolAddress.
+static __device__ __align__(256) double shape_noalloc_scratch[4 * (size_t)GH1_SHAPE_NOALLOC_MAX_ENTRIES];
+static_assert(sizeof(Dual3) == 4 * sizeof(double), "scratch entry is one Dual3");
+
+constexpr int kNoallocMaxDevices = 64;
+static std::mutex shape_noalloc_mu;
+static void* shape_noalloc_addr[kNoallocMaxDevices] = {};
+
+// the scratch array's address on `device` (current), looked up on first use
+static Dual3* shape_noalloc_scratch_on(int device) {
+  GH1_CHECK(device >= 0 && device < kNoallocMaxDevices, GH1_ERR_UNSUPPORTED,
+            "gh1_shape_eval_noalloc: device index beyond the supported 64");
+  std::lock_guard<std::mutex> lock(shape_noalloc_mu);
+  if (!shape_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, shape_noalloc_scratch);
+    if (e != cudaSuccess)
+      throw Error(GH1_ERR_CUDA, std::string("gh1_shape_eval_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    shape_noalloc_addr[device] = p;
+  }
+  return (Dual3*)shape_noalloc_addr[device];
+}
+
+// true if the device can address p as memory of `device` (device or managed)
+static bool device_pointer_on(const void* p, int device) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
+}
+
+static void shape_eval_noalloc(gh1_ctx* ctx, int et, int p, const int32_t* vnums, int npts, const double* pts,
+                               double* val, double* grad) {
+  GH1_CHECK(et == 4 || et == 8, GH1_ERR_UNSUPPORTED, "element type must be 4 or 8");
+  GH1_CHECK(p >= 1 && p <= (et == 4 ? MAX_TET_ORDER : MAX_HEX_ORDER), GH1_ERR_UNSUPPORTED, "order out of range");
+  const int nloc = et == 4 ? (p + 1) * (p + 2) * (p + 3) / 6 : (p + 1) * (p + 1) * (p + 1);
+  const int64_t entries = (int64_t)npts * nloc;
+  GH1_CHECK(entries <= GH1_SHAPE_NOALLOC_MAX_ENTRIES, GH1_ERR_ARG,
+            "gh1_shape_eval_noalloc: npts * nloc = " + std::to_string(entries) + " exceeds the fixed scratch of " +
+                std::to_string(GH1_SHAPE_NOALLOC_MAX_ENTRIES) + " entries; split the points into smaller calls");
+  // the scratch lookup needs the context's device current; restore the caller's
+  int prev = -1;
+  GH1_CUDA(cudaGetDevice(&prev));
+  if (prev != ctx->device) GH1_CUDA(cudaSetDevice(ctx->device));
+  struct Restore {
+    int dev, prev;
+    ~Restore() {
+      if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+    }
+  } restore{ctx->device, prev};
+  GH1_CHECK(device_pointer_on(pts, ctx->device) && device_pointer_on(val, ctx->device) &&
+                device_pointer_on(grad, ctx->device),
+            GH1_ERR_ARG, "gh1_shape_eval_noalloc: pts, val and grad must be device memory of the context's device");
+  Dual3* scratch = shape_noalloc_scratch_on(ctx->device);
+  int v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < et; i++) v[i] = vnums[i];
+  shape_eval_kernel<<<(npts + 31) / 32, 32, 0, ctx->stream>>>(et, p, nloc, v[0], v[1], v[2], v[3], v[4], v[5], v[6],
+                                                               v[7], npts, pts, val, grad, scratch);
+  check_kernel(ctx, "shape_eval_kernel (no-allocation entry)");
+}
+
 }  // namespace gh1
+
+extern "C" int gh1_shape_eval_noalloc(gh1_ctx* ctx, int et, int order, const int32_t* vnums, int npts,
+                                      const double* pts, double* val, double* grad) {
+  if (!ctx) return GH1_ERR_ARG;
+  if (!vnums || !pts || !val || !grad || npts <= 0) {
+    ctx->err = "gh1_shape_eval_noalloc: null pointer or npts <= 0";
+    return GH1_ERR_ARG;
+  }
+  try {
+    gh1::shape_eval_noalloc(ctx, et, order, vnums, npts, pts, val, grad);
+    return GH1_OK;
+  } catch (const gh1::Error& e) {
+    ctx->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    ctx->err = e.what();
+    return GH1_ERR_ARG;
+  }
+}
