@@ -155,7 +155,9 @@ struct gh1_op {
   gh1::DBuf<float> d_M32;
   gh1::DBuf<int> d_err;       // device error flag of the pipelined apply (bounded waits)
   int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
-  int hex_gmode[2] = {0, 0};                 // autotuned G staging per precision (0: TMA tile, 1: direct)
+  int hex_gmode[2] = {0, 0};                 // autotuned hex apply variant per precision: 0/1 = G tile by TMA /
+                                             // direct loads; FP32 also 2/3 = the same with two elements per lane
+  int pair_per_sm[2] = {0, 0};               // resident blocks per SM of the paired FP32 apply [G mode]
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
   int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
@@ -196,6 +198,12 @@ void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* part
                       double* energy, const int* skip);  // matfree.cu
 void mass_apply(gh1_op* op, const double* x, double* y);            // matfree.cu
 void spmv(gh1_op* op, const void* x, void* y, int prec);            // spmv.cu
+// paired FP32 hex apply (hexpair.cu): two elements per lane, packed f32x2 arithmetic
+bool hex_pair_supported(int N);
+void upload_pair_tables(gh1_space* sp);
+int hex_pair_occupancy(gh1_op* op, int gmode);
+void hex_pair_apply(gh1_op* op, int gmode, const float* x, float* y, double* partial, unsigned int* counter,
+                    double* energy, const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
 void spmv_skip(gh1_op* op, const void* x, void* y, int prec, const int* skip);  // spmv.cu
 void csr_diag(gh1_op* op, double* diag);                            // spmv.cu

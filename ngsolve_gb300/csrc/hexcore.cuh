@@ -1,0 +1,121 @@
+// hexcore.cuh -- pieces shared by the hex sum-factorization kernels: the layout
+// of the 1D factor tables in constant memory, the thread-group configuration,
+// group barriers and votes, the end-of-kernel energy reduction, and the bulk-copy
+// (TMA) / mbarrier helpers of the pipelined element loops.
+#pragma once
+#include "common.cuh"
+
+namespace gh1 {
+
+// offset of the N x N factor table of order p = N-1 inside the concatenated
+// tables of every order
+constexpr int tab_off(int N) { return N <= 2 ? 0 : tab_off(N - 1) + (N - 1) * (N - 1); }
+constexpr int TAB_TOTAL = tab_off(MAX_HEX_ORDER + 2);
+
+// ---------------------------------------------------------------------------
+// thread-group helpers
+template <int G>
+__device__ __forceinline__ void group_sync(int gid) {
+  if (G == 32) __syncwarp();
+  else asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(G) : "memory");
+}
+
+template <class T>
+__device__ __forceinline__ void atomic_add_t(T* p, T v) { atomicAdd(p, v); }
+
+// End-of-kernel reduction of one double per thread into partial[blockIdx.x];
+// the last block to finish sums all partials into *out and resets the counter.
+// (threadfence reduction: no block waits on another.)
+static __device__ void block_reduce_finish(double v, double* partial, unsigned int* counter, double* out) {
+  __shared__ double red[32];
+  __shared__ bool last;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; i++) s += red[i];
+    partial[blockIdx.x] = s;
+    __threadfence();
+    unsigned int t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double s = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double*)partial)[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (l == 0) red[w] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0;
+      for (int i = 0; i < (int)(blockDim.x + 31) / 32; i++) tot += red[i];
+      *out = tot;
+      *counter = 0u;
+    }
+  }
+}
+
+template <int N>
+struct HexCfg {
+  static constexpr int N2 = N * N, N3 = N * N * N;
+  static constexpr int G = ((N2 + 31) / 32) * 32;  // threads per element group
+  static constexpr int EPW = N2 <= 32 ? 32 / N2 : 1;  // elements per group (low orders share a warp)
+  static constexpr int EPB = G == 32 ? 4 : 2;      // element groups per block
+  static constexpr int BLOCK = G * EPB;
+};
+
+__host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
+
+// ---- bulk-copy (TMA) and mbarrier helpers ------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// global -> shared bulk copy (size and both addresses multiples of 16 bytes)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// bulk prefetch of a contiguous global range into L2 (16-byte aligned, size a
+// multiple of 16): the later loads of the range hit L2 instead of HBM
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok)
+               : "r"(smem_u32(bar)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+// bounded wait: false after ~2^22 polls (an error, never expected)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// all threads of the element group agree on a predicate
+template <int G>
+__device__ __forceinline__ bool group_all(int gid, bool v) {
+  if (G == 32) return __all_sync(0xffffffffu, v);
+  uint32_t r;
+  asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(r)
+               : "r"((uint32_t)v), "r"(gid + 1), "r"(G)
+               : "memory");
+  return r != 0;
+}
+
+}  // namespace gh1

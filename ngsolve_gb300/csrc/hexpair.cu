@@ -1,0 +1,518 @@
+// hexpair.cu -- FP32 hex apply y += A x with two elements per lane.
+//
+// Same operator and algorithm as hex_apply_kernel (matfree.cu: sum-factorized
+// SymbolicBFI::ApplyElementMatrix, fem/symbolicintegrator.cpp:2959-3040, with the
+// per-point coefficient tile G_q = kappa w |det J| J^{-1} J^{-T}), restructured
+// for the packed FP32 pipe of sm_103a: a lane owns the same pencil of TWO
+// consecutive elements and keeps both values in one 64-bit register, so every
+// contraction step is one fma.rn.f32x2 for two elements, every work-array access
+// one 8-byte shared-memory access for two elements, and the loop / address /
+// barrier overhead of the element loop is paid once per pair.  The FP32 apply is
+// instruction-issue bound in the one-element form; this halves the arithmetic
+// and shared-memory instruction count per element.
+//
+// Layout per element group (G threads, S = HexCfg::EPW pencil slots, E = 2 S
+// elements per chunk, element 2s+h of a chunk in slot s, half h):
+//   [G tiles of the E elements (G mode 0)] | DOF-table rows x2 buffers |
+//   5 packed work arrays [S][N^3] of float2 | 3 mbarriers
+// Pipelining as in the one-element kernel: the DOF rows of the next chunk are
+// bulk-copied (TMA) during the forward contractions, the next chunk's x gather
+// is issued before the quadrature-point transform, and in G mode 0 the G tiles
+// of the next chunk are bulk-copied during the transposed contractions.
+// Every mbarrier wait is bounded; a timeout sets *err and the kernel drains its
+// copies in flight and returns.
+#include <algorithm>
+#include "common.cuh"
+#include "hexcore.cuh"
+
+namespace gh1 {
+
+typedef unsigned long long f2;  // packed pair: low half element 2s, high half element 2s+1
+
+__device__ __forceinline__ f2 pack2(float lo, float hi) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void unpack2(f2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// 1D factor tables (32-bit); a coefficient enters the packed FMA broadcast to
+// both halves, which the packed pipe takes from the constant bank at no extra
+// instruction (a table of pre-duplicated 64-bit pairs costs a move per FMA)
+__constant__ float c_Bp[TAB_TOTAL], c_Dp[TAB_TOTAL];
+__device__ __forceinline__ f2 bcast(float t) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(t));
+  return r;
+}
+
+// resident 128-thread blocks per SM the register allocation must allow: the
+// largest count each variant compiles to without spills (p=4: 4 blocks = 128
+// registers with the G tile in shared memory, 5 blocks = 96 with direct G loads)
+constexpr int pair_min_blocks(int N, bool mass, int gm) {
+  return N == 2   ? 6
+         : N == 3 ? (mass ? (gm ? 5 : 4) : (gm ? 6 : 5))
+         : N == 4 ? (mass ? (gm ? 5 : 4) : 5)
+         : N == 5 ? (mass ? (gm ? 4 : 3) : (gm ? 5 : 4))
+         : N == 6 ? 3
+                  : 2;
+}
+
+template <int N>
+struct PairCfg {
+  static constexpr int N2 = N * N, N3 = N * N * N;
+  static constexpr int G = HexCfg<N>::G;      // threads per element group
+  static constexpr int S = HexCfg<N>::EPW;    // pencil slots per group
+  static constexpr int E = 2 * S;             // elements per chunk
+  static constexpr int EPB = HexCfg<N>::EPB;  // groups per block
+  static constexpr int BLOCK = G * EPB;
+  static constexpr int NG = (S * N3 + G - 1) / G;  // (slot, local DOF) positions per lane
+  static __host__ __device__ size_t gbytes(int gstride) { return E * round16((size_t)gstride * sizeof(float)); }
+  static __host__ __device__ size_t tbytes(int tstride) { return E * round16((size_t)tstride * sizeof(int)); }
+  static constexpr size_t work = round16(5 * (size_t)S * N3 * sizeof(f2));  // keeps groups 16-byte aligned
+  static __host__ __device__ size_t group(int gstride, int tstride, int gmode) {
+    return (gmode == 0 ? gbytes(gstride) : 0) + 2 * tbytes(tstride) + work + 32;
+  }
+  static __host__ __device__ size_t total(int gstride, int tstride, int gmode) {
+    return (size_t)EPB * group(gstride, tstride, gmode);
+  }
+};
+
+// forward chain on packed pairs (see hex_forward in matfree.cu): coefficients in
+// su[(a*N+b)*N+c] -> reference gradient at the points of lane (j,k)
+template <int N, bool WANT_U>
+__device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* su, f2* s1, f2* s2, f2* t2, f2* t3,
+                                             f2* gx, f2* gy, f2* gz, f2* uq) {
+  constexpr int G = HexCfg<N>::G, O = tab_off(N);
+  f2* t1 = su;
+  if (active) {
+    const int a = pl / N, b = pl % N;
+    f2 u[N];
+#pragma unroll
+    for (int c = 0; c < N; c++) u[c] = su[(a * N + b) * N + c];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      f2 ub = mul2(bcast(c_Bp[O + k * N]), u[0]), ud = mul2(bcast(c_Dp[O + k * N]), u[0]);
+#pragma unroll
+      for (int c = 1; c < N; c++) {
+        ub = fma2(bcast(c_Bp[O + k * N + c]), u[c], ub);
+        ud = fma2(bcast(c_Dp[O + k * N + c]), u[c], ud);
+      }
+      s1[(a * N + b) * N + k] = ub;
+      s2[(a * N + b) * N + k] = ud;
+    }
+  }
+  group_sync<G>(gid);
+  if (active) {
+    const int a = pl / N, k = pl % N;
+    f2 v1[N], v2[N];
+#pragma unroll
+    for (int b = 0; b < N; b++) { v1[b] = s1[(a * N + b) * N + k]; v2[b] = s2[(a * N + b) * N + k]; }
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      f2 bb = mul2(bcast(c_Bp[O + j * N]), v1[0]), db = mul2(bcast(c_Dp[O + j * N]), v1[0]), bd = mul2(bcast(c_Bp[O + j * N]), v2[0]);
+#pragma unroll
+      for (int b = 1; b < N; b++) {
+        bb = fma2(bcast(c_Bp[O + j * N + b]), v1[b], bb);
+        db = fma2(bcast(c_Dp[O + j * N + b]), v1[b], db);
+        bd = fma2(bcast(c_Bp[O + j * N + b]), v2[b], bd);
+      }
+      t1[(a * N + j) * N + k] = bb;
+      t2[(a * N + j) * N + k] = db;
+      t3[(a * N + j) * N + k] = bd;
+    }
+  }
+  group_sync<G>(gid);
+  if (active) {
+    const int j = pl / N, k = pl % N;
+    f2 w1[N], w2[N], w3[N];
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+      w1[a] = t1[(a * N + j) * N + k];
+      w2[a] = t2[(a * N + j) * N + k];
+      w3[a] = t3[(a * N + j) * N + k];
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      f2 x = mul2(bcast(c_Dp[O + i * N]), w1[0]), y = mul2(bcast(c_Bp[O + i * N]), w2[0]), z = mul2(bcast(c_Bp[O + i * N]), w3[0]);
+      f2 uu = 0;
+      if (WANT_U) uu = mul2(bcast(c_Bp[O + i * N]), w1[0]);
+#pragma unroll
+      for (int a = 1; a < N; a++) {
+        x = fma2(bcast(c_Dp[O + i * N + a]), w1[a], x);
+        y = fma2(bcast(c_Bp[O + i * N + a]), w2[a], y);
+        z = fma2(bcast(c_Bp[O + i * N + a]), w3[a], z);
+        if (WANT_U) uu = fma2(bcast(c_Bp[O + i * N + a]), w1[a], uu);
+      }
+      gx[i] = x; gy[i] = y; gz[i] = z;
+      if (WANT_U) uq[i] = uu;
+    }
+  }
+  group_sync<G>(gid);
+}
+
+// transposed chain on packed pairs (see hex_backward in matfree.cu)
+template <int N, bool WANT_M>
+__device__ __forceinline__ void pair_backward(int pl, bool active, int gid, f2* su, f2* s1, f2* s2, f2* t2, f2* t3,
+                                              const f2* vx, const f2* vy, const f2* vz, const f2* vm) {
+  constexpr int G = HexCfg<N>::G, O = tab_off(N);
+  f2* t1 = su;
+  if (active) {
+    const int j = pl / N, k = pl % N;
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+      f2 w1 = mul2(bcast(c_Dp[O + a]), vx[0]), w2 = mul2(bcast(c_Bp[O + a]), vy[0]), w3 = mul2(bcast(c_Bp[O + a]), vz[0]);
+      if (WANT_M) w1 = fma2(bcast(c_Bp[O + a]), vm[0], w1);
+#pragma unroll
+      for (int i = 1; i < N; i++) {
+        w1 = fma2(bcast(c_Dp[O + i * N + a]), vx[i], w1);
+        if (WANT_M) w1 = fma2(bcast(c_Bp[O + i * N + a]), vm[i], w1);
+        w2 = fma2(bcast(c_Bp[O + i * N + a]), vy[i], w2);
+        w3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], w3);
+      }
+      t1[(a * N + j) * N + k] = w1;
+      t2[(a * N + j) * N + k] = w2;
+      t3[(a * N + j) * N + k] = w3;
+    }
+  }
+  group_sync<G>(gid);
+  if (active) {
+    const int a = pl / N, k = pl % N;
+    f2 r1[N], r2[N], r3[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      r1[j] = t1[(a * N + j) * N + k];
+      r2[j] = t2[(a * N + j) * N + k];
+      r3[j] = t3[(a * N + j) * N + k];
+    }
+#pragma unroll
+    for (int b = 0; b < N; b++) {
+      f2 v1 = mul2(bcast(c_Bp[O + b]), r1[0]), v2 = mul2(bcast(c_Bp[O + b]), r3[0]);
+      v1 = fma2(bcast(c_Dp[O + b]), r2[0], v1);
+#pragma unroll
+      for (int j = 1; j < N; j++) {
+        v1 = fma2(bcast(c_Bp[O + j * N + b]), r1[j], v1);
+        v1 = fma2(bcast(c_Dp[O + j * N + b]), r2[j], v1);
+        v2 = fma2(bcast(c_Bp[O + j * N + b]), r3[j], v2);
+      }
+      s1[(a * N + b) * N + k] = v1;
+      s2[(a * N + b) * N + k] = v2;
+    }
+  }
+  group_sync<G>(gid);
+  if (active) {
+    const int a = pl / N, b = pl % N;
+    f2 r1[N], r2[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) { r1[k] = s1[(a * N + b) * N + k]; r2[k] = s2[(a * N + b) * N + k]; }
+#pragma unroll
+    for (int c = 0; c < N; c++) {
+      f2 v = mul2(bcast(c_Bp[O + c]), r1[0]);
+      v = fma2(bcast(c_Dp[O + c]), r2[0], v);
+#pragma unroll
+      for (int k = 1; k < N; k++) {
+        v = fma2(bcast(c_Bp[O + k * N + c]), r1[k], v);
+        v = fma2(bcast(c_Dp[O + k * N + c]), r2[k], v);
+      }
+      su[(a * N + b) * N + c] = v;
+    }
+  }
+  group_sync<G>(gid);
+}
+
+template <int N, bool MASS, int GM>
+__global__ void __launch_bounds__(PairCfg<N>::BLOCK, pair_min_blocks(N, MASS, GM))
+hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const float* __restrict__ Gq, int gstride,
+                      const float* __restrict__ x, float* __restrict__ y, int first_cell, double* partial,
+                      unsigned int* counter, double* energy, const int* skip, int* err) {
+  using C = PairCfg<N>;
+  constexpr int N2 = C::N2, N3 = C::N3, G = C::G, S = C::S, E = C::E, SN3 = S * N3, NG = C::NG;
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int gid = threadIdx.x / G, lane = threadIdx.x % G;
+  const int slot = lane / N2, pl = lane % N2;
+  const int rowg = (int)(round16((size_t)gstride * sizeof(float)) / sizeof(float));  // floats per G row
+  const int rowt = (int)(round16((size_t)tstride * sizeof(int)) / sizeof(int));       // ints per DOF row
+  const size_t gb = GM == 0 ? C::gbytes(gstride) : 0, tb = C::tbytes(tstride);
+  unsigned char* gp = smem_raw + (size_t)gid * C::group(gstride, tstride, GM);
+  float* gbuf = (float*)gp;
+  auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };
+  f2* work = (f2*)(gp + gb + 2 * tb);
+  const int so = slot < S ? slot * N3 : 0;
+  f2 *su = work + so, *s1 = work + SN3 + so, *s2 = work + 2 * SN3 + so, *t2 = work + 3 * SN3 + so,
+     *t3 = work + 4 * SN3 + so;
+  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + C::work);  // [0],[1]: DOF rows, [2]: G tiles
+  if (lane == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int nch = (ne + E - 1) / E;
+  const int stride = gridDim.x * C::EPB;
+  int ch = blockIdx.x * C::EPB + gid;
+  auto rows_of = [&](int c) { return min(E, ne - c * E); };
+  auto issue_t = [&](int c, int b) {
+    const uint32_t bytes = (uint32_t)(rows_of(c) * rowt * sizeof(int));
+    mbar_expect_tx(&mbar[b], bytes);
+    bulk_g2s(tbuf(b), tdof + (size_t)c * E * tstride, bytes, &mbar[b]);
+  };
+  auto issue_g = [&](int c) {
+    const uint32_t bytes = (uint32_t)(rows_of(c) * rowg * sizeof(float));
+    mbar_expect_tx(&mbar[2], bytes);
+    bulk_g2s(gbuf, Gq + (size_t)c * E * gstride, bytes, &mbar[2]);
+  };
+  // gathered pairs of the chunk: position t = s*N3 + l -> (element 2s, 2s+1; local DOF l).
+  // Plain loads only: nothing consumes them until the chunk starts (put_x), so the
+  // gather latency overlaps the rest of the current chunk.
+  auto gather = [&](int c, const int* tn, f2* xr) {
+    const int nrow = rows_of(c);
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int t = lane + j * G;
+      float v0 = 0.f, v1 = 0.f;
+      if (t < SN3) {
+        const int s = t / N3, l = t % N3;
+        if (2 * s < nrow) v0 = __ldg(x + (tn[(2 * s) * rowt + l] & 0x7fffffff));
+        if (2 * s + 1 < nrow) v1 = __ldg(x + (tn[(2 * s + 1) * rowt + l] & 0x7fffffff));
+      }
+      xr[j] = pack2(v0, v1);
+    }
+  };
+  // signed coefficients into the work array (shape signs: bit 31 of the DOF rows)
+  auto put_x = [&](int c, const int* tn, const f2* xr) {
+    const int nrow = rows_of(c);
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int t = lane + j * G;
+      if (t < SN3) {
+        const int s = t / N3, l = t % N3;
+        const unsigned d0 = 2 * s < nrow ? (unsigned)tn[(2 * s) * rowt + l] : 0u;
+        const unsigned d1 = 2 * s + 1 < nrow ? (unsigned)tn[(2 * s + 1) * rowt + l] : 0u;
+        work[t] = xr[j] ^ (((f2)(d1 & 0x80000000u) << 32) | (f2)(d0 & 0x80000000u));
+      }
+    }
+  };
+  f2 xr[NG];
+  f2 acc = 0;  // per-lane energy of both elements (working precision)
+  int t_issued = 0, t_waited = 0, g_issued = 0, g_waited = 0;
+  bool ok = true;
+  if (ch < nch) {
+    if (lane == 0) {
+      issue_t(ch, 0);
+      if (GM == 0) issue_g(ch);
+      else bulk_prefetch_l2(Gq + (size_t)ch * E * gstride, (uint32_t)(rows_of(ch) * rowg * sizeof(float)));
+    }
+    t_issued = 1;
+    g_issued = GM == 0 ? 1 : 0;
+    ok = group_all<G>(gid, mbar_wait_bounded(&mbar[0], 0));
+    t_waited = 1;
+    if (ok) gather(ch, tbuf(0), xr);
+  }
+  for (int k = 0; ok && ch < nch; ch += stride, k++) {
+    const int b = k & 1;
+    const bool has_next = ch + stride < nch;
+    const int e0 = ch * E + 2 * slot;  // first element of this lane's pair
+    const bool active = slot < S && e0 < ne;
+    const bool second = active && e0 + 1 < ne;
+    put_x(ch, tbuf(b), xr);
+    if (lane == 0 && has_next) {
+      fence_proxy_async();
+      issue_t(ch + stride, b ^ 1);
+      // G mode 1 reads the next chunk's G rows with plain loads: stage them in L2 now
+      if (GM == 1) bulk_prefetch_l2(Gq + (size_t)(ch + stride) * E * gstride, (uint32_t)(rows_of(ch + stride) * rowg * sizeof(float)));
+    }
+    if (has_next) t_issued++;
+    group_sync<G>(gid);
+    f2 gx[N], gy[N], gz[N], uq[N];
+    pair_forward<N, MASS>(pl, active, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
+    if (has_next) {
+      ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
+      t_waited++;
+      if (!ok) break;
+      gather(ch + stride, tbuf(b ^ 1), xr);
+    }
+    if (GM == 0) {
+      ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
+      g_waited++;
+      if (!ok) break;
+    }
+    // G rows of the pair; a missing second element reuses the first row (its
+    // gathered coefficients are zero, so its half stays zero and finite)
+    const int r0 = active ? 2 * slot : 0, r1 = second ? r0 + 1 : r0;
+    const float* Ga = GM == 0 ? gbuf + (size_t)r0 * rowg : Gq + ((size_t)ch * E + r0) * gstride;
+    const float* Gb = GM == 0 ? gbuf + (size_t)r1 * rowg : Gq + ((size_t)ch * E + r1) * gstride;
+    f2 vx[N], vy[N], vz[N], vm[N];
+    if (active) {
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        const int o = i * N2 + pl;
+        auto ld = [&](int comp) {
+          if (GM == 0) return pack2(Ga[comp * N3 + o], Gb[comp * N3 + o]);
+          return pack2(__ldcs(Ga + comp * N3 + o), __ldcs(Gb + comp * N3 + o));
+        };
+        const f2 gxx = ld(0), gyy = ld(1), gzz = ld(2), gxy = ld(3), gxz = ld(4), gyz = ld(5);
+        vx[i] = fma2(gxz, gz[i], fma2(gxy, gy[i], mul2(gxx, gx[i])));
+        vy[i] = fma2(gyz, gz[i], fma2(gyy, gy[i], mul2(gxy, gx[i])));
+        vz[i] = fma2(gzz, gz[i], fma2(gyz, gy[i], mul2(gxz, gx[i])));
+        f2 en = fma2(gz[i], vz[i], fma2(gy[i], vy[i], mul2(gx[i], vx[i])));
+        if (MASS) {
+          vm[i] = mul2(ld(6), uq[i]);
+          en = fma2(uq[i], vm[i], en);
+        }
+        acc = add2(acc, en);
+      }
+    }
+    if (GM == 0) {
+      group_sync<G>(gid);
+      if (lane == 0 && has_next) {
+        fence_proxy_async();
+        issue_g(ch + stride);
+      }
+      if (has_next) g_issued++;
+    }
+    pair_backward<N, MASS>(pl, active, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
+    const int* td = tbuf(b);
+    const int nrow = rows_of(ch);
+#pragma unroll
+    for (int j = 0; j < NG; j++) {
+      const int t = lane + j * G;
+      if (t < SN3) {
+        const int s = t / N3, l = t % N3;
+        float v0, v1;
+        unpack2(work[t], v0, v1);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          if (2 * s + h < nrow) {
+            const int d = td[(2 * s + h) * rowt + l];
+            const int dof = d & 0x7fffffff;
+            const float v = __int_as_float(__float_as_int(h ? v1 : v0) ^ (d & (int)0x80000000));
+            if (dof >= first_cell) y[dof] = v;  // element-interior DOF: single writer
+            else atomicAdd(y + dof, v);
+          }
+        }
+      }
+    }
+    group_sync<G>(gid);
+  }
+  if (!ok) {
+    if (lane == 0) {
+      atomicExch(err, 1);
+      for (int j = t_waited; j < t_issued; j++) mbar_wait_bounded(&mbar[j & 1], (j >> 1) & 1);
+      for (int j = g_waited; j < g_issued; j++) mbar_wait_bounded(&mbar[2], j & 1);
+    }
+    group_sync<G>(gid);
+  }
+  if (partial) {
+    float a0, a1;
+    unpack2(acc, a0, a1);
+    block_reduce_finish((double)a0 + (double)a1, partial, counter, energy);
+  }
+}
+
+// ---- host side ------------------------------------------------------------------
+bool hex_pair_supported(int N) { return N >= 2 && N <= 7; }
+
+void upload_pair_tables(gh1_space* sp) {
+  const int N = sp->p + 1;
+  if (!hex_pair_supported(N)) return;
+  const size_t off = tab_off(N) * sizeof(float);
+  cudaStream_t s = sp->ctx->stream;
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_Bp, sp->d_B32.p, N * N * sizeof(float), off, cudaMemcpyDeviceToDevice, s));
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_Dp, sp->d_D32.p, N * N * sizeof(float), off, cudaMemcpyDeviceToDevice, s));
+}
+
+template <int N, bool MASS, int GM>
+static int pair_occupancy(size_t smem) {
+  static bool attr = false;
+  auto kern = hex_apply_pair_kernel<N, MASS, GM>;
+  if (!attr) {
+    int dev = 0, optin = 0;
+    GH1_CUDA(cudaGetDevice(&dev));
+    GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+    GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    attr = true;
+  }
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, PairCfg<N>::BLOCK, smem));
+  return v;
+}
+
+template <int N, bool MASS, int GM>
+static void pair_launch(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                        const int* skip) {
+  using C = PairCfg<N>;
+  gh1_space* sp = op->sp;
+  const size_t smem = C::total(op->gstride32, sp->tstride, GM);
+  const int per_sm = op->pair_per_sm[GM];
+  GH1_CHECK(per_sm > 0, GH1_ERR_ARG, "internal: paired hex apply occupancy not prepared");
+  const int ne = sp->mesh->ne;
+  const int nch = (ne + C::E - 1) / C::E;
+  const int blocks_needed = (nch + C::EPB - 1) / C::EPB;
+  const int grid = std::min(blocks_needed, sp->ctx->nsm * per_sm);
+  hex_apply_pair_kernel<N, MASS, GM><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(
+      ne, sp->d_tdof.p, sp->tstride, op->d_G32.p, op->gstride32, x, y, (int)sp->first_cell, partial, counter, energy,
+      skip, op->d_err.p);
+  check_kernel(sp->ctx, "hex_apply_pair_kernel");
+}
+
+#define GH1_PAIR_SWITCH(N, CASE)                                                     \
+  switch (N) {                                                                       \
+    CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7)                                  \
+    default: throw Error(GH1_ERR_UNSUPPORTED, "paired hex apply: order out of range"); \
+  }
+
+int hex_pair_occupancy(gh1_op* op, int gm) {
+  const bool mass = op->has_mass;
+  const int ts = op->sp->tstride, gs = op->gstride32;
+  int v = 0;
+#define GH1_PAIR_OCC(NN)                                                                                       \
+  case NN:                                                                                                     \
+    if (gm == 0) v = mass ? pair_occupancy<NN, true, 0>(PairCfg<NN>::total(gs, ts, 0))                        \
+                          : pair_occupancy<NN, false, 0>(PairCfg<NN>::total(gs, ts, 0));                      \
+    else v = mass ? pair_occupancy<NN, true, 1>(PairCfg<NN>::total(gs, ts, 1))                                \
+                  : pair_occupancy<NN, false, 1>(PairCfg<NN>::total(gs, ts, 1));                              \
+    break;
+  GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_OCC)
+#undef GH1_PAIR_OCC
+  return v;
+}
+
+void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partial, unsigned int* counter,
+                    double* energy, const int* skip) {
+  const bool mass = op->has_mass;
+#define GH1_PAIR_CASE(NN)                                                                       \
+  case NN:                                                                                      \
+    if (gm == 0) {                                                                              \
+      if (mass) pair_launch<NN, true, 0>(op, x, y, partial, counter, energy, skip);             \
+      else pair_launch<NN, false, 0>(op, x, y, partial, counter, energy, skip);                 \
+    } else {                                                                                    \
+      if (mass) pair_launch<NN, true, 1>(op, x, y, partial, counter, energy, skip);             \
+      else pair_launch<NN, false, 1>(op, x, y, partial, counter, energy, skip);                 \
+    }                                                                                           \
+    break;
+  GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)
+#undef GH1_PAIR_CASE
+}
+
+}  // namespace gh1

@@ -28,6 +28,7 @@
 #include <vector>
 #include "common.cuh"
 #include "basis.cuh"
+#include "hexcore.cuh"
 
 namespace gh1 {
 
@@ -126,8 +127,6 @@ __global__ void tet_geom_kernel(int ne, const double* __restrict__ X, const int*
 // 1D hex factor tables B[q][a] = psi_a(x_q), D[q][a] = psi_a'(x_q) of every order
 // in constant memory: with the contraction loops unrolled the FMAs take their
 // table operand straight from the constant bank (no shared-memory load per FMA).
-constexpr int tab_off(int N) { return N <= 2 ? 0 : tab_off(N - 1) + (N - 1) * (N - 1); }
-constexpr int TAB_TOTAL = tab_off(MAX_HEX_ORDER + 2);
 __constant__ float c_B32[TAB_TOTAL], c_D32[TAB_TOTAL];
 __constant__ double c_B64[TAB_TOTAL], c_D64[TAB_TOTAL];
 template <class T> struct CTab;
@@ -149,63 +148,6 @@ void upload_const_tables(gh1_space* sp) {
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_D64, sp->d_D64.p, N * N * sizeof(double), off * sizeof(double), cudaMemcpyDeviceToDevice, s));
 }
 
-// ---------------------------------------------------------------------------
-// thread-group helpers
-template <int G>
-__device__ __forceinline__ void group_sync(int gid) {
-  if (G == 32) __syncwarp();
-  else asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(G) : "memory");
-}
-
-template <class T>
-__device__ __forceinline__ void atomic_add_t(T* p, T v) { atomicAdd(p, v); }
-
-// End-of-kernel reduction of one double per thread into partial[blockIdx.x];
-// the last block to finish sums all partials into *out and resets the counter.
-// (threadfence reduction: no block waits on another.)
-__device__ void block_reduce_finish(double v, double* partial, unsigned int* counter, double* out) {
-  __shared__ double red[32];
-  __shared__ bool last;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0;
-    for (int i = 0; i < (int)(blockDim.x + 31) / 32; i++) s += red[i];
-    partial[blockIdx.x] = s;
-    __threadfence();
-    unsigned int t = atomicAdd(counter, 1u);
-    last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    double s = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double*)partial)[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (l == 0) red[w] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double tot = 0;
-      for (int i = 0; i < (int)(blockDim.x + 31) / 32; i++) tot += red[i];
-      *out = tot;
-      *counter = 0u;
-    }
-  }
-}
-
-template <int N>
-struct HexCfg {
-  static constexpr int N2 = N * N, N3 = N * N * N;
-  static constexpr int G = ((N2 + 31) / 32) * 32;  // threads per element group
-  static constexpr int EPW = N2 <= 32 ? 32 / N2 : 1;  // elements per group (low orders share a warp)
-  static constexpr int EPB = G == 32 ? 4 : 2;      // element groups per block
-  static constexpr int BLOCK = G * EPB;
-};
-
-__host__ __device__ constexpr size_t round16(size_t b) { return (b + 15) / 16 * 16; }
-
 // shared memory of the pipelined apply, per element group:
 //   [G tile (G mode 0 only)] | DOF-table tile x2 | 5 work arrays | 3 mbarriers
 template <int N, class T>
@@ -223,49 +165,6 @@ struct HexSmem {
   }
 };
 
-// ---- bulk-copy (TMA) and mbarrier helpers ------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-// global -> shared bulk copy (size and both addresses multiples of 16 bytes)
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-               : "=r"(ok)
-               : "r"(smem_u32(bar)), "r"(parity)
-               : "memory");
-  return ok != 0;
-}
-// bounded wait: false after ~2^22 polls (an error, never expected)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 22); i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-// all threads of the element group agree on a predicate
-template <int G>
-__device__ __forceinline__ bool group_all(int gid, bool v) {
-  if (G == 32) return __all_sync(0xffffffffu, v);
-  uint32_t r;
-  asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
-               : "=r"(r)
-               : "r"((uint32_t)v), "r"(gid + 1), "r"(G)
-               : "memory");
-  return r != 0;
-}
 
 // Forward chain: gathered coefficients in su[(a*N+b)*N+c] -> reference gradient
 // components at the qp of lane (j,k) for all i (registers gx[i], gy[i], gz[i]),
@@ -1009,7 +908,14 @@ template <class T>
 void hex_apply_dispatch(gh1_op* op, const T* x, T* y, const T* G, int gstride, double* partial, unsigned int* counter,
                         double* energy, const int* skip) {
   const int pi = std::is_same<T, float>::value ? 1 : 0;
-  if (op->hex_gmode[pi] == 0) hex_apply_dispatch_gm<T, 0>(op, x, y, G, gstride, partial, counter, energy, skip);
+  const int gm = op->hex_gmode[pi];
+  if constexpr (std::is_same<T, float>::value) {
+    if (gm >= 2) {
+      hex_pair_apply(op, gm - 2, x, y, partial, counter, energy, skip);
+      return;
+    }
+  }
+  if (gm == 0) hex_apply_dispatch_gm<T, 0>(op, x, y, G, gstride, partial, counter, energy, skip);
   else hex_apply_dispatch_gm<T, 1>(op, x, y, G, gstride, partial, counter, energy, skip);
 }
 
@@ -1028,15 +934,19 @@ int hex_occupancy_dispatch(gh1_op* op, int gstride) {
   return v;
 }
 
-// Autotuner: times each G-staging variant (TMA tile in shared memory vs direct
-// coalesced loads) on this operator's own mesh and keeps the faster one.  The
-// choice is cached per (order, precision, element-count bucket) for the process.
+// Autotuner: times each variant -- G tile staged in shared memory by TMA vs
+// direct coalesced loads, and for FP32 each of those with two elements per lane
+// -- on this operator's own mesh and keeps the fastest.  The choice is cached per
+// (order, precision, element-count bucket) for the process.  GH1_HEX_GMODE=0..3
+// forces a variant (FP64 takes it modulo 2).
 template <class T>
 void hex_autotune(gh1_op* op, const T* G, int gstride) {
   const int pi = std::is_same<T, float>::value ? 1 : 0;
+  const int nmodes = (pi == 1 && op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) ? 4 : 2;
   const char* env = getenv("GH1_HEX_GMODE");
-  if (env && (env[0] == '0' || env[0] == '1')) {
-    op->hex_gmode[pi] = env[0] - '0';
+  if (env && env[0] >= '0' && env[0] <= '3') {
+    const int m = env[0] - '0';
+    op->hex_gmode[pi] = m < nmodes ? m : m % 2;
     return;
   }
   static std::vector<std::array<int, 4>> cache;  // N, precision, log2(ne), choice
@@ -1057,7 +967,7 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   GH1_CUDA(cudaEventCreate(&b));
   float best = 1e30f;
   int choice = 0;
-  for (int gm = 0; gm < 2; gm++) {
+  for (int gm = 0; gm < nmodes; gm++) {
     op->hex_gmode[pi] = gm;
     for (int r = 0; r < 2; r++) hex_apply_dispatch<T>(op, xs.p, ys.p, G, gstride, nullptr, nullptr, nullptr, nullptr);
     GH1_CUDA(cudaEventRecord(a, s));
@@ -1175,6 +1085,11 @@ void matfree_setup(gh1_op* op) {
     if (want32) {
       op->hex_per_sm[1][0] = hex_occupancy_dispatch<float, 0>(op, op->gstride32);
       op->hex_per_sm[1][1] = hex_occupancy_dispatch<float, 1>(op, op->gstride32);
+      if (hex_pair_supported(sp->p + 1)) {
+        upload_pair_tables(sp);
+        op->pair_per_sm[0] = hex_pair_occupancy(op, 0);
+        op->pair_per_sm[1] = hex_pair_occupancy(op, 1);
+      }
     }
     hex_autotune<double>(op, op->d_G64.p, op->gstride64);
     if (want32) hex_autotune<float>(op, op->d_G32.p, op->gstride32);
