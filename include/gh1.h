@@ -108,7 +108,10 @@ int gh1_matfree_create(gh1_form* form, int precision_mask, gh1_op** op);
 /* BaseMatrix::Mult / MultAdd (linalg/basematrix.hpp:117-126):
  * y = s*A*x (accumulate=0) or y += s*A*x (accumulate=1); device pointers. */
 int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, int accumulate);
-/* info[0..3] = kind (GH1_OP_*), nrows, ne, order */
+/* info[0..5] = kind (GH1_OP_*), nrows, ne, order, and for a hex matrix-free
+ * operator the autotuned apply variant in FP64 and FP32 (0 / 1: one element per
+ * lane with the G tile staged by bulk copy / loaded directly; 2 / 3: the same
+ * with two elements per lane, FP32 only; -1: not applicable) */
 int gh1_op_info(gh1_op* op, int64_t* info);
 int gh1_op_free(gh1_op* op);
 

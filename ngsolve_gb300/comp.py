@@ -392,6 +392,13 @@ class BaseMatrix:
     def __init__(self, ctx, h, height, fes=None):
         self.ctx, self.h, self.height, self.width, self.fes = ctx, h, int(height), int(height), fes
 
+    def Info(self):
+        """kind, nrows, ne, order and (hex matrix-free) the apply variant per precision."""
+        a = (ctypes.c_int64 * 6)()
+        self.ctx.check(self.ctx.lib.gh1_op_info(self.h, a))
+        return {"kind": a[0], "nrows": a[1], "ne": a[2], "order": a[3], "hex_variant_fp64": a[4],
+                "hex_variant_fp32": a[5]}
+
     def __mul__(self, x):
         return _MatVec(self, _as_vec(x))
 

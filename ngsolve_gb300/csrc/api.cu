@@ -488,6 +488,9 @@ int gh1_op_info(gh1_op* op, int64_t* info) {
   info[0] = op->kind; info[1] = op->nrows;
   info[2] = op->sp ? op->sp->mesh->ne : 0;
   info[3] = op->sp ? op->sp->p : 0;
+  const bool hexmf = op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 8;
+  info[4] = hexmf ? op->hex_gmode[0] : -1;
+  info[5] = hexmf && (op->prec_mask & 2) ? op->hex_gmode[1] : -1;
   return GH1_OK;
 }
 
