@@ -161,6 +161,14 @@ struct gh1_op {
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
   int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
+  // tet tiled apply (tetapply.cu): elements sorted by orientation class, tiles of
+  // up to 32 same-class elements, per-class GEMM tables
+  gh1::DBuf<int> d_tet_perm;                 // class-sorted element order
+  gh1::DBuf<int> d_tet_tiles;                // [ntiles][4] = class, first position, count, 0
+  int tet_ntiles = 0, tet_R = 0, tet_Rp = 0, tet_Rs = 0;
+  gh1::DBuf<double> d_tetD64, d_tetw64;      // [class][nloc][Rs] table rows, per-row weights [Rp]
+  gh1::DBuf<float> d_tetD32, d_tetw32;
+  int tet_tiles_per_sm[2] = {0, 0};          // [FP64/FP32] resident blocks; 0: does not fit, element-wise kernel
   gh1::DBuf<double> d_diag;   // operator diagonal (FP64)
   bool have_diag = false;
   // scratch vectors for accumulate / scaling
@@ -198,6 +206,11 @@ void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* part
                       double* energy, const int* skip);  // matfree.cu
 void mass_apply(gh1_op* op, const double* x, double* y);            // matfree.cu
 void spmv(gh1_op* op, const void* x, void* y, int prec);            // spmv.cu
+// tiled tet apply (tetapply.cu): setup after the tet geometry; apply returns false
+// when the tiled kernel does not fit (the caller then runs the element-wise kernel)
+void tet_tiles_setup(gh1_op* op);
+bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
+                     double* energy, const int* skip);
 // paired FP32 hex apply (hexpair.cu): two elements per lane, packed f32x2 arithmetic
 bool hex_pair_supported(int N);
 void upload_pair_tables(gh1_space* sp);

@@ -1105,6 +1105,7 @@ void matfree_setup(gh1_op* op) {
                                                       want32 ? op->d_G32.p : nullptr, op->has_mass ? op->d_M64.p : nullptr,
                                                       (op->has_mass && want32) ? op->d_M32.p : nullptr);
     check_kernel(sp->ctx, "tet_geom_kernel");
+    tet_tiles_setup(op);
   }
   op->form_version = f->version;
   op->have_diag = false;
@@ -1139,6 +1140,7 @@ void matfree_apply_ex(gh1_op* op, const void* x, void* y, int prec, double* part
       hex_apply_dispatch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->gstride32, partial, counter, energy,
                                 skip);
   } else {
+    if (tet_tiles_apply(op, prec, x, y, partial, counter, energy, skip)) return;
     GH1_CHECK(sp->tet_nq_mass <= 128 || !op->has_mass, GH1_ERR_UNSUPPORTED, "tet mass rule too large");
     if (prec == GH1_F64)
       tet_apply_launch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->has_mass ? op->d_M64.p : nullptr,

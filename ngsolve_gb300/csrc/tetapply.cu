@@ -1,0 +1,323 @@
+// tetapply.cu -- matrix-free tet apply y += A x as two small GEMMs per tile of
+// same-class elements.
+//
+// Same operator as tet_apply_kernel (matfree.cu) and as the reference's
+// element-wise ApplyElementMatrix (fem/symbolicintegrator.cpp:2959-3040) on affine
+// tets: y_e = B^T diag(kappa_e w_q |det J| J^{-1} J^{-T}) B x_e (+ mass).  The
+// reference shapes depend on the element's vertex numbers only through their
+// ranks (orientation class, 24 permutations), so all elements of one class share
+// one table D_c of reference gradients (and values) at the rule points.  Elements
+// are sorted by class once; a tile is up to 32 elements of one class, and per tile
+//   P = D_c^T X           (rows: d/dx, d/dy, d/dz at nq points [+ values at the
+//                          mass rule], columns: elements)
+//   V = per-point 3x3 metric transform of P (per element constant, rule weight)
+//   Y = D_c V             (local residuals), scattered with atomics.
+// Both products are register-tiled FP32/FP64 FMA loops over shared memory
+// (8 column groups of 4 elements x 16 row groups per 128-thread block).  The
+// per-class table stays in shared memory while a block's tiles keep its class.
+#include <algorithm>
+#include <vector>
+#include "common.cuh"
+#include "hexcore.cuh"
+
+namespace gh1 {
+
+constexpr int TET_TT = 128;  // threads per block
+constexpr int TET_TE = 32;   // elements per tile
+constexpr int TET_RB = 8;    // row-tile depth of the first product (rows per thread per pass)
+constexpr int TET_TI = 6;    // maximum row-tile depth of the second product (nloc <= 96)
+
+__host__ __device__ inline size_t tet_r16(size_t b) { return (b + 15) / 16 * 16; }
+
+// shared-memory carve-up of one block
+template <class T>
+struct TetSmem {
+  int nlocp, Rp, Rs;
+  __host__ __device__ size_t d() const { return tet_r16((size_t)nlocp * Rs * sizeof(T)); }
+  __host__ __device__ size_t x() const { return tet_r16((size_t)nlocp * TET_TE * sizeof(T)); }
+  __host__ __device__ size_t p() const { return tet_r16((size_t)Rp * TET_TE * sizeof(T)); }
+  __host__ __device__ size_t w() const { return tet_r16((size_t)Rp * sizeof(T)); }
+  __host__ __device__ size_t g() const { return tet_r16((size_t)TET_TE * 7 * sizeof(T)); }
+  __host__ __device__ size_t dof() const { return tet_r16((size_t)TET_TE * nlocp * sizeof(int)); }
+  __host__ __device__ size_t total() const { return d() + x() + p() + w() + g() + dof(); }
+};
+
+// four consecutive values from shared memory (16-byte aligned)
+__device__ __forceinline__ void ld4(const float* p, float* v) {
+  const float4 a = *(const float4*)p;
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double* v) {
+  const double2 a = *(const double2*)p, b = *(const double2*)(p + 2);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+__device__ __forceinline__ void st4(float* p, const float* v) { *(float4*)p = make_float4(v[0], v[1], v[2], v[3]); }
+__device__ __forceinline__ void st4(double* p, const double* v) {
+  *(double2*)p = make_double2(v[0], v[1]);
+  *(double2*)(p + 2) = make_double2(v[2], v[3]);
+}
+
+// tiles: [ntiles][4] = class, first position in perm, element count, 0.  Block b
+// takes the contiguous tile range [b*ntiles/grid, (b+1)*ntiles/grid), which keeps
+// its class (and the table in shared memory) for most consecutive tiles.
+// D: [class][nlocp][Rs] with rows i >= nloc and columns r >= R zero; W: [Rp].
+// Shared X and DOF rows are [i][element], P is [row][element].
+template <class T, bool MASS>
+__global__ void __launch_bounds__(TET_TT)
+tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int nq,
+                int nqm, int Rp, int Rs, const int* __restrict__ eldofs, const T* __restrict__ Ge,
+                const T* __restrict__ Me, const T* __restrict__ D, const T* __restrict__ W, const T* __restrict__ x,
+                T* __restrict__ y, double* partial, unsigned int* counter, double* energy, const int* skip) {
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const TetSmem<T> L{nlocp, Rp, Rs};
+  T* sD = (T*)smem;
+  T* sX = (T*)(smem + L.d());
+  T* sP = (T*)(smem + L.d() + L.x());
+  T* sW = (T*)(smem + L.d() + L.x() + L.p());
+  T* sG = (T*)(smem + L.d() + L.x() + L.p() + L.w());
+  int* sDof = (int*)(smem + L.d() + L.x() + L.p() + L.w() + L.g());
+  const int tid = threadIdx.x, cg = tid & 7, rg = tid >> 3;  // 4 elements x (rows rg + 16 t)
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  const size_t dsize = (size_t)nlocp * Rs;
+  for (int r = tid; r < Rp; r += TET_TT) sW[r] = W[r];
+  int loaded = -1;
+  double acc = 0;  // energy x^T A x of this thread's quadrature terms
+  for (int t = t0; t < t1; t++) {
+    const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    __syncthreads();  // the previous tile is done with the shared arrays
+    if (cls != loaded) {
+      const T* src = D + (size_t)cls * dsize;
+      for (size_t k = tid; k < dsize; k += TET_TT) sD[k] = src[k];
+      loaded = cls;
+    }
+    for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {  // element index fastest: conflict-free [i][e] stores
+      const int e = k % TET_TE, i = k / TET_TE;
+      int d = 0;
+      T v = 0;
+      if (e < cnt && i < nloc) {
+        d = eldofs[(size_t)perm[start + e] * nloc + i];
+        v = x[d];
+      }
+      sDof[k] = d;
+      sX[k] = v;
+    }
+    for (int k = tid; k < TET_TE * 7; k += TET_TT) {
+      const int e = k / 7, c = k % 7;
+      T v = 0;
+      if (e < cnt) v = c < 6 ? Ge[(size_t)perm[start + e] * 6 + c] : (MASS ? Me[perm[start + e]] : T(0));
+      sG[k] = v;
+    }
+    __syncthreads();
+    // P[r][e] = sum_i D[i][r] X[i][e]
+    for (int r0 = 0; r0 < Rp; r0 += 16 * TET_RB) {
+      const int nt = min(TET_RB, (Rp - r0) / 16);  // block-uniform
+      T a[TET_RB][4];
+#pragma unroll
+      for (int u = 0; u < TET_RB; u++) a[u][0] = a[u][1] = a[u][2] = a[u][3] = 0;
+      for (int i = 0; i < nloc; i++) {
+        T xv[4];
+        ld4(sX + i * TET_TE + 4 * cg, xv);
+        const T* drow = sD + (size_t)i * Rs + r0 + rg;
+#pragma unroll
+        for (int u = 0; u < TET_RB; u++)
+          if (u < nt) {
+            const T dv = drow[16 * u];
+            a[u][0] += dv * xv[0]; a[u][1] += dv * xv[1]; a[u][2] += dv * xv[2]; a[u][3] += dv * xv[3];
+          }
+      }
+#pragma unroll
+      for (int u = 0; u < TET_RB; u++)
+        if (u < nt) {
+          st4(sP + (size_t)(r0 + rg + 16 * u) * TET_TE + 4 * cg, a[u]);
+        }
+    }
+    __syncthreads();
+    // per-point transform v = w_q G_e grad u (and the mass term), in place
+    for (int k = tid; k < nq * TET_TE; k += TET_TT) {
+      const int q = k / TET_TE, e = k % TET_TE;
+      const T* g = sG + e * 7;
+      T* px = sP + (size_t)q * TET_TE + e;
+      T* py = px + (size_t)nq * TET_TE;
+      T* pz = py + (size_t)nq * TET_TE;
+      const T ux = *px, uy = *py, uz = *pz, w = sW[q];
+      const T vx = w * (g[0] * ux + g[3] * uy + g[4] * uz);
+      const T vy = w * (g[3] * ux + g[1] * uy + g[5] * uz);
+      const T vz = w * (g[4] * ux + g[5] * uy + g[2] * uz);
+      acc += (double)(ux * vx + uy * vy + uz * vz);
+      *px = vx; *py = vy; *pz = vz;
+    }
+    if (MASS) {
+      for (int k = tid; k < nqm * TET_TE; k += TET_TT) {
+        const int q = k / TET_TE, e = k % TET_TE;
+        T* pm = sP + (size_t)(3 * nq + q) * TET_TE + e;
+        const T u = *pm, vm = sW[3 * nq + q] * sG[e * 7 + 6] * u;
+        acc += (double)(u * vm);
+        *pm = vm;
+      }
+    }
+    __syncthreads();
+    // Y[i][e] = sum_r D[i][r] V[r][e], rows i = rg + 16 t; scatter
+    T b[TET_TI][4];
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    const int ni = nlocp / 16;  // block-uniform
+    for (int r = 0; r < Rp; r++) {
+      T pv[4];
+      ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
+#pragma unroll
+      for (int u = 0; u < TET_TI; u++)
+        if (u < ni) {
+          const T dv = sD[(size_t)(rg + 16 * u) * Rs + r];
+          b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) {
+      const int i = rg + 16 * u;
+      if (u < ni && i < nloc) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int e = 4 * cg + c;
+          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+        }
+      }
+    }
+  }
+  if (partial) block_reduce_finish(acc, partial, counter, energy);
+}
+
+// D[c][i][r] from the per-class tables: rows r < 3 nq are d/dx, d/dy, d/dz of
+// shape i at the stiffness-rule points (tab[c][q][i][1..3]); the next nqm rows the
+// values at the mass-rule points (tabm[c][q][i]); everything else zero
+template <class T>
+__global__ void tet_tile_table_kernel(int ncls, int nloc, int nlocp, int nq, int nqm, int R, int Rs,
+                                      const T* __restrict__ tab, const double* __restrict__ tabm, T* D) {
+  const int64_t tot = (int64_t)ncls * nlocp * Rs;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(k % Rs), i = (int)((k / Rs) % nlocp), c = (int)(k / ((int64_t)Rs * nlocp));
+    T v = 0;
+    if (i < nloc && r < R) {
+      if (r < 3 * nq) v = tab[(((size_t)c * nq + r % nq) * nloc + i) * 4 + 1 + r / nq];
+      else v = (T)tabm[((size_t)c * nqm + (r - 3 * nq)) * nloc + i];
+    }
+    D[k] = v;
+  }
+}
+
+template <class T, bool MASS>
+static int tet_tile_occupancy(size_t smem) {
+  auto kern = tet_tile_kernel<T, MASS>;
+  int dev = 0, optin = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const int avail = optin - (int)fa.sharedSizeBytes;
+  if ((long long)smem > avail) return 0;
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, avail));
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TET_TT, smem));
+  return v;
+}
+
+// Class-sorted element order, tiles, tables and occupancy.  GH1_TET_KERNEL=elementwise
+// keeps the element-wise kernel (for comparisons).
+void tet_tiles_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->tet_tiles_per_sm[0] = op->tet_tiles_per_sm[1] = 0;
+  const char* env = getenv("GH1_TET_KERNEL");
+  if (env && std::string(env) == "elementwise") return;
+  const int ne = sp->mesh->ne, nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
+  const int nlocp = (nloc + 15) / 16 * 16;
+  if (nlocp / 16 > TET_TI || ne == 0) return;
+  const int R = 3 * nq + (op->has_mass ? nqm : 0), Rp = (R + 15) / 16 * 16, Rs = Rp + 1;
+  const int ncls = N_TET_CLASSES;
+  cudaStream_t s = sp->ctx->stream;
+  // counting sort by class, tiles of up to TET_TE elements of one class
+  std::vector<uint8_t> cls(ne);
+  GH1_CUDA(cudaMemcpyAsync(cls.data(), sp->d_class.p, ne, cudaMemcpyDeviceToHost, s));
+  std::vector<double> rule(4 * (size_t)nq), rulem(4 * (size_t)nqm);
+  GH1_CUDA(cudaMemcpyAsync(rule.data(), sp->d_tq.p, rule.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (nqm) GH1_CUDA(cudaMemcpyAsync(rulem.data(), sp->d_tqm.p, rulem.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> count(ncls + 1, 0), perm(ne), tiles;
+  for (int e = 0; e < ne; e++) count[cls[e] + 1]++;
+  for (int c = 0; c < ncls; c++) count[c + 1] += count[c];
+  std::vector<int> pos(count.begin(), count.end() - 1);
+  for (int e = 0; e < ne; e++) perm[pos[cls[e]]++] = e;
+  for (int c = 0; c < ncls; c++)
+    for (int a = count[c]; a < count[c + 1]; a += TET_TE) {
+      tiles.push_back(c);
+      tiles.push_back(a);
+      tiles.push_back(std::min(TET_TE, count[c + 1] - a));
+      tiles.push_back(0);
+    }
+  std::vector<double> w(Rp, 0.0);
+  for (int r = 0; r < 3 * nq; r++) w[r] = rule[4 * (r % nq) + 3];
+  if (op->has_mass)
+    for (int q = 0; q < nqm; q++) w[3 * nq + q] = rulem[4 * q + 3];
+  op->d_tet_perm.upload(perm, s);
+  op->d_tet_tiles.upload(tiles, s);
+  op->tet_ntiles = (int)tiles.size() / 4;
+  op->tet_R = R; op->tet_Rp = Rp; op->tet_Rs = Rs;
+  const int64_t tot = (int64_t)ncls * nlocp * Rs;
+  const int tgrid = (int)std::min<int64_t>((tot + 255) / 256, 4096);
+  const bool mass = op->has_mass;
+  op->d_tetD64.alloc(tot);
+  tet_tile_table_kernel<double><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, R, Rs, sp->d_tab64.p, sp->d_tabm64.p,
+                                                      op->d_tetD64.p);
+  check_kernel(sp->ctx, "tet_tile_table_kernel");
+  op->d_tetw64.upload(w, s);
+  const TetSmem<double> L64{nlocp, Rp, Rs};
+  op->tet_tiles_per_sm[0] = mass ? tet_tile_occupancy<double, true>(L64.total()) : tet_tile_occupancy<double, false>(L64.total());
+  if (op->prec_mask & 2) {
+    op->d_tetD32.alloc(tot);
+    tet_tile_table_kernel<float><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, R, Rs, sp->d_tab32.p, sp->d_tabm64.p,
+                                                       op->d_tetD32.p);
+    check_kernel(sp->ctx, "tet_tile_table_kernel");
+    std::vector<float> w32(w.begin(), w.end());
+    op->d_tetw32.upload(w32, s);
+    const TetSmem<float> L32{nlocp, Rp, Rs};
+    op->tet_tiles_per_sm[1] = mass ? tet_tile_occupancy<float, true>(L32.total()) : tet_tile_occupancy<float, false>(L32.total());
+  }
+  GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+}
+
+template <class T>
+static void tet_tile_launch(gh1_op* op, int per_sm, const T* D, const T* W, const T* G, const T* M, const T* x, T* y,
+                            double* partial, unsigned int* counter, double* energy, const int* skip) {
+  gh1_space* sp = op->sp;
+  const int nlocp = (sp->nloc + 15) / 16 * 16;
+  const TetSmem<T> L{nlocp, op->tet_Rp, op->tet_Rs};
+  const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
+  if (op->has_mass)
+    tet_tile_kernel<T, true><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, sp->tet_nq, sp->tet_nq_mass, op->tet_Rp,
+        op->tet_Rs, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy, skip);
+  else
+    tet_tile_kernel<T, false><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, sp->tet_nq, sp->tet_nq_mass, op->tet_Rp,
+        op->tet_Rs, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy, skip);
+  check_kernel(sp->ctx, "tet_tile_kernel");
+}
+
+bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
+                     double* energy, const int* skip) {
+  const int pi = prec == GH1_F64 ? 0 : 1;
+  const int per_sm = op->tet_tiles_per_sm[pi];
+  if (per_sm <= 0) return false;
+  if (prec == GH1_F64)
+    tet_tile_launch<double>(op, per_sm, op->d_tetD64.p, op->d_tetw64.p, op->d_G64.p,
+                            op->has_mass ? op->d_M64.p : nullptr, (const double*)x, (double*)y, partial, counter,
+                            energy, skip);
+  else
+    tet_tile_launch<float>(op, per_sm, op->d_tetD32.p, op->d_tetw32.p, op->d_G32.p,
+                           op->has_mass ? op->d_M32.p : nullptr, (const float*)x, (float*)y, partial, counter,
+                           energy, skip);
+  return true;
+}
+
+}  // namespace gh1

@@ -1,0 +1,99 @@
+"""Matrix-free tet apply: the class-tiled GEMM kernel and the element-wise
+kernel (GH1_TET_KERNEL=elementwise) against the FP64 oracle, FP64 and FP32,
+with and without the mass term; tiles straddle no class boundary, so meshes with
+many classes and partially filled tiles are used."""
+import contextlib
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior, Mesh as RawMesh
+from tests.util import lognormal, permute_tets
+
+pytestmark = pytest.mark.gpu
+
+
+@contextlib.contextmanager
+def tet_kernel(name):
+    old = os.environ.get("GH1_TET_KERNEL")
+    if name is None:
+        os.environ.pop("GH1_TET_KERNEL", None)
+    else:
+        os.environ["GH1_TET_KERNEL"] = name
+    try:
+        yield
+    finally:
+        if old is None:
+            os.environ.pop("GH1_TET_KERNEL", None)
+        else:
+            os.environ["GH1_TET_KERNEL"] = old
+
+
+def _mesh(n, seed):
+    m = JitterInterior(MakeStructured3DMesh(hexes=False, nx=n), 0.2 / n, seed)
+    return RawMesh(m.points, permute_tets(m.elements, seed + 1))  # all 24 orientation classes
+
+
+def _form(gpu, fes, kappa, mu, kernel):
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, nonassemble=True, precision="fp32")
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    if mu is not None:
+        a += gpu.CoefficientFunction(mu) * u * v * gpu.dx
+    with tet_kernel(kernel):
+        a.Assemble()
+    return a
+
+
+@pytest.mark.parametrize("kernel", [None, "elementwise"])
+@pytest.mark.parametrize("mass", [False, True])
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_tet_apply_parity(gpu, p, mass, kernel):
+    if kernel == "elementwise" and mass and p >= 4:
+        pytest.skip("the element-wise kernel supports mass rules up to 128 points (p=4 uses 216)")
+    m = _mesh(3, 21 + p)
+    kappa = lognormal(m.ne, 1.0, 5)
+    mu = lognormal(m.ne, 0.5, 6) if mass else None
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, kappa, mu, kernel)
+    S = O.OracleSpace(m.points, m.elements, p)
+    x = np.random.default_rng(7).normal(size=fes.ndof)
+    yo = S.apply_mf(x, kappa=kappa, mu=mu)
+    sc = np.abs(yo).max()
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    a.mat.Mult(xv, yv)
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * sc
+    x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+    a.mat.Mult(x32, y32)
+    assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * sc
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_tet_mixed_cg_tiled(gpu, p):
+    """Mixed CG on tets (inner FP32 applies with the fused energy) reaches 1e-11
+    and matches the FP64 solution."""
+    m = _mesh(4, 3)
+    kappa = lognormal(m.ne, 0.5, 14)
+    f = np.random.default_rng(15).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, kappa, None, None)
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    solm = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-11, maxsteps=20000, printrates=False,
+                          mode="mixed", stop_rule="true")
+    r = gpu.solvers.CG.last_solver.result
+    assert r.status == 0 and r.true_relres <= 1e-11 and r.applies32 > 0
+    xm = solm.NumPy().copy()
+    sol6 = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-12, maxsteps=20000, printrates=False,
+                          mode="fp64", stop_rule="true")
+    x6 = sol6.NumPy()
+    assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
