@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
+    ap.add_argument("--c2-orders", default="2,3,4", help="orders of the C2 record (comma separated)")
     return ap.parse_args()
 
 
@@ -266,7 +267,7 @@ def workload_c2(args):
     out = {"workload": "C2: 32^3 Kuhn tets (196,608), jitter 0.2h, kappa lognormal(0,1)", "orders": {}}
     mesh = ng.JitterInterior(ng.MakeStructured3DMesh(hexes=False, nx=32), 0.2 / 32, 2)
     kappa = np.exp(np.random.default_rng(3).normal(0, 1, mesh.ne))
-    for p in (2, 3, 4):
+    for p in [int(v) for v in args.c2_orders.split(",")]:
         fes = ng.H1(mesh, order=p, dirichlet=".*")
         u, v = fes.TnT()
         a = ng.BilinearForm(fes)

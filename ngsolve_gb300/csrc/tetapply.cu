@@ -29,6 +29,20 @@ constexpr int TET_TI = 6;    // maximum row-tile depth of the second product (nl
 
 __host__ __device__ inline size_t tet_r16(size_t b) { return (b + 15) / 16 * 16; }
 
+// sizes per order: local DOFs, points of the stiffness rule (degree 2p-2) and of
+// the mass rule (degree 2p) -- the rules of tet_rule in tables.cu
+template <int P>
+struct TetDims {
+  static constexpr int NLOC = (P + 1) * (P + 2) * (P + 3) / 6;
+  static constexpr int NQ = P == 1 ? 1 : P == 2 ? 4 : P == 3 ? 14 : 24;
+  static constexpr int NQM = P == 1 ? 4 : P == 2 ? 14 : P == 3 ? 24 : 216;
+  static constexpr int NLOCP = (NLOC + 15) / 16 * 16;
+  template <bool MASS>
+  static constexpr int R() { return 3 * NQ + (MASS ? NQM : 0); }
+  template <bool MASS>
+  static constexpr int RP() { return (R<MASS>() + 15) / 16 * 16; }
+};
+
 // shared-memory carve-up of one block
 template <class T>
 struct TetSmem {
@@ -63,12 +77,15 @@ __device__ __forceinline__ void st4(double* p, const double* v) {
 // its class (and the table in shared memory) for most consecutive tiles.
 // D: [class][nlocp][Rs] with rows i >= nloc and columns r >= R zero; W: [Rp].
 // Shared X and DOF rows are [i][element], P is [row][element].
-template <class T, bool MASS>
+template <class T, bool MASS, int P>
 __global__ void __launch_bounds__(TET_TT)
-tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int nq,
-                int nqm, int Rp, int Rs, const int* __restrict__ eldofs, const T* __restrict__ Ge,
-                const T* __restrict__ Me, const T* __restrict__ D, const T* __restrict__ W, const T* __restrict__ x,
-                T* __restrict__ y, double* partial, unsigned int* counter, double* energy, const int* skip) {
+tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
+                const T* __restrict__ Ge, const T* __restrict__ Me, const T* __restrict__ D, const T* __restrict__ W,
+                const T* __restrict__ x, T* __restrict__ y, double* partial, unsigned int* counter, double* energy,
+                const int* skip) {
+  using Dm = TetDims<P>;
+  constexpr int nloc = Dm::NLOC, nlocp = Dm::NLOCP, nq = Dm::NQ, nqm = Dm::NQM;
+  constexpr int Rp = Dm::template RP<MASS>(), Rs = Rp + 1, ni = nlocp / 16;
   if (skip && *(volatile const int*)skip) return;
   extern __shared__ __align__(16) unsigned char smem[];
   const TetSmem<T> L{nlocp, Rp, Rs};
@@ -112,11 +129,14 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
     }
     __syncthreads();
     // P[r][e] = sum_i D[i][r] X[i][e]
+    // unrolled (nt compile-time) unless the mass rule makes the table long (p = 4 with mass)
+#pragma unroll(Rp <= 16 * TET_RB ? 1 : (Rp <= 256 ? 2 : 1))
     for (int r0 = 0; r0 < Rp; r0 += 16 * TET_RB) {
-      const int nt = min(TET_RB, (Rp - r0) / 16);  // block-uniform
+      const int nt = min(TET_RB, (Rp - r0) / 16);
       T a[TET_RB][4];
 #pragma unroll
       for (int u = 0; u < TET_RB; u++) a[u][0] = a[u][1] = a[u][2] = a[u][3] = 0;
+#pragma unroll
       for (int i = 0; i < nloc; i++) {
         T xv[4];
         ld4(sX + i * TET_TE + 4 * cg, xv);
@@ -163,7 +183,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
     T b[TET_TI][4];
 #pragma unroll
     for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
-    const int ni = nlocp / 16;  // block-uniform
+#pragma unroll 16
     for (int r = 0; r < Rp; r++) {
       T pv[4];
       ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
@@ -207,9 +227,12 @@ __global__ void tet_tile_table_kernel(int ncls, int nloc, int nlocp, int nq, int
   }
 }
 
-template <class T, bool MASS>
-static int tet_tile_occupancy(size_t smem) {
-  auto kern = tet_tile_kernel<T, MASS>;
+template <class T, bool MASS, int P>
+static int tet_tile_occupancy_p() {
+  auto kern = tet_tile_kernel<T, MASS, P>;
+  using Dm = TetDims<P>;
+  const TetSmem<T> L{Dm::NLOCP, Dm::template RP<MASS>(), Dm::template RP<MASS>() + 1};
+  const size_t smem = L.total();
   int dev = 0, optin = 0;
   GH1_CUDA(cudaGetDevice(&dev));
   GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -223,6 +246,35 @@ static int tet_tile_occupancy(size_t smem) {
   return v;
 }
 
+#define GH1_TET_P_SWITCH(P, CASE)                                                  \
+  switch (P) {                                                                     \
+    CASE(1) CASE(2) CASE(3) CASE(4)                                                \
+    default: throw Error(GH1_ERR_UNSUPPORTED, "tiled tet apply: order out of range"); \
+  }
+
+template <class T>
+static int tet_tile_occupancy(int p, bool mass) {
+  int v = 0;
+#define GH1_TET_OCC(PP)                                                                            \
+  case PP:                                                                                         \
+    v = mass ? tet_tile_occupancy_p<T, true, PP>() : tet_tile_occupancy_p<T, false, PP>();         \
+    break;
+  GH1_TET_P_SWITCH(p, GH1_TET_OCC)
+#undef GH1_TET_OCC
+  return v;
+}
+
+// the space's rules are the ones the compiled sizes assume
+static bool tet_dims_match(int p, int nq, int nqm) {
+  switch (p) {
+    case 1: return nq == TetDims<1>::NQ && nqm == TetDims<1>::NQM;
+    case 2: return nq == TetDims<2>::NQ && nqm == TetDims<2>::NQM;
+    case 3: return nq == TetDims<3>::NQ && nqm == TetDims<3>::NQM;
+    case 4: return nq == TetDims<4>::NQ && nqm == TetDims<4>::NQM;
+    default: return false;
+  }
+}
+
 // Class-sorted element order, tiles, tables and occupancy.  GH1_TET_KERNEL=elementwise
 // keeps the element-wise kernel (for comparisons).
 void tet_tiles_setup(gh1_op* op) {
@@ -232,7 +284,7 @@ void tet_tiles_setup(gh1_op* op) {
   if (env && std::string(env) == "elementwise") return;
   const int ne = sp->mesh->ne, nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
   const int nlocp = (nloc + 15) / 16 * 16;
-  if (nlocp / 16 > TET_TI || ne == 0) return;
+  if (nlocp / 16 > TET_TI || ne == 0 || !tet_dims_match(sp->p, nq, nqm)) return;
   const int R = 3 * nq + (op->has_mass ? nqm : 0), Rp = (R + 15) / 16 * 16, Rs = Rp + 1;
   const int ncls = N_TET_CLASSES;
   cudaStream_t s = sp->ctx->stream;
@@ -271,8 +323,7 @@ void tet_tiles_setup(gh1_op* op) {
                                                       op->d_tetD64.p);
   check_kernel(sp->ctx, "tet_tile_table_kernel");
   op->d_tetw64.upload(w, s);
-  const TetSmem<double> L64{nlocp, Rp, Rs};
-  op->tet_tiles_per_sm[0] = mass ? tet_tile_occupancy<double, true>(L64.total()) : tet_tile_occupancy<double, false>(L64.total());
+  op->tet_tiles_per_sm[0] = tet_tile_occupancy<double>(sp->p, mass);
   if (op->prec_mask & 2) {
     op->d_tetD32.alloc(tot);
     tet_tile_table_kernel<float><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, R, Rs, sp->d_tab32.p, sp->d_tabm64.p,
@@ -280,28 +331,36 @@ void tet_tiles_setup(gh1_op* op) {
     check_kernel(sp->ctx, "tet_tile_table_kernel");
     std::vector<float> w32(w.begin(), w.end());
     op->d_tetw32.upload(w32, s);
-    const TetSmem<float> L32{nlocp, Rp, Rs};
-    op->tet_tiles_per_sm[1] = mass ? tet_tile_occupancy<float, true>(L32.total()) : tet_tile_occupancy<float, false>(L32.total());
+    op->tet_tiles_per_sm[1] = tet_tile_occupancy<float>(sp->p, mass);
   }
   GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+}
+
+template <class T, bool MASS, int P>
+static void tet_tile_launch_p(gh1_op* op, int grid, const T* D, const T* W, const T* G, const T* M, const T* x, T* y,
+                              double* partial, unsigned int* counter, double* energy, const int* skip) {
+  using Dm = TetDims<P>;
+  const TetSmem<T> L{Dm::NLOCP, Dm::template RP<MASS>(), Dm::template RP<MASS>() + 1};
+  gh1_space* sp = op->sp;
+  tet_tile_kernel<T, MASS, P><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
+      op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy,
+      skip);
+  check_kernel(sp->ctx, "tet_tile_kernel");
 }
 
 template <class T>
 static void tet_tile_launch(gh1_op* op, int per_sm, const T* D, const T* W, const T* G, const T* M, const T* x, T* y,
                             double* partial, unsigned int* counter, double* energy, const int* skip) {
   gh1_space* sp = op->sp;
-  const int nlocp = (sp->nloc + 15) / 16 * 16;
-  const TetSmem<T> L{nlocp, op->tet_Rp, op->tet_Rs};
   const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
-  if (op->has_mass)
-    tet_tile_kernel<T, true><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, sp->tet_nq, sp->tet_nq_mass, op->tet_Rp,
-        op->tet_Rs, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy, skip);
-  else
-    tet_tile_kernel<T, false><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, sp->tet_nq, sp->tet_nq_mass, op->tet_Rp,
-        op->tet_Rs, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy, skip);
-  check_kernel(sp->ctx, "tet_tile_kernel");
+  const bool mass = op->has_mass;
+#define GH1_TET_LAUNCH(PP)                                                                                   \
+  case PP:                                                                                                   \
+    if (mass) tet_tile_launch_p<T, true, PP>(op, grid, D, W, G, M, x, y, partial, counter, energy, skip);   \
+    else tet_tile_launch_p<T, false, PP>(op, grid, D, W, G, M, x, y, partial, counter, energy, skip);       \
+    break;
+  GH1_TET_P_SWITCH(sp->p, GH1_TET_LAUNCH)
+#undef GH1_TET_LAUNCH
 }
 
 bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
