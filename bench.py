@@ -526,6 +526,31 @@ def main():
     torch.cuda.synchronize()
     t64 = e0.elapsed_time(e1) / 1e3 / k64
 
+    # general-geometry apply (per-point metric), when the headline used the affine variant
+    general = None
+    if variant == 4:
+        os.environ["GH1_HEX_AFFINE"] = "0"
+        ag = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+        ag += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+        ag.Assemble()
+        del os.environ["GH1_HEX_AFFINE"]
+        gvar = ag.mat.Info()["hex_variant_fp32"]
+        for _ in range(3):
+            ag.mat.Mult(x32, y32)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ag.mat.Mult(x32, y32)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tg = e0.elapsed_time(e1) / 1e3 / args.steps
+        Bg, _ = model_bytes_flops(ne, N, args.order, 4, 4)
+        general = {"variant": gvar, "ms": tg * 1e3, "gdofs": N / tg / 1e9, "achieved_gbs": Bg / tg / 1e9,
+                   "frac": Bg / tg / 1e9 / load_peaks()[0]}
+        del ag
+        torch.cuda.empty_cache()
+
     # ---- e2e through the public API with host buffers -------------------------
     xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
     xh.copy_(x32.t.cpu())
@@ -598,10 +623,18 @@ def main():
               "hex_apply_pair_kernel<%d, 0, %d>" % (nn, variant - 2))
     traffic = None
     if args.order == ORDER and args.nx == NX:  # the committed profiles cover the benchmark configuration
-        traffic = load_traffic("hex_apply_pair_fp32_c3.md" if variant >= 2 else "hex_apply_fp32_c3.md")
+        traffic = load_traffic({0: "hex_apply_fp32_c3.md", 1: "hex_apply_fp32_c3.md", 2: "hex_apply_pair_fp32_c3.md",
+                                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md"}[variant])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": B32, "kernel": kernel, "variant": variant}
+    if variant == 4:
+        # every element map is affine: the kernel reads one 32-byte metric record per
+        # element instead of q^3 x 6 values; achieved keeps the per-point byte model
+        B_aff = 2 * N * 4 + ne * 32
+        roofline["note"] = ("variant 4 reads one metric per element (affine mesh); achieved/frac use the per-point "
+                            "byte model, achieved_affine_model the bytes this variant's model moves")
+        roofline["achieved_affine_model"] = B_aff / t_step / 1e9
     B64, _ = model_bytes_flops(ne, N, args.order, 8, 8)
 
     cpu = None
@@ -617,6 +650,7 @@ def main():
                           "parallelism": "replicas" if ws > 1 else "single",
                           "l2": "inputs larger than L2 (G tile stream %.0f MB per apply)" % (ne * (args.order + 1) ** 3 * 24 / 1e6)},
                "e2e": e2e, "gpu_launches": args.steps, "clocks": ck, "roofline": roofline,
+               "general_geometry_apply": general,
                "fp64_apply": {"ms": t64 * 1e3, "gdofs": N / t64 / 1e9, "achieved_tflops_model": F / t64 / 1e12,
                               "achieved_gbs_model": B64 / t64 / 1e9},
                "cg": cg, "cpu_baseline": cpu}

@@ -111,7 +111,9 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
 /* info[0..5] = kind (GH1_OP_*), nrows, ne, order, and for a hex matrix-free
  * operator the autotuned apply variant in FP64 and FP32 (0 / 1: one element per
  * lane with the G tile staged by bulk copy / loaded directly; 2 / 3: the same
- * with two elements per lane, FP32 only; -1: not applicable) */
+ * with two elements per lane, FP32 only; 4: two elements per lane with one metric
+ * per element, FP32, chosen only when every element map is affine; -1: not
+ * applicable) */
 int gh1_op_info(gh1_op* op, int64_t* info);
 int gh1_op_free(gh1_op* op);
 

@@ -156,8 +156,11 @@ struct gh1_op {
   gh1::DBuf<int> d_err;       // device error flag of the pipelined apply (bounded waits)
   int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
   int hex_gmode[2] = {0, 0};                 // autotuned hex apply variant per precision: 0/1 = G tile by TMA /
-                                             // direct loads; FP32 also 2/3 = the same with two elements per lane
-  int pair_per_sm[2] = {0, 0};               // resident blocks per SM of the paired FP32 apply [G mode]
+                                             // direct loads; FP32 also 2/3 = the same with two elements per lane,
+                                             // 4 = two elements per lane with per-element (affine) metrics
+  int pair_per_sm[3] = {0, 0, 0};            // resident blocks per SM of the paired FP32 apply [G mode]
+  bool all_affine = false;                   // hex: every element map affine (G mode 2 available)
+  gh1::DBuf<float> d_Ga32;                   // hex, all affine: per-element metric records [ne][8]
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
   int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
@@ -215,6 +218,7 @@ bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* parti
 bool hex_pair_supported(int N);
 void upload_pair_tables(gh1_space* sp);
 int hex_pair_occupancy(gh1_op* op, int gmode);
+void hex_affine_setup(gh1_op* op);
 void hex_pair_apply(gh1_op* op, int gmode, const float* x, float* y, double* partial, unsigned int* counter,
                     double* energy, const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)

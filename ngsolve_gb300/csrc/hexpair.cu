@@ -22,6 +22,8 @@
 // Every mbarrier wait is bounded; a timeout sets *err and the kernel drains its
 // copies in flight and returns.
 #include <algorithm>
+#include <cstdlib>
+#include <vector>
 #include "common.cuh"
 #include "hexcore.cuh"
 
@@ -57,6 +59,8 @@ __device__ __forceinline__ f2 add2(f2 a, f2 b) {
 // both halves, which the packed pipe takes from the constant bank at no extra
 // instruction (a table of pre-duplicated 64-bit pairs costs a move per FMA)
 __constant__ float c_Bp[TAB_TOTAL], c_Dp[TAB_TOTAL];
+// 1D Gauss weights of every order: N weights at offset N(N-1)/2 - 1
+__constant__ float c_Wp[64];
 __device__ __forceinline__ f2 bcast(float t) {
   f2 r;
   asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(t));
@@ -319,7 +323,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     if (lane == 0) {
       issue_t(ch, 0);
       if (GM == 0) issue_g(ch);
-      else bulk_prefetch_l2(Gq + (size_t)ch * E * gstride, (uint32_t)(rows_of(ch) * rowg * sizeof(float)));
+      else if (GM == 1) bulk_prefetch_l2(Gq + (size_t)ch * E * gstride, (uint32_t)(rows_of(ch) * rowg * sizeof(float)));
     }
     t_issued = 1;
     g_issued = GM == 0 ? 1 : 0;
@@ -362,6 +366,18 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     const float* Gb = GM == 0 ? gbuf + (size_t)r1 * rowg : Gq + ((size_t)ch * E + r1) * gstride;
     f2 vx[N], vy[N], vz[N], vm[N];
     if (active) {
+      // G mode 2 (every element affine): one metric per element, records of 8
+      // floats (xx yy zz xy xz yz, mass, pad), times the rule weight w_i w_j w_k
+      constexpr int WO = N * (N - 1) / 2 - 1;
+      f2 ea[7];
+      float wjk = 0.f;
+      if (GM == 2) {
+        const float* Ea = Gq + ((size_t)ch * E + r0) * 8;
+        const float* Eb = Gq + ((size_t)ch * E + r1) * 8;
+#pragma unroll
+        for (int c = 0; c < (MASS ? 7 : 6); c++) ea[c] = pack2(__ldg(Ea + c), __ldg(Eb + c));
+        wjk = c_Wp[WO + pl / N] * c_Wp[WO + pl % N];
+      }
 #pragma unroll
       for (int i = 0; i < N; i++) {
         const int o = i * N2 + pl;
@@ -369,13 +385,22 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
           if (GM == 0) return pack2(Ga[comp * N3 + o], Gb[comp * N3 + o]);
           return pack2(__ldcs(Ga + comp * N3 + o), __ldcs(Gb + comp * N3 + o));
         };
-        const f2 gxx = ld(0), gyy = ld(1), gzz = ld(2), gxy = ld(3), gxz = ld(4), gyz = ld(5);
-        vx[i] = fma2(gxz, gz[i], fma2(gxy, gy[i], mul2(gxx, gx[i])));
-        vy[i] = fma2(gyz, gz[i], fma2(gyy, gy[i], mul2(gxy, gx[i])));
-        vz[i] = fma2(gzz, gz[i], fma2(gyz, gy[i], mul2(gxz, gx[i])));
+        if (GM == 2) {
+          const f2 w = bcast(c_Wp[WO + i] * wjk);
+          const f2 sx = mul2(w, gx[i]), sy = mul2(w, gy[i]), sz = mul2(w, gz[i]);
+          vx[i] = fma2(ea[4], sz, fma2(ea[3], sy, mul2(ea[0], sx)));
+          vy[i] = fma2(ea[5], sz, fma2(ea[1], sy, mul2(ea[3], sx)));
+          vz[i] = fma2(ea[2], sz, fma2(ea[5], sy, mul2(ea[4], sx)));
+        } else {
+          const f2 gxx = ld(0), gyy = ld(1), gzz = ld(2), gxy = ld(3), gxz = ld(4), gyz = ld(5);
+          vx[i] = fma2(gxz, gz[i], fma2(gxy, gy[i], mul2(gxx, gx[i])));
+          vy[i] = fma2(gyz, gz[i], fma2(gyy, gy[i], mul2(gxy, gx[i])));
+          vz[i] = fma2(gzz, gz[i], fma2(gyz, gy[i], mul2(gxz, gx[i])));
+        }
         f2 en = fma2(gz[i], vz[i], fma2(gy[i], vy[i], mul2(gx[i], vx[i])));
         if (MASS) {
-          vm[i] = mul2(ld(6), uq[i]);
+          if (GM == 2) vm[i] = mul2(mul2(bcast(c_Wp[WO + i] * wjk), ea[6]), uq[i]);
+          else vm[i] = mul2(ld(6), uq[i]);
           en = fma2(uq[i], vm[i], en);
         }
         acc = add2(acc, en);
@@ -438,6 +463,78 @@ void upload_pair_tables(gh1_space* sp) {
   cudaStream_t s = sp->ctx->stream;
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_Bp, sp->d_B32.p, N * N * sizeof(float), off, cudaMemcpyDeviceToDevice, s));
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_Dp, sp->d_D32.p, N * N * sizeof(float), off, cudaMemcpyDeviceToDevice, s));
+  std::vector<float> w(sp->gw.begin(), sp->gw.end());
+  GH1_CUDA(cudaMemcpyToSymbolAsync(c_Wp, w.data(), N * sizeof(float), (N * (N - 1) / 2 - 1) * sizeof(float),
+                                   cudaMemcpyHostToDevice, s));
+  GH1_CUDA(cudaStreamSynchronize(s));  // the host staging vector goes out of scope
+}
+
+// Per-element metric of an affine hex (x = P0 + J xi: J[3k+j] = d x_k / d xi_j
+// with the columns P1-P0, P3-P0, P4-P0 in the reference vertex order), and a
+// flag if any element's trilinear map has a bilinear or trilinear part (its
+// coefficients P0-P1+P2-P3, P0-P1-P4+P5, P0-P3-P4+P7, -P0+P1-P2+P3+P4-P5+P6-P7)
+// above 1e-12 of the element's edge vectors.
+__global__ void hex_affine_kernel(int ne, const double* __restrict__ X, const int* __restrict__ el,
+                                  const double* __restrict__ kappa, const double* __restrict__ mu, float* Ga,
+                                  int* nonaffine) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double P[8][3];
+  for (int a = 0; a < 8; a++)
+    for (int k = 0; k < 3; k++) P[a][k] = X[3 * (size_t)el[(size_t)e * 8 + a] + k];
+  double J[9], scale = 0, dev = 0;
+  for (int k = 0; k < 3; k++) {
+    J[3 * k + 0] = P[1][k] - P[0][k];
+    J[3 * k + 1] = P[3][k] - P[0][k];
+    J[3 * k + 2] = P[4][k] - P[0][k];
+    scale = fmax(scale, fmax(fabs(J[3 * k]), fmax(fabs(J[3 * k + 1]), fabs(J[3 * k + 2]))));
+    dev = fmax(dev, fabs(P[0][k] - P[1][k] + P[2][k] - P[3][k]));
+    dev = fmax(dev, fabs(P[0][k] - P[1][k] - P[4][k] + P[5][k]));
+    dev = fmax(dev, fabs(P[0][k] - P[3][k] - P[4][k] + P[7][k]));
+    dev = fmax(dev, fabs(-P[0][k] + P[1][k] - P[2][k] + P[3][k] + P[4][k] - P[5][k] + P[6][k] - P[7][k]));
+  }
+  if (dev > 1e-12 * scale) atomicExch(nonaffine, 1);
+  const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                     J[2] * (J[3] * J[7] - J[4] * J[6]);
+  const double id = 1.0 / det;
+  const double Ji[9] = {(J[4] * J[8] - J[5] * J[7]) * id, (J[2] * J[7] - J[1] * J[8]) * id,
+                        (J[1] * J[5] - J[2] * J[4]) * id, (J[5] * J[6] - J[3] * J[8]) * id,
+                        (J[0] * J[8] - J[2] * J[6]) * id, (J[2] * J[3] - J[0] * J[5]) * id,
+                        (J[3] * J[7] - J[4] * J[6]) * id, (J[1] * J[6] - J[0] * J[7]) * id,
+                        (J[0] * J[4] - J[1] * J[3]) * id};
+  const double f = kappa[e] * fabs(det);
+  float* g = Ga + (size_t)e * 8;
+  g[0] = (float)(f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]));
+  g[1] = (float)(f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]));
+  g[2] = (float)(f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]));
+  g[3] = (float)(f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]));
+  g[4] = (float)(f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]));
+  g[5] = (float)(f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]));
+  g[6] = mu ? (float)(mu[e] * fabs(det)) : 0.f;
+  g[7] = 0.f;
+}
+
+// Detects an all-affine hex mesh and builds the per-element metric records for
+// G mode 2 (GH1_HEX_AFFINE=0 keeps the per-point metric only).
+void hex_affine_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->all_affine = false;
+  op->d_Ga32.release();
+  const char* env = getenv("GH1_HEX_AFFINE");
+  if ((env && env[0] == '0') || !hex_pair_supported(sp->p + 1)) return;
+  const int ne = sp->mesh->ne;
+  cudaStream_t s = sp->ctx->stream;
+  op->d_Ga32.alloc((size_t)ne * 8);
+  DBuf<int> flag(1);
+  flag.zero(s);
+  hex_affine_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, op->form->d_kappa.p,
+                                                     op->has_mass ? op->form->d_mu.p : nullptr, op->d_Ga32.p, flag.p);
+  check_kernel(sp->ctx, "hex_affine_kernel");
+  int h = 1;
+  GH1_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  op->all_affine = (h == 0);
+  if (!op->all_affine) op->d_Ga32.release();
 }
 
 template <int N, bool MASS, int GM>
@@ -463,16 +560,17 @@ static void pair_launch(gh1_op* op, const float* x, float* y, double* partial, u
                         const int* skip) {
   using C = PairCfg<N>;
   gh1_space* sp = op->sp;
-  const size_t smem = C::total(op->gstride32, sp->tstride, GM);
+  const size_t smem = C::total(GM == 2 ? 8 : op->gstride32, sp->tstride, GM);
   const int per_sm = op->pair_per_sm[GM];
   GH1_CHECK(per_sm > 0, GH1_ERR_ARG, "internal: paired hex apply occupancy not prepared");
   const int ne = sp->mesh->ne;
   const int nch = (ne + C::E - 1) / C::E;
   const int blocks_needed = (nch + C::EPB - 1) / C::EPB;
   const int grid = std::min(blocks_needed, sp->ctx->nsm * per_sm);
+  const float* G = GM == 2 ? op->d_Ga32.p : op->d_G32.p;
+  const int gs = GM == 2 ? 8 : op->gstride32;
   hex_apply_pair_kernel<N, MASS, GM><<<grid, C::BLOCK, smem, sp->ctx->stream>>>(
-      ne, sp->d_tdof.p, sp->tstride, op->d_G32.p, op->gstride32, x, y, (int)sp->first_cell, partial, counter, energy,
-      skip, op->d_err.p);
+      ne, sp->d_tdof.p, sp->tstride, G, gs, x, y, (int)sp->first_cell, partial, counter, energy, skip, op->d_err.p);
   check_kernel(sp->ctx, "hex_apply_pair_kernel");
 }
 
@@ -490,8 +588,10 @@ int hex_pair_occupancy(gh1_op* op, int gm) {
   case NN:                                                                                                     \
     if (gm == 0) v = mass ? pair_occupancy<NN, true, 0>(PairCfg<NN>::total(gs, ts, 0))                        \
                           : pair_occupancy<NN, false, 0>(PairCfg<NN>::total(gs, ts, 0));                      \
-    else v = mass ? pair_occupancy<NN, true, 1>(PairCfg<NN>::total(gs, ts, 1))                                \
-                  : pair_occupancy<NN, false, 1>(PairCfg<NN>::total(gs, ts, 1));                              \
+    else if (gm == 1) v = mass ? pair_occupancy<NN, true, 1>(PairCfg<NN>::total(gs, ts, 1))                   \
+                               : pair_occupancy<NN, false, 1>(PairCfg<NN>::total(gs, ts, 1));                 \
+    else v = mass ? pair_occupancy<NN, true, 2>(PairCfg<NN>::total(8, ts, 2))                                 \
+                  : pair_occupancy<NN, false, 2>(PairCfg<NN>::total(8, ts, 2));                               \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_OCC)
 #undef GH1_PAIR_OCC
@@ -506,9 +606,12 @@ void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partia
     if (gm == 0) {                                                                              \
       if (mass) pair_launch<NN, true, 0>(op, x, y, partial, counter, energy, skip);             \
       else pair_launch<NN, false, 0>(op, x, y, partial, counter, energy, skip);                 \
-    } else {                                                                                    \
+    } else if (gm == 1) {                                                                       \
       if (mass) pair_launch<NN, true, 1>(op, x, y, partial, counter, energy, skip);             \
       else pair_launch<NN, false, 1>(op, x, y, partial, counter, energy, skip);                 \
+    } else {                                                                                    \
+      if (mass) pair_launch<NN, true, 2>(op, x, y, partial, counter, energy, skip);             \
+      else pair_launch<NN, false, 2>(op, x, y, partial, counter, energy, skip);                 \
     }                                                                                           \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)

@@ -937,14 +937,16 @@ int hex_occupancy_dispatch(gh1_op* op, int gstride) {
 // Autotuner: times each variant -- G tile staged in shared memory by TMA vs
 // direct coalesced loads, and for FP32 each of those with two elements per lane
 // -- on this operator's own mesh and keeps the fastest.  The choice is cached per
-// (order, precision, element-count bucket) for the process.  GH1_HEX_GMODE=0..3
-// forces a variant (FP64 takes it modulo 2).
+// (order, precision, element-count bucket, affine mesh) for the process.
+// GH1_HEX_GMODE=0..4 forces a variant (FP64 takes it modulo 2; 4 needs an
+// all-affine mesh).
 template <class T>
 void hex_autotune(gh1_op* op, const T* G, int gstride) {
   const int pi = std::is_same<T, float>::value ? 1 : 0;
-  const int nmodes = (pi == 1 && op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) ? 4 : 2;
+  int nmodes = (pi == 1 && op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) ? 4 : 2;
+  if (nmodes == 4 && op->pair_per_sm[2] > 0) nmodes = 5;
   const char* env = getenv("GH1_HEX_GMODE");
-  if (env && env[0] >= '0' && env[0] <= '3') {
+  if (env && env[0] >= '0' && env[0] <= '4') {
     const int m = env[0] - '0';
     op->hex_gmode[pi] = m < nmodes ? m : m % 2;
     return;
@@ -953,8 +955,9 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   const int N = op->sp->p + 1, ne = op->sp->mesh->ne;
   int lb = 0;
   while ((1 << (lb + 1)) <= ne) lb++;
+  const int key = lb + (op->has_mass ? 100 : 0) + (op->all_affine ? 1000 : 0);  // mesh-size bucket, mass, affine
   for (auto& c : cache)
-    if (c[0] == N && c[1] == pi && c[2] == lb + (op->has_mass ? 100 : 0)) { op->hex_gmode[pi] = c[3]; return; }
+    if (c[0] == N && c[1] == pi && c[2] == key && c[3] < nmodes) { op->hex_gmode[pi] = c[3]; return; }
   if (ne < 4096) {  // small meshes: no measurable difference, skip the timing
     op->hex_gmode[pi] = 0;
     return;
@@ -981,7 +984,7 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   op->hex_gmode[pi] = choice;
-  cache.push_back({N, pi, lb + (op->has_mass ? 100 : 0), choice});
+  cache.push_back({N, pi, key, choice});
 }
 
 // ---- multi-right-hand-side apply (batched solves) ----------------------------
@@ -1089,6 +1092,8 @@ void matfree_setup(gh1_op* op) {
         upload_pair_tables(sp);
         op->pair_per_sm[0] = hex_pair_occupancy(op, 0);
         op->pair_per_sm[1] = hex_pair_occupancy(op, 1);
+        hex_affine_setup(op);
+        op->pair_per_sm[2] = op->all_affine ? hex_pair_occupancy(op, 2) : 0;
       }
     }
     hex_autotune<double>(op, op->d_G64.p, op->gstride64);

@@ -1,7 +1,8 @@
 """Every FP32 hex apply variant -- G tile staged by TMA (0) or loaded directly
 (1), one element per lane (0, 1) or two elements per lane with packed f32x2
 arithmetic (2, 3) -- forced through GH1_HEX_GMODE and checked against the FP64
-oracle.  Odd element counts leave the last element pair half empty."""
+oracle.  Odd element counts leave the last element pair half empty.  Variant 4
+(one metric per element) exists only on meshes whose element maps are all affine."""
 import contextlib
 import os
 
@@ -10,7 +11,7 @@ import pytest
 import torch
 
 from oracle import oracle as O
-from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior
+from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior, Mesh as RawMesh
 from tests.util import lognormal
 
 pytestmark = pytest.mark.gpu
@@ -60,13 +61,47 @@ def test_fp32_variant_parity(gpu, mode, p, mass):
         assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
 
 
-@pytest.mark.parametrize("mode", [2, 3])
+def _sheared(nx):
+    """Structured hexes under a general affine map: every element is the same
+    parallelepiped, so the metric is one full symmetric 3x3 per element."""
+    m = MakeStructured3DMesh(hexes=True, nx=nx)
+    A = np.array([[1.0, 0.3, -0.2], [0.1, 0.8, 0.25], [-0.15, 0.2, 1.3]])
+    return RawMesh(m.points @ A.T + np.array([0.5, -1.0, 2.0]), m.elements)
+
+
+@pytest.mark.parametrize("mass", [False, True])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
+def test_fp32_affine_variant(gpu, p, mass):
+    """Variant 4 (one metric per element) on affine meshes (an axis-aligned and a
+    sheared one, odd and even element counts) within 2e-5 of the oracle; on a
+    jittered mesh the variant is not offered and the apply stays correct."""
+    for m in (MakeStructured3DMesh(hexes=True, nx=3), _sheared(2), _sheared(3)):
+        kappa = lognormal(m.ne, 1.0, 5)
+        mu = lognormal(m.ne, 0.5, 6) if mass else None
+        fes = gpu.H1(m, order=p, dirichlet=".*")
+        a = _form(gpu, fes, kappa, mu, 4)
+        if p <= 6:
+            assert a.mat.Info()["hex_variant_fp32"] == 4
+        S = O.OracleSpace(m.points, m.elements, p)
+        x = np.random.default_rng(7).normal(size=fes.ndof)
+        yo = S.apply_mf(x, kappa=kappa, mu=mu)
+        x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        a.mat.Mult(x32, y32)
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+    m = JitterInterior(MakeStructured3DMesh(hexes=True, nx=3), 0.1 / 3, 11)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, lognormal(m.ne, 1.0, 5), None, 4)
+    assert a.mat.Info()["hex_variant_fp32"] in (0, 1, 2, 3)
+
+
+@pytest.mark.parametrize("mode", [2, 3, 4])
 @pytest.mark.parametrize("p", [2, 4])
 def test_mixed_cg_paired_variant(gpu, mode, p):
     """Mixed-precision CG whose inner FP32 iterations run the paired apply (with
     its fused energy x^T A x) reaches 1e-10 true relative residual and agrees
     with the FP64 CG solution."""
-    m = JitterInterior(MakeStructured3DMesh(hexes=True, nx=5), 0.1 / 5, 3)
+    m = _sheared(5) if mode == 4 else JitterInterior(MakeStructured3DMesh(hexes=True, nx=5), 0.1 / 5, 3)
     kappa = lognormal(m.ne, 0.5, 14)
     f = np.random.default_rng(15).uniform(-1, 1, m.ne)
     fes = gpu.H1(m, order=p, dirichlet=".*")
