@@ -14,7 +14,8 @@
 // Layout per element group (G threads, S = HexCfg::EPW pencil slots, E = 2 S
 // elements per chunk, element 2s+h of a chunk in slot s, half h):
 //   [G tiles of the E elements (G mode 0)] | DOF-table rows x2 buffers |
-//   5 packed work arrays [S][N^3] of float2 | 3 mbarriers
+//   6 packed work arrays of float2 (u dense, s and t padded, see PairLayout) |
+//   3 mbarriers
 // Pipelining as in the one-element kernel: the DOF rows of the next chunk are
 // bulk-copied (TMA) during the forward contractions, the next chunk's x gather
 // is issued before the quadrature-point transform, and in G mode 0 the G tiles
@@ -79,6 +80,25 @@ constexpr int pair_min_blocks(int N, bool mass, int gm) {
                   : 2;
 }
 
+// Work-array layouts.  Element index (a,b,c) sits at a*SA + b*SB + c in the s
+// arrays (stage-1 outputs) and at a*TA + b*TB + c in the t arrays (stage-2
+// outputs); the coefficient array u is dense.  Each stage reads and writes
+// 8-byte words with one of three lane patterns (lanes over (a,b), (a,c) or
+// (b,c)).  At N = 5 no single padding serves all three conflict-free, but
+// per-array paddings do: SA, SB = 35, 7 and TA, TB = 27, 5 with the stage-2 lanes
+// permuted by c_p2 leave every access at the minimum of two wavefronts per warp
+// (dense layout: three for the stage-2 pattern).  Other orders stay dense.
+template <int N>
+struct PairLayout {
+  static constexpr int SA = N == 5 ? 35 : N * N, SB = N == 5 ? 7 : N;
+  static constexpr int TA = N == 5 ? 27 : N * N, TB = N;
+  static constexpr int SW = (N - 1) * (SA + SB) + N, TW = (N - 1) * (TA + TB) + N;  // words per array
+};
+// stage-2 lane -> (a, c) = (v / 5, v % 5) at N = 5: lanes 0-15 and 16-24 each hit
+// 16 (9) distinct bank pairs in both the s and the t layout
+__constant__ unsigned char c_p2[25] = {0, 1, 2, 4, 5, 7, 10, 11, 12, 13, 14, 17, 19, 20, 22, 23,
+                                       3, 6, 8, 9, 15, 16, 18, 21, 24};
+
 template <int N>
 struct PairCfg {
   static constexpr int N2 = N * N, N3 = N * N * N;
@@ -90,7 +110,9 @@ struct PairCfg {
   static constexpr int NG = (S * N3 + G - 1) / G;  // (slot, local DOF) positions per lane
   static __host__ __device__ size_t gbytes(int gstride) { return E * round16((size_t)gstride * sizeof(float)); }
   static __host__ __device__ size_t tbytes(int tstride) { return E * round16((size_t)tstride * sizeof(int)); }
-  static constexpr size_t work = round16(5 * (size_t)S * N3 * sizeof(f2));  // keeps groups 16-byte aligned
+  // u (dense), s1, s2 (layout S), t1, t2, t3 (layout T), per slot; 16-byte rounded
+  static constexpr size_t work =
+      round16((size_t)S * (N3 + 2 * PairLayout<N>::SW + 3 * PairLayout<N>::TW) * sizeof(f2));
   static __host__ __device__ size_t group(int gstride, int tstride, int gmode) {
     return (gmode == 0 ? gbytes(gstride) : 0) + 2 * tbytes(tstride) + work + 32;
   }
@@ -100,12 +122,13 @@ struct PairCfg {
 };
 
 // forward chain on packed pairs (see hex_forward in matfree.cu): coefficients in
-// su[(a*N+b)*N+c] -> reference gradient at the points of lane (j,k)
+// su[(a*N+b)*N+c] -> reference gradient at the points of lane (j,k).  (pa, pk):
+// this lane's stage-2 pair.
 template <int N, bool WANT_U>
-__device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* su, f2* s1, f2* s2, f2* t2, f2* t3,
-                                             f2* gx, f2* gy, f2* gz, f2* uq) {
+__device__ __forceinline__ void pair_forward(int pl, int pa, int pk, bool active, int gid, const f2* su, f2* s1, f2* s2,
+                                             f2* t1, f2* t2, f2* t3, f2* gx, f2* gy, f2* gz, f2* uq) {
   constexpr int G = HexCfg<N>::G, O = tab_off(N);
-  f2* t1 = su;
+  using L = PairLayout<N>;
   if (active) {
     const int a = pl / N, b = pl % N;
     f2 u[N];
@@ -119,16 +142,16 @@ __device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* s
         ub = fma2(bcast(c_Bp[O + k * N + c]), u[c], ub);
         ud = fma2(bcast(c_Dp[O + k * N + c]), u[c], ud);
       }
-      s1[(a * N + b) * N + k] = ub;
-      s2[(a * N + b) * N + k] = ud;
+      s1[a * L::SA + b * L::SB + k] = ub;
+      s2[a * L::SA + b * L::SB + k] = ud;
     }
   }
   group_sync<G>(gid);
   if (active) {
-    const int a = pl / N, k = pl % N;
+    const int a = pa, k = pk;
     f2 v1[N], v2[N];
 #pragma unroll
-    for (int b = 0; b < N; b++) { v1[b] = s1[(a * N + b) * N + k]; v2[b] = s2[(a * N + b) * N + k]; }
+    for (int b = 0; b < N; b++) { v1[b] = s1[a * L::SA + b * L::SB + k]; v2[b] = s2[a * L::SA + b * L::SB + k]; }
 #pragma unroll
     for (int j = 0; j < N; j++) {
       f2 bb = mul2(bcast(c_Bp[O + j * N]), v1[0]), db = mul2(bcast(c_Dp[O + j * N]), v1[0]), bd = mul2(bcast(c_Bp[O + j * N]), v2[0]);
@@ -138,9 +161,9 @@ __device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* s
         db = fma2(bcast(c_Dp[O + j * N + b]), v1[b], db);
         bd = fma2(bcast(c_Bp[O + j * N + b]), v2[b], bd);
       }
-      t1[(a * N + j) * N + k] = bb;
-      t2[(a * N + j) * N + k] = db;
-      t3[(a * N + j) * N + k] = bd;
+      t1[a * L::TA + j * L::TB + k] = bb;
+      t2[a * L::TA + j * L::TB + k] = db;
+      t3[a * L::TA + j * L::TB + k] = bd;
     }
   }
   group_sync<G>(gid);
@@ -149,9 +172,9 @@ __device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* s
     f2 w1[N], w2[N], w3[N];
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      w1[a] = t1[(a * N + j) * N + k];
-      w2[a] = t2[(a * N + j) * N + k];
-      w3[a] = t3[(a * N + j) * N + k];
+      w1[a] = t1[a * L::TA + j * L::TB + k];
+      w2[a] = t2[a * L::TA + j * L::TB + k];
+      w3[a] = t3[a * L::TA + j * L::TB + k];
     }
 #pragma unroll
     for (int i = 0; i < N; i++) {
@@ -174,10 +197,11 @@ __device__ __forceinline__ void pair_forward(int pl, bool active, int gid, f2* s
 
 // transposed chain on packed pairs (see hex_backward in matfree.cu)
 template <int N, bool WANT_M>
-__device__ __forceinline__ void pair_backward(int pl, bool active, int gid, f2* su, f2* s1, f2* s2, f2* t2, f2* t3,
-                                              const f2* vx, const f2* vy, const f2* vz, const f2* vm) {
+__device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool active, int gid, f2* su, f2* s1, f2* s2,
+                                              f2* t1, f2* t2, f2* t3, const f2* vx, const f2* vy, const f2* vz,
+                                              const f2* vm) {
   constexpr int G = HexCfg<N>::G, O = tab_off(N);
-  f2* t1 = su;
+  using L = PairLayout<N>;
   if (active) {
     const int j = pl / N, k = pl % N;
 #pragma unroll
@@ -191,20 +215,20 @@ __device__ __forceinline__ void pair_backward(int pl, bool active, int gid, f2* 
         w2 = fma2(bcast(c_Bp[O + i * N + a]), vy[i], w2);
         w3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], w3);
       }
-      t1[(a * N + j) * N + k] = w1;
-      t2[(a * N + j) * N + k] = w2;
-      t3[(a * N + j) * N + k] = w3;
+      t1[a * L::TA + j * L::TB + k] = w1;
+      t2[a * L::TA + j * L::TB + k] = w2;
+      t3[a * L::TA + j * L::TB + k] = w3;
     }
   }
   group_sync<G>(gid);
   if (active) {
-    const int a = pl / N, k = pl % N;
+    const int a = pa, k = pk;
     f2 r1[N], r2[N], r3[N];
 #pragma unroll
     for (int j = 0; j < N; j++) {
-      r1[j] = t1[(a * N + j) * N + k];
-      r2[j] = t2[(a * N + j) * N + k];
-      r3[j] = t3[(a * N + j) * N + k];
+      r1[j] = t1[a * L::TA + j * L::TB + k];
+      r2[j] = t2[a * L::TA + j * L::TB + k];
+      r3[j] = t3[a * L::TA + j * L::TB + k];
     }
 #pragma unroll
     for (int b = 0; b < N; b++) {
@@ -216,8 +240,8 @@ __device__ __forceinline__ void pair_backward(int pl, bool active, int gid, f2* 
         v1 = fma2(bcast(c_Dp[O + j * N + b]), r2[j], v1);
         v2 = fma2(bcast(c_Bp[O + j * N + b]), r3[j], v2);
       }
-      s1[(a * N + b) * N + k] = v1;
-      s2[(a * N + b) * N + k] = v2;
+      s1[a * L::SA + b * L::SB + k] = v1;
+      s2[a * L::SA + b * L::SB + k] = v2;
     }
   }
   group_sync<G>(gid);
@@ -225,7 +249,7 @@ __device__ __forceinline__ void pair_backward(int pl, bool active, int gid, f2* 
     const int a = pl / N, b = pl % N;
     f2 r1[N], r2[N];
 #pragma unroll
-    for (int k = 0; k < N; k++) { r1[k] = s1[(a * N + b) * N + k]; r2[k] = s2[(a * N + b) * N + k]; }
+    for (int k = 0; k < N; k++) { r1[k] = s1[a * L::SA + b * L::SB + k]; r2[k] = s2[a * L::SA + b * L::SB + k]; }
 #pragma unroll
     for (int c = 0; c < N; c++) {
       f2 v = mul2(bcast(c_Bp[O + c]), r1[0]);
@@ -259,9 +283,20 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
   float* gbuf = (float*)gp;
   auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };
   f2* work = (f2*)(gp + gb + 2 * tb);
-  const int so = slot < S ? slot * N3 : 0;
-  f2 *su = work + so, *s1 = work + SN3 + so, *s2 = work + 2 * SN3 + so, *t2 = work + 3 * SN3 + so,
-     *t3 = work + 4 * SN3 + so;
+  using LY = PairLayout<N>;
+  const int sl = slot < S ? slot : 0;  // this lane's slot (inactive lanes alias slot 0)
+  f2* su = work + sl * N3;             // gathered x on entry, local residual on exit
+  f2* s1 = work + S * N3 + sl * LY::SW;
+  f2* s2 = s1 + S * LY::SW;
+  f2* t1 = work + S * N3 + 2 * S * LY::SW + sl * LY::TW;
+  f2* t2 = t1 + S * LY::TW;
+  f2* t3 = t2 + S * LY::TW;
+  int pa = pl / N, pk = pl % N;  // stage-2 lane pair
+  if (N == 5) {
+    const int v = c_p2[pl];
+    pa = v / 5;
+    pk = v % 5;
+  }
   uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + C::work);  // [0],[1]: DOF rows, [2]: G tiles
   if (lane == 0) {
     mbar_init(&mbar[0], 1);
@@ -347,7 +382,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     if (has_next) t_issued++;
     group_sync<G>(gid);
     f2 gx[N], gy[N], gz[N], uq[N];
-    pair_forward<N, MASS>(pl, active, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
+    pair_forward<N, MASS>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
     if (has_next) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
       t_waited++;
@@ -414,7 +449,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
       }
       if (has_next) g_issued++;
     }
-    pair_backward<N, MASS>(pl, active, gid, su, s1, s2, t2, t3, vx, vy, vz, vm);
+    pair_backward<N, MASS>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
     const int* td = tbuf(b);
     const int nrow = rows_of(ch);
 #pragma unroll
