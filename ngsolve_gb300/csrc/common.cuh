@@ -162,6 +162,7 @@ struct gh1_op {
   bool all_affine = false;                   // hex: every element map affine (G mode 2 available)
   gh1::DBuf<float> d_Ga32;                   // hex, all affine: per-element metric records [ne][8]
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
+  int multi_pair_per_sm = 0;                 // ... of the FP32 multi-rhs apply with two rhs per lane
   int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
   // tet tiled apply (tetapply.cu): elements sorted by orientation class, tiles of
@@ -219,6 +220,8 @@ bool hex_pair_supported(int N);
 void upload_pair_tables(gh1_space* sp);
 int hex_pair_occupancy(gh1_op* op, int gmode);
 void hex_affine_setup(gh1_op* op);
+int hex_multi_pair_launch(gh1_op* op, int R, const int* phase, int want, const float* x, float* y, double* partial,
+                          unsigned int* counter, double* energy, bool prepare_only);
 void hex_pair_apply(gh1_op* op, int gmode, const float* x, float* y, double* partial, unsigned int* counter,
                     double* energy, const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)

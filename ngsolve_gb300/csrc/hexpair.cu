@@ -488,6 +488,198 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
   }
 }
 
+// ---- multi-right-hand-side apply, two right-hand sides per lane -------------------
+// Y_r += A X_r for the rhs r < R with phase[r] == want (batched solves; vectors
+// rhs-major with stride n), FP32.  Same chunk pipeline as hex_apply_multi_kernel
+// (matfree.cu): the G tile and DOF rows of a chunk of EPW elements are bulk-copied
+// once and reused for every rhs.  The active rhs are processed in pairs: a lane
+// holds its pencil for rhs (ra, rb) in one packed register, so the gather indices,
+// signs and G values are shared and every contraction step serves two rhs (an odd
+// count leaves the second half zero).  Per-rhs energies x_r^T A x_r go to energy[r].
+template <int N, bool MASS>
+__global__ void __launch_bounds__(HexCfg<N>::BLOCK)
+hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ phase, int want,
+                            const int* __restrict__ tdof, int tstride, const float* __restrict__ Gq, int gstride,
+                            const float* __restrict__ x, float* __restrict__ y, int first_cell, double* partial,
+                            unsigned int* counter, double* energy, int* err) {
+  using C = HexCfg<N>;
+  using LY = PairLayout<N>;
+  constexpr int N2 = C::N2, N3 = C::N3, G = C::G, S = C::EPW, SN3 = S * N3, RMAX = 16;
+  __shared__ float sacc[C::EPB][RMAX];
+  __shared__ int slist[RMAX], scount;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int gid = threadIdx.x / G, lane = threadIdx.x % G;
+  const int slot = lane / N2, pl = lane % N2;
+  const int rowg = (int)(round16((size_t)gstride * sizeof(float)) / sizeof(float));
+  const int rowt = (int)(round16((size_t)tstride * sizeof(int)) / sizeof(int));
+  const size_t gb = (size_t)S * rowg * sizeof(float), tb = (size_t)S * rowt * sizeof(int);
+  const size_t work_bytes = round16((size_t)S * (N3 + 2 * LY::SW + 3 * LY::TW) * sizeof(f2));
+  unsigned char* gp = smem_raw + (size_t)gid * (gb + 2 * tb + work_bytes + 32);
+  float* gbuf = (float*)gp;
+  auto tbuf = [&](int b) { return (int*)(gp + gb + b * tb); };
+  f2* work = (f2*)(gp + gb + 2 * tb);
+  const int sl = slot < S ? slot : 0;
+  f2* su = work + sl * N3;
+  f2* s1 = work + SN3 + sl * LY::SW;
+  f2* s2 = s1 + S * LY::SW;
+  f2* t1 = work + SN3 + 2 * S * LY::SW + sl * LY::TW;
+  f2* t2 = t1 + S * LY::TW;
+  f2* t3 = t2 + S * LY::TW;
+  int pa = pl / N, pk = pl % N;
+  if (N == 5) {
+    const int v = c_p2[pl];
+    pa = v / 5;
+    pk = v % 5;
+  }
+  uint64_t* mbar = (uint64_t*)(gp + gb + 2 * tb + work_bytes);
+  if (threadIdx.x == 0) {  // active rhs in ascending order
+    int c = 0;
+    for (int r = 0; r < R && r < RMAX; r++)
+      if (phase[r] == want) slist[c++] = r;
+    scount = c;
+  }
+  for (int t = threadIdx.x; t < C::EPB * RMAX; t += blockDim.x) (&sacc[0][0])[t] = 0.f;
+  if (lane == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const int nact = scount;
+  const int nch = (ne + S - 1) / S;
+  const int stride = gridDim.x * C::EPB;
+  int ch = blockIdx.x * C::EPB + gid;
+  auto rows_of = [&](int c) { return min(S, ne - c * S); };
+  auto issue = [&](int c, int b) {
+    const uint32_t bt = (uint32_t)(rows_of(c) * rowt * sizeof(int)), bg = (uint32_t)(rows_of(c) * rowg * sizeof(float));
+    mbar_expect_tx(&mbar[b], bt);
+    bulk_g2s(tbuf(b), tdof + (size_t)c * S * tstride, bt, &mbar[b]);
+    mbar_expect_tx(&mbar[2], bg);
+    bulk_g2s(gbuf, Gq + (size_t)c * S * gstride, bg, &mbar[2]);
+  };
+  int issued = 0, waited = 0;
+  bool ok = true;
+  if (nact > 0 && ch < nch && lane == 0) issue(ch, 0);
+  if (nact > 0 && ch < nch) issued = 1;
+  for (int k = 0; nact > 0 && ok && ch < nch; ch += stride, k++) {
+    const int b = k & 1;
+    ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b], (k >> 1) & 1) && mbar_wait_bounded(&mbar[2], k & 1));
+    waited++;
+    if (!ok) break;
+    const int* td = tbuf(b);
+    const int nrow = rows_of(ch);
+    const bool act_el = slot < S && ch * S + slot < ne;
+    const float* Ge = gbuf + (size_t)sl * rowg;
+    for (int q = 0; q < nact; q += 2) {
+      const int ra = slist[q], rb = q + 1 < nact ? slist[q + 1] : -1;
+      const float* xa = x + (size_t)ra * n;
+      const float* xb = x + (size_t)(rb >= 0 ? rb : ra) * n;
+      for (int t = lane; t < SN3; t += G) {
+        float va = 0.f, vb = 0.f;
+        unsigned sg = 0u;
+        if (t / N3 < nrow) {
+          const int d = td[(t / N3) * rowt + t % N3];
+          const int dof = d & 0x7fffffff;
+          va = __ldg(xa + dof);
+          if (rb >= 0) vb = __ldg(xb + dof);
+          sg = (unsigned)d & 0x80000000u;
+        }
+        work[t] = pack2(va, vb) ^ (((f2)sg << 32) | (f2)sg);
+      }
+      group_sync<G>(gid);
+      f2 gx[N], gy[N], gz[N], uq[N];
+      pair_forward<N, MASS>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
+      f2 vx[N], vy[N], vz[N], vm[N];
+      f2 en = 0;
+      if (act_el) {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+          const int o = i * N2 + pl;
+          const f2 gxx = bcast(Ge[o]), gyy = bcast(Ge[N3 + o]), gzz = bcast(Ge[2 * N3 + o]);
+          const f2 gxy = bcast(Ge[3 * N3 + o]), gxz = bcast(Ge[4 * N3 + o]), gyz = bcast(Ge[5 * N3 + o]);
+          vx[i] = fma2(gxz, gz[i], fma2(gxy, gy[i], mul2(gxx, gx[i])));
+          vy[i] = fma2(gyz, gz[i], fma2(gyy, gy[i], mul2(gxy, gx[i])));
+          vz[i] = fma2(gzz, gz[i], fma2(gyz, gy[i], mul2(gxz, gx[i])));
+          en = fma2(gz[i], vz[i], fma2(gy[i], vy[i], fma2(gx[i], vx[i], en)));
+          if (MASS) {
+            vm[i] = mul2(bcast(Ge[6 * N3 + o]), uq[i]);
+            en = fma2(uq[i], vm[i], en);
+          }
+        }
+      }
+      float ea, eb;
+      unpack2(en, ea, eb);
+      for (int o = 16; o > 0; o >>= 1) {
+        ea += __shfl_xor_sync(0xffffffffu, ea, o);
+        eb += __shfl_xor_sync(0xffffffffu, eb, o);
+      }
+      if ((lane & 31) == 0) {
+        atomicAdd(&sacc[gid][ra], ea);
+        if (rb >= 0) atomicAdd(&sacc[gid][rb], eb);
+      }
+      pair_backward<N, MASS>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
+      float* ya = y + (size_t)ra * n;
+      float* yb = y + (size_t)(rb >= 0 ? rb : ra) * n;
+      for (int t = lane; t < SN3; t += G) {
+        if (t / N3 >= nrow) continue;
+        const int d = td[(t / N3) * rowt + t % N3];
+        const int dof = d & 0x7fffffff;
+        const unsigned sg = (unsigned)d & 0x80000000u;
+        float wa, wb;
+        unpack2(work[t] ^ (((f2)sg << 32) | (f2)sg), wa, wb);
+        if (dof >= first_cell) {  // element-interior DOF: single writer
+          ya[dof] = wa;
+          if (rb >= 0) yb[dof] = wb;
+        } else {
+          atomicAdd(ya + dof, wa);
+          if (rb >= 0) atomicAdd(yb + dof, wb);
+        }
+      }
+      group_sync<G>(gid);
+    }
+    group_sync<G>(gid);
+    if (lane == 0 && ch + stride < nch) {
+      fence_proxy_async();
+      issue(ch + stride, b ^ 1);
+    }
+    if (ch + stride < nch) issued++;
+  }
+  if (!ok) {
+    if (lane == 0) {
+      atomicExch(err, 1);
+      for (int j = waited; j < issued; j++) {
+        mbar_wait_bounded(&mbar[j & 1], (j >> 1) & 1);
+        mbar_wait_bounded(&mbar[2], j & 1);
+      }
+    }
+    group_sync<G>(gid);
+  }
+  // block sums per rhs -> partial[r][block]; the last block totals into energy[r]
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x < RMAX) {
+    float sum = 0;
+    for (int g = 0; g < C::EPB; g++) sum += sacc[g][threadIdx.x];
+    if (threadIdx.x < R) partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = (double)sum;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    if (threadIdx.x < R && phase[threadIdx.x] == want) {
+      double sum = 0;
+      for (int i = 0; i < (int)gridDim.x; i++) sum += ((volatile double*)partial)[(size_t)threadIdx.x * gridDim.x + i];
+      energy[threadIdx.x] = sum;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+  }
+}
+
 // ---- host side ------------------------------------------------------------------
 bool hex_pair_supported(int N) { return N >= 2 && N <= 7; }
 
@@ -651,6 +843,54 @@ void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partia
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)
 #undef GH1_PAIR_CASE
+}
+
+// paired multi-rhs apply: occupancy (prepare_only, outside stream capture) and launch
+template <int N, bool MASS>
+static int multi_pair_launch_n(gh1_op* op, int R, const int* phase, int want, const float* x, float* y,
+                               double* partial, unsigned int* counter, double* energy, bool prepare_only) {
+  using C = HexCfg<N>;
+  using LY = PairLayout<N>;
+  gh1_space* sp = op->sp;
+  const size_t gb = (size_t)C::EPW * round16((size_t)op->gstride32 * sizeof(float));
+  const size_t tb = (size_t)C::EPW * round16((size_t)sp->tstride * sizeof(int));
+  const size_t work = round16((size_t)C::EPW * (C::N3 + 2 * LY::SW + 3 * LY::TW) * sizeof(f2));
+  const size_t smem = (size_t)C::EPB * (gb + 2 * tb + work + 32);
+  auto kern = hex_apply_multi_pair_kernel<N, MASS>;
+  if (prepare_only || op->multi_pair_per_sm <= 0) {
+    int dev = 0, optin = 0;
+    GH1_CUDA(cudaGetDevice(&dev));
+    GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+    GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    int v = 0;
+    GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, C::BLOCK, smem));
+    GH1_CHECK(v >= 1, GH1_ERR_UNSUPPORTED, "paired multi-rhs hex apply does not fit on an SM");
+    op->multi_pair_per_sm = v;
+  }
+  const int ne = sp->mesh->ne, nch = (ne + C::EPW - 1) / C::EPW;
+  const int grid = std::min((nch + C::EPB - 1) / C::EPB, sp->ctx->nsm * op->multi_pair_per_sm);
+  if (prepare_only) return grid;
+  kern<<<grid, C::BLOCK, smem, sp->ctx->stream>>>(ne, op->nrows, R, phase, want, sp->d_tdof.p, sp->tstride, op->d_G32.p,
+                                                  op->gstride32, x, y, (int)sp->first_cell, partial, counter, energy,
+                                                  op->d_err.p);
+  check_kernel(sp->ctx, "hex_apply_multi_pair_kernel");
+  return grid;
+}
+
+int hex_multi_pair_launch(gh1_op* op, int R, const int* phase, int want, const float* x, float* y, double* partial,
+                          unsigned int* counter, double* energy, bool prepare_only) {
+  const bool mass = op->has_mass;
+  int g = 0;
+#define GH1_MPAIR_CASE(NN)                                                                                         \
+  case NN:                                                                                                         \
+    g = mass ? multi_pair_launch_n<NN, true>(op, R, phase, want, x, y, partial, counter, energy, prepare_only)      \
+             : multi_pair_launch_n<NN, false>(op, R, phase, want, x, y, partial, counter, energy, prepare_only);    \
+    break;
+  GH1_PAIR_SWITCH(op->sp->p + 1, GH1_MPAIR_CASE)
+#undef GH1_MPAIR_CASE
+  return g;
 }
 
 }  // namespace gh1

@@ -1012,6 +1012,12 @@ int hex_multi_launch(gh1_op* op, int R, const int* phase, int want, const T* x, 
                      unsigned int* counter, double* energy, bool prepare_only) {
   using C = HexCfg<N>;
   gh1_space* sp = op->sp;
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32: two right-hand sides per lane (GH1_MULTI_PAIR=0 keeps one per lane)
+    static const bool paired = !(getenv("GH1_MULTI_PAIR") && getenv("GH1_MULTI_PAIR")[0] == '0');
+    if (paired && hex_pair_supported(N))
+      return hex_multi_pair_launch(op, R, phase, want, x, y, partial, counter, energy, prepare_only);
+  }
   const int gs = std::is_same<T, float>::value ? op->gstride32 : op->gstride64;
   const T* G = std::is_same<T, float>::value ? (const T*)op->d_G32.p : (const T*)op->d_G64.p;
   const size_t smem = HexSmem<N, T>::total(gs, sp->tstride, 0);

@@ -32,7 +32,7 @@ def _problem(gpu, n, p, seed, nrhs):
 
 
 def test_batch_matches_single_and_oracle(gpu):
-    specs = [(3, 2, 1, 3), (4, 3, 2, 2), (2, 5, 3, 4), (5, 1, 4, 1)]
+    specs = [(3, 2, 1, 3), (4, 3, 2, 2), (2, 5, 3, 4), (5, 1, 4, 1), (3, 4, 5, 5)]
     probs = [_problem(gpu, n, p, seed, r) for n, p, seed, r in specs]
     solver = gpu.solvers.BatchCG([pr[3] for pr in probs], [s[3] for s in specs])
     X = solver.Solve([pr[4] for pr in probs], tol=1e-10)
