@@ -11,6 +11,7 @@
 #include <cstring>
 #include <numeric>
 #include <thread>
+#include <cstdlib>
 #include "common.cuh"
 #include "basis.cuh"
 
@@ -414,7 +415,12 @@ int gh1_assemble_csr(gh1_form* f, gh1_op** out) {
   return guard(f->sp->ctx, [&] {
     gh1_space* sp = f->sp;
     GH1_CUDA(cudaSetDevice(sp->ctx->device));
-    if (!sp->have_graph) build_graph(sp);
+    if (!sp->have_graph) {
+      // GPU pattern build; the host one for very high orders or GH1_GRAPH=host
+      const char* g = getenv("GH1_GRAPH");
+      const bool host = g && std::string(g) == "host";
+      if (host || !build_graph_gpu(sp)) build_graph(sp);
+    }
     gh1_op* op = new gh1_op();
     op->ctx = sp->ctx; op->kind = GH1_OP_CSR; op->form = f; op->sp = sp;
     op->nrows = sp->ndof; op->nnz = sp->nnz;

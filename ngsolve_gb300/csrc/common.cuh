@@ -195,7 +195,8 @@ void check_kernel(gh1_ctx* ctx, const char* what);
 
 // kernels / drivers (implemented in the .cu files)
 void build_tables(gh1_space* sp);                                   // tables.cu
-void build_graph(gh1_space* sp);                                    // assemble.cu
+void build_graph(gh1_space* sp);                                    // assemble.cu (host)
+bool build_graph_gpu(gh1_space* sp);                                // graph.cu
 void assemble_csr(gh1_form* f, double* vals);                       // assemble.cu
 void rhs_elementwise(gh1_space* sp, const double* f, double* b);    // assemble.cu
 void matfree_setup(gh1_op* op);                                     // matfree.cu
