@@ -3,8 +3,8 @@
 //
 // Pattern: MatrixGraph (linalg/sparsematrix.cpp:450-900) -- row r holds the
 // sorted union of the DOFs of all elements containing DOF r, diagonal included,
-// full storage.  Built on the host like the reference does (it is setup, run
-// once per space).
+// full storage.  build_graph here is the host build (threads, marker arrays),
+// used when graph.cu's GPU build does not apply (rows over its candidate cap).
 // Element matrices: kappa grad.grad + mu u v (T_CalcElementMatrixAdd,
 // fem/symbolicintegrator.cpp:1548-1830).
 //   tet: K_e = sum_blk Gbar_blk S^c_blk + M_e S^c_mass with the per-class
