@@ -171,6 +171,9 @@ int gh1_elem_grad_dot(gh1_space* space, const double* u, const double* w, double
 /* J(kappa) = 1/2 int (u - u_target)^2 with A(kappa) u = f (zero Dirichlet);
  * dJ/dkappa_e = -int_e grad u . grad lambda,  A lambda = M (u - u_target).
  * f, u_target: device double[ndof] (f already assembled); kappa: the form's.
+ * Both solves run the mixed-precision CG (FP32 inner, FP64 refinement) to the
+ * true relative residual tol.  The form keeps its operator between calls
+ * (released by gh1_form_free); only the Jacobi diagonal is rebuilt per call.
  * Outputs (device): u[ndof], lambda[ndof], dJdkappa[ne]; J on the host.   */
 int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u_target, double tol,
                      double* u, double* lambda, double* dJdkappa, double* J);

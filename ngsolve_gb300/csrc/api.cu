@@ -257,6 +257,12 @@ void check_kernel(gh1_ctx* ctx, const char* what) {
 }
 }  // namespace gh1
 
+gh1_form::~gh1_form() {
+  delete adj_M;  // before the mass form it refers to
+  delete adj_A;
+  delete adj_mass;
+}
+
 // =============================================================================
 extern "C" {
 

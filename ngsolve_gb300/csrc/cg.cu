@@ -529,27 +529,40 @@ extern "C" int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u
     gh1_space* sp = form->sp;
     const int64_t n = sp->ndof;
     cudaStream_t s = ctx->stream;
-    gh1_op* A = nullptr;
+    // the operator with FP64 and FP32 data, kept on the form between calls; the
+    // metrics follow the current kappa, the Jacobi diagonal is rebuilt per call
+    int rc = GH1_OK;
+    if (!form->adj_A) {
+      rc = gh1_matfree_create(form, 3, &form->adj_A);
+      if (rc) return rc;
+    }
+    gh1_op* A = form->adj_A;
+    if (A->form_version != form->version) matfree_setup(A);
     gh1_pre* P = nullptr;
-    int rc = gh1_matfree_create(form, 1, &A);
-    if (rc) return rc;
     rc = gh1_jacobi_create(A, nullptr, 0, &P);
-    if (rc) { gh1_op_free(A); return rc; }
+    if (rc) return rc;
+    // forward and adjoint solves: FP32 inner CG inside FP64 refinement, FP64 true residual
     gh1_cg_opts o{};
-    o.tol = tol; o.maxit = 100000; o.mode = GH1_CG_FP64; o.stop_rule = GH1_STOP_TRUE; o.initialize = 1;
+    o.tol = tol; o.maxit = 100000; o.mode = GH1_CG_MIXED; o.stop_rule = GH1_STOP_TRUE; o.initialize = 1;
     gh1_cg_result res{};
     rc = gh1_cg(A, P, f, u, &o, &res);
-    if (rc != GH1_OK) { gh1_pre_free(P); gh1_op_free(A); return rc; }
-    // mass operator (unit coefficient) for J and the adjoint right-hand side
-    gh1_form mf;
-    mf.sp = sp;
-    std::vector<double> zeros(sp->mesh->ne, 0.0), ones(sp->mesh->ne, 1.0);
-    mf.d_kappa.upload(zeros, s);
-    mf.d_mu.upload(ones, s);
-    mf.has_mu = true;
-    gh1_op M;
-    M.ctx = ctx; M.kind = GH1_OP_MATFREE; M.form = &mf; M.sp = sp; M.nrows = n; M.prec_mask = 1;
-    matfree_setup(&M);
+    if (rc != GH1_OK) { gh1_pre_free(P); return rc; }
+    // unit-mass operator for J and the adjoint right-hand side (built once)
+    if (!form->adj_M) {
+      gh1_form* mf = new gh1_form();
+      form->adj_mass = mf;
+      mf->sp = sp;
+      std::vector<double> zeros(sp->mesh->ne, 0.0), ones(sp->mesh->ne, 1.0);
+      mf->d_kappa.upload(zeros, s);
+      mf->d_mu.upload(ones, s);
+      mf->has_mu = true;
+      gh1_op* M = new gh1_op();
+      form->adj_M = M;
+      M->ctx = ctx; M->kind = GH1_OP_MATFREE; M->form = mf; M->sp = sp; M->nrows = n; M->prec_mask = 1;
+      matfree_setup(M);
+      GH1_CUDA(cudaStreamSynchronize(s));  // the host staging vectors go out of scope
+    }
+    gh1_op* Mop = form->adj_M;
     DBuf<double> e(n), Me(n), tmp(1);
     axpby_kernel<double, double><<<grid_for(ctx, n, 256), 256, 0, s>>>(n, 1.0, u, 0.0, e.p);
     axpby_kernel<double, double><<<grid_for(ctx, n, 256), 256, 0, s>>>(n, -1.0, u_target, 1.0, e.p);
@@ -558,18 +571,17 @@ extern "C" int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u
     DBuf<unsigned int> cnt(1);
     cnt.zero(s);
     DBuf<double> en(1);
-    matfree_apply_ex(&M, e.p, Me.p, GH1_F64, partial.p, cnt.p, en.p, nullptr);
+    matfree_apply_ex(Mop, e.p, Me.p, GH1_F64, partial.p, cnt.p, en.p, nullptr);
     double hJ = 0;
     GH1_CUDA(cudaMemcpyAsync(&hJ, en.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     GH1_CUDA(cudaStreamSynchronize(s));
     *J = 0.5 * hJ;
     rc = gh1_cg(A, P, Me.p, lam, &o, &res);
-    if (rc != GH1_OK) { gh1_pre_free(P); gh1_op_free(A); return rc; }
+    if (rc != GH1_OK) { gh1_pre_free(P); return rc; }
     elem_grad_dot_with(A, u, lam, dJdkappa);
     axpby_kernel<double, double><<<grid_for(ctx, sp->mesh->ne, 256), 256, 0, s>>>(sp->mesh->ne, -1.0, dJdkappa, 0.0, dJdkappa);
     GH1_CUDA(cudaStreamSynchronize(s));
     gh1_pre_free(P);
-    gh1_op_free(A);
     return GH1_OK;
   } catch (const gh1::Error& e) {
     ctx->err = e.what();

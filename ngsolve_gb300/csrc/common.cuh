@@ -126,6 +126,16 @@ struct gh1_form {
   gh1::DBuf<double> d_mu;     // ne (empty: mu = 0)
   bool has_mu = false;
   int version = 0;            // bumped on coefficient change
+  // gh1_adjoint_grad cache: this form's operator (FP64 + FP32 data; its metrics
+  // follow coefficient changes) and the unit-mass operator for J and the adjoint
+  // right-hand side; released with the form
+  gh1_op* adj_A = nullptr;
+  gh1_form* adj_mass = nullptr;
+  gh1_op* adj_M = nullptr;
+  gh1_form() = default;
+  gh1_form(const gh1_form&) = delete;
+  gh1_form& operator=(const gh1_form&) = delete;
+  ~gh1_form();  // api.cu
 };
 
 struct gh1_op {

@@ -239,8 +239,9 @@ def test_hex_p_exactness_gpu(gpu):
 
 
 def test_adjoint_gradient(gpu):
-    """dJ/dkappa from the adjoint kernel vs fourth-order central finite
-    differences and vs the oracle's adjoint recipe."""
+    """dJ/dkappa from the adjoint kernel (mixed-precision forward and adjoint
+    solves) vs sixth-order central finite differences and vs the oracle's
+    adjoint recipe."""
     m = _mesh("hex", 4, 0.0)
     p = 2
     fes = gpu.H1(m, order=p, dirichlet=".*")
@@ -261,15 +262,15 @@ def test_adjoint_gradient(gpu):
     J.backward()
     g = kt.grad.numpy()
     for e in rng.choice(m.ne, 8, replace=False):
-        # fourth-order central difference, step 1e-3 kappa_e (truncation ~1e-12,
-        # solve noise / step ~1e-11 relative)
-        h = 1e-3 * kappa[e]
-        Jk = []
-        for sft in (2, 1, -1, -2):
+        # sixth-order central difference, step 1e-2 kappa_e (truncation ~1e-12,
+        # solve noise / step ~1e-12 relative)
+        h = 1e-2 * kappa[e]
+        Jk = {}
+        for sft in (-3, -2, -1, 1, 2, 3):
             k = kappa.copy()
             k[e] += sft * h
-            Jk.append(prob.evaluate(k)[0])
-        fd = (-Jk[0] + 8 * Jk[1] - 8 * Jk[2] + Jk[3]) / (12 * h)
+            Jk[sft] = prob.evaluate(k)[0]
+        fd = (45 * (Jk[1] - Jk[-1]) - 9 * (Jk[2] - Jk[-2]) + (Jk[3] - Jk[-3])) / (60 * h)
         # 1e-6 relative; a gradient below 1e-4 of the largest is held to 1e-6 of that
         assert abs(fd - g[e]) <= 1e-6 * max(abs(g[e]), 1e-4 * np.abs(g).max())
     # oracle recipe: u, lambda by direct solves, -int grad u . grad lambda
