@@ -145,8 +145,11 @@ def dist_setup(n_gpus):
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if torch.cuda.is_available() and os.environ.get("GH1_DIST_BACKEND", "nccl") == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:  # host-only replicas (tests of the multi-process path on CPU)
+            dist.init_process_group("gloo")
     return ws, rank, local
 
 
@@ -161,9 +164,14 @@ def max_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank, t_step, ws):
+    """Whole-job throughput of N replicas: all ranks' units / the slowest rank's time."""
+    return ws * units_per_rank / max_over_ranks(t_step, ws) / 1e9
 
 
 def cpu_apply_sample(nx, order, target_s=10.0, threads=None):
