@@ -337,7 +337,33 @@ def workload_c2(args):
             amf.mat.Mult(x32, y32)
         t_mf32, _ = _timed(lambda: amf.mat.Mult(x32, y32), reps=20)
         B = nnz * 12 + 8 * (N + 1) + 2 * N * 8
-        out["orders"][p] = {"ndof": N, "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm,
+        cpu = None
+        if not args.no_cpu:
+            # the oracle's CPU restatement on all host cores: pattern, assembly (checked
+            # against the GPU CSR at this full size), SpMV and the element-wise apply
+            from oracle import oracle as O
+            S = O.OracleSpace(mesh.points, mesh.elements, p)
+            t0 = time.perf_counter()
+            S.graph()
+            c_graph = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            orp, oci, ova = S.assemble(kappa=kappa)
+            c_asm = time.perf_counter() - t0
+            same_pattern = bool(np.array_equal(np.asarray(rp), orp) and np.array_equal(np.asarray(ci), oci))
+            val_err = float(np.abs(np.asarray(va) - ova).max() / np.abs(ova).max()) if same_pattern else None
+            xs = x.t.cpu().numpy()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                O.spmv(orp, oci, ova, xs)
+            c_spmv = (time.perf_counter() - t0) / 3
+            t0 = time.perf_counter()
+            S.apply_mf(xs, kappa=kappa)
+            c_apply = time.perf_counter() - t0
+            cpu = {"cores": O.max_threads(), "kind": "port", "graph_s": c_graph, "assemble_s": c_asm,
+                   "spmv_ms": c_spmv * 1e3, "apply_elementwise_ms": c_apply * 1e3,
+                   "gpu_pattern_equals_cpu": same_pattern, "gpu_vals_max_diff_rel_to_max": val_err}
+            del S, orp, oci, ova
+        out["orders"][p] = {"ndof": N, "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm, "cpu_oracle": cpu,
                             "spmv_ms": t_spmv * 1e3, "spmv_gbs": B / t_spmv / 1e9, "cusparse_ms": t_cusp * 1e3,
                             "spmv_vs_cusparse": t_cusp / t_spmv, "spmv_err_vs_cusparse": err,
                             "matfree_fp64_ms": t_mf64 * 1e3, "matfree_fp32_ms": t_mf32 * 1e3,
