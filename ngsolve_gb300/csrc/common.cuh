@@ -183,6 +183,10 @@ struct gh1_op {
   gh1::DBuf<double> d_tetD64, d_tetw64;      // [class][nloc][Rs] table rows, per-row weights [Rp]
   gh1::DBuf<float> d_tetD32, d_tetw32;
   int tet_tiles_per_sm[2] = {0, 0};          // [FP64/FP32] resident blocks; 0: does not fit, element-wise kernel
+  bool tet_chunked = false;                  // tables streamed in 16-point chunks (orders with large rules)
+  int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
+  gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights
+  gh1::DBuf<float> d_tetDm32, d_tetwm32;
   gh1::DBuf<double> d_diag;   // operator diagonal (FP64)
   bool have_diag = false;
   // scratch vectors for accumulate / scaling

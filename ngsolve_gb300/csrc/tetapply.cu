@@ -209,6 +209,145 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
   if (partial) block_reduce_finish(acc, partial, counter, energy);
 }
 
+// ---- chunked variant (orders whose whole class table does not fit in shared memory)
+// The rule points go through shared memory 16 at a time: per chunk the table
+// slice (48 gradient rows, or 16 value rows of the mass rule) is loaded, the two
+// products run on it and Y accumulates in registers across chunks.
+//   Dg: [class][gradient chunk][nlocp][48] (rows: d/dx, d/dy, d/dz of 16 points)
+//   Dm: [class][mass chunk][nlocp][16];  Wg, Wm: rule weights, zero-padded
+constexpr int TET_QC = 16;
+
+template <class T, bool MASS>
+__global__ void __launch_bounds__(TET_TT)
+tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncg,
+                      int ncm, const int* __restrict__ eldofs, const T* __restrict__ Ge, const T* __restrict__ Me,
+                      const T* __restrict__ Dg, const T* __restrict__ Dm, const T* __restrict__ Wg,
+                      const T* __restrict__ Wm, const T* __restrict__ x, T* __restrict__ y, double* partial,
+                      unsigned int* counter, double* energy, const int* skip) {
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int RS = 3 * TET_QC + 1;  // row stride of the table slice (odd: conflict-free column reads)
+  T* sD = (T*)smem;                                                   // [nlocp][RS]
+  T* sX = (T*)(smem + tet_r16((size_t)nlocp * RS * sizeof(T)));       // [nlocp][TE]
+  T* sP = sX + (size_t)nlocp * TET_TE;                                // [48][TE]
+  T* sG = sP + (size_t)3 * TET_QC * TET_TE;                           // [TE][7]
+  int* sDof = (int*)(sG + TET_TE * 7);                                // [nlocp][TE]
+  const int tid = threadIdx.x, cg = tid & 7, rg = tid >> 3;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  const int ni = nlocp / 16;  // block-uniform
+  double acc = 0;
+  for (int t = t0; t < t1; t++) {
+    const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    __syncthreads();
+    for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {
+      const int e = k % TET_TE, i = k / TET_TE;
+      int d = 0;
+      T v = 0;
+      if (e < cnt && i < nloc) {
+        d = eldofs[(size_t)perm[start + e] * nloc + i];
+        v = x[d];
+      }
+      sDof[k] = d;
+      sX[k] = v;
+    }
+    for (int k = tid; k < TET_TE * 7; k += TET_TT) {
+      const int e = k / 7, c = k % 7;
+      T v = 0;
+      if (e < cnt) v = c < 6 ? Ge[(size_t)perm[start + e] * 6 + c] : (MASS ? Me[perm[start + e]] : T(0));
+      sG[k] = v;
+    }
+    T b[TET_TI][4];
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    const int nchunk = ncg + (MASS ? ncm : 0);
+    for (int cc = 0; cc < nchunk; cc++) {
+      const bool grad = cc < ncg;
+      const int RC = grad ? 3 * TET_QC : TET_QC;  // rows of this slice
+      const T* src = grad ? Dg + ((size_t)cls * ncg + cc) * nlocp * (3 * TET_QC)
+                          : Dm + ((size_t)cls * ncm + (cc - ncg)) * nlocp * TET_QC;
+      __syncthreads();  // X, G, DOFs ready; the previous slice is consumed
+      for (int k = tid; k < nlocp * RC; k += TET_TT) sD[(k / RC) * RS + k % RC] = src[k];
+      __syncthreads();
+      // P[r][e] = sum_i D[i][r] X[i][e], rows r = rg + 16 u
+      {
+        T a[3][4];
+#pragma unroll
+        for (int u = 0; u < 3; u++) a[u][0] = a[u][1] = a[u][2] = a[u][3] = 0;
+        const int nt = RC / 16;
+        for (int i = 0; i < nloc; i++) {
+          T xv[4];
+          ld4(sX + i * TET_TE + 4 * cg, xv);
+#pragma unroll
+          for (int u = 0; u < 3; u++)
+            if (u < nt) {
+              const T dv = sD[i * RS + rg + 16 * u];
+              a[u][0] += dv * xv[0]; a[u][1] += dv * xv[1]; a[u][2] += dv * xv[2]; a[u][3] += dv * xv[3];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 3; u++)
+          if (u < nt) st4(sP + (size_t)(rg + 16 * u) * TET_TE + 4 * cg, a[u]);
+      }
+      __syncthreads();
+      if (grad) {
+        for (int k = tid; k < TET_QC * TET_TE; k += TET_TT) {
+          const int q = k / TET_TE, e = k % TET_TE;
+          const T* g = sG + e * 7;
+          T* px = sP + (size_t)q * TET_TE + e;
+          T* py = px + (size_t)TET_QC * TET_TE;
+          T* pz = py + (size_t)TET_QC * TET_TE;
+          const T ux = *px, uy = *py, uz = *pz, w = Wg[cc * TET_QC + q];
+          const T vx = w * (g[0] * ux + g[3] * uy + g[4] * uz);
+          const T vy = w * (g[3] * ux + g[1] * uy + g[5] * uz);
+          const T vz = w * (g[4] * ux + g[5] * uy + g[2] * uz);
+          acc += (double)(ux * vx + uy * vy + uz * vz);
+          *px = vx; *py = vy; *pz = vz;
+        }
+      } else {
+        for (int k = tid; k < TET_QC * TET_TE; k += TET_TT) {
+          const int q = k / TET_TE, e = k % TET_TE;
+          T* pm = sP + (size_t)q * TET_TE + e;
+          const T u = *pm, vm = Wm[(cc - ncg) * TET_QC + q] * sG[e * 7 + 6] * u;
+          acc += (double)(u * vm);
+          *pm = vm;
+        }
+      }
+      __syncthreads();
+      // Y[i][e] += sum_r D[i][r] V[r][e], rows i = rg + 16 u
+      for (int r = 0; r < RC; r++) {
+        T pv[4];
+        ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
+#pragma unroll
+        for (int u = 0; u < TET_TI; u++)
+          if (u < ni) {
+            const T dv = sD[(rg + 16 * u) * RS + r];
+            b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
+          }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) {
+      const int i = rg + 16 * u;
+      if (u < ni && i < nloc) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int e = 4 * cg + c;
+          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+        }
+      }
+    }
+  }
+  if (partial) block_reduce_finish(acc, partial, counter, energy);
+}
+
+template <class T>
+__host__ __device__ inline size_t tet_chunk_smem(int nlocp) {
+  return tet_r16((size_t)nlocp * (3 * TET_QC + 1) * sizeof(T)) +
+         tet_r16(((size_t)nlocp * TET_TE + 3 * TET_QC * TET_TE + TET_TE * 7) * sizeof(T) +
+                 (size_t)nlocp * TET_TE * sizeof(int));
+}
+
 // D[c][i][r] from the per-class tables: rows r < 3 nq are d/dx, d/dy, d/dz of
 // shape i at the stiffness-rule points (tab[c][q][i][1..3]); the next nqm rows the
 // values at the mass-rule points (tabm[c][q][i]); everything else zero
@@ -275,6 +414,83 @@ static bool tet_dims_match(int p, int nq, int nqm) {
   }
 }
 
+// chunked tables: Dg[c][cc][i][r] (r < 48: component r / 16 of point cc*16 + r % 16)
+// and Dm[c][cm][i][r] (value at mass point cm*16 + r); zero beyond the rules
+template <class T>
+__global__ void tet_chunk_table_kernel(int ncls, int nloc, int nlocp, int nq, int nqm, int ncg, int ncm,
+                                       const T* __restrict__ tab, const double* __restrict__ tabm, T* Dg, T* Dm) {
+  const int64_t tg = (int64_t)ncls * ncg * nlocp * 3 * TET_QC, tm = (int64_t)ncls * ncm * nlocp * TET_QC;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tg + tm; k += (int64_t)gridDim.x * blockDim.x) {
+    if (k < tg) {
+      const int r = (int)(k % (3 * TET_QC)), i = (int)((k / (3 * TET_QC)) % nlocp);
+      const int64_t ccc = k / ((int64_t)3 * TET_QC * nlocp);
+      const int cc = (int)(ccc % ncg), c = (int)(ccc / ncg);
+      const int q = cc * TET_QC + r % TET_QC, comp = r / TET_QC;
+      Dg[k] = (i < nloc && q < nq) ? tab[(((size_t)c * nq + q) * nloc + i) * 4 + 1 + comp] : T(0);
+    } else {
+      const int64_t km = k - tg;
+      const int r = (int)(km % TET_QC), i = (int)((km / TET_QC) % nlocp);
+      const int64_t ccc = km / ((int64_t)TET_QC * nlocp);
+      const int cm = (int)(ccc % ncm), c = (int)(ccc / ncm);
+      const int q = cm * TET_QC + r;
+      Dm[km] = (i < nloc && q < nqm) ? (T)tabm[((size_t)c * nqm + q) * nloc + i] : T(0);
+    }
+  }
+}
+
+template <class T, bool MASS>
+static int tet_chunk_occupancy(int nlocp) {
+  auto kern = tet_tile_chunk_kernel<T, MASS>;
+  const size_t smem = tet_chunk_smem<T>(nlocp);
+  int dev = 0, optin = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const int avail = optin - (int)fa.sharedSizeBytes;
+  if ((long long)smem > avail) return 0;
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, avail));
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TET_TT, smem));
+  return v;
+}
+
+// chunked tables and weights for all precisions the operator carries
+static void tet_chunk_setup(gh1_op* op, const std::vector<double>& rule, const std::vector<double>& rulem) {
+  gh1_space* sp = op->sp;
+  cudaStream_t s = sp->ctx->stream;
+  const int nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass, nlocp = (nloc + 15) / 16 * 16;
+  const int ncg = (nq + TET_QC - 1) / TET_QC, ncm = (nqm + TET_QC - 1) / TET_QC, ncls = N_TET_CLASSES;
+  op->tet_chunked = true;
+  op->tet_ncg = ncg;
+  op->tet_ncm = ncm;
+  const int64_t ng = (int64_t)ncls * ncg * nlocp * 3 * TET_QC, nm = (int64_t)ncls * ncm * nlocp * TET_QC;
+  std::vector<double> wg((size_t)ncg * TET_QC, 0.0), wm((size_t)ncm * TET_QC, 0.0);
+  for (int q = 0; q < nq; q++) wg[q] = rule[4 * q + 3];
+  for (int q = 0; q < nqm; q++) wm[q] = rulem[4 * q + 3];
+  const int tgrid = (int)std::min<int64_t>((ng + nm + 255) / 256, 4096);
+  op->d_tetD64.alloc(ng);
+  op->d_tetDm64.alloc(nm);
+  tet_chunk_table_kernel<double><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, ncg, ncm, sp->d_tab64.p,
+                                                       sp->d_tabm64.p, op->d_tetD64.p, op->d_tetDm64.p);
+  check_kernel(sp->ctx, "tet_chunk_table_kernel");
+  op->d_tetw64.upload(wg, s);
+  op->d_tetwm64.upload(wm, s);
+  op->tet_tiles_per_sm[0] = op->has_mass ? tet_chunk_occupancy<double, true>(nlocp) : tet_chunk_occupancy<double, false>(nlocp);
+  if (op->prec_mask & 2) {
+    op->d_tetD32.alloc(ng);
+    op->d_tetDm32.alloc(nm);
+    tet_chunk_table_kernel<float><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, ncg, ncm, sp->d_tab32.p,
+                                                        sp->d_tabm64.p, op->d_tetD32.p, op->d_tetDm32.p);
+    check_kernel(sp->ctx, "tet_chunk_table_kernel");
+    std::vector<float> wg32(wg.begin(), wg.end()), wm32(wm.begin(), wm.end());
+    op->d_tetw32.upload(wg32, s);
+    op->d_tetwm32.upload(wm32, s);
+    op->tet_tiles_per_sm[1] = op->has_mass ? tet_chunk_occupancy<float, true>(nlocp) : tet_chunk_occupancy<float, false>(nlocp);
+  }
+  GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+}
+
 // Class-sorted element order, tiles, tables and occupancy.  GH1_TET_KERNEL=elementwise
 // keeps the element-wise kernel (for comparisons).
 void tet_tiles_setup(gh1_op* op) {
@@ -284,7 +500,8 @@ void tet_tiles_setup(gh1_op* op) {
   if (env && std::string(env) == "elementwise") return;
   const int ne = sp->mesh->ne, nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
   const int nlocp = (nloc + 15) / 16 * 16;
-  if (nlocp / 16 > TET_TI || ne == 0 || !tet_dims_match(sp->p, nq, nqm)) return;
+  op->tet_chunked = false;
+  if (nlocp / 16 > TET_TI || ne == 0) return;
   const int R = 3 * nq + (op->has_mass ? nqm : 0), Rp = (R + 15) / 16 * 16, Rs = Rp + 1;
   const int ncls = N_TET_CLASSES;
   cudaStream_t s = sp->ctx->stream;
@@ -307,17 +524,23 @@ void tet_tiles_setup(gh1_op* op) {
       tiles.push_back(std::min(TET_TE, count[c + 1] - a));
       tiles.push_back(0);
     }
+  op->d_tet_perm.upload(perm, s);
+  op->d_tet_tiles.upload(tiles, s);
+  op->tet_ntiles = (int)tiles.size() / 4;
+  const bool mass = op->has_mass;
+  // the whole class table in shared memory (compiled orders), else 16-point chunks
+  const TetSmem<double> full{nlocp, Rp, Rs};
+  if (!tet_dims_match(sp->p, nq, nqm) || full.total() > (size_t)200 * 1024) {
+    tet_chunk_setup(op, rule, rulem);
+    return;
+  }
   std::vector<double> w(Rp, 0.0);
   for (int r = 0; r < 3 * nq; r++) w[r] = rule[4 * (r % nq) + 3];
   if (op->has_mass)
     for (int q = 0; q < nqm; q++) w[3 * nq + q] = rulem[4 * q + 3];
-  op->d_tet_perm.upload(perm, s);
-  op->d_tet_tiles.upload(tiles, s);
-  op->tet_ntiles = (int)tiles.size() / 4;
   op->tet_R = R; op->tet_Rp = Rp; op->tet_Rs = Rs;
   const int64_t tot = (int64_t)ncls * nlocp * Rs;
   const int tgrid = (int)std::min<int64_t>((tot + 255) / 256, 4096);
-  const bool mass = op->has_mass;
   op->d_tetD64.alloc(tot);
   tet_tile_table_kernel<double><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, nqm, R, Rs, sp->d_tab64.p, sp->d_tabm64.p,
                                                       op->d_tetD64.p);
@@ -363,11 +586,41 @@ static void tet_tile_launch(gh1_op* op, int per_sm, const T* D, const T* W, cons
 #undef GH1_TET_LAUNCH
 }
 
+template <class T>
+static void tet_chunk_launch(gh1_op* op, int per_sm, const T* Dg, const T* Dm, const T* Wg, const T* Wm, const T* G,
+                             const T* M, const T* x, T* y, double* partial, unsigned int* counter, double* energy,
+                             const int* skip) {
+  gh1_space* sp = op->sp;
+  const int nlocp = (sp->nloc + 15) / 16 * 16;
+  const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
+  const size_t smem = tet_chunk_smem<T>(nlocp);
+  if (op->has_mass)
+    tet_tile_chunk_kernel<T, true><<<grid, TET_TT, smem, sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,
+        sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip);
+  else
+    tet_tile_chunk_kernel<T, false><<<grid, TET_TT, smem, sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,
+        sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip);
+  check_kernel(sp->ctx, "tet_tile_chunk_kernel");
+}
+
 bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
                      double* energy, const int* skip) {
   const int pi = prec == GH1_F64 ? 0 : 1;
   const int per_sm = op->tet_tiles_per_sm[pi];
   if (per_sm <= 0) return false;
+  if (op->tet_chunked) {
+    if (prec == GH1_F64)
+      tet_chunk_launch<double>(op, per_sm, op->d_tetD64.p, op->d_tetDm64.p, op->d_tetw64.p, op->d_tetwm64.p,
+                               op->d_G64.p, op->has_mass ? op->d_M64.p : nullptr, (const double*)x, (double*)y,
+                               partial, counter, energy, skip);
+    else
+      tet_chunk_launch<float>(op, per_sm, op->d_tetD32.p, op->d_tetDm32.p, op->d_tetw32.p, op->d_tetwm32.p,
+                              op->d_G32.p, op->has_mass ? op->d_M32.p : nullptr, (const float*)x, (float*)y,
+                              partial, counter, energy, skip);
+    return true;
+  }
   if (prec == GH1_F64)
     tet_tile_launch<double>(op, per_sm, op->d_tetD64.p, op->d_tetw64.p, op->d_G64.p,
                             op->has_mass ? op->d_M64.p : nullptr, (const double*)x, (double*)y, partial, counter,

@@ -1,7 +1,8 @@
-"""Matrix-free tet apply: the class-tiled GEMM kernel and the element-wise
-kernel (GH1_TET_KERNEL=elementwise) against the FP64 oracle, FP64 and FP32,
-with and without the mass term; tiles straddle no class boundary, so meshes with
-many classes and partially filled tiles are used."""
+"""Matrix-free tet apply: the class-tiled GEMM kernel (whole class table in
+shared memory for p <= 4, streamed in 16-point chunks for the large rules of
+p = 5, 6) and the element-wise kernel (GH1_TET_KERNEL=elementwise) against the
+FP64 oracle, FP64 and FP32, with and without the mass term; tiles straddle no
+class boundary, so meshes with many classes and partially filled tiles are used."""
 import contextlib
 import os
 
@@ -50,10 +51,10 @@ def _form(gpu, fes, kappa, mu, kernel):
 
 @pytest.mark.parametrize("kernel", [None, "elementwise"])
 @pytest.mark.parametrize("mass", [False, True])
-@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
 def test_tet_apply_parity(gpu, p, mass, kernel):
-    if kernel == "elementwise" and mass and p >= 4:
-        pytest.skip("the element-wise kernel supports mass rules up to 128 points (p=4 uses 216)")
+    if kernel == "elementwise" and (p >= 5 or (mass and p >= 4)):
+        pytest.skip("the element-wise kernel supports rules up to 128 points (p=4 mass: 216, p=5: 216, p=6: 343)")
     m = _mesh(3, 21 + p)
     kappa = lognormal(m.ne, 1.0, 5)
     mu = lognormal(m.ne, 0.5, 6) if mass else None
