@@ -125,6 +125,18 @@ int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** pr
 int gh1_pre_apply(gh1_pre* pre, double s, const void* x, void* y, int precision, int accumulate);
 int gh1_pre_free(gh1_pre* pre);
 
+/* ---- projector ----------------------------------------------------------------
+ * Projector(mask, range) (linalg/diagonalmatrix.cpp:13-110; the reference's GPU
+ * DevProjector, ngscuda/linalg_kernels.cu:304-376): keeps the entries whose mask
+ * byte is nonzero (range = 1) or zero (range = 0) and zeroes the others.
+ * mask: one byte per entry (the gh1_space_get_freedofs layout), host or device.
+ * apply: y = s*P*x (accumulate = 0) or y += s*P*x; project: x = P*x in place.  */
+typedef struct gh1_proj gh1_proj;
+int gh1_projector_create(gh1_ctx* ctx, int64_t n, const uint8_t* mask, int range, int mem, gh1_proj** proj);
+int gh1_projector_apply(gh1_proj* proj, double s, const void* x, void* y, int precision, int accumulate);
+int gh1_projector_project(gh1_proj* proj, void* x, int precision);
+int gh1_projector_free(gh1_proj* proj);
+
 /* ---- right-hand side ------------------------------------------------------
  * LinearForm(f*v*dx) with f piecewise constant per element, integration
  * order 2p (fem/symbolicintegrator.cpp:1109).  b: device double[ndof].    */

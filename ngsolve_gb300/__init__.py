@@ -7,11 +7,11 @@ from . import _lib
 from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMesh
 from .comp import (Mesh, H1, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
                    BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, JacobiPrecond, Preconditioner,
-                   Integrate_grad_dot, ShapeEval, context)
+                   Projector, Integrate_grad_dot, ShapeEval, context)
 from . import solvers
 from .adjoint import AdjointProblem, AdjointJ
 
 __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "BilinearForm",
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
-           "SparseMatrix", "BilinearFormApplication", "JacobiPrecond", "Preconditioner", "Integrate_grad_dot",
+           "SparseMatrix", "BilinearFormApplication", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
            "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ"]

@@ -76,6 +76,10 @@ SIGNATURES = {
     "gh1_batch_solve": [_P, _P, _P, ctypes.POINTER(CGOpts), _P],
     "gh1_batch_free": [_P],
     "gh1_shape_eval_noalloc": [_P, _I, _I, _P, _I, _P, _P, _P],
+    "gh1_projector_create": [_P, _L, _P, _I, _I, _PP],
+    "gh1_projector_apply": [_P, _D, _P, _P, _I, _I],
+    "gh1_projector_project": [_P, _P, _I],
+    "gh1_projector_free": [_P],
 }
 
 _lib = None

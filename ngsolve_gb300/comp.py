@@ -509,6 +509,43 @@ class JacobiPrecond(BaseMatrix):
             pass
 
 
+class Projector(BaseMatrix):
+    """Projector(mask, range) (linalg/diagonalmatrix.cpp:13-110): keeps the entries
+    whose mask bit equals `range` and zeroes the others; .Project(vec) in place."""
+
+    def __init__(self, mask, range=True, device=0):
+        ctx = context(device)
+        m = np.ascontiguousarray(np.asarray(mask, dtype=bool).astype(np.uint8))
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_projector_create(ctx.h, len(m), _np_ptr(m), 1 if range else 0, _lib.GH1_MEM_HOST,
+                                               ctypes.byref(h)))
+        self.ctx, self.h, self.height, self.width, self.fes = ctx, h, len(m), len(m), None
+        self.range = bool(range)
+
+    def _apply(self, s, x, y, acc):
+        x, y = _as_vec(x), _as_vec(y)
+        if x.t.dtype != y.t.dtype or x.t.numel() != self.height or y.t.numel() != self.height:
+            raise ValueError("vectors must match the projector in size and precision")
+        prec = _lib.GH1_F64 if x.t.dtype == torch.float64 else _lib.GH1_F32
+        self.ctx.sync_stream()
+        self.ctx.check(self.ctx.lib.gh1_projector_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
+
+    def Project(self, vec):
+        v = _as_vec(vec)
+        if v.t.numel() != self.height:
+            raise ValueError("vector size does not match the projector")
+        prec = _lib.GH1_F64 if v.t.dtype == torch.float64 else _lib.GH1_F32
+        self.ctx.sync_stream()
+        self.ctx.check(self.ctx.lib.gh1_projector_project(self.h, _ptr(v.t), prec))
+        return vec
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_projector_free(self.h)
+        except Exception:
+            pass
+
+
 def Preconditioner(a, kind="local"):
     """Preconditioner(a, "local") = Jacobi on the free DOFs (comp/preconditioner.cpp:684-760)."""
     if kind not in ("local", "jacobi"):
