@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
     ap.add_argument("--c2-orders", default="2,3,4", help="orders of the C2 record (comma separated)")
@@ -380,6 +380,49 @@ def workload_c2(args):
     return out
 
 
+def workload_sweep(args):
+    """Hex apply across orders p = 1..8 on structured meshes of ~17 M DOFs (the
+    64^3 p=4 size), kappa lognormal(0, 0.5): FP32 (autotuned variant) and FP64
+    GDOF/s, and the general-metric FP32 variant beside the affine one."""
+    import torch
+    import ngsolve_gb300 as ng
+    out = {"workload": "hex apply sweep p=1..8, ~17 M DOFs each", "orders": {}}
+    for p in range(1, 9):
+        nx = max(2, int(round((16.97e6) ** (1 / 3) / p)))
+        mesh = ng.MakeStructured3DMesh(hexes=True, nx=nx)
+        kappa = np.exp(np.random.default_rng(SEED_KAPPA).normal(0, 0.5, mesh.ne))
+        fes = ng.H1(mesh, order=p, dirichlet=".*")
+        u, v = fes.TnT()
+        rec = {"nx": nx, "ndof": fes.ndof}
+        for tag, env in (("fp32", None), ("fp32_general", "0")):
+            if env is not None:
+                os.environ["GH1_HEX_AFFINE"] = env
+            a = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+            a += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+            a.Assemble()
+            os.environ.pop("GH1_HEX_AFFINE", None)
+            N = fes.ndof
+            for prec, dt in (("32", torch.float32), ("64", torch.float64)):
+                if tag == "fp32_general" and prec == "64":
+                    continue
+                x = ng.BaseVector(data=torch.rand(N, dtype=dt, device="cuda"))
+                y = ng.BaseVector(data=torch.zeros(N, dtype=dt, device="cuda"))
+                for _ in range(3):
+                    a.mat.Mult(x, y)
+                reps = 20 if prec == "32" else 5
+                t, _ = _timed(lambda: a.mat.Mult(x, y), reps=reps)
+                key = tag if prec == "32" else "fp64"
+                rec[key + "_ms"] = t * 1e3
+                rec[key + "_gdofs"] = N / t / 1e9
+            info = a.mat.Info()
+            rec[tag + "_variant"] = info["hex_variant_fp32"]
+            rec["fp64_variant"] = info["hex_variant_fp64"]
+            del a
+            torch.cuda.empty_cache()
+        out["orders"][p] = rec
+    return out
+
+
 def workload_c4(args):
     """32^3 hex, p=3, kappa lognormal(0,1) (seed 6), kappa* (seed 7): dJ/dkappa by
     the adjoint kernel vs sixth-order central finite differences (h = 1e-2 kappa_e)
@@ -512,7 +555,8 @@ def main():
     dev = local
     torch.cuda.set_device(dev)
     if args.workload != "c3":
-        fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4, "c5": workload_c5}[args.workload]
+        fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4, "c5": workload_c5,
+              "sweep": workload_sweep}[args.workload]
         rec = fn(args)
         if rank == 0:
             print(json.dumps({"record": args.workload, **rec}), flush=True)
