@@ -129,15 +129,28 @@ __global__ void tet_geom_kernel(int ne, const double* __restrict__ X, const int*
 // table operand straight from the constant bank (no shared-memory load per FMA).
 __constant__ float c_B32[TAB_TOTAL], c_D32[TAB_TOTAL];
 __constant__ double c_B64[TAB_TOTAL], c_D64[TAB_TOTAL];
+// Even-odd (reflection) form of the 1D contractions.  The Gauss points are
+// symmetric about 1/2, psi_0 and psi_1 swap under x -> 1-x and psi_c picks up
+// (-1)^c for c >= 2, so with q' = N-1-q:
+//   B[q'][0] = B[q][1], B[q'][1] = B[q][0], B[q'][c] = (-1)^c B[q][c];
+//   D[q'][0] = -D[q][1], D[q'][1] = -D[q][0], D[q'][c] = -(-1)^c D[q][c].
+// A contraction then splits into an even part (inputs u0+u1 and the even c) and
+// an odd part (u0-u1 and the odd c) evaluated for q < N/2 only, ~25 % fewer FMAs.
+// c_EO*[0..3][W(N) + q] hold (B[q][0] +- B[q][1]) / 2 and (D[q][0] +- D[q][1]) / 2.
+__constant__ float c_EO32[4][64];
+__constant__ double c_EO64[4][64];
 template <class T> struct CTab;
 template <> struct CTab<float> {
   static __device__ __forceinline__ float B(int i) { return c_B32[i]; }
   static __device__ __forceinline__ float D(int i) { return c_D32[i]; }
+  static __device__ __forceinline__ float EO(int k, int i) { return c_EO32[k][i]; }
 };
 template <> struct CTab<double> {
   static __device__ __forceinline__ double B(int i) { return c_B64[i]; }
   static __device__ __forceinline__ double D(int i) { return c_D64[i]; }
+  static __device__ __forceinline__ double EO(int k, int i) { return c_EO64[k][i]; }
 };
+constexpr int eo_off(int N) { return N * (N - 1) / 2 - 1; }
 
 void upload_const_tables(gh1_space* sp) {
   const int N = sp->p + 1, off = tab_off(N);
@@ -146,6 +159,111 @@ void upload_const_tables(gh1_space* sp) {
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_D32, sp->d_D32.p, N * N * sizeof(float), off * sizeof(float), cudaMemcpyDeviceToDevice, s));
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_B64, sp->d_B64.p, N * N * sizeof(double), off * sizeof(double), cudaMemcpyDeviceToDevice, s));
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_D64, sp->d_D64.p, N * N * sizeof(double), off * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // even-odd coefficients, after checking the reflection symmetry they rely on
+  std::vector<double> B(N * N), D(N * N);
+  GH1_CUDA(cudaMemcpyAsync(B.data(), sp->d_B64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaMemcpyAsync(D.data(), sp->d_D64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  double scale = 0, dev = 0;
+  for (int q = 0; q < N; q++)
+    for (int c = 0; c < N; c++) {
+      const int qr = N - 1 - q, cr = c < 2 ? 1 - c : c;
+      const double sg = c < 2 ? 1.0 : ((c % 2) ? -1.0 : 1.0);
+      scale = std::max(scale, std::max(std::fabs(B[q * N + c]), std::fabs(D[q * N + c])));
+      dev = std::max(dev, std::fabs(B[qr * N + c] - sg * B[q * N + cr]));
+      dev = std::max(dev, std::fabs(D[qr * N + c] + sg * D[q * N + cr]));
+    }
+  GH1_CHECK(dev <= 1e-12 * scale, GH1_ERR_ARG, "internal: 1D hex tables lack the reflection symmetry");
+  double eo[4][16] = {};
+  float eo32[4][16] = {};
+  for (int q = 0; q < N; q++) {
+    eo[0][q] = 0.5 * (B[q * N] + B[q * N + 1]);
+    eo[1][q] = 0.5 * (B[q * N] - B[q * N + 1]);
+    eo[2][q] = 0.5 * (D[q * N] + D[q * N + 1]);
+    eo[3][q] = 0.5 * (D[q * N] - D[q * N + 1]);
+    for (int k = 0; k < 4; k++) eo32[k][q] = (float)eo[k][q];
+  }
+  for (int k = 0; k < 4; k++) {
+    GH1_CUDA(cudaMemcpyToSymbol(c_EO64, eo[k], N * sizeof(double), (k * 64 + eo_off(N)) * sizeof(double)));
+    GH1_CUDA(cudaMemcpyToSymbol(c_EO32, eo32[k], N * sizeof(float), (k * 64 + eo_off(N)) * sizeof(float)));
+  }
+}
+
+// out_b[q] = sum_c B[q][c] u[c] and out_d[q] = sum_c D[q][c] u[c] (either may be
+// skipped): the forward contraction in even-odd form
+template <int N, class T, bool WB, bool WD>
+__device__ __forceinline__ void eo_fwd(const T* u, T* ob, T* od) {
+  constexpr int O = tab_off(N), W = eo_off(N), M = N / 2;
+  using TB = CTab<T>;
+  const T s = u[0] + u[1], d = u[0] - u[1];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    T eb = 0, obb = 0, ed = 0, odd = 0;
+    if (WB) { eb = TB::EO(0, W + q) * s; obb = TB::EO(1, W + q) * d; }
+    if (WD) { ed = TB::EO(2, W + q) * s; odd = TB::EO(3, W + q) * d; }
+#pragma unroll
+    for (int c = 2; c < N; c++) {
+      if (c % 2 == 0) {
+        if (WB) eb += TB::B(O + q * N + c) * u[c];
+        if (WD) ed += TB::D(O + q * N + c) * u[c];
+      } else {
+        if (WB) obb += TB::B(O + q * N + c) * u[c];
+        if (WD) odd += TB::D(O + q * N + c) * u[c];
+      }
+    }
+    if (WB) { ob[q] = eb + obb; ob[N - 1 - q] = eb - obb; }
+    if (WD) { od[q] = ed + odd; od[N - 1 - q] = odd - ed; }
+  }
+  if (N % 2 == 1) {  // middle point: B keeps its even part, D its odd part
+    constexpr int q = M;
+    T eb = 0, odd = 0;
+    if (WB) eb = TB::EO(0, W + q) * s;
+    if (WD) odd = TB::EO(3, W + q) * d;
+#pragma unroll
+    for (int c = 2; c < N; c++) {
+      if (c % 2 == 0) { if (WB) eb += TB::B(O + q * N + c) * u[c]; }
+      else { if (WD) odd += TB::D(O + q * N + c) * u[c]; }
+    }
+    if (WB) ob[q] = eb;
+    if (WD) od[q] = odd;
+  }
+}
+
+// out[a] (+)= sum_q B[q][a] v[q] (WANT_D = false) or sum_q D[q][a] v[q]: the
+// transposed contraction in even-odd form; ACC adds into out
+template <int N, class T, bool WANT_D, bool ACC>
+__device__ __forceinline__ void eo_bwd(const T* v, T* out) {
+  constexpr int O = tab_off(N), W = eo_off(N), M = N / 2;
+  using TB = CTab<T>;
+  T vs[M > 0 ? M : 1], vd[M > 0 ? M : 1];
+#pragma unroll
+  for (int k = 0; k < M; k++) { vs[k] = v[k] + v[N - 1 - k]; vd[k] = v[k] - v[N - 1 - k]; }
+  // a = 0, 1
+  T P = 0, Q = 0;
+#pragma unroll
+  for (int k = 0; k < M; k++) {
+    if (!WANT_D) { P += TB::EO(0, W + k) * vs[k]; Q += TB::EO(1, W + k) * vd[k]; }
+    else { P += TB::EO(2, W + k) * vd[k]; Q += TB::EO(3, W + k) * vs[k]; }
+  }
+  if (N % 2 == 1) {
+    if (!WANT_D) P += TB::B(O + M * N) * v[M];
+    else Q += TB::D(O + M * N) * v[M];
+  }
+  T r[N];
+  r[0] = P + Q;
+  r[1] = P - Q;
+#pragma unroll
+  for (int a = 2; a < N; a++) {
+    // B: even a uses vs (+ the middle point), odd a uses vd; D: the reverse
+    const bool sym = WANT_D ? (a % 2 == 1) : (a % 2 == 0);
+    T t = 0;
+#pragma unroll
+    for (int k = 0; k < M; k++) t += (WANT_D ? TB::D(O + k * N + a) : TB::B(O + k * N + a)) * (sym ? vs[k] : vd[k]);
+    if (N % 2 == 1 && sym) t += (WANT_D ? TB::D(O + M * N + a) : TB::B(O + M * N + a)) * v[M];
+    r[a] = t;
+  }
+#pragma unroll
+  for (int a = 0; a < N; a++) out[a] = ACC ? out[a] + r[a] : r[a];
 }
 
 // shared memory of the pipelined apply, per element group:
@@ -172,41 +290,34 @@ struct HexSmem {
 template <int N, class T, bool WANT_U>
 __device__ __forceinline__ void hex_forward(int pl, bool active, int gid, T* su, T* s1, T* s2, T* t2, T* t3, T* gx, T* gy,
                                             T* gz, T* uq) {
-  constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
+  constexpr int G = HexCfg<N>::G;
   using TB = CTab<T>;
   T* t1 = su;  // alias: u is consumed by stage 1 before t1 is written
   if (active) {
     const int a = pl / N, b = pl % N;
-    T u[N];
+    T u[N], ub[N], ud[N];
 #pragma unroll
     for (int c = 0; c < N; c++) u[c] = su[(a * N + b) * N + c];
+    eo_fwd<N, T, true, true>(u, ub, ud);
 #pragma unroll
     for (int k = 0; k < N; k++) {
-      T ub = 0, ud = 0;
-#pragma unroll
-      for (int c = 0; c < N; c++) { ub += TB::B(O + k * N + c) * u[c]; ud += TB::D(O + k * N + c) * u[c]; }
-      s1[(a * N + b) * N + k] = ub;
-      s2[(a * N + b) * N + k] = ud;
+      s1[(a * N + b) * N + k] = ub[k];
+      s2[(a * N + b) * N + k] = ud[k];
     }
   }
   group_sync<G>(gid);
   if (active) {
     const int a = pl / N, k = pl % N;
-    T v1[N], v2[N];
+    T v1[N], v2[N], bb[N], db[N], bd[N];
 #pragma unroll
     for (int b = 0; b < N; b++) { v1[b] = s1[(a * N + b) * N + k]; v2[b] = s2[(a * N + b) * N + k]; }
+    eo_fwd<N, T, true, true>(v1, bb, db);
+    eo_fwd<N, T, true, false>(v2, bd, nullptr);
 #pragma unroll
     for (int j = 0; j < N; j++) {
-      T bb = 0, db = 0, bd = 0;
-#pragma unroll
-      for (int b = 0; b < N; b++) {
-        bb += TB::B(O + j * N + b) * v1[b];
-        db += TB::D(O + j * N + b) * v1[b];
-        bd += TB::B(O + j * N + b) * v2[b];
-      }
-      t1[(a * N + j) * N + k] = bb;
-      t2[(a * N + j) * N + k] = db;
-      t3[(a * N + j) * N + k] = bd;
+      t1[(a * N + j) * N + k] = bb[j];
+      t2[(a * N + j) * N + k] = db[j];
+      t3[(a * N + j) * N + k] = bd[j];
     }
   }
   group_sync<G>(gid);
@@ -219,19 +330,9 @@ __device__ __forceinline__ void hex_forward(int pl, bool active, int gid, T* su,
       w2[a] = t2[(a * N + j) * N + k];
       w3[a] = t3[(a * N + j) * N + k];
     }
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-      T x = 0, y = 0, z = 0, uu = 0;
-#pragma unroll
-      for (int a = 0; a < N; a++) {
-        x += TB::D(O + i * N + a) * w1[a];
-        y += TB::B(O + i * N + a) * w2[a];
-        z += TB::B(O + i * N + a) * w3[a];
-        if (WANT_U) uu += TB::B(O + i * N + a) * w1[a];
-      }
-      gx[i] = x; gy[i] = y; gz[i] = z;
-      if (WANT_U) uq[i] = uu;
-    }
+    eo_fwd<N, T, WANT_U, true>(w1, uq, gx);
+    eo_fwd<N, T, true, false>(w2, gy, nullptr);
+    eo_fwd<N, T, true, false>(w3, gz, nullptr);
   }
   group_sync<G>(gid);
 }
@@ -241,24 +342,21 @@ __device__ __forceinline__ void hex_forward(int pl, bool active, int gid, T* su,
 template <int N, class T, bool WANT_M>
 __device__ __forceinline__ void hex_backward(int pl, bool active, int gid, T* su, T* s1, T* s2, T* t2, T* t3,
                                              const T* vx, const T* vy, const T* vz, const T* vm) {
-  constexpr int N2 = N * N, G = HexCfg<N>::G, O = tab_off(N);
+  constexpr int G = HexCfg<N>::G;
   using TB = CTab<T>;
   T* t1 = su;
   if (active) {
     const int j = pl / N, k = pl % N;
+    T w1[N], w2[N], w3[N];
+    eo_bwd<N, T, true, false>(vx, w1);
+    if (WANT_M) eo_bwd<N, T, false, true>(vm, w1);
+    eo_bwd<N, T, false, false>(vy, w2);
+    eo_bwd<N, T, false, false>(vz, w3);
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      T w1 = 0, w2 = 0, w3 = 0;
-#pragma unroll
-      for (int i = 0; i < N; i++) {
-        w1 += TB::D(O + i * N + a) * vx[i];
-        if (WANT_M) w1 += TB::B(O + i * N + a) * vm[i];
-        w2 += TB::B(O + i * N + a) * vy[i];
-        w3 += TB::B(O + i * N + a) * vz[i];
-      }
-      t1[(a * N + j) * N + k] = w1;
-      t2[(a * N + j) * N + k] = w2;
-      t3[(a * N + j) * N + k] = w3;
+      t1[(a * N + j) * N + k] = w1[a];
+      t2[(a * N + j) * N + k] = w2[a];
+      t3[(a * N + j) * N + k] = w3[a];
     }
   }
   group_sync<G>(gid);
@@ -271,16 +369,14 @@ __device__ __forceinline__ void hex_backward(int pl, bool active, int gid, T* su
       r2[j] = t2[(a * N + j) * N + k];
       r3[j] = t3[(a * N + j) * N + k];
     }
+    T v1[N], v2[N];
+    eo_bwd<N, T, false, false>(r1, v1);
+    eo_bwd<N, T, true, true>(r2, v1);
+    eo_bwd<N, T, false, false>(r3, v2);
 #pragma unroll
     for (int b = 0; b < N; b++) {
-      T v1 = 0, v2 = 0;
-#pragma unroll
-      for (int j = 0; j < N; j++) {
-        v1 += TB::B(O + j * N + b) * r1[j] + TB::D(O + j * N + b) * r2[j];
-        v2 += TB::B(O + j * N + b) * r3[j];
-      }
-      s1[(a * N + b) * N + k] = v1;
-      s2[(a * N + b) * N + k] = v2;
+      s1[(a * N + b) * N + k] = v1[b];
+      s2[(a * N + b) * N + k] = v2[b];
     }
   }
   group_sync<G>(gid);
@@ -289,13 +385,11 @@ __device__ __forceinline__ void hex_backward(int pl, bool active, int gid, T* su
     T r1[N], r2[N];
 #pragma unroll
     for (int k = 0; k < N; k++) { r1[k] = s1[(a * N + b) * N + k]; r2[k] = s2[(a * N + b) * N + k]; }
+    T v[N];
+    eo_bwd<N, T, false, false>(r1, v);
+    eo_bwd<N, T, true, true>(r2, v);
 #pragma unroll
-    for (int c = 0; c < N; c++) {
-      T v = 0;
-#pragma unroll
-      for (int k = 0; k < N; k++) v += TB::B(O + k * N + c) * r1[k] + TB::D(O + k * N + c) * r2[k];
-      su[(a * N + b) * N + c] = v;
-    }
+    for (int c = 0; c < N; c++) su[(a * N + b) * N + c] = v[c];
   }
   group_sync<G>(gid);
 }
@@ -433,12 +527,12 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
         vx[i] = gxx * gx[i] + gxy * gy[i] + gxz * gz[i];
         vy[i] = gxy * gx[i] + gyy * gy[i] + gyz * gz[i];
         vz[i] = gxz * gx[i] + gyz * gy[i] + gzz * gz[i];
-        T en = gx[i] * vx[i] + gy[i] * vy[i] + gz[i] * vz[i];
-        if (MASS) {
-          vm[i] = (GM == 0 ? Gsrc[6 * N3 + o] : __ldcs(Gsrc + 6 * N3 + o)) * uq[i];
-          en += uq[i] * vm[i];
+        if (MASS) vm[i] = (GM == 0 ? Gsrc[6 * N3 + o] : __ldcs(Gsrc + 6 * N3 + o)) * uq[i];
+        if (partial) {  // x^T A x only when the caller asks for it (CG)
+          T en = gx[i] * vx[i] + gy[i] * vy[i] + gz[i] * vz[i];
+          if (MASS) en += uq[i] * vm[i];
+          acc += en;
         }
-        acc += en;
       }
     }
     if (GM == 0) {
