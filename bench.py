@@ -627,7 +627,7 @@ def main():
 
     # general-geometry apply (per-point metric), when the headline used the affine variant
     general = None
-    if variant == 4:
+    if variant in (4, 5):
         os.environ["GH1_HEX_AFFINE"] = "0"
         ag = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
         ag += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
@@ -755,19 +755,22 @@ def main():
     achieved = B32 / t_step / 1e9 * 1.0 if ws == 1 else B32 / t_step / 1e9
     nn = args.order + 1
     kernel = ("hex_apply_kernel<%d, float, 0, %d>" % (nn, variant) if variant in (0, 1) else
+              "hex_apply_slice_kernel<%d, 0>" % nn if variant == 5 else
               "hex_apply_pair_kernel<%d, 0, %d>" % (nn, variant - 2))
     traffic = None
     if args.order == ORDER and args.nx == NX:  # the committed profiles cover the benchmark configuration
         traffic = load_traffic({0: "hex_apply_fp32_c3.md", 1: "hex_apply_fp32_c3.md", 2: "hex_apply_pair_fp32_c3.md",
-                                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md"}[variant])
+                                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md",
+                                5: "hex_apply_slice_affine_fp32_c3.md"}[variant])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": B32, "kernel": kernel, "variant": variant}
-    if variant == 4:
+    if variant in (4, 5):
         # every element map is affine: the kernel reads one 32-byte metric record per
         # element instead of q^3 x 6 values; achieved keeps the per-point byte model
         B_aff = 2 * N * 4 + ne * 32
-        roofline["note"] = ("variant 4 reads one metric per element (affine mesh); achieved/frac use the per-point "
+        roofline["note"] = ("variant %d reads one metric per element (affine mesh); achieved/frac use the per-point "
+                            % variant +
                             "byte model, achieved_affine_model the bytes this variant's model moves")
         roofline["achieved_affine_model"] = B_aff / t_step / 1e9
     B64, _ = model_bytes_flops(ne, N, args.order, 8, 8)

@@ -167,8 +167,10 @@ struct gh1_op {
   int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
   int hex_gmode[2] = {0, 0};                 // autotuned hex apply variant per precision: 0/1 = G tile by TMA /
                                              // direct loads; FP32 also 2/3 = the same with two elements per lane,
-                                             // 4 = two elements per lane with per-element (affine) metrics
+                                             // 4 = two elements per lane with per-element (affine) metrics,
+                                             // 5 = slice / pencil form of 4 (hexpair.cu)
   int pair_per_sm[3] = {0, 0, 0};            // resident blocks per SM of the paired FP32 apply [G mode]
+  int slice_per_sm = 0;                      // ... of the slice-form FP32 apply (0: not available)
   bool all_affine = false;                   // hex: every element map affine (G mode 2 available)
   gh1::DBuf<float> d_Ga32;                   // hex, all affine: per-element metric records [ne][8]
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
@@ -239,6 +241,11 @@ int hex_multi_pair_launch(gh1_op* op, int R, const int* phase, int want, const f
                           unsigned int* counter, double* energy, bool prepare_only);
 void hex_pair_apply(gh1_op* op, int gmode, const float* x, float* y, double* partial, unsigned int* counter,
                     double* energy, const int* skip);
+// slice / pencil form of the paired apply for all-affine meshes (hexpair.cu)
+bool hex_slice_supported(int N);
+void hex_slice_setup(gh1_op* op);
+void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                     const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
 void spmv_skip(gh1_op* op, const void* x, void* y, int prec, const int* skip);  // spmv.cu
 void csr_diag(gh1_op* op, double* diag);                            // spmv.cu

@@ -680,8 +680,267 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
   }
 }
 
+// ---- slice / pencil form (affine meshes) ------------------------------------------
+// Same operator as hex_apply_pair_kernel in G mode 2, with a different split of
+// the contractions between the threads of a warp.  A warp owns P = 32/N element
+// pairs (two elements per lane, packed as above).  Lane (t, p) = (lane / P, lane % P):
+//   slice phase:  t = a (x index).  The lane holds the N x N slice u[a][.][.]
+//                 of both elements in registers and contracts it along z and
+//                 then y there (stages 1 and 2), writing only the three stage-2
+//                 results bb, db, bd at (a, j, k) to shared memory;
+//   pencil phase: t = j.  For each k the lane reads the N values along a of the
+//                 three arrays, forms the gradient at the N points (i, j, k),
+//                 applies the metric, contracts back along a and writes the
+//                 results in place (the same words it read);
+//   slice phase again: the lane reads its slice of the three arrays and
+//                 contracts back along y and z in registers.
+// The contractions move 3 N^3 words per element pair through shared memory each
+// way (the pencil-per-lane form moves 5 N^3), all at the two-wavefront minimum
+// of an 8-byte warp access: the exchange array X[array][k][j][a][p] has unit
+// stride in p and stride P in a, so the slice phase touches consecutive words,
+// and the j stride SJ = P (mod 16), so the pencil phase does too modulo 16.
+// The x gather and the scatter run in DOF order (consecutive lanes on
+// consecutive local DOFs of one element: coalesced index and x loads, atomics
+// that share sectors) through the array su[p][a][m] (m = b N + c), whose a
+// stride SUA = P and pair stride SPU = 1 (mod 16) keep the slice reads and
+// writes at the minimum as well.  su aliases X.  All exchanges stay inside one
+// warp (__syncwarp; no block barriers and no waits).
+template <int N>
+struct SliceCfg {
+  static constexpr int P = 32 / N;                                      // element pairs per warp
+  static constexpr int NP = N * P;                                      // active lanes
+  static constexpr int N2 = N * N, N3 = N * N * N;
+  static constexpr int SJ = NP + ((P - NP) % 16 + 16) % 16;             // >= NP, == P (mod 16)
+  static constexpr int PL = (N - 1) * SJ + NP;                          // words per (array, k) plane
+  static constexpr int XW = 3 * N * PL;                                 // exchange words per warp
+  static constexpr int SUA = N2 + ((P - N2) % 16 + 16) % 16;            // >= N^2, == P (mod 16)
+  static constexpr int SPU0 = (N - 1) * SUA + N2;
+  static constexpr int SPU = SPU0 + ((1 - SPU0) % 16 + 16) % 16;        // >= SPU0, == 1 (mod 16)
+  static constexpr int W = XW > P * SPU ? XW : P * SPU;                 // words per warp
+  static constexpr int NT = P * N3, NI = (NT + 31) / 32;                // DOF-order items per warp / lane
+  static constexpr int WARPS = 2, BLOCK = 32 * WARPS;
+  static constexpr size_t smem = (size_t)WARPS * W * sizeof(f2);
+};
+// resident 64-thread blocks per SM the register allocation must allow (shared
+// memory allows 5 blocks at N = 5, more below)
+constexpr int slice_min_blocks(int N) { return N <= 3 ? 8 : N == 4 ? 6 : 5; }
+
+template <int N, bool MASS>
+__global__ void __launch_bounds__(SliceCfg<N>::BLOCK, slice_min_blocks(N))
+hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const float* __restrict__ Ga,
+                       const float* __restrict__ x, float* __restrict__ y, int first_cell, double* partial,
+                       unsigned int* counter, double* energy, const int* skip) {
+  using C = SliceCfg<N>;
+  constexpr int P = C::P, NP = C::NP, SJ = C::SJ, PL = C::PL, N2 = C::N2, N3 = C::N3, O = tab_off(N);
+  constexpr int AR = N * PL;                // words per exchange array
+  constexpr int SUA = C::SUA, SPU = C::SPU, NT = C::NT, NI = C::NI;
+  constexpr int WO = N * (N - 1) / 2 - 1;   // offset of this order's Gauss weights
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(16) unsigned char slice_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  f2* X = (f2*)slice_raw + (size_t)warp * C::W;
+  f2* su = X;                               // gather / scatter staging, aliases X
+  const bool act = lane < NP;
+  const int t = act ? lane / P : 0, p = lane % P;
+  const int ps = t * SJ + p;                // pencil-phase word offset of this lane (j = t)
+  const int ss = p * SPU + t * SUA;         // slice-phase su offset of this lane (a = t)
+  const int nch = (ne + 2 * P - 1) / (2 * P);
+  f2 acc = 0;
+  for (int ch = blockIdx.x * C::WARPS + warp; ch < nch; ch += gridDim.x * C::WARPS) {
+    const int eb = ch * 2 * P, nrow = min(2 * P, ne - eb);
+    const int e0 = eb + 2 * p;
+    const bool v0 = act && e0 < ne, v1 = act && e0 + 1 < ne;
+    __syncwarp();  // the previous chunk's readers of su are done
+    // gather in DOF order: item q = (pair, local DOF l), both elements of the pair
+#pragma unroll 8
+    for (int j = 0; j < NI; j++) {
+      const int q = lane + 32 * j;
+      if (q < NT) {
+        const int pp = q / N3, l = q % N3;
+        float a0 = 0.f, a1 = 0.f;
+        if (2 * pp < nrow) {
+          const int d = __ldg(tdof + (size_t)(eb + 2 * pp) * tstride + l);
+          a0 = __int_as_float(__float_as_int(__ldg(x + (d & 0x7fffffff))) ^ (d & (int)0x80000000));
+        }
+        if (2 * pp + 1 < nrow) {
+          const int d = __ldg(tdof + (size_t)(eb + 2 * pp + 1) * tstride + l);
+          a1 = __int_as_float(__float_as_int(__ldg(x + (d & 0x7fffffff))) ^ (d & (int)0x80000000));
+        }
+        su[pp * SPU + (l / N2) * SUA + l % N2] = pack2(a0, a1);
+      }
+    }
+    __syncwarp();
+    f2 u[N2];
+#pragma unroll
+    for (int m = 0; m < N2; m++) u[m] = act ? su[ss + m] : (f2)0;
+    __syncwarp();  // su is overwritten by X below
+    // stages 1 (along z: c -> k) and 2 (along y: b -> j), one k at a time
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      f2 ub[N], ud[N];
+#pragma unroll
+      for (int b = 0; b < N; b++) {
+        f2 sb = mul2(bcast(c_Bp[O + k * N]), u[b * N]), sd = mul2(bcast(c_Dp[O + k * N]), u[b * N]);
+#pragma unroll
+        for (int c = 1; c < N; c++) {
+          sb = fma2(bcast(c_Bp[O + k * N + c]), u[b * N + c], sb);
+          sd = fma2(bcast(c_Dp[O + k * N + c]), u[b * N + c], sd);
+        }
+        ub[b] = sb;
+        ud[b] = sd;
+      }
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        f2 bb = mul2(bcast(c_Bp[O + j * N]), ub[0]), db = mul2(bcast(c_Dp[O + j * N]), ub[0]),
+           bd = mul2(bcast(c_Bp[O + j * N]), ud[0]);
+#pragma unroll
+        for (int b = 1; b < N; b++) {
+          bb = fma2(bcast(c_Bp[O + j * N + b]), ub[b], bb);
+          db = fma2(bcast(c_Dp[O + j * N + b]), ub[b], db);
+          bd = fma2(bcast(c_Bp[O + j * N + b]), ud[b], bd);
+        }
+        if (act) {
+          f2* w = X + k * PL + j * SJ + lane;
+          w[0] = bb;
+          w[AR] = db;
+          w[2 * AR] = bd;
+        }
+      }
+    }
+    __syncwarp();
+    // pencil phase: lane (j = t, p), points (i, j, k)
+    if (act) {
+      const int r0 = v0 ? e0 : eb, r1 = v1 ? e0 + 1 : r0;  // a missing element reuses a valid metric
+      f2 ea[7];
+#pragma unroll
+      for (int c = 0; c < (MASS ? 7 : 6); c++) ea[c] = pack2(__ldg(Ga + (size_t)r0 * 8 + c), __ldg(Ga + (size_t)r1 * 8 + c));
+      const float wj = c_Wp[WO + t];
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        f2* w = X + k * PL + ps;
+        f2 w1[N], w2[N], w3[N];
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          w1[a] = w[a * P];
+          w2[a] = w[AR + a * P];
+          w3[a] = w[2 * AR + a * P];
+        }
+        const float wjk = wj * c_Wp[WO + k];
+        f2 vx[N], vy[N], vz[N], vm[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+          f2 gx = mul2(bcast(c_Dp[O + i * N]), w1[0]), gy = mul2(bcast(c_Bp[O + i * N]), w2[0]),
+             gz = mul2(bcast(c_Bp[O + i * N]), w3[0]);
+          f2 uq = 0;
+          if (MASS) uq = mul2(bcast(c_Bp[O + i * N]), w1[0]);
+#pragma unroll
+          for (int a = 1; a < N; a++) {
+            gx = fma2(bcast(c_Dp[O + i * N + a]), w1[a], gx);
+            gy = fma2(bcast(c_Bp[O + i * N + a]), w2[a], gy);
+            gz = fma2(bcast(c_Bp[O + i * N + a]), w3[a], gz);
+            if (MASS) uq = fma2(bcast(c_Bp[O + i * N + a]), w1[a], uq);
+          }
+          const f2 wq = bcast(c_Wp[WO + i] * wjk);
+          const f2 sx = mul2(wq, gx), sy = mul2(wq, gy), sz = mul2(wq, gz);
+          vx[i] = fma2(ea[4], sz, fma2(ea[3], sy, mul2(ea[0], sx)));
+          vy[i] = fma2(ea[5], sz, fma2(ea[1], sy, mul2(ea[3], sx)));
+          vz[i] = fma2(ea[2], sz, fma2(ea[5], sy, mul2(ea[4], sx)));
+          f2 en = fma2(gz, vz[i], fma2(gy, vy[i], mul2(gx, vx[i])));
+          if (MASS) {
+            vm[i] = mul2(mul2(wq, ea[6]), uq);
+            en = fma2(uq, vm[i], en);
+          }
+          acc = add2(acc, en);
+        }
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          f2 q1 = mul2(bcast(c_Dp[O + a]), vx[0]), q2 = mul2(bcast(c_Bp[O + a]), vy[0]),
+             q3 = mul2(bcast(c_Bp[O + a]), vz[0]);
+          if (MASS) q1 = fma2(bcast(c_Bp[O + a]), vm[0], q1);
+#pragma unroll
+          for (int i = 1; i < N; i++) {
+            q1 = fma2(bcast(c_Dp[O + i * N + a]), vx[i], q1);
+            if (MASS) q1 = fma2(bcast(c_Bp[O + i * N + a]), vm[i], q1);
+            q2 = fma2(bcast(c_Bp[O + i * N + a]), vy[i], q2);
+            q3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], q3);
+          }
+          w[a * P] = q1;
+          w[AR + a * P] = q2;
+          w[2 * AR + a * P] = q3;
+        }
+      }
+    }
+    __syncwarp();
+    // slice phase, transposed: stage 2 (j -> b) and stage 1 (k -> c) into the slice
+    f2 out[N2];
+#pragma unroll
+    for (int m = 0; m < N2; m++) out[m] = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      f2 r1[N], r2[N], r3[N];
+      const f2* w = X + k * PL + lane;
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        if (act) {
+          r1[j] = w[j * SJ];
+          r2[j] = w[AR + j * SJ];
+          r3[j] = w[2 * AR + j * SJ];
+        } else {
+          r1[j] = r2[j] = r3[j] = 0;
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < N; b++) {
+        f2 ub = mul2(bcast(c_Bp[O + b]), r1[0]), ud = mul2(bcast(c_Bp[O + b]), r3[0]);
+        ub = fma2(bcast(c_Dp[O + b]), r2[0], ub);
+#pragma unroll
+        for (int j = 1; j < N; j++) {
+          ub = fma2(bcast(c_Bp[O + j * N + b]), r1[j], ub);
+          ub = fma2(bcast(c_Dp[O + j * N + b]), r2[j], ub);
+          ud = fma2(bcast(c_Bp[O + j * N + b]), r3[j], ud);
+        }
+#pragma unroll
+        for (int c = 0; c < N; c++)
+          out[b * N + c] = fma2(bcast(c_Dp[O + k * N + c]), ud, fma2(bcast(c_Bp[O + k * N + c]), ub, out[b * N + c]));
+      }
+    }
+    __syncwarp();  // X is overwritten by su below
+    if (act) {
+#pragma unroll
+      for (int m = 0; m < N2; m++) su[ss + m] = out[m];
+    }
+    __syncwarp();
+    // scatter in DOF order (DOFs >= first_cell belong to one element: plain stores)
+#pragma unroll 8
+    for (int j = 0; j < NI; j++) {
+      const int q = lane + 32 * j;
+      if (q < NT) {
+        const int pp = q / N3, l = q % N3;
+        float o0, o1;
+        unpack2(su[pp * SPU + (l / N2) * SUA + l % N2], o0, o1);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          if (2 * pp + h < nrow) {
+            const int d = __ldg(tdof + (size_t)(eb + 2 * pp + h) * tstride + l);
+            const int dof = d & 0x7fffffff;
+            const float v = __int_as_float(__float_as_int(h ? o1 : o0) ^ (d & (int)0x80000000));
+            if (dof >= first_cell) y[dof] = v;
+            else atomicAdd(y + dof, v);
+          }
+        }
+      }
+    }
+  }
+  if (partial) {
+    float a0, a1;
+    unpack2(acc, a0, a1);
+    block_reduce_finish((double)a0 + (double)a1, partial, counter, energy);
+  }
+}
+
 // ---- host side ------------------------------------------------------------------
 bool hex_pair_supported(int N) { return N >= 2 && N <= 7; }
+bool hex_slice_supported(int N) { return N >= 2 && N <= 5; }
 
 void upload_pair_tables(gh1_space* sp) {
   const int N = sp->p + 1;
@@ -843,6 +1102,61 @@ void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partia
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)
 #undef GH1_PAIR_CASE
+}
+
+// slice-form apply (all-affine meshes): DOF table copy, occupancy, launch
+template <int N, bool MASS>
+static int slice_occupancy() {
+  using C = SliceCfg<N>;
+  auto kern = hex_apply_slice_kernel<N, MASS>;
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem));
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, C::BLOCK, C::smem));
+  return v;
+}
+
+// Occupancy of the slice-form apply when the mesh is all affine and the order is
+// supported (GH1_HEX_SLICE=0 turns the variant off); op->slice_per_sm = 0 otherwise.
+void hex_slice_setup(gh1_op* op) {
+  op->slice_per_sm = 0;
+  const int N = op->sp->p + 1;
+  const char* env = getenv("GH1_HEX_SLICE");
+  if (!op->all_affine || !hex_slice_supported(N) || (env && env[0] == '0')) return;
+  const bool m = op->has_mass;
+  int v = 0;
+  switch (N) {
+    case 2: v = m ? slice_occupancy<2, true>() : slice_occupancy<2, false>(); break;
+    case 3: v = m ? slice_occupancy<3, true>() : slice_occupancy<3, false>(); break;
+    case 4: v = m ? slice_occupancy<4, true>() : slice_occupancy<4, false>(); break;
+    case 5: v = m ? slice_occupancy<5, true>() : slice_occupancy<5, false>(); break;
+    default: break;
+  }
+  op->slice_per_sm = std::max(v, 0);
+}
+
+template <int N, bool MASS>
+static void slice_launch(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                         const int* skip) {
+  using C = SliceCfg<N>;
+  gh1_space* sp = op->sp;
+  GH1_CHECK(op->slice_per_sm > 0, GH1_ERR_ARG, "internal: slice hex apply not prepared");
+  const int ne = sp->mesh->ne, nch = (ne + 2 * C::P - 1) / (2 * C::P);
+  const int grid = std::max(1, std::min((nch + C::WARPS - 1) / C::WARPS, sp->ctx->nsm * op->slice_per_sm));
+  hex_apply_slice_kernel<N, MASS><<<grid, C::BLOCK, C::smem, sp->ctx->stream>>>(
+      ne, sp->d_tdof.p, sp->tstride, op->d_Ga32.p, x, y, (int)sp->first_cell, partial, counter, energy, skip);
+  check_kernel(sp->ctx, "hex_apply_slice_kernel");
+}
+
+void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                     const int* skip) {
+  const bool m = op->has_mass;
+  switch (op->sp->p + 1) {
+    case 2: m ? slice_launch<2, true>(op, x, y, partial, counter, energy, skip) : slice_launch<2, false>(op, x, y, partial, counter, energy, skip); break;
+    case 3: m ? slice_launch<3, true>(op, x, y, partial, counter, energy, skip) : slice_launch<3, false>(op, x, y, partial, counter, energy, skip); break;
+    case 4: m ? slice_launch<4, true>(op, x, y, partial, counter, energy, skip) : slice_launch<4, false>(op, x, y, partial, counter, energy, skip); break;
+    case 5: m ? slice_launch<5, true>(op, x, y, partial, counter, energy, skip) : slice_launch<5, false>(op, x, y, partial, counter, energy, skip); break;
+    default: throw Error(GH1_ERR_UNSUPPORTED, "slice hex apply: order out of range");
+  }
 }
 
 // paired multi-rhs apply: occupancy (prepare_only, outside stream capture) and launch

@@ -1004,6 +1004,10 @@ void hex_apply_dispatch(gh1_op* op, const T* x, T* y, const T* G, int gstride, d
   const int pi = std::is_same<T, float>::value ? 1 : 0;
   const int gm = op->hex_gmode[pi];
   if constexpr (std::is_same<T, float>::value) {
+    if (gm == 5) {
+      hex_slice_apply(op, x, y, partial, counter, energy, skip);
+      return;
+    }
     if (gm >= 2) {
       hex_pair_apply(op, gm - 2, x, y, partial, counter, energy, skip);
       return;
@@ -1032,15 +1036,16 @@ int hex_occupancy_dispatch(gh1_op* op, int gstride) {
 // direct coalesced loads, and for FP32 each of those with two elements per lane
 // -- on this operator's own mesh and keeps the fastest.  The choice is cached per
 // (order, precision, element-count bucket, affine mesh) for the process.
-// GH1_HEX_GMODE=0..4 forces a variant (FP64 takes it modulo 2; 4 needs an
-// all-affine mesh).
+// GH1_HEX_GMODE=0..5 forces a variant (FP64 takes it modulo 2; 4 and 5 need an
+// all-affine mesh, 5 an order the slice form supports).
 template <class T>
 void hex_autotune(gh1_op* op, const T* G, int gstride) {
   const int pi = std::is_same<T, float>::value ? 1 : 0;
   int nmodes = (pi == 1 && op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) ? 4 : 2;
   if (nmodes == 4 && op->pair_per_sm[2] > 0) nmodes = 5;
+  if (nmodes == 5 && op->slice_per_sm > 0) nmodes = 6;
   const char* env = getenv("GH1_HEX_GMODE");
-  if (env && env[0] >= '0' && env[0] <= '4') {
+  if (env && env[0] >= '0' && env[0] <= '5') {
     const int m = env[0] - '0';
     op->hex_gmode[pi] = m < nmodes ? m : m % 2;
     return;
@@ -1194,6 +1199,7 @@ void matfree_setup(gh1_op* op) {
         op->pair_per_sm[1] = hex_pair_occupancy(op, 1);
         hex_affine_setup(op);
         op->pair_per_sm[2] = op->all_affine ? hex_pair_occupancy(op, 2) : 0;
+        hex_slice_setup(op);
       }
     }
     hex_autotune<double>(op, op->d_G64.p, op->gstride64);

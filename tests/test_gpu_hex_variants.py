@@ -2,7 +2,8 @@
 (1), one element per lane (0, 1) or two elements per lane with packed f32x2
 arithmetic (2, 3) -- forced through GH1_HEX_GMODE and checked against the FP64
 oracle.  Odd element counts leave the last element pair half empty.  Variant 4
-(one metric per element) exists only on meshes whose element maps are all affine."""
+(one metric per element) exists only on meshes whose element maps are all affine,
+and so does variant 5 (its slice / pencil form, orders 1-4)."""
 import contextlib
 import os
 
@@ -95,13 +96,36 @@ def test_fp32_affine_variant(gpu, p, mass):
     assert a.mat.Info()["hex_variant_fp32"] in (0, 1, 2, 3)
 
 
-@pytest.mark.parametrize("mode", [2, 3, 4])
+@pytest.mark.parametrize("mass", [False, True])
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_fp32_slice_variant(gpu, p, mass):
+    """Variant 5 (slice / pencil form, one metric per element) within 2e-5 of the
+    oracle on affine meshes whose element counts leave the last warp chunk
+    ragged (1, 8, 27, 64 and 125 elements against 2 * 32 / (p + 1) per chunk).
+    Its fused energy x^T A x drives the mixed CG test below."""
+    for m in (MakeStructured3DMesh(hexes=True, nx=1), _sheared(2), MakeStructured3DMesh(hexes=True, nx=3),
+              _sheared(4), MakeStructured3DMesh(hexes=True, nx=5)):
+        kappa = lognormal(m.ne, 1.0, 5)
+        mu = lognormal(m.ne, 0.5, 6) if mass else None
+        fes = gpu.H1(m, order=p, dirichlet=".*")
+        a = _form(gpu, fes, kappa, mu, 5)
+        assert a.mat.Info()["hex_variant_fp32"] == 5
+        S = O.OracleSpace(m.points, m.elements, p)
+        x = np.random.default_rng(7).normal(size=fes.ndof)
+        yo = S.apply_mf(x, kappa=kappa, mu=mu)
+        x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        a.mat.Mult(x32, y32)
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("mode", [2, 3, 4, 5])
 @pytest.mark.parametrize("p", [2, 4])
 def test_mixed_cg_paired_variant(gpu, mode, p):
     """Mixed-precision CG whose inner FP32 iterations run the paired apply (with
     its fused energy x^T A x) reaches 1e-10 true relative residual and agrees
     with the FP64 CG solution."""
-    m = _sheared(5) if mode == 4 else JitterInterior(MakeStructured3DMesh(hexes=True, nx=5), 0.1 / 5, 3)
+    m = _sheared(5) if mode >= 4 else JitterInterior(MakeStructured3DMesh(hexes=True, nx=5), 0.1 / 5, 3)
     kappa = lognormal(m.ne, 0.5, 14)
     f = np.random.default_rng(15).uniform(-1, 1, m.ne)
     fes = gpu.H1(m, order=p, dirichlet=".*")
