@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep"],
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep", "link"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
     ap.add_argument("--c2-orders", default="2,3,4", help="orders of the C2 record (comma separated)")
@@ -380,6 +380,49 @@ def workload_c2(args):
     return out
 
 
+def workload_link(args):
+    """Host link bandwidth for the end-to-end leg: pinned-host <-> device copies of
+    one 64^3 p=4 FP32 vector (67.9 MB) through the copy engines, H2D and D2H
+    alone and both directions at once on two streams.  These bound the e2e
+    GDOF/s: ndof / (bytes_h2d + bytes_d2h) x the bidirectional rate."""
+    import torch
+    n = 16974593
+    h_in = torch.empty(n, dtype=torch.float32, pin_memory=True).fill_(1.0)
+    h_out = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    d_in = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_out = torch.zeros(n, dtype=torch.float32, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    nb = n * 4
+
+    def timed(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            d_in.copy_(h_in, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+
+    t_h2d, t_d2h, t_both = timed(h2d), timed(d2h), timed(both)
+    bidir = 2 * nb / t_both / 1e9
+    return {"workload": "host link: pinned host <-> device copies of a 64^3 p=4 FP32 vector", "bytes": nb,
+            "h2d_gbs": nb / t_h2d / 1e9, "d2h_gbs": nb / t_d2h / 1e9, "bidirectional_gbs": bidir,
+            "e2e_ceiling_gdofs": n / (2 * nb / (bidir * 1e9)) / 1e9}
+
+
 def workload_sweep(args):
     """Hex apply across orders p = 1..8 on structured meshes of ~17 M DOFs (the
     64^3 p=4 size), kappa lognormal(0, 0.5): FP32 (autotuned variant) and FP64
@@ -556,7 +599,7 @@ def main():
     torch.cuda.set_device(dev)
     if args.workload != "c3":
         fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4, "c5": workload_c5,
-              "sweep": workload_sweep}[args.workload]
+              "sweep": workload_sweep, "link": workload_link}[args.workload]
         rec = fn(args)
         if rank == 0:
             print(json.dumps({"record": args.workload, **rec}), flush=True)
