@@ -372,6 +372,7 @@ def workload_c2(args):
             del S, orp, oci, ova
         out["orders"][p] = {"ndof": N, "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm, "cpu_oracle": cpu,
                             "spmv_ms": t_spmv * 1e3, "spmv_gbs": B / t_spmv / 1e9, "cusparse_ms": t_cusp * 1e3,
+                            "spmv_config": a.mat.Info()["hex_variant_fp64"],
                             "spmv_vs_cusparse": t_cusp / t_spmv, "spmv_err_vs_cusparse": err,
                             "matfree_fp64_ms": t_mf64 * 1e3, "matfree_fp32_ms": t_mf32 * 1e3,
                             "matfree_fp32_gdofs": N / t_mf32 / 1e9}

@@ -5,14 +5,15 @@
 // once; x is gathered through L2/L1.
 //
 // Mapping: a sub-warp of L lanes per row; each lane walks the row in strides of
-// L with a 4-way unrolled body so that 8 streaming loads and 4 gathers are in
-// flight per lane; shuffle reduction.  L is autotuned per matrix (4..32).
+// L with a U-way unrolled body (U = 4 or 8) so that 2U streaming loads and U
+// gathers are in flight per lane; shuffle reduction.  L and U are autotuned per
+// matrix (L = 4..32).
 #include <algorithm>
 #include "common.cuh"
 
 namespace gh1 {
 
-template <class TV, class TX, int L>
+template <class TV, class TX, int L, int U>
 __global__ void __launch_bounds__(256) csr_spmv_kernel(int64_t nrows, const int64_t* __restrict__ rowptr,
                                                        const int32_t* __restrict__ colind, const TV* __restrict__ vals,
                                                        const TX* __restrict__ x, TX* __restrict__ y, const int* skip) {
@@ -29,6 +30,21 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(int64_t nrows, const int6
     if (row < nrows) {
       const int64_t beg = __ldg(rowptr + row), end = __ldg(rowptr + row + 1);
       int64_t k = beg + sub;
+      if (U == 8) {
+        for (; k + 7 * L < end; k += 8 * L) {
+          int c[8];
+          TV v[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            c[j] = __ldcs(colind + k + j * L);
+            v[j] = __ldcs(vals + k + j * L);
+          }
+          TX t = 0;
+#pragma unroll
+          for (int j = 0; j < 8; j++) t += (TX)v[j] * __ldg(x + c[j]);
+          acc += t;
+        }
+      }
       for (; k + 3 * L < end; k += 4 * L) {
         const int c0 = __ldcs(colind + k), c1 = __ldcs(colind + k + L), c2 = __ldcs(colind + k + 2 * L),
                   c3 = __ldcs(colind + k + 3 * L);
@@ -44,25 +60,30 @@ __global__ void __launch_bounds__(256) csr_spmv_kernel(int64_t nrows, const int6
   }
 }
 
-template <class TV, class TX, int L>
+template <class TV, class TX, int L, int U>
 void launch_spmv_L(gh1_ctx* ctx, cudaStream_t s, int64_t nrows, const int64_t* rowptr, const int32_t* colind,
                    const TV* vals, const TX* x, TX* y, const int* skip) {
   const int block = 256;
   const int64_t rows_per_block = block / L;
   const int64_t need = (nrows + rows_per_block - 1) / rows_per_block;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)ctx->nsm * 16));
-  csr_spmv_kernel<TV, TX, L><<<grid, block, 0, s>>>(nrows, rowptr, colind, vals, x, y, skip);
+  csr_spmv_kernel<TV, TX, L, U><<<grid, block, 0, s>>>(nrows, rowptr, colind, vals, x, y, skip);
   check_kernel(ctx, "csr_spmv_kernel");
 }
 
 template <class TV, class TX>
 void launch_spmv(gh1_ctx* ctx, cudaStream_t s, int L, int64_t nrows, const int64_t* rowptr, const int32_t* colind,
                  const TV* vals, const TX* x, TX* y, const int* skip) {
+  // L encodes the unroll too: L + 100 selects U = 8
   switch (L) {
-    case 4: launch_spmv_L<TV, TX, 4>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
-    case 8: launch_spmv_L<TV, TX, 8>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
-    case 16: launch_spmv_L<TV, TX, 16>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
-    default: launch_spmv_L<TV, TX, 32>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 4: launch_spmv_L<TV, TX, 4, 4>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 8: launch_spmv_L<TV, TX, 8, 4>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 16: launch_spmv_L<TV, TX, 16, 4>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 104: launch_spmv_L<TV, TX, 4, 8>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 108: launch_spmv_L<TV, TX, 8, 8>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 116: launch_spmv_L<TV, TX, 16, 8>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    case 132: launch_spmv_L<TV, TX, 32, 8>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
+    default: launch_spmv_L<TV, TX, 32, 4>(ctx, s, nrows, rowptr, colind, vals, x, y, skip); break;
   }
 }
 
@@ -86,10 +107,10 @@ static int spmv_tune(gh1_op* op, int prec) {
   GH1_CUDA(cudaEventCreate(&b));
   float best = 1e30f;
   int bestL = 32;
-  for (int cand : {4, 8, 16, 32}) {
-    for (int rep = 0; rep < 2; rep++) {
+  for (int cand : {4, 8, 16, 32, 104, 108, 116, 132}) {
+    for (int rep = 0; rep < 2; rep++) {  // 3 warm-up launches, then 5 timed
       if (rep == 1) GH1_CUDA(cudaEventRecord(a, s));
-      for (int k = 0; k < 3; k++) {
+      for (int k = 0; k < 3 + 2 * rep; k++) {
         if (prec == GH1_F64)
           launch_spmv<double, double>(ctx, s, cand, n, op->rowptr, op->colind, op->d_vals.p, (const double*)xs.p,
                                       (double*)ys.p, nullptr);
