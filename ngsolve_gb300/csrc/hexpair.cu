@@ -683,47 +683,51 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
 // ---- slice / pencil form (affine meshes) ------------------------------------------
 // Same operator as hex_apply_pair_kernel in G mode 2, with a different split of
 // the contractions between the threads of a warp.  A warp owns P = 32/N element
-// pairs (two elements per lane, packed as above).  Lane (t, p) = (lane / P, lane % P):
-//   slice phase:  t = a (x index).  The lane holds the N x N slice u[a][.][.]
-//                 of both elements in registers and contracts it along z and
-//                 then y there (stages 1 and 2), writing only the three stage-2
-//                 results bb, db, bd at (a, j, k) to shared memory;
-//   pencil phase: t = j.  For each k the lane reads the N values along a of the
-//                 three arrays, forms the gradient at the N points (i, j, k),
-//                 applies the metric, contracts back along a and writes the
-//                 results in place (the same words it read);
-//   slice phase again: the lane reads its slice of the three arrays and
-//                 contracts back along y and z in registers.
-// The contractions move 3 N^3 words per element pair through shared memory each
-// way (the pencil-per-lane form moves 5 N^3), all at the two-wavefront minimum
-// of an 8-byte warp access: the exchange array X[array][k][j][a][p] has unit
-// stride in p and stride P in a, so the slice phase touches consecutive words,
-// and the j stride SJ = P (mod 16), so the pencil phase does too modulo 16.
+// pairs (two elements per lane, packed as above).  Lane (t, p) = (lane / P, lane % P).
+// The lane holds the N x N slice u[a = t][.][.] of both elements in registers for
+// the whole chunk, and the chunk runs one quadrature plane k at a time:
+//   slice phase:  lane (a = t) contracts its slice along z (c -> k) and y
+//                 (b -> j) and writes bb, db, bd at (a, j) of plane k;
+//   pencil phase: lane (j = t) reads the N values along a of the three arrays,
+//                 forms the gradient at the N points (i, j, k), applies the
+//                 metric, contracts back along a and writes in place;
+//   slice phase:  lane (a = t) reads its row of the plane, contracts back along
+//                 y and accumulates the transposed z contraction of plane k into
+//                 its result slice (registers).
+// Per plane the exchange array X[array][j][a][p] (unit stride in p, stride P in
+// a, j stride SJ = P mod 16) moves 3 N^2 words per pair each way at the two-
+// wavefront minimum of an 8-byte warp access: 3 N^3 per element pair in all,
+// against 5 N^3 in the pencil-per-lane form.  Only one plane is resident, so the
+// warp needs 4.4 KB of exchange space at N = 5 and runs at 8 warps per SM with
+// registers for the slice, its result and the plane's temporaries.
 // The x gather and the scatter run in DOF order (consecutive lanes on
 // consecutive local DOFs of one element: coalesced index and x loads, atomics
-// that share sectors) through the array su[p][a][m] (m = b N + c), whose a
-// stride SUA = P and pair stride SPU = 1 (mod 16) keep the slice reads and
-// writes at the minimum as well.  su aliases X.  All exchanges stay inside one
-// warp (__syncwarp; no block barriers and no waits).
+// that share sectors) through the staging array su[p][a][m] (m = b N + c, a
+// stride SUA = P and pair stride SPU = 1 mod 16: conflict-free slice reads and
+// writes); every index load of a chunk is issued before its first x load, and
+// every x load before the first store, so a chunk waits for two load latencies.
+// All exchanges stay inside one warp (__syncwarp; no block barriers, no waits).
 template <int N>
 struct SliceCfg {
   static constexpr int P = 32 / N;                                      // element pairs per warp
   static constexpr int NP = N * P;                                      // active lanes
   static constexpr int N2 = N * N, N3 = N * N * N;
   static constexpr int SJ = NP + ((P - NP) % 16 + 16) % 16;             // >= NP, == P (mod 16)
-  static constexpr int PL = (N - 1) * SJ + NP;                          // words per (array, k) plane
-  static constexpr int XW = 3 * N * PL;                                 // exchange words per warp
+  static constexpr int PL = (N - 1) * SJ + NP;                          // words per array of one plane
+  static constexpr int XW = 3 * PL;                                     // exchange words per warp (one plane)
   static constexpr int SUA = N2 + ((P - N2) % 16 + 16) % 16;            // >= N^2, == P (mod 16)
   static constexpr int SPU0 = (N - 1) * SUA + N2;
   static constexpr int SPU = SPU0 + ((1 - SPU0) % 16 + 16) % 16;        // >= SPU0, == 1 (mod 16)
-  static constexpr int W = XW > P * SPU ? XW : P * SPU;                 // words per warp
+  static constexpr int SUW = P * SPU;                                   // staging words per warp
+  static constexpr int W = XW + SUW;                                    // words per warp
   static constexpr int NT = P * N3, NI = (NT + 31) / 32;                // DOF-order items per warp / lane
   static constexpr int WARPS = 2, BLOCK = 32 * WARPS;
   static constexpr size_t smem = (size_t)WARPS * W * sizeof(f2);
 };
-// resident 64-thread blocks per SM the register allocation must allow (shared
-// memory allows 5 blocks at N = 5, more below)
-constexpr int slice_min_blocks(int N) { return N <= 3 ? 8 : N == 4 ? 6 : 5; }
+// resident 64-thread blocks per SM the register allocation must allow: 8 warps
+// (255 registers) at N = 5, where the slice, its result and the plane
+// temporaries are live together; more warps at lower orders
+constexpr int slice_min_blocks(int N) { return N <= 3 ? 8 : N == 4 ? 6 : 4; }
 
 template <int N, bool MASS>
 __global__ void __launch_bounds__(SliceCfg<N>::BLOCK, slice_min_blocks(N))
@@ -732,51 +736,70 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
                        unsigned int* counter, double* energy, const int* skip) {
   using C = SliceCfg<N>;
   constexpr int P = C::P, NP = C::NP, SJ = C::SJ, PL = C::PL, N2 = C::N2, N3 = C::N3, O = tab_off(N);
-  constexpr int AR = N * PL;                // words per exchange array
   constexpr int SUA = C::SUA, SPU = C::SPU, NT = C::NT, NI = C::NI;
   constexpr int WO = N * (N - 1) / 2 - 1;   // offset of this order's Gauss weights
   if (skip && *(volatile const int*)skip) return;
   extern __shared__ __align__(16) unsigned char slice_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  f2* X = (f2*)slice_raw + (size_t)warp * C::W;
-  f2* su = X;                               // gather / scatter staging, aliases X
+  f2* X = (f2*)slice_raw + (size_t)warp * C::W;  // one plane: [array][j][a][p]
+  f2* su = X + C::XW;                            // gather / scatter staging [p][a][m]
   const bool act = lane < NP;
   const int t = act ? lane / P : 0, p = lane % P;
   const int ps = t * SJ + p;                // pencil-phase word offset of this lane (j = t)
-  const int ss = p * SPU + t * SUA;         // slice-phase su offset of this lane (a = t)
+  const int ss = p * SPU + t * SUA;         // slice-phase staging offset of this lane (a = t)
   const int nch = (ne + 2 * P - 1) / (2 * P);
   f2 acc = 0;
   for (int ch = blockIdx.x * C::WARPS + warp; ch < nch; ch += gridDim.x * C::WARPS) {
     const int eb = ch * 2 * P, nrow = min(2 * P, ne - eb);
     const int e0 = eb + 2 * p;
     const bool v0 = act && e0 < ne, v1 = act && e0 + 1 < ne;
-    __syncwarp();  // the previous chunk's readers of su are done
-    // gather in DOF order: item q = (pair, local DOF l), both elements of the pair
-#pragma unroll 8
-    for (int j = 0; j < NI; j++) {
-      const int q = lane + 32 * j;
-      if (q < NT) {
+    // gather in DOF order: item q = (pair, local DOF l), both elements of the pair;
+    // all index loads, then all x loads, then the stores
+    {
+      int d0[NI], d1[NI];
+#pragma unroll
+      for (int j = 0; j < NI; j++) {
+        const int q = lane + 32 * j;
         const int pp = q / N3, l = q % N3;
-        float a0 = 0.f, a1 = 0.f;
-        if (2 * pp < nrow) {
-          const int d = __ldg(tdof + (size_t)(eb + 2 * pp) * tstride + l);
-          a0 = __int_as_float(__float_as_int(__ldg(x + (d & 0x7fffffff))) ^ (d & (int)0x80000000));
+        d0[j] = (q < NT && 2 * pp < nrow) ? __ldg(tdof + (size_t)(eb + 2 * pp) * tstride + l) : -1;
+        d1[j] = (q < NT && 2 * pp + 1 < nrow) ? __ldg(tdof + (size_t)(eb + 2 * pp + 1) * tstride + l) : -1;
+      }
+      float g0[NI], g1[NI];
+#pragma unroll
+      for (int j = 0; j < NI; j++) {
+        g0[j] = d0[j] != -1 ? __ldg(x + (d0[j] & 0x7fffffff)) : 0.f;
+        g1[j] = d1[j] != -1 ? __ldg(x + (d1[j] & 0x7fffffff)) : 0.f;
+      }
+      __syncwarp();  // the previous chunk's scatter has read su
+#pragma unroll
+      for (int j = 0; j < NI; j++) {
+        const int q = lane + 32 * j;
+        if (q < NT) {
+          const int pp = q / N3, l = q % N3;
+          const float a0 = __int_as_float(__float_as_int(g0[j]) ^ (d0[j] != -1 ? (d0[j] & (int)0x80000000) : 0));
+          const float a1 = __int_as_float(__float_as_int(g1[j]) ^ (d1[j] != -1 ? (d1[j] & (int)0x80000000) : 0));
+          su[pp * SPU + (l / N2) * SUA + l % N2] = pack2(a0, a1);
         }
-        if (2 * pp + 1 < nrow) {
-          const int d = __ldg(tdof + (size_t)(eb + 2 * pp + 1) * tstride + l);
-          a1 = __int_as_float(__float_as_int(__ldg(x + (d & 0x7fffffff))) ^ (d & (int)0x80000000));
-        }
-        su[pp * SPU + (l / N2) * SUA + l % N2] = pack2(a0, a1);
       }
     }
     __syncwarp();
-    f2 u[N2];
+    f2 u[N2], out[N2];
 #pragma unroll
-    for (int m = 0; m < N2; m++) u[m] = act ? su[ss + m] : (f2)0;
-    __syncwarp();  // su is overwritten by X below
-    // stages 1 (along z: c -> k) and 2 (along y: b -> j), one k at a time
+    for (int m = 0; m < N2; m++) {
+      u[m] = act ? su[ss + m] : (f2)0;
+      out[m] = 0;
+    }
+    // metric of the pencil lane's two elements (a missing element reuses a valid one)
+    f2 ea[7];
+    {
+      const int r0 = v0 ? e0 : eb, r1 = v1 ? e0 + 1 : r0;
 #pragma unroll
+      for (int c = 0; c < (MASS ? 7 : 6); c++) ea[c] = pack2(__ldg(Ga + (size_t)r0 * 8 + c), __ldg(Ga + (size_t)r1 * 8 + c));
+    }
+    const float wj = c_Wp[WO + t];
+#pragma unroll 1
     for (int k = 0; k < N; k++) {
+      // slice phase: stages 1 (c -> k) and 2 (b -> j) for plane k
       f2 ub[N], ud[N];
 #pragma unroll
       for (int b = 0; b < N; b++) {
@@ -789,6 +812,7 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
         ub[b] = sb;
         ud[b] = sd;
       }
+      __syncwarp();  // the previous plane's readers of X are done
 #pragma unroll
       for (int j = 0; j < N; j++) {
         f2 bb = mul2(bcast(c_Bp[O + j * N]), ub[0]), db = mul2(bcast(c_Dp[O + j * N]), ub[0]),
@@ -800,30 +824,22 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
           bd = fma2(bcast(c_Bp[O + j * N + b]), ud[b], bd);
         }
         if (act) {
-          f2* w = X + k * PL + j * SJ + lane;
+          f2* w = X + j * SJ + lane;
           w[0] = bb;
-          w[AR] = db;
-          w[2 * AR] = bd;
+          w[PL] = db;
+          w[2 * PL] = bd;
         }
       }
-    }
-    __syncwarp();
-    // pencil phase: lane (j = t, p), points (i, j, k)
-    if (act) {
-      const int r0 = v0 ? e0 : eb, r1 = v1 ? e0 + 1 : r0;  // a missing element reuses a valid metric
-      f2 ea[7];
-#pragma unroll
-      for (int c = 0; c < (MASS ? 7 : 6); c++) ea[c] = pack2(__ldg(Ga + (size_t)r0 * 8 + c), __ldg(Ga + (size_t)r1 * 8 + c));
-      const float wj = c_Wp[WO + t];
-#pragma unroll
-      for (int k = 0; k < N; k++) {
-        f2* w = X + k * PL + ps;
+      __syncwarp();
+      // pencil phase: lane (j = t, p), points (i, j, k)
+      if (act) {
+        f2* w = X + ps;
         f2 w1[N], w2[N], w3[N];
 #pragma unroll
         for (int a = 0; a < N; a++) {
           w1[a] = w[a * P];
-          w2[a] = w[AR + a * P];
-          w3[a] = w[2 * AR + a * P];
+          w2[a] = w[PL + a * P];
+          w3[a] = w[2 * PL + a * P];
         }
         const float wjk = wj * c_Wp[WO + k];
         f2 vx[N], vy[N], vz[N], vm[N];
@@ -865,65 +881,69 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
             q3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], q3);
           }
           w[a * P] = q1;
-          w[AR + a * P] = q2;
-          w[2 * AR + a * P] = q3;
+          w[PL + a * P] = q2;
+          w[2 * PL + a * P] = q3;
         }
       }
-    }
-    __syncwarp();
-    // slice phase, transposed: stage 2 (j -> b) and stage 1 (k -> c) into the slice
-    f2 out[N2];
+      __syncwarp();
+      // slice phase, transposed: stage 2 (j -> b) on plane k, then this plane's
+      // share of stage 1 (k -> c) into the result slice
+      if (act) {
+        f2 r1[N], r2[N], r3[N];
+        const f2* w = X + lane;
 #pragma unroll
-    for (int m = 0; m < N2; m++) out[m] = 0;
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-      f2 r1[N], r2[N], r3[N];
-      const f2* w = X + k * PL + lane;
-#pragma unroll
-      for (int j = 0; j < N; j++) {
-        if (act) {
+        for (int j = 0; j < N; j++) {
           r1[j] = w[j * SJ];
-          r2[j] = w[AR + j * SJ];
-          r3[j] = w[2 * AR + j * SJ];
-        } else {
-          r1[j] = r2[j] = r3[j] = 0;
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < N; b++) {
-        f2 ub = mul2(bcast(c_Bp[O + b]), r1[0]), ud = mul2(bcast(c_Bp[O + b]), r3[0]);
-        ub = fma2(bcast(c_Dp[O + b]), r2[0], ub);
-#pragma unroll
-        for (int j = 1; j < N; j++) {
-          ub = fma2(bcast(c_Bp[O + j * N + b]), r1[j], ub);
-          ub = fma2(bcast(c_Dp[O + j * N + b]), r2[j], ub);
-          ud = fma2(bcast(c_Bp[O + j * N + b]), r3[j], ud);
+          r2[j] = w[PL + j * SJ];
+          r3[j] = w[2 * PL + j * SJ];
         }
 #pragma unroll
-        for (int c = 0; c < N; c++)
-          out[b * N + c] = fma2(bcast(c_Dp[O + k * N + c]), ud, fma2(bcast(c_Bp[O + k * N + c]), ub, out[b * N + c]));
+        for (int b = 0; b < N; b++) {
+          f2 vb = mul2(bcast(c_Bp[O + b]), r1[0]), vd = mul2(bcast(c_Bp[O + b]), r3[0]);
+          vb = fma2(bcast(c_Dp[O + b]), r2[0], vb);
+#pragma unroll
+          for (int j = 1; j < N; j++) {
+            vb = fma2(bcast(c_Bp[O + j * N + b]), r1[j], vb);
+            vb = fma2(bcast(c_Dp[O + j * N + b]), r2[j], vb);
+            vd = fma2(bcast(c_Bp[O + j * N + b]), r3[j], vd);
+          }
+#pragma unroll
+          for (int c = 0; c < N; c++)
+            out[b * N + c] = fma2(bcast(c_Dp[O + k * N + c]), vd, fma2(bcast(c_Bp[O + k * N + c]), vb, out[b * N + c]));
+        }
       }
     }
-    __syncwarp();  // X is overwritten by su below
+    // result slice -> staging (this lane's own words), then the scatter in DOF order
     if (act) {
 #pragma unroll
       for (int m = 0; m < N2; m++) su[ss + m] = out[m];
     }
     __syncwarp();
-    // scatter in DOF order (DOFs >= first_cell belong to one element: plain stores)
-#pragma unroll 8
-    for (int j = 0; j < NI; j++) {
-      const int q = lane + 32 * j;
-      if (q < NT) {
-        const int pp = q / N3, l = q % N3;
-        float o0, o1;
-        unpack2(su[pp * SPU + (l / N2) * SUA + l % N2], o0, o1);
+    {
+      int d0[NI], d1[NI];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          if (2 * pp + h < nrow) {
-            const int d = __ldg(tdof + (size_t)(eb + 2 * pp + h) * tstride + l);
-            const int dof = d & 0x7fffffff;
-            const float v = __int_as_float(__float_as_int(h ? o1 : o0) ^ (d & (int)0x80000000));
+      for (int j = 0; j < NI; j++) {
+        const int q = lane + 32 * j;
+        const int pp = q / N3, l = q % N3;
+        d0[j] = (q < NT && 2 * pp < nrow) ? __ldg(tdof + (size_t)(eb + 2 * pp) * tstride + l) : -1;
+        d1[j] = (q < NT && 2 * pp + 1 < nrow) ? __ldg(tdof + (size_t)(eb + 2 * pp + 1) * tstride + l) : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < NI; j++) {
+        const int q = lane + 32 * j;
+        if (q < NT) {
+          const int pp = q / N3, l = q % N3;
+          float o0, o1;
+          unpack2(su[pp * SPU + (l / N2) * SUA + l % N2], o0, o1);
+          if (d0[j] != -1) {
+            const int dof = d0[j] & 0x7fffffff;
+            const float v = __int_as_float(__float_as_int(o0) ^ (d0[j] & (int)0x80000000));
+            if (dof >= first_cell) y[dof] = v;
+            else atomicAdd(y + dof, v);
+          }
+          if (d1[j] != -1) {
+            const int dof = d1[j] & 0x7fffffff;
+            const float v = __int_as_float(__float_as_int(o1) ^ (d1[j] & (int)0x80000000));
             if (dof >= first_cell) y[dof] = v;
             else atomicAdd(y + dof, v);
           }
