@@ -684,8 +684,9 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
 // Same operator as hex_apply_pair_kernel in G mode 2, with a different split of
 // the contractions between the threads of a warp.  A warp owns P = 32/N element
 // pairs (two elements per lane, packed as above).  Lane (t, p) = (lane / P, lane % P).
-// The lane holds the N x N slice u[a = t][.][.] of both elements in registers for
-// the whole chunk, and the chunk runs one quadrature plane k at a time:
+// The lane's N x N slice u[a = t][.][.] of both elements sits in registers (N = 2,
+// 4) or is read again from the staging array per plane (N = 3, 5), its result
+// slice is in registers, and the chunk runs one quadrature plane k at a time:
 //   slice phase:  lane (a = t) contracts its slice along z (c -> k) and y
 //                 (b -> j) and writes bb, db, bd at (a, j) of plane k;
 //   pencil phase: lane (j = t) reads the N values along a of the three arrays,
@@ -697,9 +698,9 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
 // Per plane the exchange array X[array][j][a][p] (unit stride in p, stride P in
 // a, j stride SJ = P mod 16) moves 3 N^2 words per pair each way at the two-
 // wavefront minimum of an 8-byte warp access: 3 N^3 per element pair in all,
-// against 5 N^3 in the pencil-per-lane form.  Only one plane is resident, so the
-// warp needs 4.4 KB of exchange space at N = 5 and runs at 8 warps per SM with
-// registers for the slice, its result and the plane's temporaries.
+// against 5 N^3 in the pencil-per-lane form (plus N^3 re-reads of the slice).
+// Only one plane is resident, so the warp needs 4.4 KB of exchange space at
+// N = 5, and with the slice re-read per plane 12 warps per SM fit in registers.
 // The x gather and the scatter run in DOF order (consecutive lanes on
 // consecutive local DOFs of one element: coalesced index and x loads, atomics
 // that share sectors) through the staging array su[p][a][m] (m = b N + c, a
@@ -724,10 +725,10 @@ struct SliceCfg {
   static constexpr int WARPS = 2, BLOCK = 32 * WARPS;
   static constexpr size_t smem = (size_t)WARPS * W * sizeof(f2);
 };
-// resident 64-thread blocks per SM the register allocation must allow: 8 warps
-// (255 registers) at N = 5, where the slice, its result and the plane
+// resident 64-thread blocks per SM the register allocation must allow: 12 warps
+// (168 registers) at N = 4 and 5, where the result slice and the plane
 // temporaries are live together; more warps at lower orders
-constexpr int slice_min_blocks(int N) { return N <= 3 ? 8 : N == 4 ? 6 : 4; }
+constexpr int slice_min_blocks(int N) { return N <= 3 ? 8 : 6; }
 
 template <int N, bool MASS>
 __global__ void __launch_bounds__(SliceCfg<N>::BLOCK, slice_min_blocks(N))
@@ -783,11 +784,15 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
       }
     }
     __syncwarp();
-    f2 u[N2], out[N2];
+    // KEEP_U: the slice stays in registers for the whole chunk (N = 2 and 4, where
+    // it fits the register budget without spills); otherwise each plane reads
+    // it again from the staging array
+    constexpr bool KEEP_U = N == 2 || N == 4;
+    f2 out[N2], uk[KEEP_U ? N2 : 1];
 #pragma unroll
     for (int m = 0; m < N2; m++) {
-      u[m] = act ? su[ss + m] : (f2)0;
       out[m] = 0;
+      if (KEEP_U) uk[m] = act ? su[ss + m] : (f2)0;
     }
     // metric of the pencil lane's two elements (a missing element reuses a valid one)
     f2 ea[7];
@@ -799,15 +804,20 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
     const float wj = c_Wp[WO + t];
 #pragma unroll 1
     for (int k = 0; k < N; k++) {
-      // slice phase: stages 1 (c -> k) and 2 (b -> j) for plane k
+      // slice phase: stages 1 (c -> k) and 2 (b -> j) for plane k; the slice is
+      // read again from the staging array row by row (registers hold the result
+      // slice across the planes)
       f2 ub[N], ud[N];
 #pragma unroll
       for (int b = 0; b < N; b++) {
-        f2 sb = mul2(bcast(c_Bp[O + k * N]), u[b * N]), sd = mul2(bcast(c_Dp[O + k * N]), u[b * N]);
+        f2 u[N];
+#pragma unroll
+        for (int c = 0; c < N; c++) u[c] = KEEP_U ? uk[(b * N + c) % (KEEP_U ? N2 : 1)] : (act ? su[ss + b * N + c] : (f2)0);
+        f2 sb = mul2(bcast(c_Bp[O + k * N]), u[0]), sd = mul2(bcast(c_Dp[O + k * N]), u[0]);
 #pragma unroll
         for (int c = 1; c < N; c++) {
-          sb = fma2(bcast(c_Bp[O + k * N + c]), u[b * N + c], sb);
-          sd = fma2(bcast(c_Dp[O + k * N + c]), u[b * N + c], sd);
+          sb = fma2(bcast(c_Bp[O + k * N + c]), u[c], sb);
+          sd = fma2(bcast(c_Dp[O + k * N + c]), u[c], sd);
         }
         ub[b] = sb;
         ud[b] = sd;
