@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep", "link"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
+    ap.add_argument("--c5-pack", default="sorted", choices=["sorted", "seed"],
+                    help="C5 wave packing: by decreasing (order, side), or in seed order")
     ap.add_argument("--c2-orders", default="2,3,4", help="orders of the C2 record (comma separated)")
     return ap.parse_args()
 
@@ -516,9 +518,12 @@ def workload_c4(args):
 def workload_c5(args):
     """256 independent problems on structured hex meshes, side n ~ U{8..40},
     order p ~ U{1..6}, kappa ~ lognormal(0,1) per element, 16 seeded f ~ U[-1,1]
-    right-hand sides each (4,096 solves), seed 9; FP32 inner / FP64 refined to
-    1e-10.  Problems run in waves that fit the device; each wave is one batched
-    solve (one CUDA graph re-launched until every system converged)."""
+    right-hand sides each (4,096 solves), seed 9 for the sizes and orders and
+    seed (9, i) for problem i's data; FP32 inner / FP64 refined to 1e-10.
+    Problems run in waves that fit the device, packed in order of decreasing
+    (order, side) so that the problems of a wave need similar iteration counts
+    and finish together (--c5-pack seed keeps the seed order); each wave is one
+    batched solve (one CUDA graph re-launched until every system converged)."""
     import torch
     import ngsolve_gb300 as ng
     rng = np.random.default_rng(9)
@@ -527,8 +532,11 @@ def workload_c5(args):
     orders = rng.integers(1, 7, nprob)
     R = 16
     budget = 100e9
+    order = list(range(nprob))
+    if args.c5_pack == "sorted":
+        order.sort(key=lambda i: (int(orders[i]), int(sides[i])), reverse=True)
     waves, cur, cur_b = [], [], 0.0
-    for i in range(nprob):
+    for i in order:
         n, p = int(sides[i]), int(orders[i])
         ndof = (n * p + 1) ** 3
         ne = n ** 3
@@ -547,8 +555,9 @@ def workload_c5(args):
         forms, rhs = [], []
         for i in w:
             n, p = int(sides[i]), int(orders[i])
+            prng = np.random.default_rng([9, i])
             mesh = ng.MakeStructured3DMesh(hexes=True, nx=n)
-            kappa = np.exp(rng.normal(0, 1, mesh.ne))
+            kappa = np.exp(prng.normal(0, 1, mesh.ne))
             fes = ng.H1(mesh, order=p, dirichlet=".*")
             u, v = fes.TnT()
             a = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
@@ -556,7 +565,7 @@ def workload_c5(args):
             B = torch.zeros((R, fes.ndof), dtype=torch.float64, device="cuda")
             for r in range(R):
                 lf = ng.LinearForm(fes)
-                lf += ng.CoefficientFunction(rng.uniform(-1, 1, mesh.ne)) * v * ng.dx
+                lf += ng.CoefficientFunction(prng.uniform(-1, 1, mesh.ne)) * v * ng.dx
                 lf.Assemble()
                 B[r].copy_(lf.vec.t)
             forms.append(a)
@@ -580,7 +589,7 @@ def workload_c5(args):
         del solver, forms, rhs, X
         torch.cuda.empty_cache()
     return {"workload": "C5: %d problems x 16 rhs, n~U{8..40}, p~U{1..6}, mixed to 1e-10" % nprob,
-            "waves": len(waves), "solves": nprob * R, "total_dofs_x_rhs": dof_solves,
+            "waves": len(waves), "wave_packing": args.c5_pack, "solves": nprob * R, "total_dofs_x_rhs": dof_solves,
             "solve_s": t_solve, "setup_s": t_setup, "max_true_relres": worst,
             "inner_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters))},
             "outer_max": int(max(outers)), "gdof_iterations_per_s": dof_iters / t_solve / 1e9}
