@@ -109,7 +109,8 @@ void build_space(gh1_space* sp) {
     for (int i = 0; i < sp->nface; i++) {
       std::array<int32_t, 4> t{INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
       for (int j = 0; j < fv; j++) t[j] = ev(e, lface(i, j));
-      std::sort(t.begin(), t.begin() + fv);
+      for (int j = 1; j < fv; j++)  // insertion sort of the face's 3 or 4 vertex numbers
+        for (int k = j; k > 0 && t[k - 1] > t[k]; k--) std::swap(t[k - 1], t[k]);
       fkeys[e * sp->nface + i] = t;
     }
   });

@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(RED_BLOCK) residual_kernel(int64_t n, const do
 }
 
 template <class TA, class TB>
-__global__ void axpby_kernel(int64_t n, double a, const TA* __restrict__ x, double b, TB* __restrict__ y) {
+__global__ void axpby_kernel(int64_t n, double a, const TA* x, double b, TB* y) {  // x may alias y
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = (TB)(a * (double)x[i] + (b == 0.0 ? 0.0 : b * (double)y[i]));
 }
