@@ -76,7 +76,7 @@ constexpr int pair_min_blocks(int N, bool mass, int gm) {
          : N == 3 ? (mass ? (gm ? 5 : 4) : (gm ? 6 : 5))
          : N == 4 ? (mass ? (gm ? 5 : 4) : 5)
          : N == 5 ? (mass ? (gm ? 4 : 3) : (gm ? 5 : 4))
-         : N == 6 ? 3
+         : N == 6 ? 2
                   : 2;
 }
 

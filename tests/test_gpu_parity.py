@@ -76,7 +76,8 @@ def test_assemble_parity(gpu, kind, p, jit, perm):
 
 
 @pytest.mark.parametrize("kind,p,jit,mass", [("hex", 1, 0.1, False), ("hex", 2, 0.1, True), ("hex", 3, 0.15, False),
-                                             ("hex", 4, 0.1, True), ("hex", 6, 0.1, False), ("hex", 8, 0.0, False),
+                                             ("hex", 4, 0.1, True), ("hex", 5, 0.1, True), ("hex", 6, 0.1, False),
+                                             ("hex", 8, 0.0, False),
                                              ("tet", 2, 0.2, True), ("tet", 3, 0.2, False), ("tet", 4, 0.2, False)])
 def test_matfree_apply_parity(gpu, kind, p, jit, mass):
     m = _mesh(kind, 3, jit, permute=(kind == "tet"))
