@@ -790,9 +790,10 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
     constexpr bool KEEP_U = N == 2 || N == 4;
     f2 out[N2], uk[KEEP_U ? N2 : 1];
 #pragma unroll
-    for (int m = 0; m < N2; m++) {
-      out[m] = 0;
-      if (KEEP_U) uk[m] = act ? su[ss + m] : (f2)0;
+    for (int m = 0; m < N2; m++) out[m] = 0;
+    if constexpr (KEEP_U) {
+#pragma unroll
+      for (int m = 0; m < N2; m++) uk[m] = act ? su[ss + m] : (f2)0;
     }
     // metric of the pencil lane's two elements (a missing element reuses a valid one)
     f2 ea[7];
@@ -811,8 +812,13 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
 #pragma unroll
       for (int b = 0; b < N; b++) {
         f2 u[N];
+        if constexpr (KEEP_U) {
 #pragma unroll
-        for (int c = 0; c < N; c++) u[c] = KEEP_U ? uk[(b * N + c) % (KEEP_U ? N2 : 1)] : (act ? su[ss + b * N + c] : (f2)0);
+          for (int c = 0; c < N; c++) u[c] = uk[b * N + c];
+        } else {
+#pragma unroll
+          for (int c = 0; c < N; c++) u[c] = act ? su[ss + b * N + c] : (f2)0;
+        }
         f2 sb = mul2(bcast(c_Bp[O + k * N]), u[0]), sd = mul2(bcast(c_Dp[O + k * N]), u[0]);
 #pragma unroll
         for (int c = 1; c < N; c++) {
