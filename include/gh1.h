@@ -43,7 +43,7 @@ enum {
 };
 enum { GH1_F64 = 0, GH1_F32 = 1 };
 enum { GH1_MEM_HOST = 0, GH1_MEM_DEVICE = 1 };
-enum { GH1_OP_CSR = 0, GH1_OP_MATFREE = 1 };
+enum { GH1_OP_CSR = 0, GH1_OP_MATFREE = 1, GH1_OP_BLOCK = 2 };
 
 typedef struct gh1_ctx gh1_ctx;
 typedef struct gh1_mesh gh1_mesh;
@@ -118,6 +118,17 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
  * 100 when each lane keeps 8 instead of 4 nonzeros in flight (0: not tuned yet). */
 int gh1_op_info(gh1_op* op, int64_t* info);
 int gh1_op_free(gh1_op* op);
+
+/* Block-diagonal operator diag(A, ..., A) with nblocks copies of op on
+ * consecutive slices of length nrows(op): the bilinear forms
+ * InnerProduct(grad(u), grad(v)) and InnerProduct(u, v) on VectorH1, whose DOFs
+ * are the component spaces' DOFs one after the other (CompoundFESpace,
+ * comp/h1hofespace.cpp:2482-2560, VectorH1FESpace with interleaved = false).
+ * The block operator works with gh1_op_apply, gh1_jacobi_create (freedofs of
+ * length nblocks * nrows, or the inner space's repeated), gh1_cg and
+ * gh1_op_info (kind GH1_OP_BLOCK).  op is borrowed: it must outlive the block
+ * operator. */
+int gh1_op_block_create(gh1_op* op, int nblocks, gh1_op** block);
 
 /* ---- preconditioner -----------------------------------------------------
  * a.mat.CreateSmoother(freedofs) / Preconditioner(a,"local")

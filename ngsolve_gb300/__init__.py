@@ -5,13 +5,15 @@ This package mirrors the reference's Python objects on that path.
 """
 from . import _lib
 from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMesh
-from .comp import (Mesh, H1, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
-                   BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, JacobiPrecond, Preconditioner,
+from .comp import (Mesh, H1, VectorH1, InnerProduct, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
+                   BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, BlockMatrix, JacobiPrecond,
+                   Preconditioner,
                    Projector, Integrate_grad_dot, ShapeEval, context)
 from . import solvers
 from .adjoint import AdjointProblem, AdjointJ
 
-__all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "BilinearForm",
+__all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "VectorH1",
+           "InnerProduct", "BilinearForm",
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
-           "SparseMatrix", "BilinearFormApplication", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
+           "SparseMatrix", "BilinearFormApplication", "BlockMatrix", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
            "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ"]

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libgh1.so")
 GH1_OK = 0
 GH1_F64, GH1_F32 = 0, 1
 GH1_MEM_HOST, GH1_MEM_DEVICE = 0, 1
-GH1_OP_CSR, GH1_OP_MATFREE = 0, 1
+GH1_OP_CSR, GH1_OP_MATFREE, GH1_OP_BLOCK = 0, 1, 2
 GH1_CG_FP64, GH1_CG_MIXED = 0, 1
 GH1_STOP_PRECOND, GH1_STOP_TRUE = 0, 1
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_UNSUPPORTED",
@@ -65,6 +65,7 @@ SIGNATURES = {
     "gh1_op_apply": [_P, _D, _P, _P, _I, _I],
     "gh1_op_info": [_P, _P],
     "gh1_op_free": [_P],
+    "gh1_op_block_create": [_P, _I, _PP],
     "gh1_jacobi_create": [_P, _P, _I, _PP],
     "gh1_pre_apply": [_P, _D, _P, _P, _I, _I],
     "gh1_pre_free": [_P],

@@ -246,6 +246,43 @@ class H1:
         return tuple(int(d) for d in self.ElementDofs()[int(el)])
 
 
+class VectorH1:
+    """VectorH1 (comp/h1hofespace.cpp:2482-2700): dim copies of H1(order,
+    dirichlet), the DOFs of component c at c*n .. (c+1)*n - 1 with n the scalar
+    space's ndof (the CompoundFESpace numbering, interleaved = False)."""
+
+    def __init__(self, mesh, order=1, dirichlet="", dim=3):
+        self.scalar = H1(mesh, order=order, dirichlet=dirichlet)
+        self.dim = int(dim)
+        self.mesh, self.order, self.ctx = self.scalar.mesh, self.scalar.order, self.scalar.ctx
+        self.ne = self.scalar.ne
+        self.ndof = self.dim * self.scalar.ndof
+        self.nfree = self.dim * self.scalar.nfree
+
+    def TnT(self):
+        return _Proxy(self, False), _Proxy(self, True)
+
+    def TrialFunction(self):
+        return _Proxy(self, False)
+
+    def TestFunction(self):
+        return _Proxy(self, True)
+
+    def FreeDofs(self):
+        return np.tile(np.asarray(self.scalar.FreeDofs()), self.dim).view(BitArray)
+
+    def Range(self, component):
+        n = self.scalar.ndof
+        return range(component * n, (component + 1) * n)
+
+
+def InnerProduct(a, b):
+    """InnerProduct(grad(u), grad(v)) and InnerProduct(u, v) of VectorH1 (or H1)
+    trial and test functions: the sums over components of grad u_c . grad v_c and
+    u_c v_c."""
+    return _Product.of(a, b)
+
+
 # ---------------------------------------------------------------------------
 class BaseVector:
     """Device vector (FP64 unless stated) -- ngla BaseVector / UnifiedVector."""
@@ -479,6 +516,15 @@ class BilinearFormApplication(BaseMatrix):
     """Matrix-free operator: sum-factorized on hexes, element-wise on tets."""
 
 
+class BlockMatrix(BaseMatrix):
+    """diag(A, ..., A): the VectorH1 form of a scalar operator A (one block per
+    component).  Keeps A alive: the block operator borrows it."""
+
+    def __init__(self, ctx, h, fes, inner):
+        super().__init__(ctx, h, fes.ndof, fes)
+        self.inner = inner
+
+
 class JacobiPrecond(BaseMatrix):
     """JacobiPrecond (linalg/jacobi.cpp:40-110): invdiag on free DOFs, 0 elsewhere."""
 
@@ -563,6 +609,7 @@ class BilinearForm:
 
     def __init__(self, fes, nonassemble=False, precision="fp64", symmetric=True, **kwargs):
         self.fes = fes
+        self._sfes = fes.scalar if isinstance(fes, VectorH1) else fes  # the space the form lives on
         self.nonassemble = bool(nonassemble)
         self.precision = precision
         self.kappa = np.zeros(fes.ne)
@@ -589,7 +636,7 @@ class BilinearForm:
         mu = None if self.mu is None else np.ascontiguousarray(self.mu, dtype=np.float64)
         if self._form is None:
             h = ctypes.c_void_p()
-            ctx.check(ctx.lib.gh1_form_create(self.fes.h, _np_ptr(kappa), None if mu is None else _np_ptr(mu),
+            ctx.check(ctx.lib.gh1_form_create(self._sfes.h, _np_ptr(kappa), None if mu is None else _np_ptr(mu),
                                               _lib.GH1_MEM_HOST, ctypes.byref(h)))
             self._form = h
         return self._form
@@ -598,13 +645,19 @@ class BilinearForm:
         ctx = self.fes.ctx.sync_stream()
         form = self._make_form()
         h = ctypes.c_void_p()
+        sfes = self._sfes
         if self.nonassemble:
             mask = 1 | (2 if self.precision in ("fp32", "mixed") else 0)
             ctx.check(ctx.lib.gh1_matfree_create(form, mask, ctypes.byref(h)))
-            self.mat = BilinearFormApplication(ctx, h, self.fes.ndof, self.fes)
+            mat = BilinearFormApplication(ctx, h, sfes.ndof, sfes)
         else:
             ctx.check(ctx.lib.gh1_assemble_csr(form, ctypes.byref(h)))
-            self.mat = SparseMatrix(ctx, h, self.fes)
+            mat = SparseMatrix(ctx, h, sfes)
+        if sfes is not self.fes:  # VectorH1: the scalar operator once per component
+            hb = ctypes.c_void_p()
+            ctx.check(ctx.lib.gh1_op_block_create(mat.h, self.fes.dim, ctypes.byref(hb)))
+            mat = BlockMatrix(ctx, hb, self.fes, mat)
+        self.mat = mat
         return self
 
     def Apply(self, x, y):
@@ -621,14 +674,27 @@ class BilinearForm:
 
 
 class LinearForm:
-    """LinearForm(fes) += f * v * dx with f constant per element; order 2p."""
+    """LinearForm(fes) += f * v * dx with f constant per element; order 2p.  On
+    VectorH1, f is CoefficientFunction((f_1, ..., f_dim)), one value (or array per
+    element) per component."""
 
     def __init__(self, fes):
         self.fes = fes
-        self.f = np.zeros(fes.ne)
+        self._vector = isinstance(fes, VectorH1)
+        self.f = np.zeros((fes.dim, fes.ne)) if self._vector else np.zeros(fes.ne)
         self.vec = BaseVector(fes.ndof)
 
     def __iadd__(self, term):
+        if self._vector:
+            comps = [f for f in term.factors if isinstance(f, CoefficientFunction) and isinstance(f.values, (tuple, list))]
+            if len(comps) != 1 or len(comps[0].values) != self.fes.dim:
+                raise ValueError("a VectorH1 source is CoefficientFunction((f_1, ..., f_%d)) * v * dx" % self.fes.dim)
+            kind, coef = _Product([f for f in term.factors if f is not comps[0]]).classify(self.fes.ne)
+            if kind != "source":
+                raise ValueError("LinearForm takes f*v*dx")
+            for c, fc in enumerate(comps[0].values):
+                self.f[c] = self.f[c] + coef * CoefficientFunction(fc).element_values(self.fes.ne)
+            return self
         kind, coef = term.classify(self.fes.ne)
         if kind != "source":
             raise ValueError("LinearForm takes f*v*dx")
@@ -637,6 +703,13 @@ class LinearForm:
 
     def Assemble(self):
         ctx = self.fes.ctx.sync_stream()
+        if self._vector:  # component c into its DOF block
+            sfes, n = self.fes.scalar, self.fes.scalar.ndof
+            for c in range(self.fes.dim):
+                f = np.ascontiguousarray(self.f[c], dtype=np.float64)
+                ctx.check(ctx.lib.gh1_rhs_elementwise(sfes.h, _np_ptr(f), _lib.GH1_MEM_HOST,
+                                                      _ptr(self.vec.t[c * n:(c + 1) * n])))
+            return self
         f = np.ascontiguousarray(self.f, dtype=np.float64)
         ctx.check(ctx.lib.gh1_rhs_elementwise(self.fes.h, _np_ptr(f), _lib.GH1_MEM_HOST, _ptr(self.vec.t)))
         return self

@@ -265,6 +265,51 @@ gh1_form::~gh1_form() {
 }
 
 // =============================================================================
+namespace gh1 {
+
+// y = A x for every operator kind.  CSR writes y; the matrix-free apply adds into
+// a y that is zero on entry; a block operator applies its inner operator slice by
+// slice.  skip: as for the CG graph kernels (NULL outside graphs).
+void op_apply_any(gh1_op* op, const void* x, void* y, int prec, const int* skip) {
+  if (op->kind == GH1_OP_CSR) {
+    spmv_skip(op, x, y, prec, skip);
+  } else if (op->kind == GH1_OP_MATFREE) {
+    matfree_apply_ex(op, x, y, prec, nullptr, nullptr, nullptr, skip);
+  } else {
+    const size_t bytes = (size_t)op->inner->nrows * (prec == GH1_F64 ? 8 : 4);
+    for (int b = 0; b < op->nblocks; b++)
+      op_apply_any(op->inner, (const char*)x + b * bytes, (char*)y + b * bytes, prec, skip);
+  }
+}
+
+// per-operator setup that must not run inside a stream capture (SpMV autotuning)
+void op_prepare_any(gh1_op* op, int prec) {
+  if (op->kind == GH1_OP_CSR) spmv_prepare(op, prec);
+  else if (op->kind == GH1_OP_BLOCK) op_prepare_any(op->inner, prec);
+}
+
+// matrix-free data of a form whose coefficients changed since the setup
+void op_refresh_any(gh1_op* op) {
+  if (op->kind == GH1_OP_MATFREE && op->form && op->form_version != op->form->version) matfree_setup(op);
+  else if (op->kind == GH1_OP_BLOCK) op_refresh_any(op->inner);
+}
+
+// operator diagonal (FP64, device)
+static void op_diag_any(gh1_op* op, double* diag) {
+  if (op->kind == GH1_OP_CSR) {
+    csr_diag(op, diag);
+  } else if (op->kind == GH1_OP_MATFREE) {
+    matfree_diag(op, diag);
+  } else {
+    const int64_t n = op->inner->nrows;
+    op_diag_any(op->inner, diag);
+    for (int b = 1; b < op->nblocks; b++)
+      GH1_CUDA(cudaMemcpyAsync(diag + b * n, diag, n * sizeof(double), cudaMemcpyDeviceToDevice, op->ctx->stream));
+  }
+}
+
+}  // namespace gh1
+
 extern "C" {
 
 int gh1_version(void) { return 1; }
@@ -498,6 +543,12 @@ int gh1_matfree_create(gh1_form* f, int prec_mask, gh1_op** out) {
 
 int gh1_op_info(gh1_op* op, int64_t* info) {
   if (!op || !info) return GH1_ERR_ARG;
+  if (op->kind == GH1_OP_BLOCK) {  // the inner operator's description, with the block kind and size
+    const int rc = gh1_op_info(op->inner, info);
+    info[0] = GH1_OP_BLOCK;
+    info[1] = op->nrows;
+    return rc;
+  }
   info[0] = op->kind; info[1] = op->nrows;
   info[2] = op->sp ? op->sp->mesh->ne : 0;
   info[3] = op->sp ? op->sp->p : 0;
@@ -509,6 +560,24 @@ int gh1_op_info(gh1_op* op, int64_t* info) {
     info[5] = op->spmv_L[1];
   }
   return GH1_OK;
+}
+
+
+int gh1_op_block_create(gh1_op* op, int nblocks, gh1_op** out) {
+  if (!op || !out) return GH1_ERR_ARG;
+  return guard(op->ctx, [&] {
+    GH1_CHECK(nblocks >= 1, GH1_ERR_ARG, "nblocks must be positive");
+    GH1_CHECK(op->kind != GH1_OP_BLOCK, GH1_ERR_ARG, "the inner operator of a block operator is a scalar operator");
+    auto* b = new gh1_op();
+    b->ctx = op->ctx;
+    b->kind = GH1_OP_BLOCK;
+    b->inner = op;
+    b->nblocks = nblocks;
+    b->nrows = (int64_t)nblocks * op->nrows;
+    b->sp = op->sp;  // for gh1_op_info (elements, order); the DOFs are nblocks * sp->ndof
+    b->prec_mask = op->kind == GH1_OP_CSR ? 3 : op->prec_mask;
+    *out = b;
+  });
 }
 
 int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int prec, int accumulate) {
@@ -529,9 +598,10 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int prec, int acc
     } else {
       GH1_CHECK(prec == GH1_F64 ? (op->prec_mask & 1) : (op->prec_mask & 2), GH1_ERR_UNSUPPORTED,
                 "operator was not set up for this precision");
-      if (op->form && op->form_version != op->form->version) matfree_setup(op);
+      op_refresh_any(op);
+      op_prepare_any(op, prec);
       GH1_CUDA(cudaMemsetAsync(target, 0, op->nrows * es, st));
-      matfree_apply(op, x, target, prec, nullptr, nullptr, nullptr);
+      op_apply_any(op, x, target, prec, nullptr);
     }
     if (!plain) vec_axpby(op->ctx, op->nrows, s, target, accumulate ? 1.0 : 0.0, y, prec);
   });
@@ -551,14 +621,15 @@ int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** ou
       if (freedofs) {
         GH1_CUDA(cudaMemcpyAsync(pr->d_free.p, freedofs, op->nrows,
                                  mem == GH1_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-      } else if (op->sp) {
-        GH1_CUDA(cudaMemcpyAsync(pr->d_free.p, op->sp->d_free.p, op->nrows, cudaMemcpyDeviceToDevice, st));
+      } else if (op->sp) {  // the space's free DOFs, once per block of a block operator
+        const int64_t n = op->sp->ndof;
+        for (int64_t o = 0; o < op->nrows; o += n)
+          GH1_CUDA(cudaMemcpyAsync(pr->d_free.p + o, op->sp->d_free.p, n, cudaMemcpyDeviceToDevice, st));
       } else {
         GH1_CUDA(cudaMemsetAsync(pr->d_free.p, 1, op->nrows, st));
       }
       DBuf<double> diag(op->nrows);
-      if (op->kind == GH1_OP_CSR) csr_diag(op, diag.p);
-      else matfree_diag(op, diag.p);
+      op_diag_any(op, diag.p);
       pr->d_inv64.alloc(op->nrows);
       pr->d_inv32.alloc(op->nrows);
       jacobi_invert(op->ctx, op->nrows, diag.p, pr->d_free.p, pr->d_inv64.p, pr->d_inv32.p);
@@ -594,7 +665,7 @@ int gh1_cg(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_op
     GH1_CHECK(o->mode == GH1_CG_FP64 || o->mode == GH1_CG_MIXED, GH1_ERR_ARG, "unknown CG mode");
     GH1_CHECK(o->mode == GH1_CG_FP64 || pre, GH1_ERR_ARG, "mixed-precision CG needs the Jacobi preconditioner");
     GH1_CHECK(o->maxit > 0 && o->tol >= 0, GH1_ERR_ARG, "maxit must be positive and tol non-negative");
-    if (op->form && op->kind == GH1_OP_MATFREE && op->form_version != op->form->version) matfree_setup(op);
+    op_refresh_any(op);
     status = cg_solve(op, pre, b, x, o, r);
   });
   return rc != GH1_OK ? rc : status;

@@ -299,8 +299,8 @@ struct PCG {
     int g = red_grid(ctx, n);
     if (op->kind == GH1_OP_MATFREE) {
       op_apply_energy(op, s, y, prec, partial + 2 * ctx->nsm * 64, counters + 1, &st->energy, &st->done);
-    } else {
-      spmv_skip(op, s, y, prec, &st->done);
+    } else {  // CSR or block operator: s^T A s by a separate reduction
+      op_apply_any(op, s, y, prec, &st->done);
       dot_energy_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, s, y, &st->energy, partial + 2 * ctx->nsm * 64, counters + 1, &st->done);
       check_kernel(ctx, "dot_energy_kernel");
     }
@@ -326,7 +326,7 @@ struct PCG {
     cudaGraphExec_t exec = *cache_exec;
     if (!exec || *cache_chunk != chunk) {
       if (exec) cudaGraphExecDestroy(exec);
-      if (op->kind == GH1_OP_CSR) spmv_prepare(op, prec);
+      op_prepare_any(op, prec);
       cudaGraph_t graph;
       GH1_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < chunk; k++) launch_iteration(cs);
@@ -410,8 +410,8 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     W.d64.alloc(n); W.w64.alloc(n); W.s64.alloc(n); W.y64.alloc(n);
     auto apply64 = [&](const double* in, double* out) {
       GH1_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), cs));
-      if (op->kind == GH1_OP_MATFREE) matfree_apply_ex(op, in, out, GH1_F64, nullptr, nullptr, nullptr, nullptr);
-      else spmv(op, in, out, GH1_F64);
+      op_prepare_any(op, GH1_F64);
+      op_apply_any(op, in, out, GH1_F64, nullptr);
       r->applies64++;
     };
     if (o->initialize) GH1_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), cs));
@@ -446,7 +446,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
       W.x32.alloc(n); W.d32.alloc(n); W.w32.alloc(n); W.s32.alloc(n); W.y32.alloc(n); W.r64.alloc(n);
       GH1_CHECK(op->kind == GH1_OP_CSR || (op->prec_mask & 2), GH1_ERR_UNSUPPORTED,
                 "mixed precision needs an operator set up with FP32 data (precision mask bit 1)");
-      if (op->kind == GH1_OP_CSR) spmv_prepare(op, GH1_F32);
+      op_prepare_any(op, GH1_F32);
       const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
       const int max_outer = o->max_outer > 0 ? o->max_outer : 30;
       const double target = o->tol * std::sqrt(bb);

@@ -144,6 +144,8 @@ struct gh1_op {
   gh1_form* form = nullptr;   // NULL for imported CSR
   gh1_space* sp = nullptr;
   int64_t nrows = 0;
+  gh1_op* inner = nullptr;    // GH1_OP_BLOCK: the repeated operator (borrowed)
+  int nblocks = 0;            // GH1_OP_BLOCK: copies of inner on consecutive slices
   // CSR data
   int64_t nnz = 0;
   gh1::DBuf<int64_t> d_rowptr_own;
@@ -247,6 +249,11 @@ void hex_slice_setup(gh1_op* op);
 void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                      const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
+// any operator kind (api.cu): y = A x into a y the call zeroes first where the kind
+// needs it; skip as for the CG graph kernels; prepare / refresh before capture
+void op_apply_any(gh1_op* op, const void* x, void* y, int prec, const int* skip);
+void op_prepare_any(gh1_op* op, int prec);
+void op_refresh_any(gh1_op* op);
 void spmv_skip(gh1_op* op, const void* x, void* y, int prec, const int* skip);  // spmv.cu
 void csr_diag(gh1_op* op, double* diag);                            // spmv.cu
 int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* o, gh1_cg_result* r);  // cg.cu
