@@ -182,6 +182,39 @@ def test_oracle_cg_reference_rule():
     assert np.abs(x - xr).max() < 1e-8 * np.abs(xr).max()
 
 
+@pytest.mark.parametrize("nblocks", [1, 3])
+def test_cg_history_bound_accepts_rounding(nblocks):
+    """The CG history bound of the GPU parity tests holds between two oracle CG
+    runs whose matrices differ only by a 2e-16 relative rounding of each entry
+    (scalar and 3-block VectorH1 systems, hex p=3 as in those tests); their
+    iteration counts differ by at most one and their solutions by 1e-9."""
+    from tests.util import assert_cg_history_close
+    m = JitterInterior(MakeStructured3DMesh(hexes=True, nx=4), 0.1 / 4, 21)
+    S = O.OracleSpace(m.points, m.elements, 3)
+    rp, ci, va = S.assemble(kappa=lognormal(S.ne, 1.0, 35))
+    free = S.freedofs().astype(bool)
+    diag = va[[rp[i] + np.searchsorted(ci[rp[i]:rp[i + 1]], i) for i in range(S.ndof)]]
+    f = np.random.default_rng(36).uniform(-1, 1, (nblocks, S.ne))
+    b = np.concatenate([S.rhs(f[c]) for c in range(nblocks)])
+    inv = np.tile(np.where(free, 1.0 / diag, 0.0), nblocks)
+    n, nnz = S.ndof, len(va)
+    brp = np.concatenate([rp[:-1] + c * nnz for c in range(nblocks)] + [[nblocks * nnz]]).astype(rp.dtype)
+    bci = np.concatenate([ci + c * n for c in range(nblocks)]).astype(ci.dtype)
+    runs = []
+    for vals in (va, va * (1 + 2e-16 * np.random.default_rng(1).standard_normal(nnz))):
+        bva = np.tile(vals, nblocks)  # held: the oracle takes a raw pointer
+        x = np.zeros(nblocks * n)
+        hist = np.zeros(3002)
+        its = np.zeros(1, dtype=np.int32)
+        O.lib().orc_cg(None, nblocks * n, O._p(brp), O._p(bci), O._p(bva), None, None, O._p(inv),
+                       O._p(b), O._p(x), 1e-10, 3000, O._p(hist), O._p(its))
+        runs.append((x, int(its[0]), hist[:int(its[0])]))
+    (xa, ia, ha), (xb, ib, hb) = runs
+    assert abs(ia - ib) <= 1
+    assert_cg_history_close(hb, ha)
+    assert np.abs(xa - xb).max() <= 1e-9 * np.abs(xa).max()
+
+
 def test_matfree_equals_csr_oracle():
     m = JitterInterior(MakeStructured3DMesh(hexes=True, nx=3), 0.08, 2)
     S = O.OracleSpace(m.points, m.elements, 3)
