@@ -101,19 +101,26 @@ class BatchCG:
     """Batched mixed-precision CG over many independent hex problems.
 
     forms: list of BilinearForm (hex meshes, kappa/mu per element); nrhs: right-hand
-    sides per problem (<= 16).  Solve(rhs_list, tol) takes per problem a (nrhs, ndof)
+    sides per problem.  Solve(rhs_list, tol) takes per problem a (nrhs, ndof)
     FP64 CUDA tensor and returns the solutions in the same layout; `results` holds
-    one CGResult per (problem, rhs)."""
+    one CGResult per (problem, rhs).
+
+    A form on VectorH1 (dim components) is solved as its scalar form with
+    nrhs * dim right-hand sides: the (nrhs, dim * n) tensor is, in memory, the
+    (nrhs * dim, n) one.  Each component then stops on its own relative residual
+    (result index rhs * dim + component); at most 16 scalar right-hand sides per
+    problem."""
 
     def __init__(self, forms, nrhs):
         if len(forms) != len(nrhs):
             raise ValueError("one rhs count per form")
         self.forms = list(forms)
         self.nrhs = [int(r) for r in nrhs]
+        self._ncomp = [getattr(f.fes, "dim", 1) if f._sfes is not f.fes else 1 for f in self.forms]
         ctx = self.forms[0].fes.ctx.sync_stream()
         self.ctx = ctx
         handles = (ctypes.c_void_p * len(forms))(*[f._make_form().value for f in self.forms])
-        counts = (ctypes.c_int * len(forms))(*self.nrhs)
+        counts = (ctypes.c_int * len(forms))(*[r * c for r, c in zip(self.nrhs, self._ncomp)])
         h = ctypes.c_void_p()
         ctx.check(ctx.lib.gh1_batch_create(ctx.h, len(forms), handles, counts, ctypes.byref(h)))
         self.h = h
@@ -132,7 +139,7 @@ class BatchCG:
         o = _lib.CGOpts()
         o.tol, o.maxit, o.mode, o.stop_rule, o.initialize = float(tol), int(maxit), _lib.GH1_CG_MIXED, _lib.GH1_STOP_TRUE, 1
         o.inner_tol, o.max_outer, o.check_every = float(inner_tol), int(max_outer), int(check_every)
-        res = (_lib.CGResult * sum(self.nrhs))()
+        res = (_lib.CGResult * sum(r * c for r, c in zip(self.nrhs, self._ncomp)))()
         rc = ctx.lib.gh1_batch_solve(self.h, bp, xp, ctypes.byref(o), res)
         if rc not in (_lib.GH1_OK, 6, 7):
             ctx.check(rc)
