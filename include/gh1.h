@@ -87,6 +87,16 @@ int gh1_shape_eval(gh1_ctx* ctx, int et, int order, const int32_t* vnums, int np
  * kappa / mu: per-element coefficients (NULL: kappa = 1, mu = 0).        */
 int gh1_form_create(gh1_space* space, const double* kappa, const double* mu, int mem, gh1_form** form);
 int gh1_form_set_coefs(gh1_form* form, const double* kappa, const double* mu, int mem);
+/* Anisotropic diffusion (K grad u).grad v with one symmetric tensor per element,
+ * NGSolve's InnerProduct(K*grad(u), grad(v)) with a matrix-valued
+ * CoefficientFunction: the D matrix of B^T D B (fem/symbolicintegrator.cpp:
+ * 1548-1830) becomes w|det J| K in place of w|det J| kappa I.
+ * K6: ne*6 doubles per element (xx yy zz xy xz yz), host or device per mem;
+ * NULL returns the form to the scalar kappa.  While a tensor is set, kappa is
+ * ignored (fold a scalar term in as kappa I), and gh1_adjoint_grad rejects the
+ * form (dJ/dkappa needs the scalar coefficient).  Operators made from the form
+ * afterwards, and matrix-free operators at their next apply, use the tensor. */
+int gh1_form_set_tensor(gh1_form* form, const double* K6, int mem);
 int gh1_form_free(gh1_form* form);
 
 /* BilinearForm.Assemble() -> SparseMatrix (comp/bilinearform.cpp:832-1000,

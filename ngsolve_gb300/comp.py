@@ -130,12 +130,37 @@ def grad(u):
 
 
 class CoefficientFunction:
-    """Piecewise-constant coefficient: one value per element (or a scalar)."""
+    """Piecewise-constant coefficient: one value per element (or a scalar); a
+    tuple of such values is a vector (VectorH1 sources); a 3x3 matrix -- an
+    ndarray of shape (3, 3) or (ne, 3, 3), or 9 entries with dims=(3, 3) as in
+    NGSolve -- is a diffusion tensor for InnerProduct(K * grad(u), grad(v))."""
 
-    def __init__(self, values):
+    def __init__(self, values, dims=None):
+        if dims is not None:
+            if tuple(dims) != (3, 3) or len(values) != 9:
+                raise ValueError("matrix coefficients are 3x3: 9 entries with dims=(3, 3)")
+            values = np.moveaxis(np.array(np.broadcast_arrays(*[np.asarray(v, dtype=np.float64) for v in values])),
+                                 0, -1).reshape(np.shape(np.broadcast(*values)) + (3, 3))
         self.values = values
 
+    def is_tensor(self):
+        return isinstance(self.values, np.ndarray) and self.values.ndim in (2, 3) and self.values.shape[-2:] == (3, 3)
+
+    def tensor_values(self, ne):
+        """(ne, 6): xx yy zz xy xz yz of the symmetric tensor on each element."""
+        K = np.asarray(self.values, dtype=np.float64)
+        if K.ndim == 2:
+            K = np.broadcast_to(K, (ne, 3, 3))
+        if K.shape != (ne, 3, 3):
+            raise ValueError("element-wise tensor needs shape (%d, 3, 3), got %s" % (ne, K.shape))
+        if np.abs(K - K.transpose(0, 2, 1)).max() > 1e-12 * max(np.abs(K).max(), 1e-300):
+            raise ValueError("the diffusion tensor must be symmetric")
+        return np.ascontiguousarray(np.stack([K[:, 0, 0], K[:, 1, 1], K[:, 2, 2], K[:, 0, 1], K[:, 0, 2], K[:, 1, 2]],
+                                             axis=1))
+
     def element_values(self, ne):
+        if self.is_tensor():
+            raise ValueError("a matrix coefficient goes into InnerProduct(K * grad(u), grad(v))")
         v = np.asarray(self.values, dtype=np.float64)
         if v.ndim == 0:
             return np.full(ne, float(v))
@@ -176,9 +201,12 @@ class _Product:
     def classify(self, ne):
         grads = [f for f in self.factors if isinstance(f, _Grad)]
         proxies = [f for f in self.factors if isinstance(f, _Proxy)]
+        tensors = [f for f in self.factors if isinstance(f, CoefficientFunction) and f.is_tensor()]
         coef = np.ones(ne)
         has_dx = False
         for f in self.factors:
+            if isinstance(f, CoefficientFunction) and f.is_tensor():
+                continue
             if isinstance(f, CoefficientFunction):
                 coef = coef * f.element_values(ne)
             elif isinstance(f, (int, float, np.floating)):
@@ -187,6 +215,10 @@ class _Product:
                 has_dx = True
         if not has_dx:
             raise ValueError("integrand needs * dx")
+        if tensors:
+            if len(tensors) == 1 and len(grads) == 2 and not proxies and grads[0].proxy.test != grads[1].proxy.test:
+                return "laplace_tensor", tensors[0].tensor_values(ne) * coef[:, None]
+            raise NotImplementedError("a matrix coefficient is only on the path as InnerProduct(K * grad(u), grad(v))")
         if len(grads) == 2 and not proxies and grads[0].proxy.test != grads[1].proxy.test:
             return "laplace", coef
         if len(proxies) == 2 and not grads and proxies[0].test != proxies[1].test:
@@ -613,6 +645,7 @@ class BilinearForm:
         self.nonassemble = bool(nonassemble)
         self.precision = precision
         self.kappa = np.zeros(fes.ne)
+        self.K6 = None  # (ne, 6) sum of the tensor diffusion terms
         self.mu = None
         self._has_laplace = False
         self._form = None
@@ -622,6 +655,9 @@ class BilinearForm:
         kind, coef = term.classify(self.fes.ne)
         if kind == "laplace":
             self.kappa = self.kappa + coef
+            self._has_laplace = True
+        elif kind == "laplace_tensor":
+            self.K6 = coef if self.K6 is None else self.K6 + coef
             self._has_laplace = True
         elif kind == "mass":
             self.mu = coef if self.mu is None else self.mu + coef
@@ -639,6 +675,10 @@ class BilinearForm:
             ctx.check(ctx.lib.gh1_form_create(self._sfes.h, _np_ptr(kappa), None if mu is None else _np_ptr(mu),
                                               _lib.GH1_MEM_HOST, ctypes.byref(h)))
             self._form = h
+            if self.K6 is not None:  # scalar terms folded in as kappa I
+                K6 = np.array(self.K6, dtype=np.float64)
+                K6[:, :3] += kappa[:, None]
+                ctx.check(ctx.lib.gh1_form_set_tensor(h, _np_ptr(K6), _lib.GH1_MEM_HOST))
         return self._form
 
     def Assemble(self, reallocate=False):

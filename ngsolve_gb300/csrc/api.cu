@@ -460,6 +460,22 @@ int gh1_form_set_coefs(gh1_form* f, const double* kappa, const double* mu, int m
   });
 }
 
+int gh1_form_set_tensor(gh1_form* f, const double* K6, int mem) {
+  if (!f) return GH1_ERR_ARG;
+  return guard(f->sp->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    if (K6) {
+      upload_coef(f->sp->ctx, f->d_K6, K6, mem, (size_t)6 * f->sp->mesh->ne, 0.0);
+      f->has_K6 = true;
+    } else {
+      f->d_K6.release();
+      f->has_K6 = false;
+    }
+    f->version++;
+    GH1_CUDA(cudaStreamSynchronize(f->sp->ctx->stream));
+  });
+}
+
 int gh1_form_free(gh1_form* f) { delete f; return GH1_OK; }
 
 int gh1_assemble_csr(gh1_form* f, gh1_op** out) {

@@ -120,11 +120,28 @@ struct gh1_space {
   gh1::DBuf<int32_t> d_colind;
 };
 
+// G = s * Ji K Ji^T for the symmetric tensor K = (xx yy zz xy xz yz), written
+// as the metric components (xx yy zz xy xz yz); Ji is the inverse Jacobian,
+// row-major, so that the mapped gradient is Ji^T times the reference gradient.
+__device__ __forceinline__ void tensor_metric(const double* Ji, const double* K, double s, double* g) {
+  const double Km[9] = {K[0], K[3], K[4], K[3], K[1], K[5], K[4], K[5], K[2]};
+  double T[9];  // Ji K
+  for (int a = 0; a < 3; a++)
+    for (int l = 0; l < 3; l++) T[3 * a + l] = Ji[3 * a] * Km[l] + Ji[3 * a + 1] * Km[3 + l] + Ji[3 * a + 2] * Km[6 + l];
+  const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+  for (int c = 0; c < 6; c++) {
+    const int a = ia[c], b = ib[c];
+    g[c] = s * (T[3 * a] * Ji[3 * b] + T[3 * a + 1] * Ji[3 * b + 1] + T[3 * a + 2] * Ji[3 * b + 2]);
+  }
+}
+
 struct gh1_form {
   gh1_space* sp = nullptr;
   gh1::DBuf<double> d_kappa;  // ne
   gh1::DBuf<double> d_mu;     // ne (empty: mu = 0)
   bool has_mu = false;
+  gh1::DBuf<double> d_K6;     // ne x 6 symmetric diffusion tensors (xx yy zz xy xz yz); empty: kappa I
+  bool has_K6 = false;
   int version = 0;            // bumped on coefficient change
   // gh1_adjoint_grad cache: this form's operator (FP64 + FP32 data; its metrics
   // follow coefficient changes) and the unit-mass operator for J and the adjoint

@@ -997,8 +997,8 @@ void upload_pair_tables(gh1_space* sp) {
 // coefficients P0-P1+P2-P3, P0-P1-P4+P5, P0-P3-P4+P7, -P0+P1-P2+P3+P4-P5+P6-P7)
 // above 1e-12 of the element's edge vectors.
 __global__ void hex_affine_kernel(int ne, const double* __restrict__ X, const int* __restrict__ el,
-                                  const double* __restrict__ kappa, const double* __restrict__ mu, float* Ga,
-                                  int* nonaffine) {
+                                  const double* __restrict__ kappa, const double* __restrict__ K6,
+                                  const double* __restrict__ mu, float* Ga, int* nonaffine) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   double P[8][3];
@@ -1024,14 +1024,20 @@ __global__ void hex_affine_kernel(int ne, const double* __restrict__ X, const in
                         (J[0] * J[8] - J[2] * J[6]) * id, (J[2] * J[3] - J[0] * J[5]) * id,
                         (J[3] * J[7] - J[4] * J[6]) * id, (J[1] * J[6] - J[0] * J[7]) * id,
                         (J[0] * J[4] - J[1] * J[3]) * id};
-  const double f = kappa[e] * fabs(det);
   float* g = Ga + (size_t)e * 8;
-  g[0] = (float)(f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]));
-  g[1] = (float)(f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]));
-  g[2] = (float)(f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]));
-  g[3] = (float)(f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]));
-  g[4] = (float)(f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]));
-  g[5] = (float)(f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]));
+  if (K6) {
+    double t[6];
+    tensor_metric(Ji, K6 + 6 * (size_t)e, fabs(det), t);
+    for (int c = 0; c < 6; c++) g[c] = (float)t[c];
+  } else {
+    const double f = kappa[e] * fabs(det);
+    g[0] = (float)(f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]));
+    g[1] = (float)(f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]));
+    g[2] = (float)(f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]));
+    g[3] = (float)(f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]));
+    g[4] = (float)(f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]));
+    g[5] = (float)(f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]));
+  }
   g[6] = mu ? (float)(mu[e] * fabs(det)) : 0.f;
   g[7] = 0.f;
 }
@@ -1050,7 +1056,7 @@ void hex_affine_setup(gh1_op* op) {
   DBuf<int> flag(1);
   flag.zero(s);
   hex_affine_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, op->form->d_kappa.p,
-                                                     op->has_mass ? op->form->d_mu.p : nullptr, op->d_Ga32.p, flag.p);
+                                                     op->form->has_K6 ? op->form->d_K6.p : nullptr, op->has_mass ? op->form->d_mu.p : nullptr, op->d_Ga32.p, flag.p);
   check_kernel(sp->ctx, "hex_affine_kernel");
   int h = 1;
   GH1_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -61,8 +61,8 @@ __device__ __forceinline__ void hex_jacobian(const double* X, const int* v, doub
 // is given) for hex elements; FP64 arithmetic, stored in FP64 and/or FP32
 __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
                                 const double* __restrict__ gx, const double* __restrict__ gw,
-                                const double* __restrict__ kappa, const double* __restrict__ mu, double* G64, int gs64,
-                                float* G32, int gs32) {
+                                const double* __restrict__ kappa, const double* __restrict__ K6,
+                                const double* __restrict__ mu, double* G64, int gs64, float* G32, int gs32) {
   const int nq = nq1 * nq1 * nq1;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -74,14 +74,18 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
   hex_jacobian(X, v, gx[i], gx[j], gx[k], J);
   inv3(J, Ji, det);
   double wdet = gw[i] * gw[j] * gw[k] * fabs(det);
-  double f = kappa[e] * wdet;
   double g[7];
-  g[0] = f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
-  g[1] = f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
-  g[2] = f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
-  g[3] = f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
-  g[4] = f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
-  g[5] = f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
+  if (K6) {
+    tensor_metric(Ji, K6 + 6 * (size_t)e, wdet, g);
+  } else {
+    double f = kappa[e] * wdet;
+    g[0] = f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
+    g[1] = f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
+    g[2] = f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
+    g[3] = f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
+    g[4] = f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
+    g[5] = f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
+  }
   const int nc = mu ? 7 : 6;
   if (mu) g[6] = mu[e] * wdet;
   for (int c = 0; c < nc; c++) {
@@ -92,8 +96,8 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
 
 // tet: G[e][6] = kappa |det| J^{-1} J^{-T}, M[e] = mu |det|
 __global__ void tet_geom_kernel(int ne, const double* __restrict__ X, const int* __restrict__ el,
-                                const double* __restrict__ kappa, const double* __restrict__ mu, double* G64,
-                                float* G32, double* M64, float* M32) {
+                                const double* __restrict__ kappa, const double* __restrict__ K6,
+                                const double* __restrict__ mu, double* G64, float* G32, double* M64, float* M32) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const int* v = el + (size_t)e * 4;
@@ -104,14 +108,18 @@ __global__ void tet_geom_kernel(int ne, const double* __restrict__ X, const int*
     for (int k = 0; k < 3; k++) J[3 * k + j] = pj[k] - p3[k];
   }
   inv3(J, Ji, det);
-  double f = kappa[e] * fabs(det);
   double g[6];
-  g[0] = f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
-  g[1] = f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
-  g[2] = f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
-  g[3] = f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
-  g[4] = f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
-  g[5] = f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
+  if (K6) {
+    tensor_metric(Ji, K6 + 6 * (size_t)e, fabs(det), g);
+  } else {
+    double f = kappa[e] * fabs(det);
+    g[0] = f * (Ji[0] * Ji[0] + Ji[1] * Ji[1] + Ji[2] * Ji[2]);
+    g[1] = f * (Ji[3] * Ji[3] + Ji[4] * Ji[4] + Ji[5] * Ji[5]);
+    g[2] = f * (Ji[6] * Ji[6] + Ji[7] * Ji[7] + Ji[8] * Ji[8]);
+    g[3] = f * (Ji[0] * Ji[3] + Ji[1] * Ji[4] + Ji[2] * Ji[5]);
+    g[4] = f * (Ji[0] * Ji[6] + Ji[1] * Ji[7] + Ji[2] * Ji[8]);
+    g[5] = f * (Ji[3] * Ji[6] + Ji[4] * Ji[7] + Ji[5] * Ji[8]);
+  }
   for (int c = 0; c < 6; c++) {
     if (G64) G64[(size_t)e * 6 + c] = g[c];
     if (G32) G32[(size_t)e * 6 + c] = (float)g[c];
@@ -1185,7 +1193,7 @@ void matfree_setup(gh1_op* op) {
     int64_t tot = (int64_t)ne * nq;
     hex_geom_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
         ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_kappa.p,
-        op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
+        f->has_K6 ? f->d_K6.p : nullptr, op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
     check_kernel(sp->ctx, "hex_geom_kernel");
     upload_const_tables(sp);
     op->hex_per_sm[0][0] = hex_occupancy_dispatch<double, 0>(op, op->gstride64);
@@ -1212,7 +1220,7 @@ void matfree_setup(gh1_op* op) {
       if (want32) op->d_M32.alloc(ne);
     }
     tet_geom_kernel<<<(ne + 255) / 256, 256, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, f->d_kappa.p,
-                                                      op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p,
+                                                      f->has_K6 ? f->d_K6.p : nullptr, op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p,
                                                       want32 ? op->d_G32.p : nullptr, op->has_mass ? op->d_M64.p : nullptr,
                                                       (op->has_mass && want32) ? op->d_M32.p : nullptr);
     check_kernel(sp->ctx, "tet_geom_kernel");

@@ -435,16 +435,48 @@ Rule bilinear_rule(const Space& S) {
 }
 Rule mass_rule(const Space& S) { return S.et == 4 ? tet_rule(2 * S.p) : hex_rule(2 * S.p); }
 
+// Symmetric 3x3 tensor from its components (xx yy zz xy xz yz), row-major.
+inline void tensor33(const double* k6, double* k) {
+  k[0] = k6[0]; k[1] = k6[3]; k[2] = k6[4];
+  k[3] = k6[3]; k[4] = k6[1]; k[5] = k6[5];
+  k[6] = k6[4]; k[7] = k6[5]; k[8] = k6[2];
+}
+
 // element matrix of  kappa grad u.grad v + mu u v
 // (T_CalcElementMatrixAdd, fem/symbolicintegrator.cpp:1548-1830: B^T diag(w|detJ| c) B)
 // reverse != 0 sums the quadrature points in the opposite order: the difference
 // between the two orders measures the rounding noise of the algorithm itself.
-void element_matrix(const Space& S, int e, double kappa, double mu, std::vector<double>& K, int reverse = 0) {
+// k6 != NULL: the diffusion term is (K grad u).grad v with the element's
+// symmetric tensor K = k6 (xx yy zz xy xz yz) in place of kappa (the D matrix
+// of B^T D B is then w|detJ| K instead of w|detJ| kappa I).
+void element_matrix(const Space& S, int e, double kappa, double mu, std::vector<double>& K, int reverse = 0,
+                    const double* k6 = nullptr) {
   const int n = S.nloc;
   K.assign((size_t)n * n, 0.0);
   std::vector<AD> sh(n);
   std::vector<double> gx(n), gy(n), gz(n);
-  if (kappa != 0.0) {
+  if (k6) {
+    double kt[9];
+    tensor33(k6, kt);
+    Rule r = bilinear_rule(S);
+    std::vector<double> fx(n), fy(n), fz(n);
+    for (int qq = 0; qq < r.size(); qq++) {
+      const int q = reverse ? r.size() - 1 - qq : qq;
+      shape_ad(S, e, r.x[q], r.y[q], r.z[q], sh.data());
+      Geo g = geometry(S, e, r.x[q], r.y[q], r.z[q]);
+      double fac = r.w[q] * std::fabs(g.det);
+      for (int i = 0; i < n; i++) {  // mapped gradient J^{-T} grad_ref, and the flux K * it
+        gx[i] = g.Jinv[0] * sh[i].d[0] + g.Jinv[3] * sh[i].d[1] + g.Jinv[6] * sh[i].d[2];
+        gy[i] = g.Jinv[1] * sh[i].d[0] + g.Jinv[4] * sh[i].d[1] + g.Jinv[7] * sh[i].d[2];
+        gz[i] = g.Jinv[2] * sh[i].d[0] + g.Jinv[5] * sh[i].d[1] + g.Jinv[8] * sh[i].d[2];
+        fx[i] = kt[0] * gx[i] + kt[1] * gy[i] + kt[2] * gz[i];
+        fy[i] = kt[3] * gx[i] + kt[4] * gy[i] + kt[5] * gz[i];
+        fz[i] = kt[6] * gx[i] + kt[7] * gy[i] + kt[8] * gz[i];
+      }
+      for (int i = 0; i < n; i++) for (int j = 0; j < n; j++)
+        K[(size_t)i * n + j] += fac * (gx[i] * fx[j] + gy[i] * fy[j] + gz[i] * fz[j]);
+    }
+  } else if (kappa != 0.0) {
     Rule r = bilinear_rule(S);
     for (int qq = 0; qq < r.size(); qq++) {
       const int q = reverse ? r.size() - 1 - qq : qq;
@@ -547,7 +579,7 @@ void orc_graph_get(void* h, long* rowptr, int* colind) {
   std::memcpy(colind, S->colind.data(), S->colind.size() * sizeof(int));
 }
 // Assemble (comp/bilinearform.cpp:1562-2200): vals of kappa_e grad.grad + mu_e u v
-int orc_assemble(void* h, const double* kappa, const double* mu, double* vals, int reverse) {
+static int assemble_impl(void* h, const double* kappa, const double* k6, const double* mu, double* vals, int reverse) {
   Space* S = (Space*)h;
   if (S->rowptr.empty()) build_graph(*S);
   std::memset(vals, 0, S->colind.size() * sizeof(double));
@@ -557,7 +589,7 @@ int orc_assemble(void* h, const double* kappa, const double* mu, double* vals, i
     std::vector<double> K;
 #pragma omp for schedule(dynamic, 16)
     for (int e = 0; e < S->ne; e++) {
-      element_matrix(*S, e, kappa ? kappa[e] : 1.0, mu ? mu[e] : 0.0, K, reverse);
+      element_matrix(*S, e, kappa ? kappa[e] : 1.0, mu ? mu[e] : 0.0, K, reverse, k6 ? k6 + 6 * (size_t)e : nullptr);
       if (!add_element_matrix(*S, &S->edofs[(size_t)e * S->nloc], K, vals)) {
 #pragma omp atomic write
         bad = 1;
@@ -565,6 +597,13 @@ int orc_assemble(void* h, const double* kappa, const double* mu, double* vals, i
     }
   }
   return bad ? -1 : 0;
+}
+int orc_assemble(void* h, const double* kappa, const double* mu, double* vals, int reverse) {
+  return assemble_impl(h, kappa, nullptr, mu, vals, reverse);
+}
+// anisotropic diffusion: k6[e*6 .. e*6+5] = (xx yy zz xy xz yz) of element e's tensor
+int orc_assemble_k6(void* h, const double* k6, const double* mu, double* vals, int reverse) {
+  return assemble_impl(h, nullptr, k6, mu, vals, reverse);
 }
 void orc_element_matrix(void* h, int e, double kappa, double mu, double* K) {
   std::vector<double> Kv; element_matrix(*(Space*)h, e, kappa, mu, Kv);
@@ -585,7 +624,8 @@ void orc_spmv(long n, const long* rowptr, const int* colind, const double* vals,
 // (S_BilinearForm::AddMatrix1 comp/bilinearform.cpp:4668-4760 with
 // SymbolicBFI::ApplyElementMatrix fem/symbolicintegrator.cpp:2959-3040):
 // y = A x over elements [e0,e1) (whole mesh when e1<0), no element matrix formed.
-void orc_apply_mf(void* h, const double* kappa, const double* mu, const double* x, double* y, int e0, int e1) {
+static void apply_mf_impl(void* h, const double* kappa, const double* k6, const double* mu, const double* x, double* y,
+                          int e0, int e1) {
   Space* S = (Space*)h;
   if (e1 < 0) e1 = S->ne;
   // a partial range (a timing sample) expects a zeroed y from the caller
@@ -602,7 +642,9 @@ void orc_apply_mf(void* h, const double* kappa, const double* mu, const double* 
       const long* dn = &S->edofs[(size_t)e * n];
       for (int i = 0; i < n; i++) { xe[i] = x[dn[i]]; ye[i] = 0; }
       double ka = kappa ? kappa[e] : 1.0, m = mu ? mu[e] : 0.0;
-      if (ka != 0.0)
+      double kt[9];
+      if (k6) tensor33(k6 + 6 * (size_t)e, kt);
+      if (k6 || ka != 0.0)
         for (int q = 0; q < r.size(); q++) {
           shape_ad(*S, e, r.x[q], r.y[q], r.z[q], sh.data());
           Geo g = geometry(*S, e, r.x[q], r.y[q], r.z[q]);
@@ -611,6 +653,11 @@ void orc_apply_mf(void* h, const double* kappa, const double* mu, const double* 
           double gp[3];  // physical gradient J^{-T} gr
           for (int k = 0; k < 3; k++) gp[k] = g.Jinv[0 * 3 + k] * gr[0] + g.Jinv[1 * 3 + k] * gr[1] + g.Jinv[2 * 3 + k] * gr[2];
           double fac = ka * r.w[q] * std::fabs(g.det);
+          if (k6) {  // flux K gp; the weight carries no kappa
+            const double g0 = gp[0], g1 = gp[1], g2 = gp[2];
+            for (int k = 0; k < 3; k++) gp[k] = kt[3 * k] * g0 + kt[3 * k + 1] * g1 + kt[3 * k + 2] * g2;
+            fac = r.w[q] * std::fabs(g.det);
+          }
           double fl[3];   // flux back to reference: J^{-1} (fac*gp)
           for (int k = 0; k < 3; k++) fl[k] = fac * (g.Jinv[3 * k + 0] * gp[0] + g.Jinv[3 * k + 1] * gp[1] + g.Jinv[3 * k + 2] * gp[2]);
           for (int i = 0; i < n; i++) ye[i] += sh[i].d[0] * fl[0] + sh[i].d[1] * fl[1] + sh[i].d[2] * fl[2];
@@ -629,6 +676,13 @@ void orc_apply_mf(void* h, const double* kappa, const double* mu, const double* 
       }
     }
   }
+}
+
+void orc_apply_mf(void* h, const double* kappa, const double* mu, const double* x, double* y, int e0, int e1) {
+  apply_mf_impl(h, kappa, nullptr, mu, x, y, e0, e1);
+}
+void orc_apply_mf_k6(void* h, const double* k6, const double* mu, const double* x, double* y, int e0, int e1) {
+  apply_mf_impl(h, nullptr, k6, mu, x, y, e0, e1);
 }
 
 // LinearForm f*v with f piecewise constant per element, integration order 2p

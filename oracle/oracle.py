@@ -48,6 +48,8 @@ def lib():
         L.orc_graph.argtypes = [P]
         L.orc_graph_get.argtypes = [P, P, P]
         L.orc_assemble.argtypes = [P, P, P, P, i]
+        L.orc_assemble_k6.argtypes = [P, P, P, P, i]
+        L.orc_apply_mf_k6.argtypes = [P, P, P, P, P, i, i]
         L.orc_element_matrix.argtypes = [P, i, d, d, P]
         L.orc_spmv.argtypes = [l, P, P, P, d, P, P, i]
         L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
@@ -116,14 +118,20 @@ class OracleSpace:
             self._csr = (rowptr, colind)
         return self._csr
 
-    def assemble(self, kappa=None, mu=None, reverse=False):
+    def assemble(self, kappa=None, mu=None, reverse=False, K6=None):
         """CSR of the assembled form; reverse=True sums quadrature points in the
-        opposite order (the rounding noise of the algorithm)."""
+        opposite order (the rounding noise of the algorithm).  K6 (ne, 6): the
+        element-wise symmetric diffusion tensor (xx yy zz xy xz yz) in place of
+        kappa."""
         rowptr, colind = self.graph()
         vals = np.zeros(len(colind), dtype=np.float64)
         k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
         m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
-        rc = lib().orc_assemble(self.h, _p(k), _p(m), _p(vals), 1 if reverse else 0)
+        if K6 is not None:
+            k6 = np.ascontiguousarray(K6, dtype=np.float64).reshape(self.ne, 6)
+            rc = lib().orc_assemble_k6(self.h, _p(k6), _p(m), _p(vals), 1 if reverse else 0)
+        else:
+            rc = lib().orc_assemble(self.h, _p(k), _p(m), _p(vals), 1 if reverse else 0)
         if rc != 0:
             raise RuntimeError("illegal dnums in AddElementMatrix")
         return rowptr, colind, vals
@@ -133,12 +141,16 @@ class OracleSpace:
         lib().orc_element_matrix(self.h, int(e), float(kappa), float(mu), _p(K))
         return K
 
-    def apply_mf(self, x, kappa=None, mu=None, e0=0, e1=-1):
+    def apply_mf(self, x, kappa=None, mu=None, e0=0, e1=-1, K6=None):
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros(self.ndof)
         k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
         m = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
-        lib().orc_apply_mf(self.h, _p(k), _p(m), _p(x), _p(y), int(e0), int(e1))
+        if K6 is not None:
+            k6 = np.ascontiguousarray(K6, dtype=np.float64).reshape(self.ne, 6)
+            lib().orc_apply_mf_k6(self.h, _p(k6), _p(m), _p(x), _p(y), int(e0), int(e1))
+        else:
+            lib().orc_apply_mf(self.h, _p(k), _p(m), _p(x), _p(y), int(e0), int(e1))
         return y
 
     def rhs(self, f_elem):

@@ -1,0 +1,148 @@
+"""Anisotropic diffusion InnerProduct(K * grad(u), grad(v)) with one symmetric
+tensor per element (gh1_form_set_tensor) against the oracle's tensor path."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior
+from tests.util import lognormal, csr_rowscaled_close, assert_cg_history_close
+
+pytestmark = pytest.mark.gpu
+
+
+def _mesh(kind, n, jitter, seed=51):
+    m = MakeStructured3DMesh(hexes=(kind == "hex"), nx=n)
+    return JitterInterior(m, jitter / n, seed) if jitter else m
+
+
+def _tensors(ne, seed):
+    """Symmetric positive definite (ne, 3, 3) and its (xx yy zz xy xz yz) rows."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(ne, 3, 3))
+    K = A @ A.transpose(0, 2, 1) + 0.5 * np.eye(3)
+    return K, np.stack([K[:, 0, 0], K[:, 1, 1], K[:, 2, 2], K[:, 0, 1], K[:, 0, 2], K[:, 1, 2]], axis=1)
+
+
+def _form(gpu, fes, K, mu=None, kappa=None, **kw):
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes, **kw)
+    a += gpu.InnerProduct(gpu.CoefficientFunction(K) * gpu.grad(u), gpu.grad(v)) * gpu.dx
+    if kappa is not None:
+        a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    if mu is not None:
+        a += gpu.CoefficientFunction(mu) * u * v * gpu.dx
+    return a.Assemble()
+
+
+@pytest.mark.parametrize("kind,p,jit,mass", [("hex", 2, 0.1, True), ("hex", 3, 0.0, False), ("hex", 4, 0.0, True),
+                                             ("hex", 5, 0.1, False), ("tet", 3, 0.2, True)])
+def test_tensor_apply_parity(gpu, kind, p, jit, mass):
+    """Matrix-free apply (per-point metric on jittered hexes, the per-element
+    metric variants on affine hexes, tets) in FP64 (1e-12) and FP32 (2e-5)."""
+    m = _mesh(kind, 3, jit)
+    K, K6 = _tensors(m.ne, 52)
+    mu = lognormal(m.ne, 0.5, 53) if mass else None
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, K, mu=mu, nonassemble=True, precision="fp32")
+    S = O.OracleSpace(m.points, m.elements, p)
+    x = np.random.default_rng(54).normal(size=fes.ndof)
+    yo = S.apply_mf(x, K6=K6, mu=mu)
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    a.mat.Mult(xv, yv)
+    sc = np.abs(yo).max()
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * sc
+    x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+    a.mat.Mult(x32, y32)
+    assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * sc
+
+
+@pytest.mark.parametrize("kind,p", [("hex", 2), ("hex", 3), ("tet", 2)])
+def test_tensor_assemble_parity(gpu, kind, p):
+    """CSR pattern bit-exact and entries within 1e-12 (row-scaled) of the oracle."""
+    m = _mesh(kind, 3, 0.15)
+    K, K6 = _tensors(m.ne, 55)
+    mu = lognormal(m.ne, 0.5, 56)
+    kappa = lognormal(m.ne, 1.0, 57)
+    fes = gpu.H1(m, order=p)
+    a = _form(gpu, fes, K, mu=mu, kappa=kappa)
+    rp, ci, va = a.mat.CSR()
+    S = O.OracleSpace(m.points, m.elements, p)
+    Kt = K6.copy()
+    Kt[:, :3] += kappa[:, None]  # the scalar term adds kappa I
+    orp, oci, ova = S.assemble(K6=Kt, mu=mu)
+    _, _, noise = S.assemble(K6=Kt, mu=mu, reverse=True)
+    csr_rowscaled_close(rp, ci, va, orp, oci, ova, noise=noise)
+
+
+def test_tensor_kappa_identity_and_reset(gpu):
+    """K = kappa I as a tensor gives the scalar-kappa operator; clearing the
+    tensor (gh1_form_set_tensor with NULL) returns an existing matrix-free
+    operator to kappa at its next apply."""
+    m = _mesh("hex", 3, 0.1)
+    kappa = lognormal(m.ne, 1.0, 58)
+    fes = gpu.H1(m, order=3)
+    K = kappa[:, None, None] * np.eye(3)
+    a = _form(gpu, fes, K, nonassemble=True)
+    S = O.OracleSpace(m.points, m.elements, 3)
+    x = np.random.default_rng(59).normal(size=fes.ndof)
+    yo = S.apply_mf(x, kappa=kappa)
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    a.mat.Mult(xv, yv)
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
+    # a form with kappa and a tensor; clearing the tensor leaves kappa grad.grad
+    _, K6 = _tensors(m.ne, 60)
+    b = _form(gpu, fes, _tensors(m.ne, 60)[0], kappa=kappa, nonassemble=True)
+    lib = fes.ctx.lib
+    b.mat.Mult(xv, yv)
+    yt = S.apply_mf(x, K6=K6 + np.hstack([np.repeat(kappa[:, None], 3, 1), np.zeros((m.ne, 3))]))
+    assert np.abs(yv.NumPy() - yt).max() <= 1e-12 * np.abs(yt).max()
+    assert lib.gh1_form_set_tensor(b._form, None, 0) == 0
+    b.mat.Mult(xv, yv)
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
+    assert lib.gh1_form_set_tensor(b._form, None, 7) == 1  # bad memory kind
+
+
+def test_tensor_cg_and_adjoint(gpu):
+    """FP64 PCG on an anisotropic problem follows the oracle's CG (iterations
+    within one, residual history, solution 1e-9); mixed precision reaches a true
+    relative residual of 1e-10; the adjoint kappa-gradient rejects a tensor form."""
+    m = _mesh("hex", 4, 0.0)
+    K, K6 = _tensors(m.ne, 61)
+    f = np.random.default_rng(62).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=3, dirichlet=".*")
+    a = _form(gpu, fes, K, nonassemble=True, precision="fp32")
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    sol = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=5000, printrates=False)
+    solver = gpu.solvers.CG.last_solver
+    S = O.OracleSpace(m.points, m.elements, 3)
+    orp, oci, ova = S.assemble(K6=K6)
+    d = ova[[orp[i] + np.searchsorted(oci[orp[i]:orp[i + 1]], i) for i in range(S.ndof)]]
+    inv = np.where(S.freedofs().astype(bool), 1.0 / d, 0.0)
+    xo, its, hist = S.cg(S.rhs(f), inv, tol=1e-10, maxit=5000, csr=(orp, oci, ova))
+    assert abs(solver.iterations - its) <= 1
+    assert_cg_history_close(solver.residuals, hist)
+    assert np.abs(sol.NumPy() - xo).max() <= 1e-9 * np.abs(xo).max()
+    gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=20000, printrates=False,
+                   mode="mixed", stop_rule="true")
+    r = gpu.solvers.CG.last_solver.result
+    assert r.status == 0 and r.true_relres <= 1e-10
+    n = fes.ndof
+    bufs = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(4)]
+    g = torch.zeros(m.ne, dtype=torch.float64, device="cuda")
+    J = ctypes.c_double()
+    rc = fes.ctx.lib.gh1_adjoint_grad(a._form, ctypes.c_void_p(bufs[0].data_ptr()), ctypes.c_void_p(bufs[1].data_ptr()),
+                                      1e-8, ctypes.c_void_p(bufs[2].data_ptr()), ctypes.c_void_p(bufs[3].data_ptr()),
+                                      ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(ctypes.addressof(J)))
+    assert rc == 4

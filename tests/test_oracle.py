@@ -239,3 +239,48 @@ def test_vol_reader_roundtrip(tmp_path):
         fh.write("endmesh\n")
     r = ReadVolMesh(str(path))
     assert np.array_equal(r.elements, m.elements) and np.allclose(r.points, m.points)
+
+
+def _spd_tensors(ne, seed):
+    """Element-wise symmetric positive definite tensors as (xx yy zz xy xz yz)."""
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(ne, 3, 3))
+    K = A @ A.transpose(0, 2, 1) + 0.5 * np.eye(3)
+    return np.stack([K[:, 0, 0], K[:, 1, 1], K[:, 2, 2], K[:, 0, 1], K[:, 0, 2], K[:, 1, 2]], axis=1)
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 2), (False, 2), (True, 3)])
+def test_oracle_tensor_diffusion(hexes, p):
+    """(K grad u).grad v with an element-wise tensor: u = x + 2y + 3z (exact in
+    the vertex functions on the unit cube) gives u^T A u = g^T K g, g = (1,2,3),
+    for a constant K (this pins the placement of every off-diagonal entry);
+    K = kappa I reproduces the scalar-kappa matrix; the matrix-free apply equals
+    the assembled matrix; the operator is linear in K."""
+    m = MakeStructured3DMesh(hexes=hexes, nx=2)
+    S = O.OracleSpace(m.points, m.elements, p)
+    K1 = np.array([2.0, 3.0, 5.0, 0.7, -0.4, 1.1])
+    rp, ci, va = S.assemble(K6=np.tile(K1, (S.ne, 1)))
+    A = sp.csr_matrix((va, ci, rp), shape=(S.ndof, S.ndof))
+    u = np.zeros(S.ndof)
+    P = m.points
+    u[:len(P)] = P[:, 0] + 2 * P[:, 1] + 3 * P[:, 2]
+    g = np.array([1.0, 2.0, 3.0])
+    Km = np.array([[K1[0], K1[3], K1[4]], [K1[3], K1[1], K1[5]], [K1[4], K1[5], K1[2]]])
+    assert abs(u @ (A @ u) - g @ Km @ g) < 1e-12 * abs(g @ Km @ g)
+    # kappa I
+    m2 = JitterInterior(MakeStructured3DMesh(hexes=hexes, nx=3), 0.08, 3)
+    S2 = O.OracleSpace(m2.points, m2.elements, p)
+    kap = lognormal(S2.ne, 1.0, 4)
+    _, _, v_iso = S2.assemble(kappa=kap)
+    _, _, v_ten = S2.assemble(K6=np.stack([kap, kap, kap, 0 * kap, 0 * kap, 0 * kap], axis=1))
+    assert np.abs(v_ten - v_iso).max() <= 1e-14 * np.abs(v_iso).max()
+    # matrix-free = assembled, and linearity in K
+    Ka, Kb = _spd_tensors(S2.ne, 5), _spd_tensors(S2.ne, 6)
+    mu = lognormal(S2.ne, 0.5, 7)
+    rp2, ci2, va_a = S2.assemble(K6=Ka, mu=mu)
+    x = np.random.default_rng(8).normal(size=S2.ndof)
+    y = S2.apply_mf(x, K6=Ka, mu=mu)
+    assert np.abs(y - O.spmv(rp2, ci2, va_a, x)).max() <= 1e-13 * np.abs(y).max()
+    _, _, va_b = S2.assemble(K6=Kb)
+    _, _, va_ab = S2.assemble(K6=Ka + Kb, mu=mu)
+    assert np.abs(va_ab - (va_a + va_b)).max() <= 1e-13 * np.abs(va_ab).max()
