@@ -498,6 +498,27 @@ class BaseMatrix:
     def MultAdd(self, s, x, y):
         self._apply(s, x, y, 1)
 
+    # Every operator on this path is symmetric: sum_e B^T G B with a symmetric G
+    # (scalar kappa, a symmetric tensor, the mass term), the Jacobi diagonal and
+    # the projectors.  So the transpose products apply the same operator.
+    def MultTrans(self, value, x, y):
+        """y = A^T x.  As in the reference binding (linalg/python_linalg.cpp:1074),
+        y is cleared and A^T x added; `value` is accepted and not applied."""
+        self._apply(1.0, x, y, 0)
+
+    def MultTransAdd(self, value, x, y):
+        """y += value * A^T x (linalg/python_linalg.cpp:1075)."""
+        self._apply(value, x, y, 1)
+
+    @property
+    def T(self):
+        """The transpose: this operator itself (it is symmetric)."""
+        return self
+
+    @property
+    def shape(self):
+        return (self.height, self.width)
+
     def CreateSmoother(self, freedofs=None):
         return JacobiPrecond(self, freedofs)
 

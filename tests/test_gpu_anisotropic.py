@@ -108,6 +108,13 @@ def test_tensor_kappa_identity_and_reset(gpu):
     b.mat.Mult(xv, yv)
     assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
     assert lib.gh1_form_set_tensor(b._form, None, 7) == 1  # bad memory kind
+    # transpose products of the (symmetric) operator, with the reference's
+    # Python semantics: MultTrans ignores its value, MultTransAdd scales
+    assert b.mat.shape == (fes.ndof, fes.ndof) and b.mat.T is b.mat
+    b.mat.MultTrans(3.0, xv, yv)
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
+    b.mat.MultTransAdd(-0.5, xv, yv)
+    assert np.abs(yv.NumPy() - 0.5 * yo).max() <= 1e-12 * np.abs(yo).max()
 
 
 def test_tensor_cg_and_adjoint(gpu):
