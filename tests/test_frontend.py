@@ -1,0 +1,72 @@
+"""Host logic of the Python front end (no GPU): coefficient parsing and the
+classification of integrands into the forms the library runs."""
+import numpy as np
+import pytest
+
+from ngsolve_gb300 import comp as C
+
+
+class _Space:  # the proxies only need the element count
+    ne = 4
+
+
+def _uv():
+    fes = _Space()
+    return C._Proxy(fes, False), C._Proxy(fes, True)
+
+
+def test_scalar_and_elementwise_coefficients():
+    cf = C.CoefficientFunction(2.5)
+    assert np.array_equal(cf.element_values(4), np.full(4, 2.5))
+    v = np.arange(4.0)
+    assert np.array_equal(C.CoefficientFunction(v).element_values(4), v)
+    with pytest.raises(ValueError):
+        C.CoefficientFunction(np.arange(3.0)).element_values(4)
+
+
+def test_tensor_coefficients():
+    """dims=(3, 3) takes 9 row-major entries, scalar or per element; the tensor
+    goes to the library as (xx yy zz xy xz yz); non-symmetric tensors and
+    tensors used as scalars are rejected; a tuple of 3 arrays stays a vector."""
+    K = C.CoefficientFunction((1, 0.5, 0.2, 0.5, 2, 0.1, 0.2, 0.1, 3), dims=(3, 3))
+    assert K.is_tensor()
+    assert np.array_equal(K.tensor_values(4), np.tile([1, 2, 3, 0.5, 0.2, 0.1], (4, 1)))
+    a = np.arange(1.0, 5.0)
+    Ke = C.CoefficientFunction((a, 0, 0, 0, 2 * a, 0, 0, 0, 3), dims=(3, 3))
+    t = Ke.tensor_values(4)
+    assert np.array_equal(t[:, 0], a) and np.array_equal(t[:, 1], 2 * a) and np.all(t[:, 2] == 3)
+    assert C.CoefficientFunction(np.eye(3)[None].repeat(4, 0)).is_tensor()
+    with pytest.raises(ValueError):
+        C.CoefficientFunction(np.array([[1, 2, 0], [0, 1, 0], [0, 0, 1.0]])).tensor_values(4)
+    with pytest.raises(ValueError):
+        K.element_values(4)
+    with pytest.raises(ValueError):
+        C.CoefficientFunction((1, 2, 3), dims=(3, 3))
+    assert not C.CoefficientFunction((a, a, a)).is_tensor()
+    with pytest.raises(ValueError):
+        C.CoefficientFunction(np.eye(3)[None].repeat(3, 0)).tensor_values(4)
+
+
+def test_classify_integrands():
+    u, v = _uv()
+    kap = np.arange(1.0, 5.0)
+    kind, coef = (C.CoefficientFunction(kap) * C.grad(u) * C.grad(v) * C.dx).classify(4)
+    assert kind == "laplace" and np.array_equal(coef, kap)
+    kind, coef = (3.0 * C.InnerProduct(C.grad(u), C.grad(v)) * C.dx).classify(4)
+    assert kind == "laplace" and np.all(coef == 3.0)
+    kind, coef = (C.InnerProduct(u, v) * C.dx).classify(4)
+    assert kind == "mass" and np.all(coef == 1.0)
+    kind, coef = (C.CoefficientFunction(kap) * v * C.dx).classify(4)
+    assert kind == "source" and np.array_equal(coef, kap)
+    K = C.CoefficientFunction(np.diag([1.0, 2.0, 3.0]))
+    kind, coef = (C.CoefficientFunction(kap) * C.InnerProduct(K * C.grad(u), C.grad(v)) * C.dx).classify(4)
+    assert kind == "laplace_tensor" and coef.shape == (4, 6)
+    assert np.array_equal(coef[:, 1], 2 * kap) and np.all(coef[:, 3:] == 0)
+    with pytest.raises(ValueError):  # no measure
+        (C.grad(u) * C.grad(v)).classify(4)
+    with pytest.raises(NotImplementedError):  # a tensor outside the diffusion term
+        (K * u * v * C.dx).classify(4)
+    with pytest.raises(NotImplementedError):  # two trial functions
+        (C.grad(u) * C.grad(u) * C.dx).classify(4)
+    with pytest.raises(TypeError):
+        C.grad(2.0)
