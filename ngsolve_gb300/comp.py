@@ -678,6 +678,10 @@ class BilinearForm:
             self.kappa = self.kappa + coef
             self._has_laplace = True
         elif kind == "laplace_tensor":
+            if self._sfes is not self.fes:
+                # on VectorH1, K * grad(u) is the matrix product K (du_i/dx_j),
+                # which couples the components: not the block-diagonal operator
+                raise NotImplementedError("a tensor diffusion term is on the path for scalar H1 only")
             self.K6 = coef if self.K6 is None else self.K6 + coef
             self._has_laplace = True
         elif kind == "mass":

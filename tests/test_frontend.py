@@ -70,3 +70,17 @@ def test_classify_integrands():
         (C.grad(u) * C.grad(u) * C.dx).classify(4)
     with pytest.raises(TypeError):
         C.grad(2.0)
+
+
+def test_vector_space_rejects_tensor_term():
+    """On VectorH1, K * grad(u) multiplies the Jacobian of u and couples the
+    components, so the block-diagonal operator cannot represent it."""
+    class _Vec(C.VectorH1):
+        def __init__(self):  # no GPU space: only what BilinearForm reads
+            self.scalar, self.dim, self.ne, self.ndof = _Space(), 3, 4, 12
+    fes = _Vec()
+    u, v = C._Proxy(fes, False), C._Proxy(fes, True)
+    a = C.BilinearForm(fes)
+    a += C.InnerProduct(C.grad(u), C.grad(v)) * C.dx
+    with pytest.raises(NotImplementedError):
+        a += C.InnerProduct(C.CoefficientFunction(np.eye(3)) * C.grad(u), C.grad(v)) * C.dx
