@@ -68,6 +68,14 @@ int gh1_mesh_upload(gh1_ctx* ctx, int nv, const double* coords /*nv*3*/, int ne,
 int gh1_mesh_free(gh1_mesh* mesh);
 /* dirichlet: 1 = all boundary DOFs are Dirichlet (dirichlet=".*"), 0 = none */
 int gh1_space_h1(gh1_mesh* mesh, int order, int dirichlet, gh1_space** space);
+/* H1 space with Dirichlet conditions on the listed boundary faces only: the
+ * FESpace "dirichlet" regular expression resolved to the boundary elements
+ * whose condition name it matches (comp/fespace.cpp:440-516, 765-830); the
+ * DOFs of those faces, of their edges and of their vertices are not free.
+ * faces: host int32[nbf*3] (tets) or [nbf*4] (hexes), vertex numbers in any
+ * order.  A face that is not a face of the mesh, or an interior face, is
+ * GH1_ERR_ARG; nbf = 0 leaves every DOF free.                                */
+int gh1_space_h1_bnd(gh1_mesh* mesh, int order, int64_t nbf, const int32_t* faces, gh1_space** space);
 int gh1_space_free(gh1_space* space);
 /* info[0..5] = ndof, nloc, nedges, nfaces, nfree, ne */
 int gh1_space_info(gh1_space* space, int64_t* info);

@@ -49,6 +49,7 @@ SIGNATURES = {
     "gh1_mesh_upload": [_P, _I, _P, _I, _I, _P, _PP],
     "gh1_mesh_free": [_P],
     "gh1_space_h1": [_P, _I, _I, _PP],
+    "gh1_space_h1_bnd": [_P, _I, _L, _P, _PP],
     "gh1_space_free": [_P],
     "gh1_space_info": [_P, _P],
     "gh1_space_get_dofs": [_P, _P],

@@ -19,6 +19,7 @@ python/krylovspace.py (solvers.CG).  Coefficients are per-element constants
 numerical call goes to libgh1.so on the GPU; there is no CPU path.
 """
 import ctypes
+import re
 
 import numpy as np
 import torch
@@ -228,6 +229,22 @@ class _Product:
         raise NotImplementedError("only kappa*grad(u)*grad(v)*dx, mu*u*v*dx and f*v*dx are on the H1 path")
 
 
+def _dirichlet_faces(raw, dirichlet):
+    """The boundary faces the "dirichlet" regular expression selects (matched in
+    full against each boundary-condition name, comp/fespace.cpp:440-516), or
+    None where the all-or-nothing flag says the same: no Dirichlet boundary, a
+    regex matching every name, or a mesh without named boundaries (where any
+    non-empty dirichlet means the whole boundary)."""
+    if dirichlet in ("", None, False) or dirichlet is True or raw.bc_names is None:
+        return None
+    if not isinstance(dirichlet, str):
+        raise TypeError("dirichlet is a regular expression over the boundary names")
+    pat = re.compile(dirichlet)
+    if all(pat.fullmatch(n) is not None for n in raw.bc_names):
+        return None
+    return np.ascontiguousarray(raw.BoundaryFaces(dirichlet), dtype=np.int32)
+
+
 # ---------------------------------------------------------------------------
 class H1:
     """H1HighOrderFESpace of uniform order (comp/h1hofespace.cpp)."""
@@ -238,9 +255,14 @@ class H1:
         self.mesh = mesh
         self.order = int(order)
         self.ctx = mesh.ctx
-        dir_all = 1 if dirichlet not in ("", None, False) else 0
+        faces = _dirichlet_faces(mesh.raw, dirichlet)
         h = ctypes.c_void_p()
-        self.ctx.check(self.ctx.lib.gh1_space_h1(mesh.h, self.order, dir_all, ctypes.byref(h)))
+        if faces is None:
+            dir_all = 1 if dirichlet not in ("", None, False) else 0
+            self.ctx.check(self.ctx.lib.gh1_space_h1(mesh.h, self.order, dir_all, ctypes.byref(h)))
+        else:
+            self.ctx.check(self.ctx.lib.gh1_space_h1_bnd(mesh.h, self.order, len(faces), _np_ptr(faces),
+                                                         ctypes.byref(h)))
         self.h = h
         info = np.zeros(6, dtype=np.int64)
         self.ctx.check(self.ctx.lib.gh1_space_info(h, _np_ptr(info)))

@@ -141,15 +141,33 @@ void build_space(gh1_space* sp) {
     for (int k = 0; k < sp->n_cell_dofs; k++) d[ii++] = (int32_t)(sp->first_cell + e * sp->n_cell_dofs + k);
   });
 
-  // boundary faces (one adjacent element) -> Dirichlet DOFs
+  // Dirichlet faces: every boundary face (one adjacent element), or the
+  // caller's selection of boundary faces -> their closure's DOFs are not free
   std::vector<int32_t> fcount(sp->nfa, 0);
   for (size_t k = 0; k < el_faces.size(); k++) fcount[el_faces[k]]++;
+  std::vector<uint8_t> fdir(sp->nfa, 0);
+  if (sp->dir_select) {
+    std::vector<std::array<int32_t, 4>> sel = sp->dir_faces;
+    std::sort(sel.begin(), sel.end());
+    sel.erase(std::unique(sel.begin(), sel.end()), sel.end());
+    std::vector<uint8_t> found(sel.size(), 0);
+    for (size_t k = 0; k < fkeys.size(); k++) {
+      auto it = std::lower_bound(sel.begin(), sel.end(), fkeys[k]);
+      if (it == sel.end() || *it != fkeys[k]) continue;
+      GH1_CHECK(fcount[el_faces[k]] == 1, GH1_ERR_ARG, "a Dirichlet face is an interior face");
+      fdir[el_faces[k]] = 1;
+      found[it - sel.begin()] = 1;
+    }
+    for (auto v : found) GH1_CHECK(v, GH1_ERR_ARG, "a Dirichlet face is not a face of the mesh");
+  } else {
+    for (int f = 0; f < sp->nfa; f++) fdir[f] = fcount[f] == 1;
+  }
   sp->freedof.assign(sp->ndof, 1);
   if (sp->mesh && sp->freedof.size()) {
     for (int e = 0; e < ne; e++)
       for (int i = 0; i < sp->nface; i++) {
         int f = el_faces[(size_t)e * sp->nface + i];
-        if (fcount[f] != 1) continue;
+        if (!fdir[f]) continue;
         for (int k = 0; k < sp->n_face_dofs; k++) sp->freedof[sp->first_face + (int64_t)f * sp->n_face_dofs + k] = 0;
         for (int j = 0; j < fv; j++) sp->freedof[ev(e, lface(i, j))] = 0;
         for (int j = 0; j < fv; j++) {
@@ -397,6 +415,34 @@ int gh1_space_h1(gh1_mesh* m, int order, int dirichlet, gh1_space** out) {
         sp->d_free.upload(sp->freedof, sp->ctx->stream);
         GH1_CUDA(cudaStreamSynchronize(sp->ctx->stream));
       }
+    } catch (...) { delete sp; throw; }
+    *out = sp;
+  });
+}
+
+int gh1_space_h1_bnd(gh1_mesh* m, int order, int64_t nbf, const int32_t* faces, gh1_space** out) {
+  if (!m || !out || nbf < 0 || (nbf > 0 && !faces)) return GH1_ERR_ARG;
+  return guard(m->ctx, [&] {
+    int maxp = m->et == 4 ? MAX_TET_ORDER : MAX_HEX_ORDER;
+    GH1_CHECK(order >= 1 && order <= maxp, GH1_ERR_UNSUPPORTED, "order out of the supported range");
+    GH1_CUDA(cudaSetDevice(m->ctx->device));
+    gh1_space* sp = new gh1_space();
+    sp->ctx = m->ctx; sp->mesh = m; sp->p = order;
+    try {
+      const int fv = m->et == 4 ? 3 : 4;
+      sp->dir_select = true;
+      sp->dir_faces.resize(nbf);
+      for (int64_t k = 0; k < nbf; k++) {
+        std::array<int32_t, 4> t{INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
+        for (int j = 0; j < fv; j++) {
+          t[j] = faces[k * fv + j];
+          GH1_CHECK(t[j] >= 0 && t[j] < m->nv, GH1_ERR_ARG, "Dirichlet face vertex out of range");
+        }
+        std::sort(t.begin(), t.begin() + fv);
+        sp->dir_faces[k] = t;
+      }
+      build_space(sp);
+      sp->dir_faces = {};
     } catch (...) { delete sp; throw; }
     *out = sp;
   });

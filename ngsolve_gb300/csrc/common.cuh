@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <string>
 #include <vector>
+#include <array>
 #include <stdexcept>
 #include <cstdio>
 #include "../../include/gh1.h"
@@ -93,6 +94,10 @@ struct gh1_space {
   int64_t first_edge = 0, first_face = 0, first_cell = 0;
   std::vector<int32_t> el_dofs;   // ne*nloc, reference local order
   std::vector<uint8_t> freedof;   // ndof
+  // Dirichlet on the caller's boundary faces only (sorted vertex numbers,
+  // padded with INT32_MAX); read by the space construction, then released
+  bool dir_select = false;
+  std::vector<std::array<int32_t, 4>> dir_faces;
   gh1::DBuf<int32_t> d_eldofs;    // ne*nloc (reference local order)
   gh1::DBuf<uint8_t> d_free;      // ndof
   // hex: tensor-ordered signed DOF table  tdof[e*tstride + (a*n+b)*n+c] = dof | (sign<0 ? 1<<31 : 0);

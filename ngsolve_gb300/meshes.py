@@ -9,18 +9,34 @@ vertex lists identical keeps the element orientation classes identical, which
 fixes the orientation of every edge and face shape function.
 
 ``ReadVolMesh`` reads the ASCII netgen ``.vol`` / ``.vol.gz`` format (the
-``volumeelements`` and ``points`` sections) used by the reference test meshes.
+``points``, ``volumeelements``, ``surfaceelements`` and ``bcnames`` sections)
+used by the reference test meshes.
+
+Boundary faces carry a boundary-condition name, as netgen's surface elements
+do, so that ``H1(mesh, dirichlet="left|top")`` can select them by regular
+expression.
 """
 import gzip
+import re
 
 import numpy as np
+
+# local faces of the reference hex (vertices 0-3 bottom, 4-7 top) and tet
+_HEX_FACES = np.array([[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7]])
+_TET_FACES = np.array([[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]])
+# names of the structured cube's sides (python/meshes.py:457-475 of NGSolve)
+_CUBE_SIDES = ("back", "left", "front", "right", "bottom", "top")
 
 
 class Mesh:
     """Volume mesh of one element type: ``points`` (nv,3) float64 and
-    ``elements`` (ne, 4 | 8) int32 vertex lists in the reference's local order."""
+    ``elements`` (ne, 4 | 8) int32 vertex lists in the reference's local order.
 
-    def __init__(self, points, elements):
+    Optional boundary data: ``bnd_faces`` (nbf, 3 | 4) vertex numbers of
+    boundary faces, ``bnd_index`` (nbf,) 0-based index of each face's name in
+    ``bc_names``."""
+
+    def __init__(self, points, elements, bnd_faces=None, bnd_index=None, bc_names=None):
         self.points = np.ascontiguousarray(points, dtype=np.float64)
         self.elements = np.ascontiguousarray(elements, dtype=np.int32)
         if self.elements.ndim != 2 or self.elements.shape[1] not in (4, 8):
@@ -29,6 +45,45 @@ class Mesh:
             raise ValueError("points must be (nv,3)")
         if len(self.elements) and (self.elements.min() < 0 or self.elements.max() >= len(self.points)):
             raise ValueError("element vertex index out of range")
+        self._bnd = None
+        self._bnd_fn = None
+        self.bc_names = None
+        if bnd_faces is not None:
+            faces = np.ascontiguousarray(bnd_faces, dtype=np.int32)
+            index = np.ascontiguousarray(bnd_index, dtype=np.int32)
+            if faces.ndim != 2 or faces.shape[1] != (3 if self.et == 4 else 4) or index.shape != (len(faces),):
+                raise ValueError("bnd_faces must be (nbf, %d) with one bnd_index each" % (3 if self.et == 4 else 4))
+            if len(faces) and (faces.min() < 0 or faces.max() >= self.nv):
+                raise ValueError("boundary face vertex index out of range")
+            if bc_names is None or (len(index) and (index.min() < 0 or index.max() >= len(bc_names))):
+                raise ValueError("every bnd_index needs a name in bc_names")
+            self._bnd = (faces, index)
+            self.bc_names = list(bc_names)
+
+    def _boundary(self):
+        if self._bnd is None and self._bnd_fn is not None:
+            self._bnd = self._bnd_fn()
+        return self._bnd
+
+    def GetBoundaries(self):
+        """Names of the boundary conditions (Mesh.GetBoundaries)."""
+        return tuple(self.bc_names or ())
+
+    def BoundaryFaces(self, regex):
+        """Vertex lists of the boundary faces whose name matches `regex` in full
+        (the FESpace "dirichlet" flag)."""
+        bnd = self._boundary()
+        if bnd is None:
+            raise ValueError("this mesh has no named boundary faces")
+        faces, index = bnd
+        pat = re.compile(regex)
+        hit = np.array([pat.fullmatch(n) is not None for n in self.bc_names], dtype=bool)
+        return faces[hit[index]] if len(hit) else faces[:0]
+
+    def _with_points(self, points):
+        m = Mesh(points, self.elements)
+        m._bnd, m._bnd_fn, m.bc_names = self._bnd, self._bnd_fn, self.bc_names
+        return m
 
     @property
     def et(self):
@@ -72,7 +127,26 @@ def MakeStructured3DMesh(hexes=True, nx=10, ny=None, nz=None, mapping=None):
         els = pnum
     else:
         els = pnum[:, _KUHN].reshape(-1, 4)
-    return Mesh(pts, els.astype(np.int32))
+    mesh = Mesh(pts, els.astype(np.int32))
+    mesh.bc_names = list(_CUBE_SIDES)
+    mesh._bnd_fn = lambda: _cube_boundary(mesh.elements, nx, ny, nz)
+    return mesh
+
+
+def _cube_boundary(els, nx, ny, nz):
+    """Boundary faces of the structured cube and the index of their side: an
+    element face whose vertices all lie on one side of the lattice (the
+    mapping, if any, does not change the lattice)."""
+    local = _HEX_FACES if els.shape[1] == 8 else _TET_FACES
+    F = els[:, local].reshape(-1, local.shape[1])
+    i, r = np.divmod(F, (ny + 1) * (nz + 1))
+    j, k = np.divmod(r, nz + 1)
+    faces, index = [], []
+    for side, (c, v) in enumerate(((i, 0), (j, 0), (i, nx), (j, ny), (k, 0), (k, nz))):
+        on = np.all(c == v, axis=1)
+        faces.append(F[on])
+        index.append(np.full(int(on.sum()), side, dtype=np.int32))
+    return np.ascontiguousarray(np.concatenate(faces), dtype=np.int32), np.concatenate(index)
 
 
 def MakeHexMesh(nx=10, ny=10, nz=10, mapping=None):
@@ -87,19 +161,35 @@ def JitterInterior(mesh, amplitude, seed):
     off = rng.uniform(-amplitude, amplitude, size=pts.shape)
     interior = np.all((pts > 1e-12) & (pts < 1 - 1e-12), axis=1)
     pts[interior] += off[interior]
-    return Mesh(pts, mesh.elements)
+    return mesh._with_points(pts)
 
 
 def ReadVolMesh(path):
-    """Volume elements and points of an ASCII netgen mesh file."""
+    """Points, volume elements and (when present) the named boundary faces of an
+    ASCII netgen mesh file.  A surface element row is
+    ``surfnr bcnr domin domout np p1 .. p_np``; ``bcnames`` rows are
+    ``bcnr name``.  A bc number without a name gets the name ``default``."""
     opener = gzip.open if str(path).endswith(".gz") else open
     with opener(path, "rt") as fh:
         lines = fh.read().split("\n")
-    pts, els = None, None
+    pts, els, sels, names = None, None, None, {}
     n = len(lines)
     i = 0
     while i < n:
         tok = lines[i].strip()
+        if tok == "surfaceelements":
+            cnt = int(lines[i + 1].split()[0])
+            rows = [lines[i + 2 + r].split() for r in range(cnt)]
+            sels = [(int(row[1]), [int(v) - 1 for v in row[5:5 + int(row[4])]]) for row in rows]
+            i += 2 + cnt
+            continue
+        if tok == "bcnames":
+            cnt = int(lines[i + 1].split()[0])
+            for r in range(cnt):
+                nr, name = lines[i + 2 + r].split()[:2]
+                names[int(nr)] = name
+            i += 2 + cnt
+            continue
         if tok == "volumeelements":
             cnt = int(lines[i + 1].split()[0])
             rows = [lines[i + 2 + r].split() for r in range(cnt)]
@@ -114,4 +204,13 @@ def ReadVolMesh(path):
         i += 1
     if pts is None or els is None:
         raise ValueError("no points/volumeelements section in %s" % path)
-    return Mesh(np.array(pts), np.array(els, dtype=np.int32))
+    els = np.array(els, dtype=np.int32)
+    fv = 3 if els.shape[1] == 4 else 4
+    if not sels:
+        return Mesh(np.array(pts), els)
+    sels = [(bc, v) for bc, v in sels if len(v) == fv]
+    bcs = sorted({bc for bc, _ in sels})
+    slot = {bc: k for k, bc in enumerate(bcs)}
+    return Mesh(np.array(pts), els, bnd_faces=np.array([v for _, v in sels], dtype=np.int32).reshape(-1, fv),
+                bnd_index=np.array([slot[bc] for bc, _ in sels], dtype=np.int32),
+                bc_names=[names.get(bc, "default") for bc in bcs])

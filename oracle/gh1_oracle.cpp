@@ -310,6 +310,10 @@ struct Space {
   std::vector<int> el_edges, el_faces;  // global ids per element (local order)
   std::vector<long> edofs;     // ne*nloc (as long for safety)
   std::vector<unsigned char> freedof;
+  // Dirichlet on these boundary faces only (sorted vertex numbers, padded with
+  // INT32_MAX) when dir_select; dir_bad set if one is not a boundary face
+  bool dir_select = false, dir_bad = false;
+  std::vector<std::array<int, 4>> dir_faces;
   int n_edge_dofs = 0, n_face_dofs = 0, n_cell_dofs = 0;
   long first_edge = 0, first_face = 0, first_cell = 0;
   // CSR
@@ -367,13 +371,21 @@ void build_space(Space& S) {
     for (int i = 0; i < S.nface; i++) for (int k = 0; k < S.n_face_dofs; k++) d[ii++] = S.first_face + (long)S.el_faces[(size_t)e * S.nface + i] * S.n_face_dofs + k;
     for (int k = 0; k < S.n_cell_dofs; k++) d[ii++] = S.first_cell + (long)e * S.n_cell_dofs + k;
   }
-  // Dirichlet on the whole boundary (comp/fespace.cpp:440-516, :765-830):
-  // DOFs of boundary faces and of their edges and vertices are not free.
+  // Dirichlet boundary (comp/fespace.cpp:440-516, :765-830): the boundary
+  // faces (one adjacent element), or those of them the dirichlet regex
+  // selected; DOFs of these faces and of their edges and vertices are not free.
+  std::vector<char> dir(S.nfa, 0);
+  for (int f = 0; f < S.nfa; f++) dir[f] = !S.dir_select && face_count[f] == 1;
+  for (const auto& t : S.dir_faces) {
+    auto it = std::lower_bound(Fu.begin(), Fu.end(), t);
+    if (it == Fu.end() || *it != t || face_count[it - Fu.begin()] != 1) { S.dir_bad = true; continue; }
+    dir[it - Fu.begin()] = 1;
+  }
   S.freedof.assign(S.ndof, 1);
   for (int e = 0; e < S.ne; e++)
     for (int i = 0; i < S.nface; i++) {
       int f = S.el_faces[(size_t)e * S.nface + i];
-      if (face_count[f] != 1) continue;
+      if (!dir[f]) continue;
       for (int k = 0; k < S.n_face_dofs; k++) S.freedof[S.first_face + (long)f * S.n_face_dofs + k] = 0;
       const int* lf = tet ? TET_FACES[i] : HEX_FACES[i];
       for (int j = 0; j < fv; j++) S.freedof[S.el[(size_t)e * S.nvert + lf[j]]] = 0;
@@ -556,6 +568,25 @@ void* orc_space_create(int et, int nv, const double* X, int ne, const int* el, i
   S->X.assign(X, X + 3 * (size_t)nv);
   S->el.assign(el, el + (size_t)ne * (et == 4 ? 4 : 8));
   build_space(*S);
+  return S;
+}
+// a space with Dirichlet conditions on nbf given boundary faces (fv = 3 or 4
+// vertex numbers each); NULL if one of them is not a boundary face
+void* orc_space_create_bnd(int et, int nv, const double* X, int ne, const int* el, int p, long nbf, const int* faces) {
+  Space* S = new Space();
+  S->et = et; S->nv = nv; S->ne = ne; S->p = p;
+  S->X.assign(X, X + 3 * (size_t)nv);
+  S->el.assign(el, el + (size_t)ne * (et == 4 ? 4 : 8));
+  const int fv = et == 4 ? 3 : 4;
+  S->dir_select = true;
+  for (long k = 0; k < nbf; k++) {
+    std::array<int, 4> t{INT32_MAX, INT32_MAX, INT32_MAX, INT32_MAX};
+    for (int j = 0; j < fv; j++) t[j] = faces[k * fv + j];
+    std::sort(t.begin(), t.begin() + fv);
+    S->dir_faces.push_back(t);
+  }
+  build_space(*S);
+  if (S->dir_bad) { delete S; return nullptr; }
   return S;
 }
 void orc_space_destroy(void* h) { delete (Space*)h; }

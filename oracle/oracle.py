@@ -39,6 +39,8 @@ def lib():
         i, l, d = ctypes.c_int, ctypes.c_long, ctypes.c_double
         L.orc_space_create.restype = P
         L.orc_space_create.argtypes = [i, i, P, i, P, i]
+        L.orc_space_create_bnd.restype = P
+        L.orc_space_create_bnd.argtypes = [i, i, P, i, P, i, l, P]
         L.orc_space_destroy.argtypes = [P]
         L.orc_space_info.argtypes = [P, P]
         L.orc_space_dofs.argtypes = [P, P]
@@ -69,16 +71,26 @@ def _p(a):
 
 
 class OracleSpace:
-    """H1 space of uniform order p on a tet (et=4) or hex (et=8) mesh."""
+    """H1 space of uniform order p on a tet (et=4) or hex (et=8) mesh.
+    dirichlet_faces: (nbf, 3 | 4) boundary faces whose closure is Dirichlet
+    (default: the whole boundary, as freedofs() reports it)."""
 
-    def __init__(self, points, elements, order):
+    def __init__(self, points, elements, order, dirichlet_faces=None):
         self.points = np.ascontiguousarray(points, dtype=np.float64)
         self.elements = np.ascontiguousarray(elements, dtype=np.int32)
         self.et = int(self.elements.shape[1])
         self.order = int(order)
         self.ne = int(self.elements.shape[0])
-        self.h = lib().orc_space_create(self.et, len(self.points), _p(self.points), self.ne,
-                                        _p(self.elements), self.order)
+        self.h = None
+        if dirichlet_faces is None:
+            self.h = lib().orc_space_create(self.et, len(self.points), _p(self.points), self.ne,
+                                            _p(self.elements), self.order)
+        else:
+            fc = np.ascontiguousarray(dirichlet_faces, dtype=np.int32)
+            self.h = lib().orc_space_create_bnd(self.et, len(self.points), _p(self.points), self.ne,
+                                                _p(self.elements), self.order, len(fc), _p(fc))
+            if not self.h:
+                raise ValueError("a Dirichlet face is not a boundary face of the mesh")
         info = np.zeros(7, dtype=np.int64)
         lib().orc_space_info(self.h, _p(info))
         self.ndof, self.nloc, self.ned, self.nfa = (int(v) for v in info[:4])

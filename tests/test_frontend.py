@@ -84,3 +84,18 @@ def test_vector_space_rejects_tensor_term():
     a += C.InnerProduct(C.grad(u), C.grad(v)) * C.dx
     with pytest.raises(NotImplementedError):
         a += C.InnerProduct(C.CoefficientFunction(np.eye(3)) * C.grad(u), C.grad(v)) * C.dx
+
+
+def test_dirichlet_regex_resolution():
+    """None (the all-or-nothing flag) for no Dirichlet boundary, a regex that
+    matches every name, or a mesh without names; else the matched faces."""
+    from ngsolve_gb300.meshes import MakeStructured3DMesh, Mesh
+    m = MakeStructured3DMesh(hexes=True, nx=2)
+    assert C._dirichlet_faces(m, "") is None and C._dirichlet_faces(m, ".*") is None
+    assert C._dirichlet_faces(m, "back|left|front|right|bottom|top") is None
+    f = C._dirichlet_faces(m, "left|top")
+    assert f.shape == (8, 4) and f.dtype == np.int32
+    assert C._dirichlet_faces(m, "nothing").shape == (0, 4)
+    assert C._dirichlet_faces(Mesh(m.points, m.elements), "left") is None
+    with pytest.raises(TypeError):
+        C._dirichlet_faces(m, [1, 2])

@@ -284,3 +284,73 @@ def test_oracle_tensor_diffusion(hexes, p):
     _, _, va_b = S2.assemble(K6=Kb)
     _, _, va_ab = S2.assemble(K6=Ka + Kb, mu=mu)
     assert np.abs(va_ab - (va_a + va_b)).max() <= 1e-13 * np.abs(va_ab).max()
+
+
+@pytest.mark.parametrize("hexes", [True, False])
+def test_structured_boundary_names(hexes):
+    """The structured cube names its sides as the reference does: x=0 back,
+    y=0 left, x=1 front, y=1 right, z=0 bottom, z=1 top (also under a mapping,
+    which does not change the lattice); each side has n^2 quads or 2 n^2
+    triangles, and they are exactly the faces with one adjacent element."""
+    n = 3
+    m = MakeStructured3DMesh(hexes=hexes, nx=n, mapping=lambda x, y, z: (2 * x, y + 0.1 * x, z))
+    assert m.GetBoundaries() == ("back", "left", "front", "right", "bottom", "top")
+    plain = MakeStructured3DMesh(hexes=hexes, nx=n)
+    P = plain.points
+    for side, (ax, v) in enumerate(((0, 0), (1, 0), (0, 1), (1, 1), (2, 0), (2, 1))):
+        f = m.BoundaryFaces(m.GetBoundaries()[side])
+        assert len(f) == (1 if hexes else 2) * n * n
+        assert np.all(np.abs(P[f][..., ax] - v) < 1e-14)
+    S = O.OracleSpace(m.points, m.elements, 1)
+    allf = m.BoundaryFaces(".*")
+    # every boundary face once: the whole-boundary mask equals the listed faces'
+    assert np.array_equal(S.freedofs(), O.OracleSpace(m.points, m.elements, 1, dirichlet_faces=allf).freedofs())
+    assert len(np.unique(np.sort(allf, axis=1), axis=0)) == len(allf) == 6 * (1 if hexes else 2) * n * n
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 2), (True, 4), (False, 3)])
+def test_oracle_dirichlet_regions(hexes, p):
+    """Dirichlet on selected sides: exactly the DOFs of the selected faces' closure
+    (vertices, edges, faces, counted here from the faces themselves) are not
+    free; an interior face is rejected; no face leaves every DOF free."""
+    m = JitterInterior(MakeStructured3DMesh(hexes=hexes, nx=3), 0.05, 9)
+    for regex in ("bottom", "left|top", "back|front|right"):
+        faces = m.BoundaryFaces(regex)
+        S = O.OracleSpace(m.points, m.elements, p, dirichlet_faces=faces)
+        fv = faces.shape[1]
+        verts = np.unique(faces)
+        edges = np.unique(np.sort(np.stack([faces, np.roll(faces, -1, axis=1)], axis=2).reshape(-1, 2), axis=1),
+                          axis=0)
+        nfd = (p - 1) ** 2 if hexes else max(0, (p - 1) * (p - 2) // 2)
+        expect = len(verts) + len(edges) * (p - 1) + len(faces) * nfd
+        fd = S.freedofs().astype(bool)
+        assert (~fd).sum() == expect
+        assert not fd[verts].any() and fd[np.setdiff1d(np.arange(m.nv), verts)].all()
+        assert fv == (4 if hexes else 3)
+    assert O.OracleSpace(m.points, m.elements, p, dirichlet_faces=np.zeros((0, 4 if hexes else 3))).freedofs().all()
+    interior = np.sort(m.elements[:, :3] if not hexes else m.elements[:, [0, 1, 2, 3]], axis=1)
+    inner = [f for f in interior if not np.all(np.isin(f, np.unique(m.BoundaryFaces(".*"))))][:1]
+    with pytest.raises(ValueError):
+        O.OracleSpace(m.points, m.elements, p, dirichlet_faces=np.array(inner))
+
+
+def test_vol_reader_boundary_names(tmp_path):
+    """surfaceelements rows (surfnr bcnr domin domout np p1..pnp) and bcnames
+    (bcnr name) give named boundary faces; a bc number without a name is
+    "default"."""
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1.0]])
+    path = tmp_path / "t.vol"
+    with open(path, "w") as fh:
+        fh.write("mesh3d\nsurfaceelements\n4\n")
+        for bc, f in ((1, (1, 3, 2)), (1, (1, 2, 4)), (2, (1, 4, 3)), (3, (2, 3, 4))):
+            fh.write(" 1 %d 1 0 3 %d %d %d\n" % ((bc,) + f))
+        fh.write("volumeelements\n1\n1 4 1 2 3 4\npoints\n4\n")
+        for p in pts:
+            fh.write("%.16f %.16f %.16f\n" % tuple(p))
+        fh.write("bcnames\n2\n1 bottom\n2 side\nendmesh\n")
+    r = ReadVolMesh(str(path))
+    assert r.GetBoundaries() == ("bottom", "side", "default")
+    assert np.array_equal(r.BoundaryFaces("bottom"), [[0, 2, 1], [0, 1, 3]])
+    assert len(r.BoundaryFaces("side|default")) == 2 and len(r.BoundaryFaces("nothing")) == 0
+    S = O.OracleSpace(r.points, r.elements, 2, dirichlet_faces=r.BoundaryFaces("bottom"))
+    assert S.freedofs().sum() == S.ndof - (4 + 5)  # vertices 0..3 and the edges of the two faces
