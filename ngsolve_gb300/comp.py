@@ -19,7 +19,6 @@ python/krylovspace.py (solvers.CG).  Coefficients are per-element constants
 numerical call goes to libgh1.so on the GPU; there is no CPU path.
 """
 import ctypes
-import re
 
 import numpy as np
 import torch
@@ -229,18 +228,23 @@ class _Product:
         raise NotImplementedError("only kappa*grad(u)*grad(v)*dx, mu*u*v*dx and f*v*dx are on the H1 path")
 
 
+def _no_dirichlet(dirichlet):
+    return dirichlet is None or dirichlet is False or (isinstance(dirichlet, (str, list, tuple)) and len(dirichlet) == 0)
+
+
 def _dirichlet_faces(raw, dirichlet):
-    """The boundary faces the "dirichlet" regular expression selects (matched in
-    full against each boundary-condition name, comp/fespace.cpp:440-516), or
-    None where the all-or-nothing flag says the same: no Dirichlet boundary, a
-    regex matching every name, or a mesh without named boundaries (where any
-    non-empty dirichlet means the whole boundary)."""
-    if dirichlet in ("", None, False) or dirichlet is True or raw.bc_names is None:
+    """The boundary faces the "dirichlet" flag selects -- a regular expression
+    matched in full against each boundary-condition name, or a list of 1-based
+    boundary-condition numbers (comp/fespace.cpp:440-516) -- or None where the
+    all-or-nothing flag says the same: no Dirichlet boundary, a selection of
+    every name, or a mesh without named boundaries (where any non-empty
+    dirichlet means the whole boundary)."""
+    if _no_dirichlet(dirichlet) or dirichlet is True or raw.bc_names is None:
         return None
-    if not isinstance(dirichlet, str):
-        raise TypeError("dirichlet is a regular expression over the boundary names")
-    pat = re.compile(dirichlet)
-    if all(pat.fullmatch(n) is not None for n in raw.bc_names):
+    if not isinstance(dirichlet, (str, list, tuple)) or (
+            not isinstance(dirichlet, str) and not all(isinstance(k, (int, np.integer)) for k in dirichlet)):
+        raise TypeError("dirichlet is a regular expression over the boundary names or a list of their numbers")
+    if raw.SelectBoundaries(dirichlet).all():
         return None
     return np.ascontiguousarray(raw.BoundaryFaces(dirichlet), dtype=np.int32)
 
@@ -258,7 +262,7 @@ class H1:
         faces = _dirichlet_faces(mesh.raw, dirichlet)
         h = ctypes.c_void_p()
         if faces is None:
-            dir_all = 1 if dirichlet not in ("", None, False) else 0
+            dir_all = 0 if _no_dirichlet(dirichlet) else 1
             self.ctx.check(self.ctx.lib.gh1_space_h1(mesh.h, self.order, dir_all, ctypes.byref(h)))
         else:
             self.ctx.check(self.ctx.lib.gh1_space_h1_bnd(mesh.h, self.order, len(faces), _np_ptr(faces),

@@ -69,15 +69,29 @@ class Mesh:
         """Names of the boundary conditions (Mesh.GetBoundaries)."""
         return tuple(self.bc_names or ())
 
-    def BoundaryFaces(self, regex):
-        """Vertex lists of the boundary faces whose name matches `regex` in full
-        (the FESpace "dirichlet" flag)."""
+    def SelectBoundaries(self, which):
+        """Which boundary conditions the FESpace "dirichlet" flag names: a
+        regular expression matched in full against each name, or a list of
+        1-based boundary-condition numbers.  A bool per name."""
+        names = self.bc_names or []
+        if isinstance(which, str):
+            pat = re.compile(which)
+            return np.array([pat.fullmatch(n) is not None for n in names], dtype=bool)
+        nums = [int(k) for k in which]
+        if any(k < 1 or k > len(names) for k in nums):
+            raise ValueError("boundary-condition numbers run from 1 to %d" % len(names))
+        hit = np.zeros(len(names), dtype=bool)
+        hit[[k - 1 for k in nums]] = True
+        return hit
+
+    def BoundaryFaces(self, which):
+        """Vertex lists of the boundary faces that `which` (a regex or a list of
+        1-based boundary-condition numbers, see SelectBoundaries) selects."""
         bnd = self._boundary()
         if bnd is None:
             raise ValueError("this mesh has no named boundary faces")
         faces, index = bnd
-        pat = re.compile(regex)
-        hit = np.array([pat.fullmatch(n) is not None for n in self.bc_names], dtype=bool)
+        hit = self.SelectBoundaries(which)
         return faces[hit[index]] if len(hit) else faces[:0]
 
     def _with_points(self, points):

@@ -97,5 +97,13 @@ def test_dirichlet_regex_resolution():
     assert f.shape == (8, 4) and f.dtype == np.int32
     assert C._dirichlet_faces(m, "nothing").shape == (0, 4)
     assert C._dirichlet_faces(Mesh(m.points, m.elements), "left") is None
+    # 1-based boundary-condition numbers, as in H1(mesh, dirichlet=[1, 2, 3, 4])
+    assert np.array_equal(C._dirichlet_faces(m, [2, 6]), f)
+    assert C._dirichlet_faces(m, [1, 2, 3, 4, 5, 6]) is None and C._dirichlet_faces(m, []) is None
+    assert C._no_dirichlet([]) and C._no_dirichlet("") and not C._no_dirichlet(".*") and not C._no_dirichlet([1])
+    with pytest.raises(ValueError):
+        C._dirichlet_faces(m, [0])
     with pytest.raises(TypeError):
-        C._dirichlet_faces(m, [1, 2])
+        C._dirichlet_faces(m, ["left"])
+    with pytest.raises(TypeError):
+        C._dirichlet_faces(m, 3)
