@@ -4,7 +4,9 @@ Run in a container that has the reference checkout (default path below):
     python tests/golden/make_golden.py [/path/to/ngsolve]
 Writes
   cube_vol.npz   points + tet vertex lists of tests/pytest/cube.vol.gz (the
-                 mesh of tests/pytest/test_matrix.py:84-93), 0-based;
+                 mesh of tests/pytest/test_matrix.py:84-93), 0-based, and its
+                 surface elements: bnd_faces (0-based vertex triples),
+                 bnd_index (index into bc_names), bc_names;
   golden.json    the known answers quoted from the reference tests.
 The GPU tests read only these files, never the reference tree.
 """
@@ -22,7 +24,9 @@ from ngsolve_gb300.meshes import ReadVolMesh  # noqa: E402
 
 def main(ref):
     mesh = ReadVolMesh(os.path.join(ref, "tests", "pytest", "cube.vol.gz"))
-    np.savez_compressed(os.path.join(HERE, "cube_vol.npz"), points=mesh.points, tets=mesh.elements)
+    faces, index = mesh._boundary()
+    np.savez_compressed(os.path.join(HERE, "cube_vol.npz"), points=mesh.points, tets=mesh.elements,
+                        bnd_faces=faces, bnd_index=index, bc_names=np.array(mesh.bc_names))
     # reference_values of test_sparsematrix_access (tests/pytest/test_matrix.py:58-62):
     # [0] P1 mass a.mat[1,1] on square.vol.gz, [2] the same on cube.vol.gz
     src = open(os.path.join(ref, "tests", "pytest", "test_matrix.py")).read()

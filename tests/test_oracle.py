@@ -354,3 +354,30 @@ def test_vol_reader_boundary_names(tmp_path):
     assert len(r.BoundaryFaces("side|default")) == 2 and len(r.BoundaryFaces("nothing")) == 0
     S = O.OracleSpace(r.points, r.elements, 2, dirichlet_faces=r.BoundaryFaces("bottom"))
     assert S.freedofs().sum() == S.ndof - (4 + 5)  # vertices 0..3 and the edges of the two faces
+
+
+def test_cube_vol_boundary_names():
+    """The surface elements of the reference's cube.vol.gz (tests/pytest), read by
+    ReadVolMesh into the fixture: they are exactly the tet faces with one
+    adjacent element; each named side is one axis-aligned plane, the six
+    planes distinct; and Dirichlet on all of them is the whole-boundary mask."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "cube_vol.npz"))
+    m = Mesh(d["points"], d["tets"], bnd_faces=d["bnd_faces"], bnd_index=d["bnd_index"],
+             bc_names=[str(n) for n in d["bc_names"]])
+    assert m.GetBoundaries() == ("back", "left", "front", "right", "bottom", "top")
+    F = np.sort(m.elements[:, [[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]]].reshape(-1, 3), axis=1)
+    uniq, cnt = np.unique(F, axis=0, return_counts=True)
+    outer = uniq[cnt == 1]
+    listed = np.unique(np.sort(m.BoundaryFaces(".*"), axis=1), axis=0)
+    assert len(listed) == len(m.BoundaryFaces(".*")) and np.array_equal(listed, outer)
+    planes = set()
+    for name in m.GetBoundaries():
+        P = m.points[m.BoundaryFaces(name)].reshape(-1, 3)
+        ax = int(np.argmin(np.ptp(P, axis=0)))
+        assert np.ptp(P[:, ax]) < 1e-12
+        planes.add((ax, round(float(P[0, ax]), 9)))
+    assert len(planes) == 6
+    S = O.OracleSpace(m.points, m.elements, 3)
+    Sb = O.OracleSpace(m.points, m.elements, 3, dirichlet_faces=m.BoundaryFaces(".*"))
+    assert np.array_equal(S.freedofs(), Sb.freedofs())
