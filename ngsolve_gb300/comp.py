@@ -807,9 +807,21 @@ class LinearForm:
 
 
 class GridFunction:
-    def __init__(self, fes, name="gfu"):
+    def __init__(self, fes, name="gfu", vec=None):
         self.fes = fes
-        self.vec = BaseVector(fes.ndof)
+        self.name = name
+        self.vec = BaseVector(fes.ndof) if vec is None else vec
+
+    @property
+    def components(self):
+        """On VectorH1: one GridFunction of the scalar space per component, each
+        viewing its block of this vector (no copy: writes go through), as
+        GridFunction.components of a compound space."""
+        if not isinstance(self.fes, VectorH1):
+            raise TypeError("components are defined on VectorH1")
+        n = self.fes.scalar.ndof
+        return tuple(GridFunction(self.fes.scalar, "%s.%d" % (self.name, c), BaseVector(data=self.vec.t[c * n:(c + 1) * n]))
+                     for c in range(self.fes.dim))
 
 
 def Integrate_grad_dot(fes, u, w):

@@ -107,3 +107,23 @@ def test_dirichlet_regex_resolution():
         C._dirichlet_faces(m, ["left"])
     with pytest.raises(TypeError):
         C._dirichlet_faces(m, 3)
+
+
+def test_vector_gridfunction_components():
+    """gfu.components on VectorH1 are views of the component blocks (host
+    tensors stand in for device vectors here)."""
+    import torch
+
+    class _Vec(C.VectorH1):
+        def __init__(self):  # no GPU space: only what GridFunction reads
+            self.scalar, self.dim, self.ne, self.ndof = _Space(), 3, 4, 12
+            self.scalar.ndof = 4
+    fes = _Vec()
+    g = C.GridFunction(fes, vec=C.BaseVector(data=torch.arange(12.0)))
+    comps = g.components
+    assert len(comps) == 3 and all(c.fes is fes.scalar for c in comps)
+    assert torch.equal(comps[1].vec.t, torch.tensor([4.0, 5, 6, 7]))
+    comps[2].vec.t[:] = -1.0
+    assert torch.all(g.vec.t[8:] == -1.0) and torch.all(g.vec.t[:8] >= 0)
+    with pytest.raises(TypeError):
+        C.GridFunction(_Space(), vec=C.BaseVector(data=torch.zeros(4))).components
