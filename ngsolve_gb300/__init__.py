@@ -5,7 +5,7 @@ This package mirrors the reference's Python objects on that path.
 """
 from . import _lib
 from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMesh
-from .comp import (Mesh, H1, VectorH1, InnerProduct, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
+from .comp import (Mesh, H1, VectorH1, InnerProduct, Norm, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
                    BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, BlockMatrix, JacobiPrecond,
                    Preconditioner,
                    Projector, Integrate_grad_dot, ShapeEval, context)
@@ -13,7 +13,7 @@ from . import solvers
 from .adjoint import AdjointProblem, AdjointJ
 
 __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "VectorH1",
-           "InnerProduct", "BilinearForm",
+           "InnerProduct", "Norm", "BilinearForm",
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
            "SparseMatrix", "BilinearFormApplication", "BlockMatrix", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
            "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ"]

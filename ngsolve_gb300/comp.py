@@ -334,11 +334,19 @@ class VectorH1:
         return range(component * n, (component + 1) * n)
 
 
-def InnerProduct(a, b):
+def InnerProduct(a, b, conjugate=False):
     """InnerProduct(grad(u), grad(v)) and InnerProduct(u, v) of VectorH1 (or H1)
     trial and test functions: the sums over components of grad u_c . grad v_c and
-    u_c v_c."""
+    u_c v_c.  On two vectors (BaseVector or tensors) it is their dot product, a
+    float, as ngsolve.InnerProduct of BaseVectors."""
+    if isinstance(a, (BaseVector, torch.Tensor)) and isinstance(b, (BaseVector, torch.Tensor)):
+        return _as_vec(a).InnerProduct(_as_vec(b))
     return _Product.of(a, b)
+
+
+def Norm(x):
+    """Euclidean norm of a vector (ngsolve.Norm of a BaseVector)."""
+    return _as_vec(x).Norm()
 
 
 # ---------------------------------------------------------------------------

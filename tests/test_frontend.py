@@ -127,3 +127,14 @@ def test_vector_gridfunction_components():
     assert torch.all(g.vec.t[8:] == -1.0) and torch.all(g.vec.t[:8] >= 0)
     with pytest.raises(TypeError):
         C.GridFunction(_Space(), vec=C.BaseVector(data=torch.zeros(4))).components
+
+
+def test_vector_inner_product_and_norm():
+    """InnerProduct / Norm of vectors are numbers; of proxies, integrands."""
+    import torch
+    x = C.BaseVector(data=torch.tensor([1.0, 2.0, 2.0]))
+    y = C.BaseVector(data=torch.tensor([3.0, 0.0, -1.0]))
+    assert C.InnerProduct(x, y) == 1.0 and C.InnerProduct(x, torch.tensor([1.0, 1.0, 1.0])) == 5.0
+    assert C.Norm(x) == 3.0
+    u, v = _uv()
+    assert isinstance(C.InnerProduct(u, v), C._Product)
