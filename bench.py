@@ -1,6 +1,6 @@
 """Benchmark of the H1 operator hot path on one GB300 (replicas for --gpus N).
 
-Workload (BASELINE config "mixed precision, matrix-free"): structured 64^3 hex
+Workload (the mixed-precision, matrix-free configuration): structured 64^3 hex
 mesh of the unit cube (MakeStructured3DMesh), H1 order 4, 16,974,593 DOFs,
 per-element kappa ~ lognormal(0, 0.5) (seed 4), f ~ U[-1,1] per element
 (seed 5), zero Dirichlet on the boundary.  Synthetic data of the configured
