@@ -1,6 +1,6 @@
 // gh1_oracle.cpp -- CPU restatement (FP64, OpenMP) of NGSolve's high-order H1
 // Poisson path.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check
-// and the CPU-baseline leg of the benchmark load this library as the checker.
+// and the CPU-baseline leg of the benchmark load this library to compare with.
 // Nothing in the GPU product links or calls it.
 //
 // Every routine names the reference file:line whose algorithm it restates

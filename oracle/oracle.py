@@ -1,7 +1,7 @@
 """ctypes front end of the FP64 CPU oracle (``gh1_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY.  The oracle restates NGSolve's H1 assemble / apply /
-CG algorithms on the CPU; it is the checker for the GPU library.  Only the
+CG algorithms on the CPU; the GPU results are compared with it.  Only the
 tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
 import this module, and only to compare against or time the reference
 algorithm -- never as a product code path.

@@ -1,4 +1,4 @@
-"""Pins of the CPU oracle (the checker of the GPU library) against the
+"""Pins of the CPU oracle (the FP64 reference of the GPU library) against the
 reference's own known answers and closed-form properties."""
 import math
 
