@@ -556,11 +556,76 @@ class BaseMatrix:
     def CreateSmoother(self, freedofs=None):
         return JacobiPrecond(self, freedofs)
 
+    def Inverse(self, freedofs=None, inverse=None, tol=1e-14, maxsteps=100000):
+        """A^{-1} on the free DOFs, for a.mat.Inverse(fes.FreeDofs()).  The
+        reference factorizes (sparsecholesky, umfpack, pardiso ...); this path has
+        no sparse direct solver, so every `inverse` name gives the same operator:
+        FP64 Jacobi-PCG on the GPU to `tol` (relative preconditioned residual),
+        raising if it does not get there.  Rows of non-free DOFs are zero, as in
+        the reference.  freedofs=None: the space's free DOFs."""
+        if inverse not in _INVERSE_NAMES:
+            raise ValueError("unknown inverse %r" % (inverse,))
+        return InverseOperator(self, freedofs, tol, maxsteps)
+
     def __del__(self):
         try:
             self.ctx.lib.gh1_op_free(self.h)
         except Exception:
             pass
+
+
+_INVERSE_NAMES = (None, "", "cg", "sparsecholesky", "umfpack", "pardiso", "pardisospd", "mumps", "masterinverse")
+
+
+class InverseOperator:
+    """The operator BaseMatrix.Inverse returns: each product is one FP64
+    Jacobi-PCG solve on the GPU from a zero start.  Symmetric, like A."""
+
+    def __init__(self, mat, freedofs=None, tol=1e-14, maxsteps=100000):
+        self.mat, self.height, self.width = mat, mat.height, mat.width
+        self.pre = mat.CreateSmoother(freedofs)
+        self.tol, self.maxsteps = float(tol), int(maxsteps)
+        self.iterations = 0
+
+    def Mult(self, x, y):
+        from .solvers import CGSolver
+        solver = CGSolver(mat=self.mat, pre=self.pre, tol=self.tol, maxiter=self.maxsteps)
+        solver.Solve(rhs=x, sol=y, initialize=True)
+        self.iterations = solver.iterations
+        if solver.result.status != 0:
+            raise _lib.GH1Error(solver.result.status, "Inverse: CG stopped after %d iterations above tol %g"
+                                % (solver.iterations, self.tol))
+
+    def MultScale(self, s, x, y):
+        self.Mult(x, y)
+        if s != 1.0:
+            _as_vec(y).t.mul_(s)
+
+    def MultAdd(self, s, x, y):
+        y = _as_vec(y)
+        tmp = y.CreateVector()
+        self.Mult(x, tmp)
+        y.t.add_(tmp.t, alpha=s)
+
+    def MultTrans(self, value, x, y):
+        self.Mult(x, y)
+
+    def MultTransAdd(self, value, x, y):
+        self.MultAdd(value, x, y)
+
+    @property
+    def T(self):
+        return self
+
+    @property
+    def shape(self):
+        return (self.height, self.width)
+
+    def CreateVector(self, colvector=False):
+        return self.mat.CreateVector()
+
+    def __mul__(self, x):
+        return _MatVec(self, _as_vec(x))
 
 
 class SparseMatrix(BaseMatrix):

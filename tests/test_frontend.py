@@ -138,3 +138,59 @@ def test_vector_inner_product_and_norm():
     assert C.Norm(x) == 3.0
     u, v = _uv()
     assert isinstance(C.InnerProduct(u, v), C._Product)
+
+
+def test_inverse_operator_plumbing(monkeypatch):
+    """a.mat.Inverse(freedofs) * f: one CG solve per product (a dense host
+    stand-in replaces the GPU solver here), scaled, added, zero on non-free
+    rows; a solve that stops above tol raises."""
+    import torch
+    from ngsolve_gb300 import solvers as SV
+
+    A = torch.tensor([[4.0, 1, 0], [1, 3, 1], [0, 1, 2]])
+    free = torch.tensor([True, True, False])
+
+    class _Mat:
+        height = width = 3
+
+        def CreateSmoother(self, freedofs=None):
+            return ("jacobi", freedofs)
+
+        def CreateVector(self):
+            return C.BaseVector(data=torch.zeros(3))
+
+    calls = []
+
+    class _Solver:
+        def __init__(self, mat, pre, tol, maxiter):
+            self.pre, self.tol = pre, tol
+            self.iterations = 7
+            self.result = type("R", (), {"status": 6 if tol > 1 else 0})()
+
+        def Solve(self, rhs, sol, initialize):
+            calls.append((self.pre, self.tol, initialize))
+            Af = A[free][:, free]
+            out = torch.zeros(3)
+            out[free] = torch.linalg.solve(Af, rhs.t[free])
+            sol.t.copy_(out)
+
+    monkeypatch.setattr(SV, "CGSolver", _Solver)
+    mat = _Mat()
+    inv = C.BaseMatrix.Inverse(mat, freedofs=[1, 1, 0], inverse="sparsecholesky")
+    f = C.BaseVector(data=torch.tensor([1.0, 2.0, 3.0]))
+    x = C.BaseVector(data=torch.zeros(3))
+    x.data = inv * f
+    expect = torch.zeros(3)
+    expect[free] = torch.linalg.solve(A[free][:, free], f.t[free])
+    assert torch.allclose(x.t, expect) and x.t[2] == 0
+    assert calls[-1] == (("jacobi", [1, 1, 0]), 1e-14, True) and inv.iterations == 7
+    x.data = 2.0 * (inv * f)
+    assert torch.allclose(x.t, 2 * expect)
+    inv.MultAdd(-1.0, f, x)
+    assert torch.allclose(x.t, expect)
+    assert inv.T is inv and inv.shape == (3, 3)
+    with pytest.raises(ValueError):
+        C.BaseMatrix.Inverse(mat, inverse="magic")
+    from ngsolve_gb300._lib import GH1Error
+    with pytest.raises(GH1Error):
+        C.InverseOperator(mat, tol=10.0).Mult(f, x)
