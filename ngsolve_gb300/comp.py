@@ -556,12 +556,12 @@ class BaseMatrix:
     def CreateSmoother(self, freedofs=None):
         return JacobiPrecond(self, freedofs)
 
-    def Inverse(self, freedofs=None, inverse=None, tol=1e-14, maxsteps=100000):
+    def Inverse(self, freedofs=None, inverse=None, tol=1e-12, maxsteps=100000):
         """A^{-1} on the free DOFs, for a.mat.Inverse(fes.FreeDofs()).  The
         reference factorizes (sparsecholesky, umfpack, pardiso ...); this path has
         no sparse direct solver, so every `inverse` name gives the same operator:
-        FP64 Jacobi-PCG on the GPU to `tol` (relative preconditioned residual),
-        raising if it does not get there.  Rows of non-free DOFs are zero, as in
+        FP64 Jacobi-PCG on the GPU to `tol` (relative preconditioned residual,
+        the default of solvers.CG), raising if it does not get there.  Rows of non-free DOFs are zero, as in
         the reference.  freedofs=None: the space's free DOFs."""
         if inverse not in _INVERSE_NAMES:
             raise ValueError("unknown inverse %r" % (inverse,))
@@ -581,7 +581,7 @@ class InverseOperator:
     """The operator BaseMatrix.Inverse returns: each product is one FP64
     Jacobi-PCG solve on the GPU from a zero start.  Symmetric, like A."""
 
-    def __init__(self, mat, freedofs=None, tol=1e-14, maxsteps=100000):
+    def __init__(self, mat, freedofs=None, tol=1e-12, maxsteps=100000):
         self.mat, self.height, self.width = mat, mat.height, mat.width
         self.pre = mat.CreateSmoother(freedofs)
         self.tol, self.maxsteps = float(tol), int(maxsteps)
