@@ -228,6 +228,17 @@ class _Product:
         raise NotImplementedError("only kappa*grad(u)*grad(v)*dx, mu*u*v*dx and f*v*dx are on the H1 path")
 
 
+def _coupling_mask(free, ne, et, order):
+    """free without the element-interior DOFs: the last ne * n_cell DOFs in this
+    numbering ((p-1)^3 per hex, (p-1)(p-2)(p-3)/6 per tet)."""
+    p = int(order)
+    n_cell = (p - 1) ** 3 if et == 8 else max(0, (p - 1) * (p - 2) * (p - 3) // 6)
+    out = np.array(free, dtype=bool)
+    if n_cell:
+        out[len(out) - ne * n_cell:] = False
+    return out
+
+
 def _no_dirichlet(dirichlet):
     return dirichlet is None or dirichlet is False or (isinstance(dirichlet, (str, list, tuple)) and len(dirichlet) == 0)
 
@@ -288,10 +299,16 @@ class H1:
     def TestFunction(self):
         return _Proxy(self, True)
 
-    def FreeDofs(self):
+    def FreeDofs(self, coupling=False):
+        """Free DOFs; coupling=True leaves out the element-interior DOFs, which
+        static condensation eliminates (GetFreeDofs(external),
+        comp/fespace.cpp:2130-2136, with LOCAL_DOF cells, comp/h1hofespace.cpp:1001-1007)."""
         out = np.zeros(self.ndof, dtype=np.uint8)
         self.ctx.check(self.ctx.lib.gh1_space_get_freedofs(self.h, _np_ptr(out)))
-        return out.astype(bool).view(BitArray)
+        free = out.astype(bool)
+        if coupling:
+            free = _coupling_mask(free, self.ne, self.mesh.raw.et, self.order)
+        return free.view(BitArray)
 
     def ElementDofs(self):
         if self._dofs is None:
@@ -326,8 +343,8 @@ class VectorH1:
     def TestFunction(self):
         return _Proxy(self, True)
 
-    def FreeDofs(self):
-        return np.tile(np.asarray(self.scalar.FreeDofs()), self.dim).view(BitArray)
+    def FreeDofs(self, coupling=False):
+        return np.tile(np.asarray(self.scalar.FreeDofs(coupling)), self.dim).view(BitArray)
 
     def Range(self, component):
         n = self.scalar.ndof

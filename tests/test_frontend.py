@@ -194,3 +194,18 @@ def test_inverse_operator_plumbing(monkeypatch):
     from ngsolve_gb300._lib import GH1Error
     with pytest.raises(GH1Error):
         C.InverseOperator(mat, tol=10.0).Mult(f, x)
+
+
+def test_coupling_free_dofs():
+    """FreeDofs(coupling=True) drops the element-interior DOFs, numbered last,
+    and keeps the rest of the mask; the oracle's numbering agrees."""
+    from oracle import oracle as O
+    from ngsolve_gb300.meshes import MakeStructured3DMesh
+    for hexes, p in ((True, 3), (False, 4), (False, 3), (True, 1)):
+        m = MakeStructured3DMesh(hexes=hexes, nx=2)
+        S = O.OracleSpace(m.points, m.elements, p)
+        free = S.freedofs().astype(bool)
+        ext = C._coupling_mask(free, S.ne, m.et, p)
+        cell = np.zeros(S.ndof, dtype=bool)
+        cell[S.first_cell:] = True
+        assert np.array_equal(ext, free & ~cell)
