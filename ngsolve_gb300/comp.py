@@ -776,7 +776,17 @@ class BilinearForm:
     comp/bilinearform.cpp:7549-7607); precision='fp32' adds the FP32 data used by
     the mixed-precision solver (the reference's fp32 flag, :7590-7607)."""
 
+    # flags of the reference's BilinearForm that would change what the operator
+    # is; accepted only at their default (other flags are accepted and unused)
+    _FIXED_FLAGS = {"condense": False, "eliminate_internal": False, "eliminate_hidden": False,
+                    "symmetric_storage": False, "diagonal": False, "hermitian": False, "nonsym": False}
+
     def __init__(self, fes, nonassemble=False, precision="fp64", symmetric=True, **kwargs):
+        for flag, default in self._FIXED_FLAGS.items():
+            if flag in kwargs and bool(kwargs[flag]) != default:
+                raise NotImplementedError("BilinearForm(%s=%r) is not on the H1 path" % (flag, kwargs[flag]))
+        if precision not in ("fp64", "fp32", "mixed"):
+            raise ValueError("precision is 'fp64', 'fp32' or 'mixed'")
         self.fes = fes
         self._sfes = fes.scalar if isinstance(fes, VectorH1) else fes  # the space the form lives on
         self.nonassemble = bool(nonassemble)

@@ -209,3 +209,16 @@ def test_coupling_free_dofs():
         cell = np.zeros(S.ndof, dtype=bool)
         cell[S.first_cell:] = True
         assert np.array_equal(ext, free & ~cell)
+
+
+def test_bilinearform_flags():
+    """Flags that would change the operator raise unless at their default;
+    unrelated flags pass; the precision is checked."""
+    fes = _Space()
+    for flag in ("condense", "eliminate_internal", "symmetric_storage", "diagonal", "hermitian"):
+        with pytest.raises(NotImplementedError):
+            C.BilinearForm(fes, **{flag: True})
+        C.BilinearForm(fes, **{flag: False})
+    C.BilinearForm(fes, check_unused=False, printelmat=False)
+    with pytest.raises(ValueError):
+        C.BilinearForm(fes, precision="bf16")
