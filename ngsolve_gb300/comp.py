@@ -260,11 +260,27 @@ def _dirichlet_faces(raw, dirichlet):
     return np.ascontiguousarray(raw.BoundaryFaces(dirichlet), dtype=np.int32)
 
 
+# space flags of the reference's H1 accepted here: these at their default only,
+# and autoupdate (mesh refinement never happens on this path) at any value
+_SPACE_FIXED_FLAGS = {"complex": False, "dgjumps": False}
+
+
+def _check_space_flags(flags):
+    for flag, value in flags.items():
+        if flag == "autoupdate":
+            continue
+        if flag not in _SPACE_FIXED_FLAGS:
+            raise TypeError("H1() got an unexpected flag %r" % flag)
+        if bool(value) != _SPACE_FIXED_FLAGS[flag]:
+            raise NotImplementedError("H1(%s=%r) is not on the H1 path" % (flag, value))
+
+
 # ---------------------------------------------------------------------------
 class H1:
     """H1HighOrderFESpace of uniform order (comp/h1hofespace.cpp)."""
 
-    def __init__(self, mesh, order=1, dirichlet=""):
+    def __init__(self, mesh, order=1, dirichlet="", **flags):
+        _check_space_flags(flags)
         if not isinstance(mesh, Mesh):
             mesh = Mesh(mesh)
         self.mesh = mesh
@@ -326,8 +342,8 @@ class VectorH1:
     dirichlet), the DOFs of component c at c*n .. (c+1)*n - 1 with n the scalar
     space's ndof (the CompoundFESpace numbering, interleaved = False)."""
 
-    def __init__(self, mesh, order=1, dirichlet="", dim=3):
-        self.scalar = H1(mesh, order=order, dirichlet=dirichlet)
+    def __init__(self, mesh, order=1, dirichlet="", dim=3, **flags):
+        self.scalar = H1(mesh, order=order, dirichlet=dirichlet, **flags)
         self.dim = int(dim)
         self.mesh, self.order, self.ctx = self.scalar.mesh, self.scalar.order, self.scalar.ctx
         self.ne = self.scalar.ne

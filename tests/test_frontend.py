@@ -222,3 +222,11 @@ def test_bilinearform_flags():
     C.BilinearForm(fes, check_unused=False, printelmat=False)
     with pytest.raises(ValueError):
         C.BilinearForm(fes, precision="bf16")
+
+
+def test_space_flags():
+    C._check_space_flags({"complex": False, "dgjumps": False, "autoupdate": True})
+    with pytest.raises(NotImplementedError):
+        C._check_space_flags({"complex": True})
+    with pytest.raises(TypeError):
+        C._check_space_flags({"orderinner": 2})
