@@ -8,7 +8,7 @@ from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMe
 from .comp import (Mesh, H1, VectorH1, InnerProduct, Norm, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
                    BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, BlockMatrix, JacobiPrecond,
                    Preconditioner,
-                   Projector, Integrate_grad_dot, ShapeEval, context)
+                   Projector, Integrate_grad_dot, ShapeEval, context, TaskManager, SetNumThreads, SetHeapSize)
 from . import solvers
 from .adjoint import AdjointProblem, AdjointJ
 
@@ -16,4 +16,5 @@ __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh
            "InnerProduct", "Norm", "BilinearForm",
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
            "SparseMatrix", "BilinearFormApplication", "BlockMatrix", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
-           "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ"]
+           "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ", "TaskManager", "SetNumThreads",
+           "SetHeapSize"]

@@ -959,3 +959,28 @@ def ShapeEval(et, order, vnums, pts, device=0):
     grd = np.zeros((len(pts), n, 3))
     ctx.check(ctx.lib.gh1_shape_eval(ctx.h, et, order, _np_ptr(vn), len(pts), _np_ptr(pts), _np_ptr(val), _np_ptr(grd)))
     return val, grd
+
+
+class TaskManager:
+    """`with TaskManager():` of NGSolve scripts.  NGSolve's TaskManager starts its
+    CPU worker threads; here the work runs on the GPU stream and the host-side
+    setup threads itself, so entering and leaving does nothing."""
+
+    def __init__(self, pajetrace=None, **kwargs):
+        pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+
+def SetNumThreads(n):
+    """NGSolve's CPU thread count; nothing to set on the GPU path."""
+    return None
+
+
+def SetHeapSize(size):
+    """NGSolve's LocalHeap size; the GPU path keeps no such heap."""
+    return None

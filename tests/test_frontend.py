@@ -230,3 +230,11 @@ def test_space_flags():
         C._check_space_flags({"complex": True})
     with pytest.raises(TypeError):
         C._check_space_flags({"orderinner": 2})
+
+
+def test_script_boilerplate():
+    import ngsolve_gb300 as ng
+    ng.SetHeapSize(10 * 1000 * 1000)
+    ng.SetNumThreads(4)
+    with ng.TaskManager(pajetrace=10 ** 8) as tm:
+        assert isinstance(tm, ng.TaskManager)
