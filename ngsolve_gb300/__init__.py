@@ -8,8 +8,9 @@ from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMe
 from .comp import (Mesh, H1, VectorH1, InnerProduct, Norm, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
                    BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, BlockMatrix, JacobiPrecond,
                    Preconditioner,
-                   Projector, Integrate_grad_dot, ShapeEval, context, TaskManager, SetNumThreads, SetHeapSize)
+                   Projector, Integrate_grad_dot, ShapeEval, context, TaskManager, SetNumThreads, SetHeapSize, ngsglobals)
 from . import solvers
+from .solvers import CGSolver
 from .adjoint import AdjointProblem, AdjointJ
 
 __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh", "Mesh", "H1", "VectorH1",
@@ -17,4 +18,4 @@ __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
            "SparseMatrix", "BilinearFormApplication", "BlockMatrix", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
            "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ", "TaskManager", "SetNumThreads",
-           "SetHeapSize"]
+           "SetHeapSize", "ngsglobals", "CGSolver"]

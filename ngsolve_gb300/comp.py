@@ -198,6 +198,18 @@ class _Product:
 
     __rmul__ = __mul__
 
+    def __neg__(self):
+        return _Product(self.factors + [-1.0])
+
+    def __add__(self, other):
+        return _Sum([self]) + other
+
+    def __radd__(self, other):
+        return _Sum([other]) + self
+
+    def __sub__(self, other):
+        return _Sum([self]) + (-other)
+
     def classify(self, ne):
         grads = [f for f in self.factors if isinstance(f, _Grad)]
         proxies = [f for f in self.factors if isinstance(f, _Proxy)]
@@ -273,6 +285,39 @@ def _check_space_flags(flags):
             raise TypeError("H1() got an unexpected flag %r" % flag)
         if bool(value) != _SPACE_FIXED_FLAGS[flag]:
             raise NotImplementedError("H1(%s=%r) is not on the H1 path" % (flag, value))
+
+
+class _Sum:
+    """A sum of integrands, grad(u)*grad(v)*dx + u*v*dx: each term goes into
+    the form on its own."""
+
+    def __init__(self, terms):
+        self.terms = list(terms)
+
+    def __add__(self, other):
+        if isinstance(other, _Sum):
+            return _Sum(self.terms + other.terms)
+        if not isinstance(other, _Product):
+            raise TypeError("only integrands (... * dx) add up")
+        return _Sum(self.terms + [other])
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __neg__(self):
+        return _Sum([-t for t in self.terms])
+
+
+def _space_of(integrand):
+    """The space of the first trial or test function in an integrand."""
+    terms = integrand.terms if isinstance(integrand, _Sum) else [integrand]
+    for t in terms:
+        for f in getattr(t, "factors", []):
+            if isinstance(f, _Proxy):
+                return f.fes
+            if isinstance(f, _Grad):
+                return f.proxy.fes
+    raise ValueError("the integrand has no trial or test function")
 
 
 # ---------------------------------------------------------------------------
@@ -372,14 +417,19 @@ def InnerProduct(a, b, conjugate=False):
     trial and test functions: the sums over components of grad u_c . grad v_c and
     u_c v_c.  On two vectors (BaseVector or tensors) it is their dot product, a
     float, as ngsolve.InnerProduct of BaseVectors."""
-    if isinstance(a, (BaseVector, torch.Tensor)) and isinstance(b, (BaseVector, torch.Tensor)):
-        return _as_vec(a).InnerProduct(_as_vec(b))
+    vec = (BaseVector, torch.Tensor, _Expr)
+    if isinstance(a, vec) and isinstance(b, vec):
+        return _value(a).InnerProduct(_value(b))
     return _Product.of(a, b)
 
 
+def _value(x):
+    return x.Evaluate() if isinstance(x, _Expr) else _as_vec(x)
+
+
 def Norm(x):
-    """Euclidean norm of a vector (ngsolve.Norm of a BaseVector)."""
-    return _as_vec(x).Norm()
+    """Euclidean norm of a vector or vector expression (ngsolve.Norm)."""
+    return _value(x).Norm()
 
 
 # ---------------------------------------------------------------------------
@@ -401,6 +451,11 @@ class BaseVector:
 
     def CreateVector(self):
         return BaseVector(data=torch.zeros_like(self.t))
+
+    def CreateDeviceVector(self, unified=True, copy=True):
+        """The vector already lives on the device: a copy (copy=True, the
+        reference's default) or a zero vector of the same size and type."""
+        return BaseVector(data=self.t.clone() if copy else torch.zeros_like(self.t))
 
     def NumPy(self):
         return self.t.detach().cpu().numpy()
@@ -468,6 +523,12 @@ class BaseVector:
 
 
 class _Expr:
+    def Evaluate(self):
+        """The expression's value as a new vector ((inv * f).Evaluate())."""
+        y = BaseVector(data=self._template())
+        self.eval_into(y)
+        return y
+
     def eval_into(self, y):
         raise NotImplementedError
 
@@ -486,6 +547,12 @@ class _LinComb(_Expr):
             return _LinComb(self.terms + [(-s, v) for s, v in other.terms])
         return _LinComb(self.terms + [(-1.0, other)])
 
+    def _template(self):
+        for _, v in self.terms:
+            if isinstance(v, BaseVector):
+                return torch.zeros_like(v.t)
+        return self.terms[0][1]._template()
+
     def eval_into(self, y):
         acc = torch.zeros_like(y.t)
         for s, v in self.terms:
@@ -501,6 +568,9 @@ class _LinComb(_Expr):
 class _MatVec(_Expr):
     def __init__(self, mat, x, s=1.0):
         self.mat, self.x, self.s = mat, x, s
+
+    def _template(self):
+        return torch.zeros(self.mat.height, dtype=self.x.t.dtype, device=self.x.t.device)
 
     def __rmul__(self, s):
         return _MatVec(self.mat, self.x, self.s * float(s))
@@ -582,6 +652,15 @@ class BaseMatrix:
         """The transpose: this operator itself (it is symmetric)."""
         return self
 
+    def CreateDeviceMatrix(self):
+        """The operator already lives on the device (BaseMatrix.CreateDeviceMatrix)."""
+        return self
+
+    def GetOperatorInfo(self):
+        i = self.Info()
+        kind = {0: "SparseMatrix (CSR)", 1: "BilinearFormApplication (matrix-free)", 2: "BlockMatrix"}.get(i["kind"], "?")
+        return "%s, h = %d, w = %d, elements %d, order %d\n" % (kind, self.height, self.width, i["ne"], i["order"])
+
     @property
     def shape(self):
         return (self.height, self.width)
@@ -656,6 +735,12 @@ class InverseOperator:
 
     def CreateVector(self, colvector=False):
         return self.mat.CreateVector()
+
+    def CreateDeviceMatrix(self):
+        return self
+
+    def GetOperatorInfo(self):
+        return "Inverse by CG (tol %g) of: %s" % (self.tol, self.mat.GetOperatorInfo())
 
     def __mul__(self, x):
         return _MatVec(self, _as_vec(x))
@@ -733,6 +818,15 @@ class JacobiPrecond(BaseMatrix):
         self.ctx.sync_stream()
         self.ctx.check(self.ctx.lib.gh1_pre_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
 
+    def Info(self):  # the handle is a preconditioner, not an operator
+        return {"kind": "jacobi", "nrows": self.height}
+
+    def GetOperatorInfo(self):
+        return "JacobiPrecond, h = %d, w = %d\n" % (self.height, self.width)
+
+    def Inverse(self, *args, **kwargs):
+        raise NotImplementedError("Inverse of a preconditioner")
+
     def __del__(self):
         try:
             self.ctx.lib.gh1_pre_free(self.h)
@@ -760,6 +854,15 @@ class Projector(BaseMatrix):
         prec = _lib.GH1_F64 if x.t.dtype == torch.float64 else _lib.GH1_F32
         self.ctx.sync_stream()
         self.ctx.check(self.ctx.lib.gh1_projector_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
+
+    def Info(self):  # the handle is a projector, not an operator
+        return {"kind": "projector", "nrows": self.height}
+
+    def GetOperatorInfo(self):
+        return "Projector (range = %s), h = %d, w = %d\n" % (self.range, self.height, self.width)
+
+    def Inverse(self, *args, **kwargs):
+        raise NotImplementedError("Inverse of a projector")
 
     def Project(self, vec):
         v = _as_vec(vec)
@@ -798,6 +901,9 @@ class BilinearForm:
                     "symmetric_storage": False, "diagonal": False, "hermitian": False, "nonsym": False}
 
     def __init__(self, fes, nonassemble=False, precision="fp64", symmetric=True, **kwargs):
+        integrand = None
+        if isinstance(fes, (_Product, _Sum)):  # BilinearForm(grad(u)*grad(v)*dx + ...)
+            integrand, fes = fes, _space_of(fes)
         for flag, default in self._FIXED_FLAGS.items():
             if flag in kwargs and bool(kwargs[flag]) != default:
                 raise NotImplementedError("BilinearForm(%s=%r) is not on the H1 path" % (flag, kwargs[flag]))
@@ -813,8 +919,14 @@ class BilinearForm:
         self._has_laplace = False
         self._form = None
         self.mat = None
+        if integrand is not None:
+            self += integrand
 
     def __iadd__(self, term):
+        if isinstance(term, _Sum):
+            for t in term.terms:
+                self += t
+            return self
         kind, coef = term.classify(self.fes.ne)
         if kind == "laplace":
             self.kappa = self.kappa + coef
@@ -886,12 +998,21 @@ class LinearForm:
     element) per component."""
 
     def __init__(self, fes):
+        integrand = None
+        if isinstance(fes, (_Product, _Sum)):  # LinearForm(f*v*dx + ...)
+            integrand, fes = fes, _space_of(fes)
         self.fes = fes
         self._vector = isinstance(fes, VectorH1)
         self.f = np.zeros((fes.dim, fes.ne)) if self._vector else np.zeros(fes.ne)
         self.vec = BaseVector(fes.ndof)
+        if integrand is not None:
+            self += integrand
 
     def __iadd__(self, term):
+        if isinstance(term, _Sum):
+            for t in term.terms:
+                self += t
+            return self
         if self._vector:
             comps = [f for f in term.factors if isinstance(f, CoefficientFunction) and isinstance(f.values, (tuple, list))]
             if len(comps) != 1 or len(comps[0].values) != self.fes.dim:
@@ -959,6 +1080,15 @@ def ShapeEval(et, order, vnums, pts, device=0):
     grd = np.zeros((len(pts), n, 3))
     ctx.check(ctx.lib.gh1_shape_eval(ctx.h, et, order, _np_ptr(vn), len(pts), _np_ptr(pts), _np_ptr(val), _np_ptr(grd)))
     return val, grd
+
+
+class _Globals:
+    """ngsglobals: msg_level is kept and has no effect (the library prints
+    nothing)."""
+    msg_level = 0
+
+
+ngsglobals = _Globals()
 
 
 class TaskManager:

@@ -86,6 +86,42 @@ class CGSolver:
     def Mult(self, x, y):
         self.Solve(rhs=x, sol=y, initialize=True)
 
+    # the solver as an operator: inv * f runs one solve (KrylovSpaceSolver)
+    @property
+    def height(self):
+        return self.mat.height
+
+    @property
+    def width(self):
+        return self.mat.width
+
+    def MultScale(self, s, x, y):
+        self.Mult(x, y)
+        if s != 1.0:
+            _as_vec(y).t.mul_(s)
+
+    def MultAdd(self, s, x, y):
+        y = _as_vec(y)
+        tmp = y.CreateVector()
+        self.Mult(x, tmp)
+        y.t.add_(tmp.t, alpha=s)
+
+    def __mul__(self, x):
+        from .comp import _MatVec
+        return _MatVec(self, _as_vec(x))
+
+    def GetSteps(self):
+        return self.iterations
+
+    def CreateVector(self, colvector=False):
+        return self.mat.CreateVector()
+
+    def CreateDeviceMatrix(self):
+        return self
+
+    def GetOperatorInfo(self):
+        return "CGSolver (tol %g, maxiter %d) of: %s" % (self.tol, self.maxiter, self.mat.GetOperatorInfo())
+
 
 def CG(mat, rhs, pre=None, sol=None, tol=1e-12, maxsteps=100, printrates=True, plotrates=False, initialize=True,
        conjugate=False, callback=None, **kwargs):

@@ -6,8 +6,9 @@ import pytest
 from ngsolve_gb300 import comp as C
 
 
-class _Space:  # the proxies only need the element count
+class _Space:  # the proxies need the element count, a LinearForm the DOF count
     ne = 4
+    ndof = 8
 
 
 def _uv():
@@ -238,3 +239,60 @@ def test_script_boilerplate():
     ng.SetNumThreads(4)
     with ng.TaskManager(pajetrace=10 ** 8) as tm:
         assert isinstance(tm, ng.TaskManager)
+
+
+def test_tutorial_idioms(monkeypatch):
+    """The idioms of NGSolve's CUDA Poisson tutorial (docs/i-tutorials/
+    unit-5.5-cuda/poisson_cuda.ipynb) on host stand-ins for the GPU parts:
+    forms built from integrand sums, CGSolver as an operator with GetSteps,
+    (inv * f).Evaluate(), Norm of a vector difference, CreateDeviceVector /
+    CreateDeviceMatrix."""
+    import torch
+    from ngsolve_gb300 import solvers as SV
+
+    class _HostVec(C.BaseVector):
+        def __init__(self, n=None, data=None, dtype=torch.float64, device=0):
+            self.t = data if data is not None else torch.zeros(int(n), dtype=dtype)
+
+    monkeypatch.setattr(C, "BaseVector", _HostVec)
+    u, v = _uv()
+    a = C.BilinearForm(C.grad(u) * C.grad(v) * C.dx + u * v * C.dx)
+    assert a.fes is u.fes and np.all(a.kappa == 1.0) and np.all(a.mu == 1.0)
+    b = C.BilinearForm(u.fes)
+    b += C.grad(u) * C.grad(v) * C.dx - 2.0 * u * v * C.dx
+    assert np.all(b.kappa == 1.0) and np.all(b.mu == -2.0)
+    lf = C.LinearForm(C.CoefficientFunction(3.0) * v * C.dx + C.CoefficientFunction(1.0) * v * C.dx)
+    assert lf.fes is u.fes and np.all(lf.f == 4.0)
+    with pytest.raises(ValueError):
+        C.BilinearForm(C.CoefficientFunction(1.0) * C.dx)
+
+    A = torch.tensor([[4.0, 1, 0], [1, 3, 1], [0, 1, 2]], dtype=torch.float64)
+
+    class _Mat:
+        height = width = 3
+
+        def CreateVector(self):
+            return _HostVec(3)
+
+        def GetOperatorInfo(self):
+            return "A\n"
+
+    def _solve(self, rhs, sol=None, initialize=True):
+        sol.t.copy_(torch.linalg.solve(A, rhs.t))
+        self.iterations = 5
+        return sol
+
+    monkeypatch.setattr(SV.CGSolver, "Solve", _solve)
+    inv = SV.CGSolver(_Mat(), None, maxiter=2000, printrates=False)
+    assert inv.CreateDeviceMatrix() is inv and "CGSolver" in inv.GetOperatorInfo()
+    f = _HostVec(data=torch.tensor([1.0, 2.0, 3.0], dtype=torch.float64))
+    fdev = f.CreateDeviceVector(copy=True)
+    assert torch.equal(fdev.t, f.t) and fdev.t.data_ptr() != f.t.data_ptr()
+    assert torch.all(f.CreateDeviceVector(copy=False).t == 0)
+    res = (inv * fdev).Evaluate()
+    assert inv.GetSteps() == 5
+    assert C.Norm(res - _HostVec(data=torch.linalg.solve(A, f.t))) < 1e-12
+    assert abs(C.InnerProduct(res, f) - float(res.t @ f.t)) < 1e-12
+    gfu = _HostVec(3)
+    gfu.data = 2.0 * (inv * f)
+    assert torch.allclose(gfu.t, 2 * torch.linalg.solve(A, f.t))
