@@ -174,6 +174,61 @@ class CoefficientFunction:
     __rmul__ = __mul__
 
 
+class _AffineCF(CoefficientFunction):
+    """a.x + b.y + c.z + d in physical coordinates: the coordinate functions x,
+    y, z and their affine combinations.  As a source, f*v*dx, it is exactly
+    the H1 interpolant of f (vertex values, all other DOFs zero: on affine tets
+    and on trilinear hexes the vertex functions reproduce the map), so the load
+    vector is M I_h(f) with the mass operator, integrated by the same order-2p
+    rule as the right-hand-side kernel."""
+
+    def __init__(self, a=(0.0, 0.0, 0.0), d=0.0):
+        self.a, self.d = np.array(a, dtype=np.float64), float(d)
+        self.values = None
+
+    def is_tensor(self):
+        return False
+
+    def element_values(self, ne):
+        raise ValueError("a coordinate function is not constant per element; it enters as f * v * dx")
+
+    def vertex_values(self, points):
+        return np.asarray(points, dtype=np.float64) @ self.a + self.d
+
+    def _num(self, other):
+        return isinstance(other, (int, float, np.floating, np.integer)) and not isinstance(other, bool)
+
+    def __mul__(self, other):
+        if self._num(other):
+            return _AffineCF(self.a * other, self.d * other)
+        return _Product.of(self, other)
+
+    __rmul__ = __mul__
+
+    def __add__(self, other):
+        if self._num(other):
+            return _AffineCF(self.a, self.d + other)
+        if isinstance(other, _AffineCF):
+            return _AffineCF(self.a + other.a, self.d + other.d)
+        return NotImplemented
+
+    __radd__ = __add__
+
+    def __neg__(self):
+        return _AffineCF(-self.a, -self.d)
+
+    def __sub__(self, other):
+        return self + (-other)
+
+    def __rsub__(self, other):
+        return (-self) + other
+
+
+x = _AffineCF((1.0, 0.0, 0.0))
+y = _AffineCF((0.0, 1.0, 0.0))
+z = _AffineCF((0.0, 0.0, 1.0))
+
+
 class _Measure:
     pass
 
@@ -214,10 +269,11 @@ class _Product:
         grads = [f for f in self.factors if isinstance(f, _Grad)]
         proxies = [f for f in self.factors if isinstance(f, _Proxy)]
         tensors = [f for f in self.factors if isinstance(f, CoefficientFunction) and f.is_tensor()]
+        affine = [f for f in self.factors if isinstance(f, _AffineCF)]
         coef = np.ones(ne)
         has_dx = False
         for f in self.factors:
-            if isinstance(f, CoefficientFunction) and f.is_tensor():
+            if isinstance(f, CoefficientFunction) and (f.is_tensor() or isinstance(f, _AffineCF)):
                 continue
             if isinstance(f, CoefficientFunction):
                 coef = coef * f.element_values(ne)
@@ -227,6 +283,13 @@ class _Product:
                 has_dx = True
         if not has_dx:
             raise ValueError("integrand needs * dx")
+        if affine:
+            if len(affine) == 1 and len(proxies) == 1 and not grads and proxies[0].test and not tensors:
+                if np.ptp(coef) != 0.0:
+                    raise NotImplementedError("a coordinate source times an element-wise coefficient")
+                f = affine[0] * float(coef[0])
+                return "source_affine", np.concatenate([f.a, [f.d]])
+            raise NotImplementedError("a coordinate function is only on the path as a source, f * v * dx")
         if tensors:
             if len(tensors) == 1 and len(grads) == 2 and not proxies and grads[0].proxy.test != grads[1].proxy.test:
                 return "laplace_tensor", tensors[0].tensor_values(ne) * coef[:, None]
@@ -1004,6 +1067,8 @@ class LinearForm:
         self.fes = fes
         self._vector = isinstance(fes, VectorH1)
         self.f = np.zeros((fes.dim, fes.ne)) if self._vector else np.zeros(fes.ne)
+        self.affine = np.zeros(4)  # a.x + b.y + c.z + d sources (scalar H1)
+        self._mass = None
         self.vec = BaseVector(fes.ndof)
         if integrand is not None:
             self += integrand
@@ -1024,6 +1089,9 @@ class LinearForm:
                 self.f[c] = self.f[c] + coef * CoefficientFunction(fc).element_values(self.fes.ne)
             return self
         kind, coef = term.classify(self.fes.ne)
+        if kind == "source_affine":
+            self.affine = self.affine + coef
+            return self
         if kind != "source":
             raise ValueError("LinearForm takes f*v*dx")
         self.f = self.f + coef
@@ -1040,7 +1108,25 @@ class LinearForm:
             return self
         f = np.ascontiguousarray(self.f, dtype=np.float64)
         ctx.check(ctx.lib.gh1_rhs_elementwise(self.fes.h, _np_ptr(f), _lib.GH1_MEM_HOST, _ptr(self.vec.t)))
+        if np.any(self.affine != 0.0):
+            _affine_source(self, _AffineCF(self.affine[:3], self.affine[3]))
         return self
+
+
+def _affine_source(lf, f):
+    """lf.vec += M I_h(f) for an affine f: the mass operator of lf's space
+    (matrix-free, built once per LinearForm) applied to f's interpolant."""
+    fes = lf.fes
+    if lf._mass is None:
+        u, v = fes.TnT()
+        m = BilinearForm(fes, nonassemble=True)
+        m += u * v * dx
+        lf._mass = m.Assemble()
+    fi = np.zeros(fes.ndof)
+    pts = fes.mesh.raw.points
+    fi[:len(pts)] = f.vertex_values(pts)
+    xi = BaseVector(data=torch.tensor(fi, dtype=lf.vec.t.dtype, device=lf.vec.t.device))
+    lf._mass.mat.MultAdd(1.0, xi, lf.vec)
 
 
 class GridFunction:

@@ -296,3 +296,58 @@ def test_tutorial_idioms(monkeypatch):
     gfu = _HostVec(3)
     gfu.data = 2.0 * (inv * f)
     assert torch.allclose(gfu.t, 2 * torch.linalg.solve(A, f.t))
+
+
+def test_coordinate_sources(monkeypatch):
+    """x, y, z and their affine combinations: classified as affine sources,
+    accumulated by the LinearForm, assembled as M I_h(f) (a dense host mass
+    matrix stands in for the GPU operator); other uses are rejected."""
+    import torch
+    f = 2 * C.x - C.y + 3
+    assert np.array_equal(f.a, [2, -1, 0]) and f.d == 3.0
+    assert np.array_equal((1 - C.z).a, [0, 0, -1]) and (1 - C.z).d == 1.0
+    u, v = _uv()
+    kind, val = (2.0 * C.x * v * C.dx).classify(4)
+    assert kind == "source_affine" and np.array_equal(val, [2, 0, 0, 0])
+    with pytest.raises(NotImplementedError):
+        (C.x * C.grad(u) * C.grad(v) * C.dx).classify(4)
+    with pytest.raises(NotImplementedError):
+        (C.CoefficientFunction(np.arange(4.0)) * C.x * v * C.dx).classify(4)
+    with pytest.raises(ValueError):
+        C.x.element_values(4)
+
+    pts = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0]])
+    Md = torch.tensor(np.diag([1.0, 2, 3, 4, 5]))
+
+    class _Mesh:
+        raw = type("R", (), {"points": pts})()
+
+    class _Fes(_Space):
+        ndof, mesh = 5, _Mesh()
+
+        def TnT(self):
+            return C._Proxy(self, False), C._Proxy(self, True)
+
+    class _Form:
+        def __init__(self, fes, nonassemble=False):
+            self.terms = []
+
+        def __iadd__(self, t):
+            self.terms.append(t.classify(4)[0])
+            return self
+
+        def Assemble(self):
+            assert self.terms == ["mass"]
+            self.mat = type("M", (), {"MultAdd": staticmethod(lambda s, xv, yv: yv.t.add_(s * (Md @ xv.t)))})()
+            return self
+
+    monkeypatch.setattr(C, "BilinearForm", _Form)
+    lf = type("LF", (), {})()
+    lf.fes, lf._mass = _Fes(), None
+    lf.vec = C.BaseVector(data=torch.ones(5, dtype=torch.float64))
+    C._affine_source(lf, f)
+    fi = np.array([3.0, 5.0, 2.0, 0, 0])
+    assert np.allclose(lf.vec.t.numpy(), 1.0 + np.diag(Md.numpy()) * fi)
+    mass = lf._mass
+    C._affine_source(lf, C.x)  # the mass operator is built once
+    assert lf._mass is mass

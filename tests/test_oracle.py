@@ -381,3 +381,28 @@ def test_cube_vol_boundary_names():
     S = O.OracleSpace(m.points, m.elements, 3)
     Sb = O.OracleSpace(m.points, m.elements, 3, dirichlet_faces=m.BoundaryFaces(".*"))
     assert np.array_equal(S.freedofs(), Sb.freedofs())
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 1), (True, 3), (False, 2)])
+def test_affine_source_identity(hexes, p):
+    """For an affine f the load vector of f*v*dx is M I_h(f) (I_h(f): f at the
+    vertices, other DOFs zero).  On a jittered unit cube, with f = x:
+    1_h . b = int x = 1/2 and I_h(x) . b = int x^2 = 1/3, to round-off (x^2 only
+    where the rule is exact for it: x^2 |det J| has degree 4 per direction on a
+    trilinear hex, beyond the 2-point rule of p=1); with f = 2x - y + 3:
+    1_h . b = int f = 3.5."""
+    m = JitterInterior(MakeStructured3DMesh(hexes=hexes, nx=3), 0.05, 12)
+    S = O.OracleSpace(m.points, m.elements, p)
+    rp, ci, va = S.assemble(kappa=np.zeros(S.ne), mu=np.ones(S.ne))
+    M = sp.csr_matrix((va, ci, rp), shape=(S.ndof, S.ndof))
+    ones = np.zeros(S.ndof)
+    ones[:m.nv] = 1.0
+    xi = np.zeros(S.ndof)
+    xi[:m.nv] = m.points[:, 0]
+    b = M @ xi
+    assert abs(ones @ b - 0.5) < 1e-13
+    if p >= 2 or not hexes:
+        assert abs(xi @ b - 1.0 / 3.0) < 1e-13
+    fi = np.zeros(S.ndof)
+    fi[:m.nv] = 2 * m.points[:, 0] - m.points[:, 1] + 3
+    assert abs(ones @ (M @ fi) - 3.5) < 1e-13
