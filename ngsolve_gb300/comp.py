@@ -434,6 +434,20 @@ class H1:
             free = _coupling_mask(free, self.ne, self.mesh.raw.et, self.order)
         return free.view(BitArray)
 
+    def _boundary_dofs(self):
+        """DOFs on the boundary (of boundary faces, their edges and vertices):
+        the non-free DOFs of the same space with the whole boundary Dirichlet."""
+        if getattr(self, "_bnd_dofs", None) is None:
+            h = ctypes.c_void_p()
+            self.ctx.check(self.ctx.lib.gh1_space_h1(self.mesh.h, self.order, 1, ctypes.byref(h)))
+            try:
+                out = np.zeros(self.ndof, dtype=np.uint8)
+                self.ctx.check(self.ctx.lib.gh1_space_get_freedofs(h, _np_ptr(out)))
+            finally:
+                self.ctx.lib.gh1_space_free(h)
+            self._bnd_dofs = out == 0
+        return self._bnd_dofs
+
     def ElementDofs(self):
         if self._dofs is None:
             out = np.zeros((self.ne, self.nloc), dtype=np.int32)
@@ -1129,11 +1143,40 @@ def _affine_source(lf, f):
     lf._mass.mat.MultAdd(1.0, xi, lf.vec)
 
 
+VOL, BND = "VOL", "BND"
+
+
 class GridFunction:
     def __init__(self, fes, name="gfu", vec=None):
         self.fes = fes
         self.name = name
         self.vec = BaseVector(fes.ndof) if vec is None else vec
+
+    def Set(self, cf, VOL_or_BND=VOL):
+        """gfu.Set(f) for f affine in x, y, z or constant, on scalar H1: the
+        interpolant is then f itself (vertex values, all other DOFs zero), which
+        is also what the reference's projection-based Set returns for a function
+        in the space.  Set(f, BND) writes only the DOFs of the boundary (all
+        boundary faces, whatever the Dirichlet flag) and keeps the others, as
+        used for inhomogeneous Dirichlet data."""
+        if isinstance(cf, (int, float, np.floating, np.integer)):
+            cf = _AffineCF((0.0, 0.0, 0.0), float(cf))
+        elif isinstance(cf, CoefficientFunction) and not isinstance(cf, _AffineCF):
+            v = np.asarray(cf.values, dtype=np.float64)
+            if v.ndim != 0:
+                raise NotImplementedError("Set takes a constant or an affine function of x, y, z")
+            cf = _AffineCF((0.0, 0.0, 0.0), float(v))
+        if not isinstance(cf, _AffineCF) or not isinstance(self.fes, H1):
+            raise NotImplementedError("Set takes a constant or an affine function of x, y, z on H1")
+        pts = self.fes.mesh.raw.points
+        new = torch.zeros_like(self.vec.t)
+        new[:len(pts)] = torch.as_tensor(cf.vertex_values(pts), dtype=new.dtype, device=new.device)
+        if VOL_or_BND == BND:
+            on = torch.as_tensor(self.fes._boundary_dofs(), device=new.device)
+            new = torch.where(on, new, self.vec.t)
+        elif VOL_or_BND != VOL:
+            raise ValueError("VOL_or_BND is VOL or BND")
+        self.vec.t.copy_(new)
 
     @property
     def components(self):

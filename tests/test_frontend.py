@@ -351,3 +351,27 @@ def test_coordinate_sources(monkeypatch):
     mass = lf._mass
     C._affine_source(lf, C.x)  # the mass operator is built once
     assert lf._mass is mass
+
+
+def test_gridfunction_set():
+    """Set(f) for constant / affine f writes the interpolant (vertex values, zero
+    elsewhere); Set(f, BND) touches only the boundary DOFs; other
+    coefficients are rejected (host stand-ins for the GPU space)."""
+    import torch
+    pts = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 0.5]])
+    fes = C.H1.__new__(C.H1)
+    fes.mesh = type("M", (), {"raw": type("R", (), {"points": pts})()})()
+    fes.ndof = 7
+    fes._bnd_dofs = np.array([1, 1, 1, 0, 1, 0, 0], dtype=bool)  # vertex 3 and DOFs 5, 6 interior
+    g = C.GridFunction(fes, vec=C.BaseVector(data=torch.arange(7.0, dtype=torch.float64)))
+    g.Set(2 * C.x + 1)
+    assert np.array_equal(g.vec.NumPy(), [1, 3, 1, 2, 0, 0, 0])
+    g.vec.t.copy_(torch.arange(7.0, dtype=torch.float64))
+    g.Set(C.y - 1, C.BND)
+    assert np.array_equal(g.vec.NumPy(), [-1, -1, 0, 3, 0, 5, 6])
+    g.Set(C.CoefficientFunction(4.0))
+    assert np.array_equal(g.vec.NumPy(), [4, 4, 4, 4, 0, 0, 0])
+    with pytest.raises(NotImplementedError):
+        g.Set(C.CoefficientFunction(np.arange(4.0)))
+    with pytest.raises(ValueError):
+        g.Set(C.x, "SURFACE")
