@@ -8,7 +8,7 @@ from .meshes import MakeStructured3DMesh, MakeHexMesh, JitterInterior, ReadVolMe
 from .comp import (Mesh, H1, VectorH1, InnerProduct, Norm, BilinearForm, LinearForm, GridFunction, CoefficientFunction, grad, dx,
                    BaseVector, BaseMatrix, SparseMatrix, BilinearFormApplication, BlockMatrix, JacobiPrecond,
                    Preconditioner,
-                   Projector, Integrate_grad_dot, ShapeEval, context, TaskManager, SetNumThreads, SetHeapSize, ngsglobals, x, y, z, VOL, BND)
+                   Projector, Integrate_grad_dot, ShapeEval, context, TaskManager, SetNumThreads, SetHeapSize, ngsglobals, x, y, z, VOL, BND, Integrate)
 from . import solvers
 from .solvers import CGSolver
 from .adjoint import AdjointProblem, AdjointJ
@@ -18,4 +18,4 @@ __all__ = ["MakeStructured3DMesh", "MakeHexMesh", "JitterInterior", "ReadVolMesh
            "LinearForm", "GridFunction", "CoefficientFunction", "grad", "dx", "BaseVector", "BaseMatrix",
            "SparseMatrix", "BilinearFormApplication", "BlockMatrix", "JacobiPrecond", "Preconditioner", "Projector", "Integrate_grad_dot",
            "ShapeEval", "context", "solvers", "AdjointProblem", "AdjointJ", "TaskManager", "SetNumThreads",
-           "SetHeapSize", "ngsglobals", "CGSolver", "x", "y", "z", "VOL", "BND"]
+           "SetHeapSize", "ngsglobals", "CGSolver", "x", "y", "z", "VOL", "BND", "Integrate"]

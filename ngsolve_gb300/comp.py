@@ -124,9 +124,23 @@ class _Grad:
 
 
 def grad(u):
+    if isinstance(u, GridFunction):
+        return _GFGrad(u)
     if not isinstance(u, _Proxy):
-        raise TypeError("grad() expects a trial or test function")
+        raise TypeError("grad() expects a trial or test function or a GridFunction")
     return _Grad(u)
+
+
+class _GFGrad:
+    """grad(gfu) of a GridFunction: for Integrate(grad(a) * grad(b), mesh)."""
+
+    def __init__(self, gf):
+        self.gf = gf
+
+    def __mul__(self, other):
+        if isinstance(other, _GFGrad):
+            return _GFIntegrand("graddot", self.gf, other.gf)
+        raise NotImplementedError("grad(gfu) multiplies grad(gfu) only")
 
 
 class CoefficientFunction:
@@ -169,6 +183,8 @@ class CoefficientFunction:
         return np.ascontiguousarray(v)
 
     def __mul__(self, other):
+        if isinstance(other, GridFunction):
+            return NotImplemented
         return _Product.of(self, other)
 
     __rmul__ = __mul__
@@ -201,6 +217,8 @@ class _AffineCF(CoefficientFunction):
     def __mul__(self, other):
         if self._num(other):
             return _AffineCF(self.a * other, self.d * other)
+        if isinstance(other, GridFunction):
+            return NotImplemented
         return _Product.of(self, other)
 
     __rmul__ = __mul__
@@ -1152,6 +1170,13 @@ class GridFunction:
         self.name = name
         self.vec = BaseVector(fes.ndof) if vec is None else vec
 
+    def __mul__(self, other):
+        if not _gf_factor(other):
+            return NotImplemented
+        return _GFIntegrand("product", self, other)
+
+    __rmul__ = __mul__
+
     def Set(self, cf, VOL_or_BND=VOL):
         """gfu.Set(f) for f affine in x, y, z or constant, on scalar H1: the
         interpolant is then f itself (vertex values, all other DOFs zero), which
@@ -1188,6 +1213,73 @@ class GridFunction:
         n = self.fes.scalar.ndof
         return tuple(GridFunction(self.fes.scalar, "%s.%d" % (self.name, c), BaseVector(data=self.vec.t[c * n:(c + 1) * n]))
                      for c in range(self.fes.dim))
+
+
+class _GFIntegrand:
+    """Integrand of Integrate made of grid functions: "graddot" (grad a .
+    grad b) or "product" (a * b, where a factor may be a constant or affine
+    coefficient, taken as its interpolant)."""
+
+    def __init__(self, kind, a, b):
+        self.kind, self.a, self.b = kind, a, b
+
+
+def _gf_factor(f):
+    return isinstance(f, (GridFunction, _AffineCF, int, float, np.floating)) or (
+        isinstance(f, CoefficientFunction) and np.ndim(f.values) == 0)
+
+
+def Integrate(cf, mesh, element_wise=False, order=None):
+    """Integrate (comp/python_comp.cpp:3703-3948) for the integrands of this
+    path: grad(a) * grad(b) of two GridFunctions, element-wise (the dJ/dkappa
+    contraction of the adjoint recipe, on the GPU element kernel) or summed;
+    and the total of a product a * b or of a single factor, where a factor is a
+    GridFunction or a constant / affine coefficient (int a b = a^T M b with the
+    mass operator, exact for functions in the space).  `order` is accepted and
+    unused: the rules are those of the forms (order 2p)."""
+    if isinstance(cf, _GFIntegrand) and cf.kind == "graddot":
+        per = Integrate_grad_dot(cf.a.fes, cf.a.vec, cf.b.vec)
+        return per if element_wise else float(per.sum())
+    if element_wise:
+        raise NotImplementedError("element-wise Integrate takes grad(a) * grad(b) of GridFunctions")
+    if isinstance(cf, _GFIntegrand):
+        a, b = cf.a, cf.b
+    elif _gf_factor(cf):
+        a, b = cf, 1.0
+    else:
+        raise NotImplementedError("Integrate takes grad(a)*grad(b), a*b or a single factor of GridFunctions "
+                                  "and constant or affine coefficients")
+    fes = next((f.fes for f in (a, b) if isinstance(f, GridFunction)), None)
+    if fes is None:
+        raise NotImplementedError("Integrate of coefficients alone: multiply by a GridFunction of the space")
+    return _mass_integral(fes, a, b)
+
+
+def _space_vector(fes, f, like):
+    """f as a DOF vector of fes: a GridFunction's own, else the interpolant."""
+    if isinstance(f, GridFunction):
+        return f.vec
+    if not isinstance(f, _AffineCF):
+        f = _AffineCF((0.0, 0.0, 0.0), float(np.asarray(getattr(f, "values", f), dtype=np.float64)))
+    fi = torch.zeros_like(like.t)
+    pts = fes.mesh.raw.points
+    fi[:len(pts)] = torch.as_tensor(f.vertex_values(pts), dtype=fi.dtype, device=fi.device)
+    return BaseVector(data=fi)
+
+
+def _mass_integral(fes, a, b):
+    """int a b = a^T M b, with the matrix-free mass operator of fes (built once
+    per space)."""
+    if getattr(fes, "_mass_form", None) is None:
+        u, v = fes.TnT()
+        m = BilinearForm(fes, nonassemble=True)
+        m += u * v * dx
+        fes._mass_form = m.Assemble()
+    like = next(f.vec for f in (a, b) if isinstance(f, GridFunction))
+    av, bv = _space_vector(fes, a, like), _space_vector(fes, b, like)
+    mb = bv.CreateVector()
+    fes._mass_form.mat.Mult(bv, mb)
+    return av.InnerProduct(mb)
 
 
 def Integrate_grad_dot(fes, u, w):

@@ -375,3 +375,57 @@ def test_gridfunction_set():
         g.Set(C.CoefficientFunction(np.arange(4.0)))
     with pytest.raises(ValueError):
         g.Set(C.x, "SURFACE")
+
+
+def test_integrate(monkeypatch):
+    """Integrate on host stand-ins: grad(a)*grad(b) element-wise through the
+    element kernel's entry (summed when not element-wise); totals of products
+    and single factors as a^T M b with the mass operator (a dense host matrix
+    here), affine / constant factors as their interpolants; the rest raises."""
+    import torch
+    pts = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0]])
+    M = torch.tensor(np.diag([1.0, 2, 3, 4]), dtype=torch.float64)
+
+    class _Fes(_Space):
+        ndof = 4
+        mesh = type("M", (), {"raw": type("R", (), {"points": pts})()})()
+
+        def TnT(self):
+            return C._Proxy(self, False), C._Proxy(self, True)
+
+    class _Form:
+        def __init__(self, fes, nonassemble=False):
+            pass
+
+        def __iadd__(self, t):
+            return self
+
+        def Assemble(self):
+            self.mat = type("Mat", (), {"Mult": staticmethod(lambda xv, yv: yv.t.copy_(M @ xv.t))})()
+            return self
+
+    seen = []
+
+    def _gd(fes, u, w):
+        seen.append((u, w))
+        return torch.tensor([1.0, 2.0, 3.0, 4.0], dtype=torch.float64)
+
+    monkeypatch.setattr(C, "BilinearForm", _Form)
+    monkeypatch.setattr(C, "Integrate_grad_dot", _gd)
+    fes = _Fes()
+    a = C.GridFunction(fes, vec=C.BaseVector(data=torch.tensor([1.0, 1, 1, 1], dtype=torch.float64)))
+    b = C.GridFunction(fes, vec=C.BaseVector(data=torch.tensor([0.0, 1, 2, 3], dtype=torch.float64)))
+    per = C.Integrate(C.grad(a) * C.grad(b), None, element_wise=True)
+    assert torch.equal(per, torch.tensor([1.0, 2, 3, 4], dtype=torch.float64)) and seen[-1] == (a.vec, b.vec)
+    assert C.Integrate(C.grad(a) * C.grad(b), None) == 10.0
+    assert C.Integrate(a * b, None) == float(a.vec.t @ M @ b.vec.t)        # 0 + 2 + 6 + 12 = 20
+    assert C.Integrate(b, None) == float(b.vec.t @ M @ torch.tensor([1.0, 1, 1, 0], dtype=torch.float64))
+    xi = torch.tensor([0.0, 1, 0, 0], dtype=torch.float64)                  # x at the vertices, 0 elsewhere
+    assert C.Integrate(C.x * a, None) == float(xi @ M @ a.vec.t) == C.Integrate(a * C.x, None)
+    assert C.Integrate(2.0 * a, None) == float(a.vec.t @ M @ (2 * torch.tensor([1.0, 1, 1, 0], dtype=torch.float64)))
+    with pytest.raises(NotImplementedError):
+        C.Integrate(a * b, None, element_wise=True)
+    with pytest.raises(NotImplementedError):
+        C.Integrate(C.x, None)
+    with pytest.raises(TypeError):
+        a * C.CoefficientFunction(np.arange(4.0))
