@@ -228,7 +228,9 @@ def run_reference(args, ws, rank):
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "GDOF/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(r["seconds_per_sample_apply"] for r in res),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "nx": args.nx, "order": args.order, "l2": "inputs larger than L2"},
+           "config": {"workload": WORKLOAD, "nx": args.nx, "order": args.order,
+                      "ndof": (args.nx * args.order + 1) ** 3, "ne": args.nx ** 3,
+                      "parallelism": "replicas" if ws > 1 else "single", "l2": "inputs larger than L2"},
            "cpu_baseline": {"value": val, "unit": "GDOF/s", "cores": r0["cores"], "kind": "port", "sample": r0["sample"]},
            "e2e": {"value": val, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "NGSolve needs netgen/ngcore (absent, no network): the CPU restatement of its element-wise "
@@ -752,6 +754,35 @@ def main():
         del ag
         torch.cuda.empty_cache()
 
+    # the same apply with the 1D contractions on the tensor cores (variant 6:
+    # tcgen05 kind::tf32 GEMMs, 3xTF32 split), timed beside the autotuner's choice
+    tensor_core = None
+    if 4 <= args.order <= 7:
+        os.environ["GH1_HEX_GMODE"] = "6"
+        at = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+        at += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+        at.Assemble()
+        del os.environ["GH1_HEX_GMODE"]
+        if at.mat.Info()["hex_variant_fp32"] == 6:
+            for _ in range(3):
+                at.mat.Mult(x32, y32)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                at.mat.Mult(x32, y32)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tt = e0.elapsed_time(e1) / 1e3 / args.steps
+            Bt, _ = model_bytes_flops(ne, N, args.order, 4, 4)
+            tensor_core = {"variant": 6, "ms": tt * 1e3, "gdofs": N / tt / 1e9, "achieved_gbs": Bt / tt / 1e9,
+                           "frac": Bt / tt / 1e9 / load_peaks()[0],
+                           "kernel": "hex_apply_tc_kernel<%d, 0, %d>" % (args.order + 1, 1 if variant in (4, 5) else 0),
+                           "note": "1D contractions as tcgen05.mma kind::tf32 (M=128 pencils, K=8, N=16), "
+                                   "3xTF32 split, FP32 accumulation in tensor memory"}
+        del at
+        torch.cuda.empty_cache()
+
     # ---- e2e through the public API with host buffers -------------------------
     xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
     xh.copy_(x32.t.cpu())
@@ -861,9 +892,11 @@ def main():
               "hex_apply_pair_kernel<%d, 0, %d>" % (nn, variant - 2))
     traffic = None
     if args.order == ORDER and args.nx == NX:  # the committed profiles cover the benchmark configuration
-        traffic = load_traffic({0: "hex_apply_fp32_c3.md", 1: "hex_apply_fp32_c3.md", 2: "hex_apply_pair_fp32_c3.md",
-                                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md",
-                                5: "hex_apply_slice_affine_fp32_c3.md"}[variant])
+        # variant 5 (the slice form) has no capture at this configuration: the
+        # autotuner has not picked it at p=4, so its traffic stays null
+        prof = {0: "hex_apply_fp32_c3.md", 1: "hex_apply_fp32_c3.md", 2: "hex_apply_pair_fp32_c3.md",
+                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md"}.get(variant)
+        traffic = load_traffic(prof) if prof else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": B32, "kernel": kernel, "variant": variant}
@@ -890,7 +923,7 @@ def main():
                           "parallelism": "replicas" if ws > 1 else "single",
                           "l2": "inputs larger than L2 (G tile stream %.0f MB per apply)" % (ne * (args.order + 1) ** 3 * 24 / 1e6)},
                "e2e": e2e, "gpu_launches": args.steps, "clocks": ck, "roofline": roofline,
-               "general_geometry_apply": general, "setup": setup,
+               "general_geometry_apply": general, "tensor_core_apply": tensor_core, "setup": setup,
                "fp64_apply": {"ms": t64 * 1e3, "gdofs": N / t64 / 1e9, "achieved_tflops_model": F / t64 / 1e12,
                               "achieved_gbs_model": B64 / t64 / 1e9},
                "cg": cg, "cpu_baseline": cpu}

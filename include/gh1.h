@@ -105,6 +105,10 @@ int gh1_form_set_coefs(gh1_form* form, const double* kappa, const double* mu, in
  * form (dJ/dkappa needs the scalar coefficient).  Operators made from the form
  * afterwards, and matrix-free operators at their next apply, use the tensor. */
 int gh1_form_set_tensor(gh1_form* form, const double* K6, int mem);
+/* Releases the caller's handle.  Operators made from the form (gh1_assemble_csr,
+ * gh1_matfree_create, gh1_batch_create) keep it alive, as the reference's
+ * BilinearFormApplication holds its BilinearForm: its memory goes when the last
+ * of them is freed.  The space must outlive the form and its operators.     */
 int gh1_form_free(gh1_form* form);
 
 /* BilinearForm.Assemble() -> SparseMatrix (comp/bilinearform.cpp:832-1000,
@@ -190,7 +194,7 @@ typedef struct {
   int initialize;      /* 1: start from x = 0, 0: use x as initial guess       */
   double inner_tol;    /* MIXED: relative reduction per inner solve (0=default)*/
   int max_outer;       /* MIXED: maximal refinement steps (0 = default 30)      */
-  int check_every;     /* iterations per graph launch between host checks (0=auto) */
+  int check_every;     /* iterations per body of the device-side WHILE loop (0=auto) */
   double* res_hist;    /* optional host buffer [maxit+1] of residuals (may be NULL) */
 } gh1_cg_opts;
 typedef struct {
@@ -226,13 +230,16 @@ int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u_target, do
  * "256 problems x 16 rhs"), solved by the mixed-precision method of gh1_cg:
  * every (problem, rhs) pair is a device-side state machine (FP64 residual ->
  * FP32 inner Jacobi-PCG -> FP64 correction) and all problems advance together
- * through ONE CUDA graph (one branch per problem) launched until all pairs
- * converged.  The multi-rhs apply reads each element's G tile once for all
- * right-hand sides.  No counterpart in the reference, which solves one system
- * per CGSolver call (python/krylovspace.py:263-291).
+ * in ONE launch of one CUDA graph: a conditional WHILE node whose body is one
+ * round of every problem (one branch per problem) repeats on the device until
+ * all pairs converged.  The multi-rhs apply reads each element's G tile once
+ * for all right-hand sides; gh1_batch_create times its two FP32 forms (one or
+ * two right-hand sides per lane) on each problem and keeps the faster.  No
+ * counterpart in the reference, which solves one system per CGSolver call
+ * (python/krylovspace.py:263-291).
  * rhs[p], x[p]: device double[nrhs[p]*ndof_p], right-hand side r at offset
  * r*ndof_p.  opts: tol, maxit (per inner solve), inner_tol, max_outer,
- * check_every (inner iterations per graph round), initialize.
+ * check_every (inner iterations per round), initialize.
  * res: sum(nrhs) results, problem-major.                                      */
 typedef struct gh1_batch gh1_batch;
 int gh1_batch_create(gh1_ctx* ctx, int nprob, gh1_form* const* forms, const int* nrhs, gh1_batch** batch);

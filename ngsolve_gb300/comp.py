@@ -1238,6 +1238,8 @@ def Integrate(cf, mesh, element_wise=False, order=None):
     mass operator, exact for functions in the space).  `order` is accepted and
     unused: the rules are those of the forms (order 2p)."""
     if isinstance(cf, _GFIntegrand) and cf.kind == "graddot":
+        if cf.a.fes is not cf.b.fes:
+            raise ValueError("grad(a) * grad(b) needs a and b on the same space")
         per = Integrate_grad_dot(cf.a.fes, cf.a.vec, cf.b.vec)
         return per if element_wise else float(per.sum())
     if element_wise:
@@ -1270,6 +1272,10 @@ def _space_vector(fes, f, like):
 def _mass_integral(fes, a, b):
     """int a b = a^T M b, with the matrix-free mass operator of fes (built once
     per space)."""
+    if isinstance(fes, VectorH1) and any(not isinstance(f, GridFunction) for f in (a, b)):
+        # a coefficient's interpolant lives in a scalar space; on VectorH1 the
+        # integral of a coefficient times a vector field is a vector
+        raise NotImplementedError("Integrate of a coefficient times a GridFunction takes scalar H1 only")
     if getattr(fes, "_mass_form", None) is None:
         u, v = fes.TnT()
         m = BilinearForm(fes, nonassemble=True)
@@ -1283,9 +1289,20 @@ def _mass_integral(fes, a, b):
 
 
 def Integrate_grad_dot(fes, u, w):
-    """Element-wise int_e grad u . grad w (Integrate(..., element_wise=True))."""
-    ctx = fes.ctx.sync_stream()
+    """Element-wise int_e grad u . grad w (Integrate(..., element_wise=True)).
+    u and w are DOF vectors of the scalar H1 space fes: contiguous FP64 CUDA
+    tensors of length fes.ndof (the kernel reads fes.ndof doubles of each)."""
+    if isinstance(fes, VectorH1):
+        raise TypeError("Integrate_grad_dot takes a scalar H1 space")
     u, w = _as_vec(u), _as_vec(w)
+    for t in (u.t, w.t):
+        if t.dtype != torch.float64:
+            raise TypeError("grad(a) * grad(b) takes FP64 vectors")
+        if not (t.is_cuda and t.is_contiguous()):
+            raise TypeError("grad(a) * grad(b) takes contiguous CUDA vectors")
+        if t.numel() != fes.ndof:
+            raise ValueError("vector length %d does not match the space (%d DOFs)" % (t.numel(), fes.ndof))
+    ctx = fes.ctx.sync_stream()
     out = torch.zeros(fes.ne, dtype=torch.float64, device=u.t.device)
     ctx.check(ctx.lib.gh1_elem_grad_dot(fes.h, _ptr(u.t), _ptr(w.t), _ptr(out)))
     return out

@@ -282,6 +282,17 @@ gh1_form::~gh1_form() {
   delete adj_mass;
 }
 
+namespace gh1 {
+void form_retain(gh1_form* f) { f->refs++; }
+void form_release(gh1_form* f) {
+  if (--f->refs == 0) delete f;
+}
+}  // namespace gh1
+
+gh1_op::~gh1_op() {
+  if (form_ref && form) gh1::form_release(form);
+}
+
 // =============================================================================
 namespace gh1 {
 
@@ -522,7 +533,12 @@ int gh1_form_set_tensor(gh1_form* f, const double* K6, int mem) {
   });
 }
 
-int gh1_form_free(gh1_form* f) { delete f; return GH1_OK; }
+// The caller's reference; operators made from the form keep it alive until the
+// last of them is freed (the operators read its coefficients when they refresh).
+int gh1_form_free(gh1_form* f) {
+  if (f) gh1::form_release(f);
+  return GH1_OK;
+}
 
 int gh1_assemble_csr(gh1_form* f, gh1_op** out) {
   if (!f || !out) return GH1_ERR_ARG;
@@ -537,6 +553,8 @@ int gh1_assemble_csr(gh1_form* f, gh1_op** out) {
     }
     gh1_op* op = new gh1_op();
     op->ctx = sp->ctx; op->kind = GH1_OP_CSR; op->form = f; op->sp = sp;
+    form_retain(f);
+    op->form_ref = true;
     op->nrows = sp->ndof; op->nnz = sp->nnz;
     op->rowptr = sp->d_rowptr.p; op->colind = sp->d_colind.p;
     try {
@@ -596,6 +614,8 @@ int gh1_matfree_create(gh1_form* f, int prec_mask, gh1_op** out) {
     gh1_op* op = new gh1_op();
     op->ctx = f->sp->ctx; op->kind = GH1_OP_MATFREE; op->form = f; op->sp = f->sp;
     op->nrows = f->sp->ndof; op->prec_mask = prec_mask & 3;
+    form_retain(f);
+    op->form_ref = true;
     try {
       matfree_setup(op);
     } catch (...) { delete op; throw; }

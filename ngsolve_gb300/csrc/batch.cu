@@ -1,5 +1,5 @@
 // batch.cu -- batched solves: many independent problems, up to 16 right-hand
-// sides each, advanced together by repeated launches of ONE CUDA graph.
+// sides each, advanced together by ONE launch of one CUDA graph.
 //
 // Every (problem, rhs) pair runs the mixed-precision solver of cg.cu as a small
 // state machine in device memory:
@@ -10,9 +10,13 @@
 //   CORRECT : x += |r| c, back to NEED
 // One graph round per problem = [FP64 apply, residual, begin] + K x [FP32 apply,
 // update, direction] + [correct]; problems are independent graph branches.
-// Kernels whose rhs is in another phase return at once, so the same graph is
-// launched until every pair is DONE (the host reads one counter per launch).
-// The multi-rhs apply stages each element's G tile once for all active rhs.
+// Kernels whose rhs is in another phase return at once, so the round is the
+// body of a conditional WHILE node that repeats on the device until every pair
+// is DONE (a one-thread kernel at the end of the body sets the condition from a
+// device counter; the host waits once, after the launch).
+// The multi-rhs apply stages each element's G tile once for all active rhs; its
+// FP32 form (two right-hand sides per lane or one) is timed per problem at
+// gh1_batch_create.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -158,6 +162,15 @@ __global__ void __launch_bounds__(BB) b_dir(int64_t n, const float* __restrict__
     s32[o + i] = w32[o + i] + beta * s32[o + i];
 }
 
+// tail of the WHILE body: count the rounds and loop while a (problem, rhs)
+// pair is not done and the round bound ctl[1] is not reached
+__global__ void b_loop_kernel(const int* done_total, int total, int* ctl, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const int rounds = ++ctl[0];
+    cudaGraphSetConditional(h, (*(volatile const int*)done_total < total && rounds < ctl[1]) ? 1u : 0u);
+  }
+}
+
 // phase CORRECT: x += |r| c ; y64 = 0 ; then back to NEED (last block)
 __global__ void __launch_bounds__(BB) b_correct(int64_t n, const float* __restrict__ x32, double* __restrict__ x,
                                                 double* __restrict__ y64, int* phase, RState* st, double* partial,
@@ -198,6 +211,7 @@ struct gh1_batch {
   };
   std::vector<Prob*> probs;
   DBuf<int> done_total;
+  DBuf<int> ctl;  // [2]: rounds so far, bound on rounds
   ~gh1_batch() {
     for (auto* p : probs) {
       if (p->pre) gh1_pre_free(p->pre);
@@ -208,6 +222,41 @@ struct gh1_batch {
 };
 
 namespace {
+// The FP32 multi-rhs apply of one problem, two right-hand sides per lane or
+// one, timed on the problem's own operator with all its rhs active; the faster
+// form is kept on the operator (the batched solves' tile choice).
+void tune_multi_pair(gh1_ctx* ctx, gh1_batch::Prob* P) {
+  gh1_op* op = P->op;
+  cudaStream_t s = ctx->stream;
+  const int R = P->R;
+  std::vector<int> inner(R, PH_INNER);
+  GH1_CUDA(cudaMemcpyAsync(P->phase.p, inner.data(), R * sizeof(int), cudaMemcpyHostToDevice, s));
+  P->s32.zero(s);
+  P->y32.zero(s);
+  cudaEvent_t a, b;
+  GH1_CUDA(cudaEventCreate(&a));
+  GH1_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  int choice = 1;
+  for (int pr = 1; pr >= 0; pr--) {
+    op->multi_pair = pr;
+    unsigned int* c = P->cnt.p + 4 * R;
+    matfree_apply_multi(op, R, P->phase.p, PH_INNER, P->s32.p, P->y32.p, GH1_F32, P->partial.p, c, P->energy.p, false);
+    GH1_CUDA(cudaEventRecord(a, s));
+    for (int k = 0; k < 3; k++)
+      matfree_apply_multi(op, R, P->phase.p, PH_INNER, P->s32.p, P->y32.p, GH1_F32, P->partial.p, c, P->energy.p, false);
+    GH1_CUDA(cudaEventRecord(b, s));
+    GH1_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    GH1_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (ms < best) { best = ms; choice = pr; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  op->multi_pair = choice;
+  GH1_CUDA(cudaMemsetAsync(P->phase.p, 0, R * sizeof(int), s));  // PH_NEED
+}
+
 template <class F>
 int bguard(gh1_ctx* ctx, F&& f) {
   try {
@@ -251,13 +300,21 @@ extern "C" int gh1_batch_create(gh1_ctx* ctx, int nprob, gh1_form* const* forms,
         P->cnt.alloc(6 * R);
         P->cnt.zero(ctx->stream);
         P->gx = (int)std::max<int64_t>(1, std::min<int64_t>((n + BB - 1) / BB, std::max<int64_t>(1, ctx->nsm * 16 / R)));
-        P->gapply = std::max(matfree_apply_multi(P->op, P->R, P->phase.p, PH_NEED, nullptr, nullptr, GH1_F64, nullptr,
-                                                 nullptr, nullptr, true),
-                             matfree_apply_multi(P->op, P->R, P->phase.p, PH_INNER, nullptr, nullptr, GH1_F32, nullptr,
-                                                 nullptr, nullptr, true));
+        // grids of the FP64 apply and of both FP32 forms (one or two rhs per lane)
+        int g32[2];
+        for (int pr = 0; pr < 2; pr++) {
+          P->op->multi_pair = pr;
+          g32[pr] = matfree_apply_multi(P->op, P->R, P->phase.p, PH_INNER, nullptr, nullptr, GH1_F32, nullptr, nullptr,
+                                        nullptr, true);
+        }
+        P->gapply = std::max({matfree_apply_multi(P->op, P->R, P->phase.p, PH_NEED, nullptr, nullptr, GH1_F64, nullptr,
+                                                  nullptr, nullptr, true),
+                              g32[0], g32[1]});
         P->partial.alloc((size_t)R * std::max(2 * P->gx, P->gapply) + 8);
+        tune_multi_pair(ctx, P);
       }
       B->done_total.alloc(1);
+      B->ctl.alloc(2);
       GH1_CUDA(cudaStreamSynchronize(ctx->stream));
     } catch (...) {
       delete B;
@@ -293,7 +350,12 @@ extern "C" int gh1_batch_solve(gh1_batch* B, const double* const* rhs, double* c
     for (auto& e : ev) GH1_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    bool capturing = false;
     auto cleanup = [&] {
+      if (capturing) {  // a failure inside the capture: end it before the stream goes
+        cudaGraph_t dummy;
+        cudaStreamEndCapture(cs, &dummy);
+      }
       ctx->stream = user;
       if (exec) cudaGraphExecDestroy(exec);
       if (graph) cudaGraphDestroy(graph);
@@ -316,8 +378,22 @@ extern "C" int gh1_batch_solve(gh1_batch* B, const double* const* rhs, double* c
         if (o->initialize) GH1_CUDA(cudaMemsetAsync(x[i], 0, (size_t)P->R * P->n * sizeof(double), cs));
       }
       GH1_CUDA(cudaMemsetAsync(B->done_total.p, 0, sizeof(int), cs));
-      // ---- capture one round of every problem as parallel branches ----------
-      GH1_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      const int max_rounds = (inner_maxit + K - 1) / K * (max_outer + 1) + max_outer + 4;
+      // ---- one WHILE node; its body is one round of every problem, as parallel
+      // branches, and the loop condition -------------------------------------
+      GH1_CUDA(cudaGraphCreate(&graph, 0));
+      cudaGraphConditionalHandle handle;
+      GH1_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t loop;
+      GH1_CUDA(cudaGraphAddNode(&loop, graph, nullptr, nullptr, 0, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      GH1_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
       GH1_CUDA(cudaEventRecord(ev[ns], cs));
       for (int s = 0; s < ns; s++) GH1_CUDA(cudaStreamWaitEvent(pool[s], ev[ns], 0));
       for (int i = 0; i < np; i++) {
@@ -353,19 +429,17 @@ extern "C" int gh1_batch_solve(gh1_batch* B, const double* const* rhs, double* c
         GH1_CUDA(cudaStreamWaitEvent(cs, ev[s], 0));
       }
       ctx->stream = cs;
-      GH1_CUDA(cudaStreamEndCapture(cs, &graph));
+      b_loop_kernel<<<1, 32, 0, cs>>>(B->done_total.p, total, B->ctl.p, handle);
+      check_kernel(ctx, "b_loop_kernel");
+      capturing = false;
+      GH1_CUDA(cudaStreamEndCapture(cs, &body));
       GH1_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-      // ---- launch rounds until every (problem, rhs) is done ------------------
-      int* hd = (int*)ctx->h_pinned;
-      const int max_rounds = (inner_maxit + K - 1) / K * (max_outer + 1) + max_outer + 4;
-      int rounds = 0;
-      while (true) {
-        GH1_CUDA(cudaMemcpyAsync(hd, B->done_total.p, sizeof(int), cudaMemcpyDeviceToHost, cs));
-        GH1_CUDA(cudaStreamSynchronize(cs));
-        if (*hd >= total || rounds >= max_rounds) break;
-        GH1_CUDA(cudaGraphLaunch(exec, cs));
-        rounds++;
-      }
+      // ---- one launch: rounds run on the device until every (problem, rhs) is
+      // done or the round bound is reached --------------------------------------
+      const int hctl[2] = {0, max_rounds};
+      GH1_CUDA(cudaMemcpyAsync(B->ctl.p, hctl, sizeof(hctl), cudaMemcpyHostToDevice, cs));
+      GH1_CUDA(cudaGraphLaunch(exec, cs));
+      GH1_CUDA(cudaStreamSynchronize(cs));
       // ---- results -------------------------------------------------------------
       int k = 0;
       for (int i = 0; i < np; i++) {

@@ -11,11 +11,13 @@
 // GPU layout of one iteration: [apply: y = A s, s.y as the sum of element
 // energies s_e^T A_e s_e] -> [update: alpha, x, d, w = P d, y = 0, w.d, |d|^2;
 // the last block forms beta and the convergence flag] -> [direction: s = w +
-// beta s].  All scalars stay on the device; a CUDA graph holds `chunk`
-// iterations and the host reads the flag once per graph launch (the role of
-// the reference's WHILE-conditional graph, ngscuda/cuda_krylov.cpp:19-203).
-// Every device loop is bounded by maxit; kernels after convergence return at
-// their first instruction.
+// beta s].  All scalars stay on the device.  One inner solve is ONE graph
+// launch: a conditional WHILE node (the reference's device CG loop,
+// ngscuda/cuda_krylov.cpp:19-203 with ngscuda/cuda_core.hpp:170-250) whose body
+// holds `chunk` iterations and a one-thread kernel that sets the loop condition
+// from the device-side convergence flag; the host synchronizes once per solve.
+// Every device loop is bounded by maxit (the body count is capped as well);
+// kernels after convergence return at their first instruction.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -147,6 +149,15 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T
     if (!isfinite(r)) { st->done = 1; st->status = GH1_BREAKDOWN; }
     else if (r <= st->stop) { st->done = 1; st->status = GH1_OK; }
     else if (st->it >= st->maxit) { st->done = 1; st->status = GH1_MAXITER; }
+  }
+}
+
+// tail of the WHILE body: count the body launches and keep looping while the
+// solve is not done and the launch bound ctl[1] is not reached
+__global__ void cg_loop_kernel(const CGState* st, int* ctl, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const int launches = ++ctl[0];
+    cudaGraphSetConditional(h, (!*(volatile const int*)&st->done && launches < ctl[1]) ? 1u : 0u);
   }
 }
 
@@ -293,6 +304,7 @@ struct PCG {
   unsigned int* counters;  // [4]
   double* hist;
   int chunk;
+  int* ctl;              // [2]: body launches so far, bound on body launches
   int applies = 0;
 
   void launch_iteration(cudaStream_t cs) {
@@ -322,29 +334,51 @@ struct PCG {
     cg_init_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, d, w, s, st, tol, hist, partial, counters + 0);
     check_kernel(ctx, "cg_init_kernel");
     CGState* hs = (CGState*)ctx->h_pinned;
-    // graph of `chunk` iterations, built once per solve shape
+    // one WHILE node whose body is `chunk` iterations plus the loop condition,
+    // built once per solve shape
     cudaGraphExec_t exec = *cache_exec;
     if (!exec || *cache_chunk != chunk) {
       if (exec) cudaGraphExecDestroy(exec);
+      *cache_exec = nullptr;
       op_prepare_any(op, prec);
       cudaGraph_t graph;
-      GH1_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < chunk; k++) launch_iteration(cs);
-      GH1_CUDA(cudaStreamEndCapture(cs, &graph));
-      GH1_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+      GH1_CUDA(cudaGraphCreate(&graph, 0));
+      try {
+        cudaGraphConditionalHandle handle;
+        GH1_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop;
+        GH1_CUDA(cudaGraphAddNode(&loop, graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GH1_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+          for (int k = 0; k < chunk; k++) launch_iteration(cs);
+          cg_loop_kernel<<<1, 32, 0, cs>>>(st, ctl, handle);
+          check_kernel(ctx, "cg_loop_kernel");
+        } catch (...) {
+          cudaGraph_t dummy;
+          cudaStreamEndCapture(cs, &dummy);
+          throw;
+        }
+        GH1_CUDA(cudaStreamEndCapture(cs, &body));
+        GH1_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+      } catch (...) {
+        cudaGraphDestroy(graph);
+        throw;
+      }
       cudaGraphDestroy(graph);
       *cache_exec = exec;
       *cache_chunk = chunk;
     }
-    int launches = 0;
-    const int max_launches = (maxit + chunk - 1) / chunk + 2;
-    while (true) {
-      GH1_CUDA(cudaMemcpyAsync(hs, st, sizeof(CGState), cudaMemcpyDeviceToHost, cs));
-      GH1_CUDA(cudaStreamSynchronize(cs));
-      if (hs->done || launches >= max_launches) break;
-      GH1_CUDA(cudaGraphLaunch(exec, cs));
-      launches++;
-    }
+    const int hctl[2] = {0, (maxit + chunk - 1) / chunk + 2};
+    GH1_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(hctl), cudaMemcpyHostToDevice, cs));
+    GH1_CUDA(cudaGraphLaunch(exec, cs));
+    GH1_CUDA(cudaMemcpyAsync(hs, st, sizeof(CGState), cudaMemcpyDeviceToHost, cs));
+    GH1_CUDA(cudaStreamSynchronize(cs));
     CGState out = *hs;
     applies = out.it - 1;
     return out;
@@ -382,6 +416,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     DBuf<CGState> st(1);
     DBuf<double> hist((size_t)o->maxit + 2);
     DBuf<double> norm2(2);
+    DBuf<int> ctl(2);
     DBuf<uint8_t> ones;
     const uint8_t* freemask = pre ? pre->d_free.p : nullptr;
     if (!freemask) {
@@ -396,7 +431,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
       inv_ident.upload(one, cs);
       inv64 = inv_ident.p;
     }
-    int chunk = o->check_every > 0 ? o->check_every : 16;
+    int chunk = o->check_every > 0 ? o->check_every : 8;
     auto bnorm2 = [&](const double* y, double* rr) {  // |b - y|^2, |b|^2 on free DOFs
       int g = red_grid(ctx, n);
       residual_kernel<<<g, RED_BLOCK, 0, cs>>>(n, b, y, freemask, rr, norm2.p, partial.p, counters.p + 3);
@@ -430,7 +465,8 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     int ch64 = 0, ch32 = 0;
     double final_rr = 0.0;  // |b - A x|^2 on free DOFs for the returned x
     if (o->mode == GH1_CG_FP64) {
-      PCG<double> P{op, ctx, n, inv64, x, W.d64.p, W.w64.p, W.s64.p, W.y64.p, GH1_F64, st.p, partial.p, counters.p, hist.p, chunk};
+      PCG<double> P{op, ctx, n, inv64, x, W.d64.p, W.w64.p, W.s64.p, W.y64.p, GH1_F64, st.p, partial.p, counters.p, hist.p, chunk,
+                    ctl.p};
       GH1_CUDA(cudaMemsetAsync(W.y64.p, 0, n * sizeof(double), cs));
       CGState res = P.run(o->tol, o->maxit, o->stop_rule, bb, cs, &exec64, &ch64);
       execs.push_back(exec64);
@@ -476,14 +512,17 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
         if (std::sqrt(rr) <= target) { status = GH1_OK; break; }
         if (outer == max_outer || total_inner >= o->maxit) break;
         // inner: A c = r / |r|  in FP32, c0 = 0.  The last refinement step only
-        // needs the reduction that is still missing (with a safety factor 0.1).
+        // needs the reduction that is still missing; it aims two decades below
+        // the target, because with the hierarchical basis at p >= 3 (cond(A) up
+        // to ~1e9) the error of x is a few hundred times the relative residual:
+        // the returned x then carries the error of a residual ~tol/100, not tol.
         const double missing = target / std::sqrt(rr);
-        const double tol_k = std::min(0.5, std::max(inner_tol, 0.1 * missing));
+        const double tol_k = std::min(0.5, std::max(inner_tol, 0.01 * missing));
         scale_to_f32_kernel<<<grid_for(ctx, n, 256), 256, 0, cs>>>(n, W.r64.p, norm2.p, W.d32.p);
         check_kernel(ctx, "scale_to_f32_kernel");
         GH1_CUDA(cudaMemsetAsync(W.x32.p, 0, n * sizeof(float), cs));
         PCG<float> P{op, ctx, n, pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32, st.p, partial.p,
-                     counters.p, nullptr, chunk};
+                     counters.p, nullptr, chunk, ctl.p};
         CGState res = P.run(tol_k, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
         total_inner += res.it;
         r->applies32 += P.applies;
@@ -542,6 +581,10 @@ extern "C" int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u
     if (!form->adj_A) {
       rc = gh1_matfree_create(form, 3, &form->adj_A);
       if (rc) return rc;
+      // the form owns this operator (it is deleted with the form), so the
+      // operator must not keep the form alive in turn
+      form->adj_A->form_ref = false;
+      form->refs--;
     }
     gh1_op* A = form->adj_A;
     if (A->form_version != form->version) matfree_setup(A);

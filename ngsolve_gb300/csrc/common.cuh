@@ -148,6 +148,10 @@ struct gh1_form {
   gh1::DBuf<double> d_K6;     // ne x 6 symmetric diffusion tensors (xx yy zz xy xz yz); empty: kappa I
   bool has_K6 = false;
   int version = 0;            // bumped on coefficient change
+  // references: the caller's (dropped by gh1_form_free) plus one per operator
+  // made from the form (dropped when the operator is freed); the form is
+  // destroyed when the last one goes
+  int refs = 1;
   // gh1_adjoint_grad cache: this form's operator (FP64 + FP32 data; its metrics
   // follow coefficient changes) and the unit-mass operator for J and the adjoint
   // right-hand side; released with the form
@@ -164,6 +168,7 @@ struct gh1_op {
   gh1_ctx* ctx = nullptr;
   int kind = GH1_OP_CSR;
   gh1_form* form = nullptr;   // NULL for imported CSR
+  bool form_ref = false;      // this operator holds a reference on form (released with it)
   gh1_space* sp = nullptr;
   int64_t nrows = 0;
   gh1_op* inner = nullptr;    // GH1_OP_BLOCK: the repeated operator (borrowed)
@@ -192,13 +197,17 @@ struct gh1_op {
   int hex_gmode[2] = {0, 0};                 // autotuned hex apply variant per precision: 0/1 = G tile by TMA /
                                              // direct loads; FP32 also 2/3 = the same with two elements per lane,
                                              // 4 = two elements per lane with per-element (affine) metrics,
-                                             // 5 = slice / pencil form of 4 (hexpair.cu)
+                                             // 5 = slice / pencil form of 4 (hexpair.cu),
+                                             // 6 = 1D contractions on the tensor cores (hextc.cu)
   int pair_per_sm[3] = {0, 0, 0};            // resident blocks per SM of the paired FP32 apply [G mode]
   int slice_per_sm = 0;                      // ... of the slice-form FP32 apply (0: not available)
+  int tc_per_sm = 0;                         // ... of the tensor-core FP32 apply (0: not available)
   bool all_affine = false;                   // hex: every element map affine (G mode 2 available)
   gh1::DBuf<float> d_Ga32;                   // hex, all affine: per-element metric records [ne][8]
   int multi_per_sm[2] = {0, 0};              // resident blocks per SM of the multi-rhs apply
   int multi_pair_per_sm = 0;                 // ... of the FP32 multi-rhs apply with two rhs per lane
+  int multi_pair = -1;                       // FP32 multi-rhs apply: 1 = two rhs per lane, 0 = one
+                                             // (timed per problem by gh1_batch_create; -1: not timed, two)
   int spmv_L[2] = {0, 0};                    // autotuned SpMV sub-warp width (FP64, FP32)
   bool has_mass = false;
   // tet tiled apply (tetapply.cu): elements sorted by orientation class, tiles of
@@ -218,6 +227,10 @@ struct gh1_op {
   // scratch vectors for accumulate / scaling
   gh1::DBuf<double> d_tmp64;
   gh1::DBuf<float> d_tmp32;
+  gh1_op() = default;
+  gh1_op(const gh1_op&) = delete;
+  gh1_op& operator=(const gh1_op&) = delete;
+  ~gh1_op();  // api.cu: drops the form reference
 };
 
 struct gh1_pre {
@@ -229,6 +242,9 @@ struct gh1_pre {
 };
 
 namespace gh1 {
+// form references held by operators (api.cu)
+void form_retain(gh1_form* f);
+void form_release(gh1_form* f);
 // host helpers implemented in api.cu
 int grid_for(gh1_ctx* ctx, int64_t work, int block, int per_sm = 8);
 void check_kernel(gh1_ctx* ctx, const char* what);
@@ -270,6 +286,11 @@ bool hex_slice_supported(int N);
 void hex_slice_setup(gh1_op* op);
 void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                      const int* skip);
+// FP32 hex apply with the 1D contractions on the tensor cores (hextc.cu)
+bool hex_tc_supported(int N);
+int hex_tc_occupancy(gh1_op* op);
+void hex_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                  const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
 // any operator kind (api.cu): y = A x into a y the call zeroes first where the kind
 // needs it; skip as for the CG graph kernels; prepare / refresh before capture

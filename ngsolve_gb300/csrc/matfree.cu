@@ -1012,6 +1012,10 @@ void hex_apply_dispatch(gh1_op* op, const T* x, T* y, const T* G, int gstride, d
   const int pi = std::is_same<T, float>::value ? 1 : 0;
   const int gm = op->hex_gmode[pi];
   if constexpr (std::is_same<T, float>::value) {
+    if (gm == 6) {
+      hex_tc_apply(op, x, y, partial, counter, energy, skip);
+      return;
+    }
     if (gm == 5) {
       hex_slice_apply(op, x, y, partial, counter, energy, skip);
       return;
@@ -1041,21 +1045,29 @@ int hex_occupancy_dispatch(gh1_op* op, int gstride) {
 }
 
 // Autotuner: times each variant -- G tile staged in shared memory by TMA vs
-// direct coalesced loads, and for FP32 each of those with two elements per lane
+// direct coalesced loads, for FP32 each of those with two elements per lane, the
+// per-element-metric and slice forms on affine meshes, and the tensor-core form
 // -- on this operator's own mesh and keeps the fastest.  The choice is cached per
 // (order, precision, element-count bucket, affine mesh) for the process.
-// GH1_HEX_GMODE=0..5 forces a variant (FP64 takes it modulo 2; 4 and 5 need an
-// all-affine mesh, 5 an order the slice form supports).
+// GH1_HEX_GMODE=0..6 forces a variant (FP64 takes it modulo 2; a variant this
+// operator does not provide falls back to its number modulo 2).
 template <class T>
 void hex_autotune(gh1_op* op, const T* G, int gstride) {
   const int pi = std::is_same<T, float>::value ? 1 : 0;
-  int nmodes = (pi == 1 && op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) ? 4 : 2;
-  if (nmodes == 4 && op->pair_per_sm[2] > 0) nmodes = 5;
-  if (nmodes == 5 && op->slice_per_sm > 0) nmodes = 6;
+  std::vector<int> modes = {0, 1};
+  if (pi == 1) {
+    if (op->pair_per_sm[0] > 0 && op->pair_per_sm[1] > 0) {
+      modes.push_back(2);
+      modes.push_back(3);
+      if (op->pair_per_sm[2] > 0) modes.push_back(4);
+      if (op->pair_per_sm[2] > 0 && op->slice_per_sm > 0) modes.push_back(5);
+    }
+    if (op->tc_per_sm > 0) modes.push_back(6);
+  }
   const char* env = getenv("GH1_HEX_GMODE");
-  if (env && env[0] >= '0' && env[0] <= '5') {
+  if (env && env[0] >= '0' && env[0] <= '6') {
     const int m = env[0] - '0';
-    op->hex_gmode[pi] = m < nmodes ? m : m % 2;
+    op->hex_gmode[pi] = std::find(modes.begin(), modes.end(), m) != modes.end() ? m : m % 2;
     return;
   }
   static std::vector<std::array<int, 4>> cache;  // N, precision, log2(ne), choice
@@ -1064,7 +1076,10 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   while ((1 << (lb + 1)) <= ne) lb++;
   const int key = lb + (op->has_mass ? 100 : 0) + (op->all_affine ? 1000 : 0);  // mesh-size bucket, mass, affine
   for (auto& c : cache)
-    if (c[0] == N && c[1] == pi && c[2] == key && c[3] < nmodes) { op->hex_gmode[pi] = c[3]; return; }
+    if (c[0] == N && c[1] == pi && c[2] == key && std::find(modes.begin(), modes.end(), c[3]) != modes.end()) {
+      op->hex_gmode[pi] = c[3];
+      return;
+    }
   if (ne < 4096) {  // small meshes: no measurable difference, skip the timing
     op->hex_gmode[pi] = 0;
     return;
@@ -1077,7 +1092,7 @@ void hex_autotune(gh1_op* op, const T* G, int gstride) {
   GH1_CUDA(cudaEventCreate(&b));
   float best = 1e30f;
   int choice = 0;
-  for (int gm = 0; gm < nmodes; gm++) {
+  for (int gm : modes) {
     op->hex_gmode[pi] = gm;
     for (int r = 0; r < 2; r++) hex_apply_dispatch<T>(op, xs.p, ys.p, G, gstride, nullptr, nullptr, nullptr, nullptr);
     GH1_CUDA(cudaEventRecord(a, s));
@@ -1120,8 +1135,10 @@ int hex_multi_launch(gh1_op* op, int R, const int* phase, int want, const T* x, 
   using C = HexCfg<N>;
   gh1_space* sp = op->sp;
   if constexpr (std::is_same<T, float>::value) {
-    // FP32: two right-hand sides per lane (GH1_MULTI_PAIR=0 keeps one per lane)
-    static const bool paired = !(getenv("GH1_MULTI_PAIR") && getenv("GH1_MULTI_PAIR")[0] == '0');
+    // FP32: two right-hand sides per lane or one, as timed for this operator
+    // (GH1_MULTI_PAIR=0 / 1 forces one / two per lane)
+    const char* env = getenv("GH1_MULTI_PAIR");
+    const bool paired = env && (env[0] == '0' || env[0] == '1') ? env[0] == '1' : op->multi_pair != 0;
     if (paired && hex_pair_supported(N))
       return hex_multi_pair_launch(op, R, phase, want, x, y, partial, counter, energy, prepare_only);
   }
@@ -1209,6 +1226,7 @@ void matfree_setup(gh1_op* op) {
         op->pair_per_sm[2] = op->all_affine ? hex_pair_occupancy(op, 2) : 0;
         hex_slice_setup(op);
       }
+      op->tc_per_sm = hex_tc_occupancy(op);
     }
     hex_autotune<double>(op, op->d_G64.p, op->gstride64);
     if (want32) hex_autotune<float>(op, op->d_G32.p, op->gstride32);

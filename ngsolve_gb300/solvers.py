@@ -20,9 +20,20 @@ class CGSolver:
 
     def __init__(self, mat, pre=None, freedofs=None, tol=None, maxiter=100, atol=None, callback=None,
                  printrates=False, mode="fp64", stop_rule="precond", inner_tol=0.0, max_outer=0,
-                 check_every=0, conjugate=False, maxsteps=None, **kwargs):
-        if atol is not None:
+                 check_every=0, conjugate=False, maxsteps=None, plotrates=False, callback_sol=None,
+                 abstol=None, printing=False):
+        # the keywords of the reference's CGSolver / LinearSolver
+        # (python/krylovspace.py:60-75, 240-255); a misspelt or unknown keyword
+        # is a TypeError, as with any Python signature
+        if atol is not None or abstol is not None:
             raise NotImplementedError("atol: the GPU solver supports the relative tolerance only")
+        if callback_sol is not None:
+            raise NotImplementedError("callback_sol: the iterates stay on the device inside one solve")
+        if mode not in ("fp64", "mixed"):
+            raise ValueError("mode is 'fp64' or 'mixed'")
+        if stop_rule not in ("precond", "true"):
+            raise ValueError("stop_rule is 'precond' or 'true'")
+        printrates = printrates or printing
         if pre is None and freedofs is not None:
             pre = mat.CreateSmoother(freedofs)
         if maxsteps is not None:
@@ -125,9 +136,11 @@ class CGSolver:
 
 def CG(mat, rhs, pre=None, sol=None, tol=1e-12, maxsteps=100, printrates=True, plotrates=False, initialize=True,
        conjugate=False, callback=None, **kwargs):
-    """preconditioned conjugate gradient method (signature of ngsolve.solvers.CG)."""
+    """preconditioned conjugate gradient method (signature of ngsolve.solvers.CG,
+    python/krylovspace.py:293-338).  Further keywords go to CGSolver, which
+    raises TypeError on a keyword it does not know."""
     solver = CGSolver(mat=mat, pre=pre, tol=tol, maxiter=maxsteps, callback=callback, printrates=printrates,
-                      conjugate=conjugate, **kwargs)
+                      plotrates=plotrates, conjugate=conjugate, **kwargs)
     solver.Solve(rhs=rhs, sol=sol, initialize=initialize)
     CG.last_solver = solver
     return solver.sol

@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the parity tests from the NGSolve source tree.
 
-Run in a container that has the reference checkout (default path below):
-    python tests/golden/make_golden.py [/path/to/ngsolve]
+Run where a checkout of the reference exists, giving its root:
+    python tests/golden/make_golden.py /path/to/ngsolve
 Writes
   cube_vol.npz   points + tet vertex lists of tests/pytest/cube.vol.gz (the
                  mesh of tests/pytest/test_matrix.py:84-93), 0-based, and its
@@ -51,4 +51,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/ngsolve (the reference source tree)")
+    main(sys.argv[1])

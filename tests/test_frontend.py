@@ -429,3 +429,53 @@ def test_integrate(monkeypatch):
         C.Integrate(C.x, None)
     with pytest.raises(TypeError):
         a * C.CoefficientFunction(np.arange(4.0))
+
+
+def test_cg_rejects_unknown_keywords():
+    """CGSolver takes the reference's keywords (plotrates, printing, maxsteps
+    ...) and raises on any other, before it touches a device."""
+    from ngsolve_gb300 import solvers as SV
+
+    class _Mat:
+        height = width = 3
+
+    s = SV.CGSolver(_Mat(), None, maxsteps=7, plotrates=True, printing=False)
+    assert s.maxiter == 7
+    with pytest.raises(TypeError):
+        SV.CGSolver(_Mat(), None, plotrate=True)
+    with pytest.raises(TypeError):
+        SV.CG(_Mat(), None, pre=None, maxstep=10)
+    with pytest.raises(ValueError):
+        SV.CGSolver(_Mat(), None, mode="fp16")
+    with pytest.raises(NotImplementedError):
+        SV.CGSolver(_Mat(), None, atol=1e-12)
+
+
+def test_integrate_rejects_bad_operands(monkeypatch):
+    """Integrate(grad(a)*grad(b)) checks its operands before the element
+    kernel reads fes.ndof doubles through each pointer: same space, scalar H1,
+    contiguous FP64 CUDA vectors of the space's length.  A coefficient times a
+    VectorH1 function raises instead of integrating one component."""
+    import torch
+
+    class _Fes(_Space):
+        ndof = 4
+
+    fes, other = _Fes(), _Fes()
+    a = C.GridFunction(fes, vec=C.BaseVector(data=torch.ones(4, dtype=torch.float64)))
+    b = C.GridFunction(other, vec=C.BaseVector(data=torch.ones(4, dtype=torch.float64)))
+    with pytest.raises(ValueError):
+        C.Integrate(C.grad(a) * C.grad(b), None, element_wise=True)
+    with pytest.raises(TypeError):  # host tensors never reach the kernel
+        C.Integrate_grad_dot(fes, a.vec, a.vec)
+    with pytest.raises(TypeError):
+        C.Integrate_grad_dot(fes, torch.ones(4, dtype=torch.float32), torch.ones(4, dtype=torch.float32))
+    vfes = object.__new__(C.VectorH1)
+    with pytest.raises(TypeError):
+        C.Integrate_grad_dot(vfes, a.vec, a.vec)
+    vf = C.GridFunction(_Fes(), vec=C.BaseVector(data=torch.ones(4, dtype=torch.float64)))
+    vf.fes = vfes
+    with pytest.raises(NotImplementedError):
+        C.Integrate(2.0 * vf, None)
+    with pytest.raises(NotImplementedError):
+        C.Integrate(C.x * vf, None)

@@ -178,3 +178,37 @@ def test_abi_argument_checks(gpu):
     xv.data = one
     a.mat.Mult(xv, yv)
     assert np.abs(yv.NumPy()).max() < 1e-13
+
+
+def test_operator_outlives_its_form(gpu):
+    """An operator keeps the form it was made from: a BilinearForm dropped
+    while its .mat lives on (matrix-free and assembled) leaves the operator
+    valid, also after other forms have been created and freed in between
+    (the reference's BilinearFormApplication holds its form the same way)."""
+    import gc
+    m = MakeStructured3DMesh(hexes=True, nx=3)
+    fes = gpu.H1(m, order=3)
+    kappa = lognormal(m.ne, 1.0, 2)
+
+    def make(nonassemble, coef):
+        u, v = fes.TnT()
+        a = gpu.BilinearForm(fes, nonassemble=nonassemble)
+        a += gpu.CoefficientFunction(coef) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+        a.Assemble()
+        return a.mat
+
+    S = O.OracleSpace(m.points, m.elements, 3)
+    x = np.random.default_rng(3).normal(size=fes.ndof)
+    yo = S.apply_mf(x, kappa=kappa)
+    for nonassemble in (True, False):
+        mat = make(nonassemble, kappa)
+        gc.collect()
+        for s in range(3):
+            make(True, lognormal(m.ne, 1.0, 10 + s))
+            gc.collect()
+        xv, yv = gpu.BaseVector(fes.ndof), gpu.BaseVector(fes.ndof)
+        xv.data = x
+        mat.Mult(xv, yv)
+        assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
+        del mat
+        gc.collect()

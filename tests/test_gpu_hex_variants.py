@@ -144,3 +144,4 @@ def test_mixed_cg_paired_variant(gpu, mode, p):
                           mode="fp64", stop_rule="true")
     x6 = sol6.NumPy()
     assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
+

@@ -1,8 +1,9 @@
 """gh1_shape_eval_noalloc: shape evaluation into caller-owned device memory with
 the library's fixed scratch array, for callers that cannot let the library
 allocate.  Checked against gh1_shape_eval (the allocating entry point) on
-consecutive calls that share the scratch; collected last so that it also runs
-after every other GPU test has used the library."""
+consecutive calls that share the scratch, and against the FP64 CPU oracle's
+shape functions directly; collected last so that it also runs after every
+other GPU test has used the library."""
 import ctypes
 import os
 import re
@@ -11,6 +12,7 @@ import numpy as np
 import pytest
 import torch
 
+from oracle import oracle as O
 from tests.conftest import ROOT
 
 pytestmark = pytest.mark.gpu
@@ -61,6 +63,8 @@ def test_noalloc_matches_allocating_entry(gpu):
         v, g = val.cpu().numpy(), grd.cpu().numpy()
         assert np.isfinite(v).all() and np.isfinite(g).all()
         assert np.abs(v - rv).max() < 1e-13 and np.abs(g - rg).max() < 1e-12
+        ov, og = O.shapes(et, p, vn, pts)
+        assert np.abs(v - ov).max() < 1e-13 and np.abs(g - og).max() < 1e-12
         outs.append((v, g))
     # repeating the first case after the others reproduces it exactly
     et, p, vn, pts = _cases()[0]
