@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the tet CSR and adjoint legs of the default line")
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep", "link", "vector"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
@@ -383,6 +385,69 @@ def workload_c2(args):
         del A, a, amf
         torch.cuda.empty_cache()
     return out
+
+
+def leg_spmv_c2(order=4, reps=100):
+    """The CSR leg of the tet configuration at full size (32^3 Kuhn tets, jitter
+    0.2h seed 2, kappa lognormal(0,1) seed 3): GPU Assemble (first call with the
+    MatrixGraph, then element matrices only) and 100 SpMVs, beside cuSPARSE's
+    SpMV (torch.sparse) on the same matrix."""
+    import torch
+    import ngsolve_gb300 as ng
+    mesh = ng.JitterInterior(ng.MakeStructured3DMesh(hexes=False, nx=32), 0.2 / 32, 2)
+    kappa = np.exp(np.random.default_rng(3).normal(0, 1, mesh.ne))
+    fes = ng.H1(mesh, order=order, dirichlet=".*")
+    u, v = fes.TnT()
+    a = ng.BilinearForm(fes)
+    a += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+    t_first, _ = _timed(lambda: a.Assemble())
+    t_asm, _ = _timed(lambda: a.Assemble(), reps=3)
+    N, nnz = fes.ndof, a.mat.nze
+    x = ng.BaseVector(data=torch.rand(N, dtype=torch.float64, device="cuda"))
+    y = ng.BaseVector(N)
+    for _ in range(5):
+        a.mat.Mult(x, y)
+    t_spmv, _ = _timed(lambda: a.mat.Mult(x, y), reps=reps)
+    rp, ci, va = a.mat.CSR()
+    A = torch.sparse_csr_tensor(torch.tensor(rp, dtype=torch.int32), torch.tensor(ci, dtype=torch.int32),
+                                torch.tensor(va), size=(N, N), device="cuda")
+    xt = x.t.view(-1, 1)
+    for _ in range(5):
+        A @ xt
+    t_cusp, _ = _timed(lambda: A @ xt, reps=reps)
+    err = float((A @ xt).view(-1).sub(y.t).abs().max() / y.t.abs().max())
+    B = nnz * 12 + 8 * (N + 1) + 2 * N * 8
+    out = {"workload": "32^3 Kuhn tets p=%d, jitter 0.2h, kappa lognormal(0,1): CSR FP64" % order, "ndof": N,
+           "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm, "spmv_ms": t_spmv * 1e3,
+           "spmv_gbs": B / t_spmv / 1e9, "spmv_frac": B / t_spmv / 1e9 / load_peaks()[0],
+           "cusparse_ms": t_cusp * 1e3, "spmv_speedup_vs_cusparse": t_cusp / t_spmv, "max_diff_vs_cusparse": err}
+    del A, a
+    torch.cuda.empty_cache()
+    return out
+
+
+def leg_adjoint_c4():
+    """One adjoint gradient of the adjoint configuration (32^3 hex p=3, kappa
+    lognormal(0,1) seed 6, kappa* seed 7, f seed 5): forward and adjoint
+    mixed-precision solves to 1e-14 and the element contraction."""
+    import torch
+    import ngsolve_gb300 as ng
+    mesh = ng.MakeStructured3DMesh(hexes=True, nx=32)
+    kappa = np.exp(np.random.default_rng(6).normal(0, 1, mesh.ne))
+    kstar = np.exp(np.random.default_rng(7).normal(0, 1, mesh.ne))
+    f = np.random.default_rng(5).uniform(-1, 1, mesh.ne)
+    fes = ng.H1(mesh, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+    lf = ng.LinearForm(fes)
+    lf += ng.CoefficientFunction(f) * v * ng.dx
+    lf.Assemble()
+    tgt = ng.AdjointProblem(fes, lf.vec, torch.zeros(fes.ndof, dtype=torch.float64, device="cuda"), tol=1e-14)
+    tgt.evaluate(kstar)
+    prob = ng.AdjointProblem(fes, lf.vec, tgt.u.clone(), tol=1e-14)
+    prob.evaluate(kappa)
+    t_grad, (J, g) = _timed(lambda: prob.evaluate(kappa))
+    return {"workload": "32^3 hex p=3 adjoint dJ/dkappa", "ndof": fes.ndof, "J": J, "gradient_s": t_grad,
+            "max_abs_gradient": float(g.abs().max())}
 
 
 def workload_link(args):
@@ -883,6 +948,11 @@ def main():
               "err_mixed_vs_fp64_gpu": err, "accuracy": accuracy,
               "stop": "||b-Ax||_free <= 1e-10 ||b||_free (FP64 true residual)"}
 
+    # the other configurations' device legs, at full size, in the same run
+    others = None
+    if not args.no_extra and args.nx == NX and args.order == ORDER:
+        others = {"tet_csr": leg_spmv_c2(), "adjoint": leg_adjoint_c4()}
+
     peak, peak_kind = load_peaks()
     B32, F = model_bytes_flops(ne, N, args.order, 4, 4)
     achieved = B32 / t_step / 1e9 * 1.0 if ws == 1 else B32 / t_step / 1e9
@@ -923,7 +993,8 @@ def main():
                           "parallelism": "replicas" if ws > 1 else "single",
                           "l2": "inputs larger than L2 (G tile stream %.0f MB per apply)" % (ne * (args.order + 1) ** 3 * 24 / 1e6)},
                "e2e": e2e, "gpu_launches": args.steps, "clocks": ck, "roofline": roofline,
-               "general_geometry_apply": general, "tensor_core_apply": tensor_core, "setup": setup,
+               "general_geometry_apply": general, "tensor_core_apply": tensor_core, "other_configs": others,
+               "setup": setup,
                "fp64_apply": {"ms": t64 * 1e3, "gdofs": N / t64 / 1e9, "achieved_tflops_model": F / t64 / 1e12,
                               "achieved_gbs_model": B64 / t64 / 1e9},
                "cg": cg, "cpu_baseline": cpu}

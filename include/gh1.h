@@ -139,6 +139,14 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
  * are the autotuned SpMV configuration in FP64 and FP32: lanes per row L, plus
  * 100 when each lane keeps 8 instead of 4 nonzeros in flight (0: not tuned yet). */
 int gh1_op_info(gh1_op* op, int64_t* info);
+/* Waits for the context's stream and reports whether a matrix-free apply of op
+ * since the last check met a device wait that ran out of its bound (GH1_ERR_CUDA:
+ * the kernel drained its copies and returned, the context stays usable, the
+ * result is invalid); GH1_OK otherwise.  gh1_op_apply is asynchronous and does
+ * not wait; gh1_cg, gh1_batch_solve and gh1_adjoint_grad run this check before
+ * they return.  The counterpart of the reference's synchronizing apply
+ * (the `synckernels` device synchronize in ngscuda/cuda_linalg.cpp:370-412). */
+int gh1_op_check(gh1_op* op);
 int gh1_op_free(gh1_op* op);
 
 /* Block-diagonal operator diag(A, ..., A) with nblocks copies of op on

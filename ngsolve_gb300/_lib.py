@@ -66,6 +66,7 @@ SIGNATURES = {
     "gh1_matfree_create": [_P, _I, _PP],
     "gh1_op_apply": [_P, _D, _P, _P, _I, _I],
     "gh1_op_info": [_P, _P],
+    "gh1_op_check": [_P],
     "gh1_op_free": [_P],
     "gh1_op_block_create": [_P, _I, _PP],
     "gh1_jacobi_create": [_P, _P, _I, _PP],

@@ -323,6 +323,23 @@ void op_refresh_any(gh1_op* op) {
   else if (op->kind == GH1_OP_BLOCK) op_refresh_any(op->inner);
 }
 
+// A bounded device wait of a matrix-free apply that ran out sets the operator's
+// error flag (the kernel drained its copies and returned, so the context is
+// usable and the result is not).  Report it, once, after the stream is synchronized.
+void op_check_err(gh1_op* op) {
+  if (op->kind == GH1_OP_BLOCK) {
+    op_check_err(op->inner);
+    return;
+  }
+  if (op->kind != GH1_OP_MATFREE || op->d_err.n == 0) return;
+  int h = 0;
+  GH1_CUDA(cudaMemcpy(&h, op->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    GH1_CUDA(cudaMemset(op->d_err.p, 0, sizeof(int)));
+    throw Error(GH1_ERR_CUDA, "a bounded wait in the matrix-free apply timed out; its results are invalid");
+  }
+}
+
 // operator diagonal (FP64, device)
 static void op_diag_any(gh1_op* op, double* diag) {
   if (op->kind == GH1_OP_CSR) {
@@ -686,6 +703,14 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int prec, int acc
       op_apply_any(op, x, target, prec, nullptr);
     }
     if (!plain) vec_axpby(op->ctx, op->nrows, s, target, accumulate ? 1.0 : 0.0, y, prec);
+  });
+}
+
+int gh1_op_check(gh1_op* op) {
+  if (!op) return GH1_ERR_ARG;
+  return guard(op->ctx, [&] {
+    GH1_CUDA(cudaStreamSynchronize(op->ctx->stream));
+    op_check_err(op);
   });
 }
 

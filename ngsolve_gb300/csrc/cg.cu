@@ -544,6 +544,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     r->true_relres = bb > 0 ? std::sqrt(final_rr / bb) : std::sqrt(final_rr);
     r->status = status;
     GH1_CUDA(cudaStreamSynchronize(cs));
+    op_check_err(op);
   } catch (...) {
     for (auto e : execs) if (e) cudaGraphExecDestroy(e);
     cudaStreamSynchronize(cs);

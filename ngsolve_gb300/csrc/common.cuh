@@ -274,6 +274,7 @@ bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* parti
                      double* energy, const int* skip);
 // paired FP32 hex apply (hexpair.cu): two elements per lane, packed f32x2 arithmetic
 bool hex_pair_supported(int N);
+void set_first_wait_polls();  // hexpair.cu: GH1_FIRST_WAIT_POLLS (timeout-path tests)
 void upload_pair_tables(gh1_space* sp);
 int hex_pair_occupancy(gh1_op* op, int gmode);
 void hex_affine_setup(gh1_op* op);
@@ -297,6 +298,7 @@ void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (
 void op_apply_any(gh1_op* op, const void* x, void* y, int prec, const int* skip);
 void op_prepare_any(gh1_op* op, int prec);
 void op_refresh_any(gh1_op* op);
+void op_check_err(gh1_op* op);  // throws GH1_ERR_CUDA if a bounded wait of the apply ran out
 void spmv_skip(gh1_op* op, const void* x, void* y, int prec, const int* skip);  // spmv.cu
 void csr_diag(gh1_op* op, double* diag);                            // spmv.cu
 int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_opts* o, gh1_cg_result* r);  // cg.cu

@@ -109,6 +109,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// the same with a given poll limit (0: report a timeout without polling)
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, uint32_t parity, int polls) {
+  for (int i = 0; i < polls; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
 // all threads of the element group agree on a predicate
 template <int G>
 __device__ __forceinline__ bool group_all(int gid, bool v) {

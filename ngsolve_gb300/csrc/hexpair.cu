@@ -56,6 +56,19 @@ __device__ __forceinline__ f2 add2(f2 a, f2 b) {
   return d;
 }
 
+// Poll limit of the paired apply's first mbarrier wait.  The default is the
+// bound of every other wait (2^22 polls); GH1_FIRST_WAIT_POLLS read at operator
+// setup lowers it so that a test can make that wait run out on purpose: the
+// kernel then sets the operator's error flag, drains its copies in flight with
+// the full bound and returns, and the host reports GH1_ERR_CUDA.
+__device__ int g_first_wait_polls = 1 << 22;
+
+void set_first_wait_polls() {
+  const char* env = getenv("GH1_FIRST_WAIT_POLLS");
+  const int v = env ? std::max(0, atoi(env)) : (1 << 22);
+  GH1_CUDA(cudaMemcpyToSymbol(g_first_wait_polls, &v, sizeof(int)));
+}
+
 // 1D factor tables (32-bit); a coefficient enters the packed FMA broadcast to
 // both halves, which the packed pipe takes from the constant bank at no extra
 // instruction (a table of pre-duplicated 64-bit pairs costs a move per FMA)
@@ -362,9 +375,12 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     }
     t_issued = 1;
     g_issued = GM == 0 ? 1 : 0;
-    ok = group_all<G>(gid, mbar_wait_bounded(&mbar[0], 0));
-    t_waited = 1;
-    if (ok) gather(ch, tbuf(0), xr);
+    // the first wait may be shortened (GH1_FIRST_WAIT_POLLS) to test the timeout path
+    ok = group_all<G>(gid, mbar_wait_polls(&mbar[0], 0, g_first_wait_polls));
+    if (ok) {
+      t_waited = 1;  // a wait counts only once it succeeded: the drain covers the rest
+      gather(ch, tbuf(0), xr);
+    }
   }
   for (int k = 0; ok && ch < nch; ch += stride, k++) {
     const int b = k & 1;
@@ -385,14 +401,14 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     pair_forward<N, MASS>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
     if (has_next) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
-      t_waited++;
       if (!ok) break;
+      t_waited++;
       gather(ch + stride, tbuf(b ^ 1), xr);
     }
     if (GM == 0) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
-      g_waited++;
       if (!ok) break;
+      g_waited++;
     }
     // G rows of the pair; a missing second element reuses the first row (its
     // gathered coefficients are zero, so its half stays zero and finite)

@@ -356,8 +356,23 @@ template <int N, bool MASS, bool AFF>
 static int tc_occupancy() {
   auto kern = hex_apply_tc_kernel<N, MASS, AFF>;
   GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<N>::smem));
+  // the largest shared-memory carveout: several CTAs per SM hide each other's
+  // MMA round trips (without it the occupancy query assumed one CTA per SM)
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
   int v = 0;
   GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, 128, TcCfg<N>::smem));
+  // The query reports one CTA per SM for this kernel; the shared memory and
+  // registers allow more (ncu's limits for the launch agree), and the persistent
+  // tile loop is correct for any grid, so size the grid by those limits.
+  int dev = 0, smem_sm = 0, regs_sm = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const int by_smem = smem_sm / (int)(TcCfg<N>::smem + fa.sharedSizeBytes + 1024);
+  const int by_regs = regs_sm / (128 * ((fa.numRegs + 7) / 8 * 8));
+  v = std::max(v, std::min(by_smem, by_regs));
   // 64 TMEM columns per CTA: at most 8 resident CTAs share the SM's 512 columns
   return std::min(v, 8);
 }
@@ -372,7 +387,7 @@ static int tc_occupancy() {
 int hex_tc_occupancy(gh1_op* op) {
   const int N = op->sp->p + 1;
   const char* env = getenv("GH1_HEX_TC");
-  if (!hex_tc_supported(N) || !(env && env[0] == '1')) return 0;
+  if (!hex_tc_supported(N) || (env && env[0] == '0')) return 0;
   const bool m = op->has_mass, aff = op->all_affine;
   int v = 0;
 #define GH1_TC_OCC(NN)                                                                                 \

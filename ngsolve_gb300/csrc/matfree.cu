@@ -485,8 +485,10 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
     t_issued = 1;
     g_issued = GM == 0 ? 1 : 0;
     ok = group_all<G>(gid, mbar_wait_bounded(&mbar[0], 0));
-    t_waited = 1;
-    if (ok) gather(ch, tbuf(0), xr);
+    if (ok) {
+      t_waited = 1;  // a wait counts only once it succeeded: the drain covers the rest
+      gather(ch, tbuf(0), xr);
+    }
   }
   for (int k = 0; ok && ch < nch; ch += stride, k++) {
     const int b = k & 1;
@@ -507,14 +509,14 @@ hex_apply_kernel(int ne, const int* __restrict__ tdof, int tstride, const T* __r
     hex_forward<N, T, MASS>(pl, active, gid, su, s1, s2, t2, t3, gx, gy, gz, uq);
     if (has_next) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
-      t_waited++;
       if (!ok) break;
+      t_waited++;
       gather(ch + stride, tbuf(b ^ 1), xr);
     }
     if (GM == 0) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
-      g_waited++;
       if (!ok) break;
+      g_waited++;
     }
     // G mode 0: the tiles are in shared memory; mode 1: coalesced loads from HBM
     const T* Gsrc = GM == 0 ? (const T*)((const unsigned char*)gbuf + (slot < EPW ? slot : 0) * rowg)
@@ -1219,6 +1221,7 @@ void matfree_setup(gh1_op* op) {
       op->hex_per_sm[1][0] = hex_occupancy_dispatch<float, 0>(op, op->gstride32);
       op->hex_per_sm[1][1] = hex_occupancy_dispatch<float, 1>(op, op->gstride32);
       if (hex_pair_supported(sp->p + 1)) {
+        set_first_wait_polls();
         upload_pair_tables(sp);
         op->pair_per_sm[0] = hex_pair_occupancy(op, 0);
         op->pair_per_sm[1] = hex_pair_occupancy(op, 1);

@@ -212,3 +212,54 @@ def test_operator_outlives_its_form(gpu):
         assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * np.abs(yo).max()
         del mat
         gc.collect()
+
+
+def test_bounded_wait_timeout_reports_error(gpu, monkeypatch):
+    """A device wait that runs out of its bound is an error the host sees, and
+    the context stays usable.  GH1_FIRST_WAIT_POLLS=0 at operator setup makes
+    the first mbarrier wait of the paired FP32 apply give up without polling
+    (the DOF-row copy it waits for is still in flight and lands); the kernel
+    records the timeout, drains its copies with the full bound and returns.
+    gh1_op_check and a mixed-precision CG solve then report ERR_CUDA; an
+    operator set up afterwards without the knob applies correctly."""
+    m = MakeStructured3DMesh(hexes=True, nx=4)
+    kappa = lognormal(m.ne, 1.0, 4)
+    fes = gpu.H1(m, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+
+    def operator():
+        a = gpu.BilinearForm(fes, nonassemble=True, precision="fp32")
+        a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+        a.Assemble()
+        assert a.mat.Info()["hex_variant_fp32"] == 3
+        return a
+
+    monkeypatch.setenv("GH1_HEX_GMODE", "3")
+    monkeypatch.setenv("GH1_FIRST_WAIT_POLLS", "0")
+    a = operator()
+    ctx = fes.ctx
+    x32 = gpu.BaseVector(data=torch.ones(fes.ndof, dtype=torch.float32, device="cuda"))
+    y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+    a.mat.Mult(x32, y32)  # asynchronous: the timeout is reported by the check
+    with pytest.raises(GH1Error) as ei:
+        ctx.check(ctx.lib.gh1_op_check(a.mat.h))
+    assert ei.value.code == 2 and "timed out" in str(ei.value)
+    ctx.check(ctx.lib.gh1_op_check(a.mat.h))  # reported once, then cleared
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(np.ones(m.ne)) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    with pytest.raises(GH1Error) as ei:
+        gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=200, printrates=False, mode="mixed",
+                       stop_rule="true")
+    assert ei.value.code == 2
+    # the same context, a new operator without the knob
+    monkeypatch.delenv("GH1_FIRST_WAIT_POLLS")
+    b = operator()
+    S = O.OracleSpace(m.points, m.elements, 3)
+    x = np.random.default_rng(5).normal(size=fes.ndof)
+    yo = S.apply_mf(x, kappa=kappa)
+    xv = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    b.mat.Mult(xv, y32)
+    ctx.check(ctx.lib.gh1_op_check(b.mat.h))
+    assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()

@@ -3,7 +3,8 @@
 arithmetic (2, 3) -- forced through GH1_HEX_GMODE and checked against the FP64
 oracle.  Odd element counts leave the last element pair half empty.  Variant 4
 (one metric per element) exists only on meshes whose element maps are all affine,
-and so does variant 5 (its slice / pencil form, orders 1-4)."""
+and so does variant 5 (its slice / pencil form, orders 1-4).  Variant 6 runs the
+1D contractions on the tensor cores (orders 4-7, either metric form)."""
 import contextlib
 import os
 
@@ -20,15 +21,17 @@ pytestmark = pytest.mark.gpu
 
 @contextlib.contextmanager
 def forced_variant(mode):
-    old = os.environ.get("GH1_HEX_GMODE")
+    saved = {k: os.environ.get(k) for k in ("GH1_HEX_GMODE", "GH1_HEX_TC")}
     os.environ["GH1_HEX_GMODE"] = str(mode)
+    os.environ.pop("GH1_HEX_TC", None)  # the tensor-core variant on (its default)
     try:
         yield
     finally:
-        if old is None:
-            del os.environ["GH1_HEX_GMODE"]
-        else:
-            os.environ["GH1_HEX_GMODE"] = old
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 def _form(gpu, fes, kappa, mu, mode):
@@ -145,3 +148,54 @@ def test_mixed_cg_paired_variant(gpu, mode, p):
     x6 = sol6.NumPy()
     assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
 
+
+@pytest.mark.parametrize("mass", [False, True])
+@pytest.mark.parametrize("p", [4, 5, 6, 7])
+def test_fp32_tensor_core_variant(gpu, p, mass):
+    """Variant 6 (the 1D contractions as tcgen05 kind::tf32 GEMMs with the
+    3xTF32 split, accumulated in FP32 in tensor memory) within 2e-5 of the
+    oracle: on a jittered mesh (per-point metric) and on affine ones (one
+    metric per element), with 27, 8 and 1 elements, so that the last tile of
+    floor(128 / (p+1)^2) elements is ragged."""
+    for m in (JitterInterior(MakeStructured3DMesh(hexes=True, nx=3), 0.1 / 3, 11), _sheared(2),
+              MakeStructured3DMesh(hexes=True, nx=1)):
+        kappa = lognormal(m.ne, 1.0, 5)
+        mu = lognormal(m.ne, 0.5, 6) if mass else None
+        fes = gpu.H1(m, order=p, dirichlet=".*")
+        a = _form(gpu, fes, kappa, mu, 6)
+        assert a.mat.Info()["hex_variant_fp32"] == 6
+        S = O.OracleSpace(m.points, m.elements, p)
+        x = np.random.default_rng(7).normal(size=fes.ndof)
+        yo = S.apply_mf(x, kappa=kappa, mu=mu)
+        x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        a.mat.Mult(x32, y32)
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("affine", [False, True])
+@pytest.mark.parametrize("p", [4, 5])
+def test_mixed_cg_tensor_core_variant(gpu, p, affine):
+    """Mixed-precision CG with the tensor-core apply (and its fused energy
+    x^T A x) as the inner FP32 operator reaches 1e-11 true relative residual
+    and agrees with the FP64 CG solution."""
+    m = _sheared(5) if affine else JitterInterior(MakeStructured3DMesh(hexes=True, nx=5), 0.1 / 5, 3)
+    kappa = lognormal(m.ne, 0.5, 14)
+    f = np.random.default_rng(15).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, kappa, None, 6)
+    assert a.mat.Info()["hex_variant_fp32"] == 6
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    solm = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-11, maxsteps=20000, printrates=False,
+                          mode="mixed", stop_rule="true")
+    r = gpu.solvers.CG.last_solver.result
+    assert r.status == 0 and r.true_relres <= 1e-11 and r.outer >= 1 and r.applies32 > 0
+    xm = solm.NumPy().copy()
+    sol6 = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-12, maxsteps=20000, printrates=False,
+                          mode="fp64", stop_rule="true")
+    x6 = sol6.NumPy()
+    assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
