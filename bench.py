@@ -417,10 +417,28 @@ def leg_spmv_c2(order=4, reps=100):
     t_cusp, _ = _timed(lambda: A @ xt, reps=reps)
     err = float((A @ xt).view(-1).sub(y.t).abs().max() / y.t.abs().max())
     B = nnz * 12 + 8 * (N + 1) + 2 * N * 8
+    # the matrix-free FP32 apply of the same form: class-tiled GEMMs on the FP32
+    # pipe, and the same GEMMs on the tensor cores
+    mf = {}
+    x32 = ng.BaseVector(data=x.t.float())
+    y32 = ng.BaseVector(data=torch.zeros(N, dtype=torch.float32, device="cuda"))
+    for kern in ("tile", "tc"):
+        os.environ["GH1_TET_KERNEL"] = kern
+        amf = ng.BilinearForm(fes, nonassemble=True, precision="fp32")
+        amf += ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx
+        amf.Assemble()
+        os.environ.pop("GH1_TET_KERNEL", None)
+        for _ in range(3):
+            amf.mat.Mult(x32, y32)
+        t_mf, _ = _timed(lambda: amf.mat.Mult(x32, y32), reps=20)
+        mf[kern] = {"ms": t_mf * 1e3, "gdofs": N / t_mf / 1e9, "on_tensor_cores": amf.mat.Info()["hex_variant_fp32"] == 6}
+        del amf
+    out_mf = {"matfree_fp32_tile": mf["tile"], "matfree_fp32_tensor_core": mf["tc"]}
     out = {"workload": "32^3 Kuhn tets p=%d, jitter 0.2h, kappa lognormal(0,1): CSR FP64" % order, "ndof": N,
            "nnz": nnz, "assemble_first_s": t_first, "assemble_s": t_asm, "spmv_ms": t_spmv * 1e3,
            "spmv_gbs": B / t_spmv / 1e9, "spmv_frac": B / t_spmv / 1e9 / load_peaks()[0],
-           "cusparse_ms": t_cusp * 1e3, "spmv_speedup_vs_cusparse": t_cusp / t_spmv, "max_diff_vs_cusparse": err}
+           "cusparse_ms": t_cusp * 1e3, "spmv_speedup_vs_cusparse": t_cusp / t_spmv, "max_diff_vs_cusparse": err,
+           **out_mf}
     del A, a
     torch.cuda.empty_cache()
     return out

@@ -135,7 +135,10 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
  * lane with the G tile staged by bulk copy / loaded directly; 2 / 3: the same
  * with two elements per lane, FP32 only; 4: two elements per lane with one metric
  * per element, FP32, chosen only when every element map is affine; 5: the slice /
- * pencil form of 4, orders 1-4; -1: not applicable).  For a CSR operator info[4..5]
+ * pencil form of 4, orders 1-4; 6: the 1D contractions on the tensor cores
+ * (tcgen05), FP32, orders 4-7; -1: not applicable).  For a tet matrix-free
+ * operator info[5] is 6 when its FP32 apply runs both tile products on the
+ * tensor cores (orders 2-4 without a mass term, kept when faster), else -1.  For a CSR operator info[4..5]
  * are the autotuned SpMV configuration in FP64 and FP32: lanes per row L, plus
  * 100 when each lane keeps 8 instead of 4 nonzeros in flight (0: not tuned yet). */
 int gh1_op_info(gh1_op* op, int64_t* info);

@@ -654,6 +654,7 @@ int gh1_op_info(gh1_op* op, int64_t* info) {
   const bool hexmf = op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 8;
   info[4] = hexmf ? op->hex_gmode[0] : -1;
   info[5] = hexmf && (op->prec_mask & 2) ? op->hex_gmode[1] : -1;
+  if (op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 4 && op->tet_use_tc) info[5] = 6;
   if (op->kind == GH1_OP_CSR) {  // autotuned SpMV configuration (0 until the first SpMV)
     info[4] = op->spmv_L[0];
     info[5] = op->spmv_L[1];

@@ -219,6 +219,10 @@ struct gh1_op {
   gh1::DBuf<float> d_tetD32, d_tetw32;
   int tet_tiles_per_sm[2] = {0, 0};          // [FP64/FP32] resident blocks; 0: does not fit, element-wise kernel
   bool tet_chunked = false;                  // tables streamed in 16-point chunks (orders with large rules)
+  int tet_tc_per_sm = 0;                     // resident CTAs of the tensor-core FP32 tet apply (0: not available)
+  int tet_tc_ntiles = 0;                     // its tiles of up to 128 same-class elements
+  gh1::DBuf<int> d_tet_tc_tiles;             // [ntiles][4] = class, first position, count, 0
+  bool tet_use_tc = false;                   // FP32 tet apply on the tensor cores (timed at setup)
   int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
   gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights
   gh1::DBuf<float> d_tetDm32, d_tetwm32;
@@ -287,6 +291,11 @@ bool hex_slice_supported(int N);
 void hex_slice_setup(gh1_op* op);
 void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                      const int* skip);
+// FP32 tet apply with both tile products on the tensor cores (tettc.cu)
+bool tet_tc_supported(int p);
+void tet_tc_setup(gh1_op* op);
+void tet_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                  const int* skip);
 // FP32 hex apply with the 1D contractions on the tensor cores (hextc.cu)
 bool hex_tc_supported(int N);
 int hex_tc_occupancy(gh1_op* op);

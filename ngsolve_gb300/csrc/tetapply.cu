@@ -16,6 +16,7 @@
 // (8 column groups of 4 elements x 16 row groups per 128-thread block).  The
 // per-class table stays in shared memory while a block's tiles keep its class.
 #include <algorithm>
+#include <string>
 #include <vector>
 #include "common.cuh"
 #include "hexcore.cuh"
@@ -557,6 +558,36 @@ void tet_tiles_setup(gh1_op* op) {
     op->tet_tiles_per_sm[1] = tet_tile_occupancy<float>(sp->p, mass);
   }
   GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+  // FP32: the same products on the tensor cores, kept when faster on this mesh
+  // (GH1_TET_KERNEL=tc / tile forces one)
+  tet_tc_setup(op);
+  op->tet_use_tc = false;
+  if (op->tet_tc_per_sm > 0) {
+    const char* force = getenv("GH1_TET_KERNEL");
+    if (force && std::string(force) == "tc") {
+      op->tet_use_tc = true;
+    } else if (!(force && std::string(force) == "tile") && ne >= 4096) {
+      DBuf<float> xs(op->nrows), ys(op->nrows);
+      xs.zero(s);
+      cudaEvent_t a, b;
+      GH1_CUDA(cudaEventCreate(&a));
+      GH1_CUDA(cudaEventCreate(&b));
+      float ms[2];
+      for (int v = 0; v < 2; v++) {
+        op->tet_use_tc = v == 1;
+        for (int r = 0; r < 5; r++) {
+          if (r == 2) GH1_CUDA(cudaEventRecord(a, s));
+          tet_tiles_apply(op, GH1_F32, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+        }
+        GH1_CUDA(cudaEventRecord(b, s));
+        GH1_CUDA(cudaEventSynchronize(b));
+        GH1_CUDA(cudaEventElapsedTime(&ms[v], a, b));
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      op->tet_use_tc = ms[1] < ms[0];
+    }
+  }
 }
 
 template <class T, bool MASS, int P>
@@ -619,6 +650,10 @@ bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* parti
       tet_chunk_launch<float>(op, per_sm, op->d_tetD32.p, op->d_tetDm32.p, op->d_tetw32.p, op->d_tetwm32.p,
                               op->d_G32.p, op->has_mass ? op->d_M32.p : nullptr, (const float*)x, (float*)y,
                               partial, counter, energy, skip);
+    return true;
+  }
+  if (prec == GH1_F32 && op->tet_use_tc) {
+    tet_tc_apply(op, (const float*)x, (float*)y, partial, counter, energy, skip);
     return true;
   }
   if (prec == GH1_F64)

@@ -1,0 +1,349 @@
+// tettc.cu -- FP32 tet apply y += A x with both products of a tile on the
+// 5th-generation tensor cores (tcgen05.mma, kind::tf32).
+//
+// Same operator as tet_tile_kernel (tetapply.cu) and the reference's element-wise
+// ApplyElementMatrix (fem/symbolicintegrator.cpp:2959-3040) on affine tets:
+// y_e = B^T diag(w_q kappa_e |det J| J^{-1} J^{-T}) B x_e.  All elements of one
+// orientation class share one table D_c[i][r] of reference gradients at the rule
+// points (r = component * nq + point), so a tile of up to 128 same-class
+// elements is two GEMMs with the table as the shared, reused operand:
+//   P[m][r] = sum_i X[m][i] D_c[i][r]     (M = 128 elements, K = nloc, N = 3 nq)
+//   V[m][r] = w_q G_m (P[m][.] at point q)   (per element and point, registers)
+//   Y[m][i] = sum_r V[m][r] D_c[i][r]     (M = 128 elements, K = 3 nq, N = nloc)
+// Two threads own one element (one row of X, P, V, Y; the second warpgroup
+// reads the same tensor-memory lanes as the first): each gathers half of its
+// DOFs, writes half of its operand row, reads the accumulator row back from
+// tensor memory (tcgen05.ld 32x32b), applies the metric to half of the columns
+// and scatters half of the result with atomics.  No transposes between the
+// products.  Operands are K-major without swizzle
+// (8-row x 16-byte core matrices, LBO = 128 B along K, SBO = K/4 x 128 B per
+// 8-row group); FP32 values are split into TF32 high and low parts and every
+// product is hi*hi + lo*hi + hi*lo (3xTF32), accumulated in FP32 in tensor memory.
+#include <algorithm>
+#include <cstdlib>
+#include <vector>
+#include "common.cuh"
+#include "hexcore.cuh"
+
+namespace gh1 {
+
+template <int P>
+struct TetTcCfg {
+  static constexpr int NLOC = (P + 1) * (P + 2) * (P + 3) / 6;
+  static constexpr int NQ = P == 2 ? 4 : P == 3 ? 14 : 24;  // stiffness rule points (tables.cu tet_rule)
+  static constexpr int R = 3 * NQ;
+  static constexpr int K1 = (NLOC + 7) / 8 * 8;    // forward K (local DOFs)
+  static constexpr int N1 = (R + 15) / 16 * 16;    // forward N (gradient rows)
+  static constexpr int K2 = (R + 7) / 8 * 8;       // backward K
+  static constexpr int N2 = (NLOC + 15) / 16 * 16; // backward N
+  static constexpr int C2 = N1;                     // TMEM column of the backward accumulator
+  static constexpr int TCOLS = (N1 + N2) <= 32 ? 32 : (N1 + N2) <= 64 ? 64 : (N1 + N2) <= 128 ? 128 : 256;
+  // float offsets in dynamic shared memory; A1 and A2 share their space (A1 is
+  // read by the first product, which completes before A2 is written, and A2 by
+  // the second, which completes before the next tile's A1)
+  static constexpr int A1 = 0;                      // [hi, lo][128][K1]
+  static constexpr int A2 = 0;                      // [hi, lo][128][K2]
+  static constexpr int AW = 2 * 128 * (K1 > K2 ? K1 : K2);
+  static constexpr int T1 = AW;                     // [hi, lo][N1][K1]
+  static constexpr int T2 = T1 + 2 * N1 * K1;       // [hi, lo][N2][K2]
+  static constexpr int W = T2 + 2 * N2 * K2;        // weights [R] (padded to 4)
+  static constexpr int BAR = W + (R + 3) / 4 * 4;   // mbarrier (8 B) + TMEM base (4 B)
+  static constexpr size_t smem = (size_t)(BAR + 4) * sizeof(float);
+};
+
+// element (row r, column k) of a K-major operand with K columns
+template <int K>
+__device__ __forceinline__ int tt_off(int r, int k) { return (r >> 3) * (K * 8) + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
+
+__device__ __forceinline__ float tt_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xffffe000u); }
+
+template <int K>
+__device__ __forceinline__ uint64_t tt_desc(const float* p) {
+  return (uint64_t)((smem_u32(p) & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((K * 32) >> 4) << 32) |
+         (1ull << 46);
+}
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128
+template <int N>
+__device__ __forceinline__ uint32_t tt_idesc() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
+}
+__device__ __forceinline__ void tt_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+               "l"(a), "l"(b), "r"(idesc), "r"(acc)
+               : "memory");
+}
+// D = A * T^T over K (K/8 steps of 8), 3xTF32: A, T are [hi][rows][K] then [lo]
+template <int K, int N, int ROWS_T>
+__device__ __forceinline__ void tt_gemm(uint32_t d, const float* A, const float* T) {
+  const uint32_t idesc = tt_idesc<N>();
+  const float* Al = A + 128 * K;
+  const float* Tl = T + ROWS_T * K;
+#pragma unroll
+  for (int s = 0; s < K / 8; s++) {
+    const int o = s * 64;  // two core matrices (2 x 32 floats) per K step of 8
+    tt_mma(d, tt_desc<K>(A + o), tt_desc<K>(T + o), idesc, s > 0 ? 1u : 0u);
+    tt_mma(d, tt_desc<K>(Al + o), tt_desc<K>(T + o), idesc, 1u);
+    tt_mma(d, tt_desc<K>(A + o), tt_desc<K>(Tl + o), idesc, 1u);
+  }
+}
+__device__ __forceinline__ void tt_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+// one row of four consecutive K values (hi and lo parts), 16-byte stores
+template <int K>
+__device__ __forceinline__ void tt_put4(float* A, int r, int k, const float* v) {
+  float h[4], l[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) { h[j] = tt_hi(v[j]); l[j] = v[j] - h[j]; }
+  *(float4*)(A + tt_off<K>(r, k)) = make_float4(h[0], h[1], h[2], h[3]);
+  *(float4*)(A + 128 * K + tt_off<K>(r, k)) = make_float4(l[0], l[1], l[2], l[3]);
+}
+
+// tiles: [ntiles][4] = class, first position in perm, element count (<= 128), 0
+constexpr int TT_THREADS = 256;
+
+template <int P>
+__global__ void __launch_bounds__(TT_THREADS)
+tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
+              const float* __restrict__ Ge, const double* __restrict__ D64, int nlocp, int Rs,
+              const double* __restrict__ W64, const float* __restrict__ x, float* __restrict__ y, double* partial,
+              unsigned int* counter, double* energy, const int* skip, int* err) {
+  using C = TetTcCfg<P>;
+  constexpr int NLOC = C::NLOC, NQ = C::NQ, R = C::R, K1 = C::K1, N1 = C::N1, K2 = C::K2, N2 = C::N2;
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(1024) float ts[];
+  float* sA1 = ts + C::A1;
+  float* sA2 = ts + C::A2;
+  float* sT1 = ts + C::T1;
+  float* sT2 = ts + C::T2;
+  float* sW = ts + C::W;
+  uint64_t* bar = (uint64_t*)(ts + C::BAR);
+  uint32_t* tslot = (uint32_t*)(ts + C::BAR + 2);
+  const int t = threadIdx.x, warp = t >> 5, m = t & 127, half = t >> 7;  // element row m, half of its work
+  // zero operands: padding columns (K >= nloc, K >= R) stay zero
+  for (int i = t; i < C::AW; i += TT_THREADS) ts[i] = 0.f;
+  for (int i = t; i < R; i += TT_THREADS) sW[i] = (float)W64[i];
+  if (t == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(C::TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // lanes of row m
+  uint32_t ph = 0;
+  bool ok = true;
+  double acc = 0.0;
+  int loaded = -1;
+  auto issue_stage = [&](auto&& issue) {  // operands visible to the tensor core, issue, commit
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      issue();
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                   : "memory");
+    }
+  };
+  auto wait_stage = [&]() {
+    const bool got = mbar_wait_bounded(bar, ph);
+    ph ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return __syncthreads_and(got) != 0;
+  };
+  // this thread's half of an element's DOF values: loaded for the next tile
+  // while the current tile's second product runs
+  constexpr int H1 = K1 / 2;  // a multiple of 4
+  float xv[H1];
+  auto gather = [&](int tl_) {
+    const int st = tiles[4 * tl_ + 1], n = tiles[4 * tl_ + 2];
+    const bool a = m < n;
+    const int* edn = eldofs + (size_t)(a ? perm[st + m] : 0) * NLOC;
+#pragma unroll
+    for (int j = 0; j < H1; j++) {
+      const int i = half * H1 + j;
+      xv[j] = (a && i < NLOC) ? __ldg(x + __ldg(edn + i)) : 0.f;
+    }
+  };
+  if (blockIdx.x < ntiles) gather(blockIdx.x);
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    const int cls = tiles[4 * tile], start = tiles[4 * tile + 1], cnt = tiles[4 * tile + 2];
+    if (cls != loaded) {  // the class table as both B operands, split hi / lo from FP64
+      const double* Dc = D64 + (size_t)cls * nlocp * Rs;
+      for (int k = t; k < N1 * K1; k += TT_THREADS) {
+        const int n = k / K1, i = k % K1;
+        const double v = (n < R && i < NLOC) ? Dc[(size_t)i * Rs + n] : 0.0;
+        const float h = tt_hi((float)v);
+        sT1[tt_off<K1>(n, i)] = h;
+        sT1[N1 * K1 + tt_off<K1>(n, i)] = (float)(v - (double)h);
+      }
+      for (int k = t; k < N2 * K2; k += TT_THREADS) {
+        const int i = k / K2, r = k % K2;
+        const double v = (i < NLOC && r < R) ? Dc[(size_t)i * Rs + r] : 0.0;
+        const float h = tt_hi((float)v);
+        sT2[tt_off<K2>(i, r)] = h;
+        sT2[N2 * K2 + tt_off<K2>(i, r)] = (float)(v - (double)h);
+      }
+      loaded = cls;
+    }
+    // ---- the gathered half of this row's element into A1 ---------------------------
+    const bool act = m < cnt;
+    const int e = act ? perm[start + m] : 0;
+    const int* ed = eldofs + (size_t)e * NLOC;
+#pragma unroll
+    for (int j = 0; j < H1; j += 4) tt_put4<K1>(sA1, m, half * H1 + j, xv + j);
+    // ---- P = X D_c ------------------------------------------------------------------
+    issue_stage([&] { tt_gemm<K1, N1, N1>(tmem, sA1, sT1); });
+    if (!(ok = wait_stage())) break;
+    float pv[N1];
+#pragma unroll
+    for (int c = 0; c < N1; c += 16) tt_ld16(tl + c, pv + c);
+    // ---- metric at the points, into row m of A2: this half writes the column
+    // groups [4j, 4j+4) with j = half (mod 2); column r = component * nq + point
+    {
+      float g[6];
+#pragma unroll
+      for (int c = 0; c < 6; c++) g[c] = act ? __ldg(Ge + (size_t)e * 6 + c) : 0.f;
+      float en = 0.f;
+#pragma unroll
+      for (int j = 0; j < K2 / 4; j++) {
+        if ((j & 1) != half) continue;
+        float vv[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const int r = 4 * j + k;
+          float v = 0.f;
+          if (r < R) {
+            const int q = r % NQ, c = r / NQ;
+            const float ux = pv[q], uy = pv[NQ + q], uz = pv[2 * NQ + q];
+            const float gx = c == 0 ? g[0] : c == 1 ? g[3] : g[4];
+            const float gy = c == 0 ? g[3] : c == 1 ? g[1] : g[5];
+            const float gz = c == 0 ? g[4] : c == 1 ? g[5] : g[2];
+            v = sW[q] * (gx * ux + gy * uy + gz * uz);
+            en += pv[r] * v;
+          }
+          vv[k] = v;
+        }
+        tt_put4<K2>(sA2, m, 4 * j, vv);
+      }
+      acc += (double)en;
+    }
+    // ---- Y = V D_c^T (the next tile's gather overlaps it), then the scatter ----------
+    issue_stage([&] { tt_gemm<K2, N2, N2>(tmem + C::C2, sA2, sT2); });
+    if (tile + (int)gridDim.x < ntiles) gather(tile + gridDim.x);
+    if (!(ok = wait_stage())) break;
+    float yv[N2];
+#pragma unroll
+    for (int c = 0; c < N2; c += 16) tt_ld16(tl + C::C2 + c, yv + c);
+    if (act) {  // compile-time register indices in both halves
+      constexpr int HS = (NLOC + 1) / 2;
+      if (half == 0) {
+#pragma unroll
+        for (int i = 0; i < HS; i++) atomicAdd(y + __ldg(ed + i), yv[i]);
+      } else {
+#pragma unroll
+        for (int i = HS; i < NLOC; i++) atomicAdd(y + __ldg(ed + i), yv[i]);
+      }
+    }
+  }
+  if (!ok && t == 0) {
+    atomicExch(err, 1);
+    mbar_wait_bounded(bar, ph ^ 1u);  // the commit the failed wait gave up on
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TCOLS) : "memory");
+  if (partial) block_reduce_finish(acc, partial, counter, energy);
+}
+
+// ---- host side -------------------------------------------------------------------
+bool tet_tc_supported(int p) { return p >= 2 && p <= 4; }
+
+template <int P>
+static int tet_tc_occupancy_p() {
+  auto kern = tet_tc_kernel<P>;
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TetTcCfg<P>::smem));
+  int dev = 0, smem_sm = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const int v = smem_sm / (int)(TetTcCfg<P>::smem + fa.sharedSizeBytes + 1024);
+  // TMEM: at most 512 columns per SM across the resident CTAs
+  return std::min(v, 512 / TetTcCfg<P>::TCOLS);
+}
+
+// tiles of up to 128 same-class elements over the class-sorted order of the
+// tiled apply, and the CTAs per SM (0: not available: order, mass term,
+// GH1_TET_TC=0)
+void tet_tc_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->tet_tc_per_sm = 0;
+  const char* env = getenv("GH1_TET_TC");
+  if (!tet_tc_supported(sp->p) || op->has_mass || !(op->prec_mask & 2) || op->tet_ntiles == 0 || op->tet_chunked ||
+      (env && env[0] == '0'))
+    return;
+  cudaStream_t s = sp->ctx->stream;
+  std::vector<int> small(4 * (size_t)op->tet_ntiles);
+  GH1_CUDA(cudaMemcpyAsync(small.data(), op->d_tet_tiles.p, small.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> tiles;  // merge consecutive 32-element tiles of one class into tiles of up to 128
+  for (int k = 0; k < op->tet_ntiles; k++) {
+    const int c = small[4 * k], a = small[4 * k + 1], n = small[4 * k + 2];
+    const size_t m = tiles.size();
+    if (m && tiles[m - 4] == c && tiles[m - 3] + tiles[m - 2] == a && tiles[m - 2] + n <= 128) {
+      tiles[m - 2] += n;
+    } else {
+      tiles.insert(tiles.end(), {c, a, n, 0});
+    }
+  }
+  op->d_tet_tc_tiles.upload(tiles, s);
+  op->tet_tc_ntiles = (int)tiles.size() / 4;
+  switch (sp->p) {
+    case 2: op->tet_tc_per_sm = tet_tc_occupancy_p<2>(); break;
+    case 3: op->tet_tc_per_sm = tet_tc_occupancy_p<3>(); break;
+    case 4: op->tet_tc_per_sm = tet_tc_occupancy_p<4>(); break;
+    default: break;
+  }
+  GH1_CUDA(cudaStreamSynchronize(s));
+}
+
+template <int P>
+static void tet_tc_launch_p(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter,
+                            double* energy, const int* skip) {
+  gh1_space* sp = op->sp;
+  const int grid = std::max(1, std::min(op->tet_tc_ntiles, sp->ctx->nsm * op->tet_tc_per_sm));
+  tet_tc_kernel<P><<<grid, TT_THREADS, TetTcCfg<P>::smem, sp->ctx->stream>>>(
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_G32.p, op->d_tetD64.p,
+      (sp->nloc + 15) / 16 * 16, op->tet_Rs, op->d_tetw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
+  check_kernel(sp->ctx, "tet_tc_kernel");
+}
+
+void tet_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                  const int* skip) {
+  GH1_CHECK(op->tet_tc_per_sm > 0, GH1_ERR_ARG, "internal: tensor-core tet apply not prepared");
+  switch (op->sp->p) {
+    case 2: tet_tc_launch_p<2>(op, x, y, partial, counter, energy, skip); break;
+    case 3: tet_tc_launch_p<3>(op, x, y, partial, counter, energy, skip); break;
+    case 4: tet_tc_launch_p<4>(op, x, y, partial, counter, energy, skip); break;
+    default: throw Error(GH1_ERR_UNSUPPORTED, "tensor-core tet apply: order out of range");
+  }
+}
+
+}  // namespace gh1

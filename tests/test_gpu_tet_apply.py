@@ -98,3 +98,57 @@ def test_tet_mixed_cg_tiled(gpu, p):
                           mode="fp64", stop_rule="true")
     x6 = sol6.NumPy()
     assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
+
+
+@pytest.mark.parametrize("p", [2, 3, 4])
+def test_tet_tensor_core_apply(gpu, p):
+    """The FP32 apply with both products of a same-class tile of up to 128
+    elements on the tensor cores (tcgen05 kind::tf32, 3xTF32 split; forced with
+    GH1_TET_KERNEL=tc) within 2e-5 of the oracle, on meshes whose classes fill
+    from a fraction of a tile (162 tets) to several tiles (3,072 tets); the FP64
+    apply of the same operator is unchanged.  With a mass term the tile kernel
+    runs instead."""
+    for n in (3, 8):
+        m = _mesh(n, 31 + p)
+        kappa = lognormal(m.ne, 1.0, 5)
+        fes = gpu.H1(m, order=p, dirichlet=".*")
+        a = _form(gpu, fes, kappa, None, "tc")
+        assert a.mat.Info()["hex_variant_fp32"] == 6
+        S = O.OracleSpace(m.points, m.elements, p)
+        x = np.random.default_rng(7).normal(size=fes.ndof)
+        yo = S.apply_mf(x, kappa=kappa)
+        sc = np.abs(yo).max()
+        x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        a.mat.Mult(x32, y32)
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * sc
+        xv, yv = gpu.BaseVector(fes.ndof), gpu.BaseVector(fes.ndof)
+        xv.data = x
+        a.mat.Mult(xv, yv)
+        assert np.abs(yv.NumPy() - yo).max() <= 1e-12 * sc
+    b = _form(gpu, fes, kappa, lognormal(m.ne, 0.5, 6), "tc")
+    assert b.mat.Info()["hex_variant_fp32"] != 6
+
+
+def test_tet_mixed_cg_tensor_core(gpu):
+    """Mixed CG whose inner FP32 applies run on the tensor cores (with the fused
+    energy x^T A x) reaches 1e-11 and matches the FP64 solution."""
+    m = _mesh(5, 3)
+    kappa = lognormal(m.ne, 0.5, 14)
+    f = np.random.default_rng(15).uniform(-1, 1, m.ne)
+    fes = gpu.H1(m, order=3, dirichlet=".*")
+    a = _form(gpu, fes, kappa, None, "tc")
+    assert a.mat.Info()["hex_variant_fp32"] == 6
+    u, v = fes.TnT()
+    lf = gpu.LinearForm(fes)
+    lf += gpu.CoefficientFunction(f) * v * gpu.dx
+    lf.Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    solm = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-11, maxsteps=20000, printrates=False,
+                          mode="mixed", stop_rule="true")
+    r = gpu.solvers.CG.last_solver.result
+    assert r.status == 0 and r.true_relres <= 1e-11 and r.applies32 > 0
+    xm = solm.NumPy().copy()
+    sol6 = gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-12, maxsteps=20000, printrates=False,
+                          mode="fp64", stop_rule="true")
+    assert np.abs(xm - sol6.NumPy()).max() <= 1e-8 * np.abs(sol6.NumPy()).max()
