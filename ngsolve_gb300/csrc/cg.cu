@@ -9,9 +9,10 @@
 // with CheckResidual (:129-219): iterations counts checks, converged when
 // iterations >= maxiter or residual <= tol * first residual.
 // GPU layout of one iteration: [apply: y = A s, s.y as the sum of element
-// energies s_e^T A_e s_e] -> [update: alpha, x, d, w = P d, y = 0, w.d, |d|^2;
-// the last block forms beta and the convergence flag] -> [direction: s = w +
-// beta s].  All scalars stay on the device.  One inner solve is ONE graph
+// energies s_e^T A_e s_e] -> [update: alpha, d, w = P d, y = 0, w.d, |d|^2;
+// the last block forms beta and the convergence flag] -> [direction: x +=
+// alpha s, then s = w + beta s; the step the solve stops at adds its alpha s
+// after the loop].  All scalars stay on the device.  One inner solve is ONE graph
 // launch: a conditional WHILE node (the reference's device CG loop,
 // ngscuda/cuda_krylov.cpp:19-203 with ngscuda/cuda_core.hpp:170-250) whose body
 // holds `chunk` iterations and a one-thread kernel that sets the loop condition
@@ -20,6 +21,7 @@
 // kernels after convergence return at their first instruction.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -30,7 +32,8 @@ namespace gh1 {
 
 struct CGState {
   double wd, wdn, energy, alpha, beta, res0, stop, res, dd, bb;
-  int it, maxit, done, status, rule, pad;
+  int it, maxit, done, status, rule;
+  int xpend;  // the last step's x += alpha s is still due (the solve stopped before the direction kernel)
 };
 
 constexpr int RED_BLOCK = 256;
@@ -80,11 +83,15 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_init_kernel(int64_t n, const T* 
   }
 }
 
-// x += alpha s; d -= alpha y; w = P d; y = 0; partial sums of w.d and |d_free|^2
+// d -= alpha y; w = P d; y = 0 on [0, zero_end); partial sums of w.d and |d_free|^2.
+// x += alpha s is left to cg_dir_kernel, which reads s anyway (one vector pass
+// less per iteration); the entries of y from zero_end on are written, not
+// accumulated, by the next apply (element-interior DOFs of a hex operator), so
+// they need no clearing.
 template <class T>
-__global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T* __restrict__ inv, T* __restrict__ x,
-                                                              T* __restrict__ d, T* __restrict__ w, const T* __restrict__ s,
-                                                              T* __restrict__ y, CGState* st, double* hist, double* partial,
+__global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, int64_t zero_end, const T* __restrict__ inv,
+                                                              T* __restrict__ d, T* __restrict__ w, T* __restrict__ y,
+                                                              CGState* st, double* hist, double* partial,
                                                               unsigned int* counter) {
   if (*(volatile int*)&st->done) return;
   const double wd = st->wd, en = st->energy;
@@ -103,34 +110,31 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T
   T a0 = 0, a1 = 0;
   const int64_t nv = n / W, tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = tid; i < nv; i += nth) {
-    T sv[W], yv[W], iv[W], xv[W], dv[W], wv[W];
-    VT::get(((const V*)s)[i], sv);
+    T yv[W], iv[W], dv[W], wv[W];
     VT::get(((const V*)y)[i], yv);
     VT::get(((const V*)inv)[i], iv);
-    VT::get(((const V*)x)[i], xv);
     VT::get(((const V*)d)[i], dv);
 #pragma unroll
     for (int c = 0; c < W; c++) {
-      xv[c] += alpha * sv[c];
       dv[c] -= alpha * yv[c];
       wv[c] = iv[c] * dv[c];
       a0 += wv[c] * dv[c];
       if (iv[c] != (T)0) a1 += dv[c] * dv[c];
-      yv[c] = (T)0;
     }
-    ((V*)x)[i] = VT::make(xv);
     ((V*)d)[i] = VT::make(dv);
     ((V*)w)[i] = VT::make(wv);
-    ((V*)y)[i] = VT::make(yv);
+    if (i * W < zero_end) {
+      const T z[W] = {};
+      ((V*)y)[i] = VT::make(z);
+    }
   }
   for (int64_t i = nv * W + tid; i < n; i += nth) {
-    T si = s[i], yi = y[i], iv = inv[i];
-    x[i] += alpha * si;
+    T yi = y[i], iv = inv[i];
     T di = d[i] - alpha * yi;
     d[i] = di;
     T wi = iv * di;
     w[i] = wi;
-    y[i] = (T)0;
+    if (i < zero_end) y[i] = (T)0;
     a0 += wi * di;
     if (iv != (T)0) a1 += di * di;
   }
@@ -149,6 +153,7 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, const T
     if (!isfinite(r)) { st->done = 1; st->status = GH1_BREAKDOWN; }
     else if (r <= st->stop) { st->done = 1; st->status = GH1_OK; }
     else if (st->it >= st->maxit) { st->done = 1; st->status = GH1_MAXITER; }
+    st->xpend = st->done;  // stopped here: cg_dir_kernel will not run, cg_xfix_kernel adds alpha s
   }
 }
 
@@ -161,25 +166,46 @@ __global__ void cg_loop_kernel(const CGState* st, int* ctl, cudaGraphConditional
   }
 }
 
-// s = w + beta s
+// x += alpha s (the update step's x correction), then s = w + beta s.  With
+// x == nullptr (a fresh start of a continued solve) only the direction update.
 template <class T>
 __global__ void __launch_bounds__(RED_BLOCK) cg_dir_kernel(int64_t n, const T* __restrict__ w, T* __restrict__ s,
-                                                           const CGState* st) {
+                                                           T* __restrict__ x, const CGState* st) {
   if (*(volatile const int*)&st->done) return;
   using VT = V16<T>;
   using V = typename VT::type;
   constexpr int W = VT::W;
-  const T beta = (T)st->beta;
+  const T beta = (T)st->beta, alpha = (T)st->alpha;
   const int64_t nv = n / W, tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = tid; i < nv; i += nth) {
     T wv[W], sv[W];
     VT::get(((const V*)w)[i], wv);
     VT::get(((const V*)s)[i], sv);
+    if (x) {
+      T xv[W];
+      VT::get(((const V*)x)[i], xv);
+#pragma unroll
+      for (int c = 0; c < W; c++) xv[c] += alpha * sv[c];
+      ((V*)x)[i] = VT::make(xv);
+    }
 #pragma unroll
     for (int c = 0; c < W; c++) sv[c] = wv[c] + beta * sv[c];
     ((V*)s)[i] = VT::make(sv);
   }
-  for (int64_t i = nv * W + tid; i < n; i += nth) s[i] = w[i] + beta * s[i];
+  for (int64_t i = nv * W + tid; i < n; i += nth) {
+    if (x) x[i] += alpha * s[i];
+    s[i] = w[i] + beta * s[i];
+  }
+}
+
+// after the loop: the x correction of the step the solve stopped at
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_xfix_kernel(int64_t n, const T* __restrict__ s, T* __restrict__ x,
+                                                            const CGState* st) {
+  if (!*(volatile const int*)&st->xpend) return;
+  const T alpha = (T)st->alpha;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += alpha * s[i];
 }
 
 // r = b - y (FP64), |r_free|^2 and |b_free|^2 ; free = mask
@@ -305,6 +331,7 @@ struct PCG {
   double* hist;
   int chunk;
   int* ctl;              // [2]: body launches so far, bound on body launches
+  int64_t zero_end;      // the apply writes (does not accumulate) y from here on
   int applies = 0;
 
   void launch_iteration(cudaStream_t cs) {
@@ -316,9 +343,9 @@ struct PCG {
       dot_energy_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, s, y, &st->energy, partial + 2 * ctx->nsm * 64, counters + 1, &st->done);
       check_kernel(ctx, "dot_energy_kernel");
     }
-    cg_update_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, x, d, w, s, y, st, hist, partial, counters + 2);
+    cg_update_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, zero_end, inv, d, w, y, st, hist, partial, counters + 2);
     check_kernel(ctx, "cg_update_kernel");
-    cg_dir_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, w, s, st);
+    cg_dir_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, w, s, x, st);
     check_kernel(ctx, "cg_dir_kernel");
   }
 
@@ -377,6 +404,8 @@ struct PCG {
     const int hctl[2] = {0, (maxit + chunk - 1) / chunk + 2};
     GH1_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(hctl), cudaMemcpyHostToDevice, cs));
     GH1_CUDA(cudaGraphLaunch(exec, cs));
+    cg_xfix_kernel<T><<<red_grid(ctx, n), RED_BLOCK, 0, cs>>>(n, s, x, st);
+    check_kernel(ctx, "cg_xfix_kernel");
     GH1_CUDA(cudaMemcpyAsync(hs, st, sizeof(CGState), cudaMemcpyDeviceToHost, cs));
     GH1_CUDA(cudaStreamSynchronize(cs));
     CGState out = *hs;
@@ -432,6 +461,9 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
       inv64 = inv_ident.p;
     }
     int chunk = o->check_every > 0 ? o->check_every : 8;
+    // every hex matrix-free apply writes the element-interior DOFs (from
+    // first_cell on) instead of adding to them, so the CG update clears y below it only
+    const int64_t zero_end = (op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 8) ? op->sp->first_cell : n;
     auto bnorm2 = [&](const double* y, double* rr) {  // |b - y|^2, |b|^2 on free DOFs
       int g = red_grid(ctx, n);
       residual_kernel<<<g, RED_BLOCK, 0, cs>>>(n, b, y, freemask, rr, norm2.p, partial.p, counters.p + 3);
@@ -466,7 +498,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     double final_rr = 0.0;  // |b - A x|^2 on free DOFs for the returned x
     if (o->mode == GH1_CG_FP64) {
       PCG<double> P{op, ctx, n, inv64, x, W.d64.p, W.w64.p, W.s64.p, W.y64.p, GH1_F64, st.p, partial.p, counters.p, hist.p, chunk,
-                    ctl.p};
+                    ctl.p, zero_end};
       GH1_CUDA(cudaMemsetAsync(W.y64.p, 0, n * sizeof(double), cs));
       CGState res = P.run(o->tol, o->maxit, o->stop_rule, bb, cs, &exec64, &ch64);
       execs.push_back(exec64);
@@ -522,7 +554,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
         check_kernel(ctx, "scale_to_f32_kernel");
         GH1_CUDA(cudaMemsetAsync(W.x32.p, 0, n * sizeof(float), cs));
         PCG<float> P{op, ctx, n, pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32, st.p, partial.p,
-                     counters.p, nullptr, chunk, ctl.p};
+                     counters.p, nullptr, chunk, ctl.p, zero_end};
         CGState res = P.run(tol_k, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
         total_inner += res.it;
         r->applies32 += P.applies;
