@@ -105,6 +105,27 @@ int gh1_form_set_coefs(gh1_form* form, const double* kappa, const double* mu, in
  * form (dJ/dkappa needs the scalar coefficient).  Operators made from the form
  * afterwards, and matrix-free operators at their next apply, use the tensor. */
 int gh1_form_set_tensor(gh1_form* form, const double* K6, int mem);
+/* Generic B^T D B form (the reference's fused symbolic operator for arbitrary
+ * bilinear integrands, comp/matrixfree.cpp:1090-1330 AssembleBDBFused, applied on
+ * the device by ngscuda/cuda_matrix_free_btdtb.cpp:60-310):
+ *   a(u, v) = sum_e int_e (B v)^T D (B u) dx,  B w = (w, dw/dx, dw/dy, dw/dz),
+ * D in physical coordinates, row = test component, column = trial component
+ * (row-major 4x4).  Diffusion K grad u . grad v is D[1+k][1+l] = K_kl, reaction
+ * c u v is D[0][0] = c, convection (b . grad u) v is D[0][1+l] = b_l, and
+ * u (b . grad v) is D[1+k][0] = b_k; D need not be symmetric.
+ * per_point = 0: D[ne][16], one matrix per element (as the reference evaluates
+ * it); per_point = 1: D[ne][nq][16] at the points of the space's rule
+ * (gh1_space_qpoints: hex tensor Gauss with p+1 points per direction, tet the
+ * degree-2p rule).  Host or device per mem; NULL returns the form to kappa / mu /
+ * K6, which a set D replaces.  Such a form gives matrix-free operators
+ * (gh1_matfree_create, FP64 and FP32, with their diagonal for Jacobi);
+ * gh1_assemble_csr, gh1_adjoint_grad and gh1_batch_create reject it. */
+int gh1_form_set_bdb(gh1_form* form, const double* D, int per_point, int mem);
+/* The rule the generic form integrates with: *nq points per element; ref (host,
+ * may be NULL): nq x 4 reference coordinates and weight; xyz (may be NULL):
+ * ne x nq x 3 physical coordinates, host or device per mem.  A point-wise D of
+ * gh1_form_set_bdb follows this point order. */
+int gh1_space_qpoints(gh1_space* space, double* ref, double* xyz, int mem, int* nq);
 /* Releases the caller's handle.  Operators made from the form (gh1_assemble_csr,
  * gh1_matfree_create, gh1_batch_create) keep it alive, as the reference's
  * BilinearFormApplication holds its BilinearForm: its memory goes when the last
@@ -136,7 +157,9 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
  * with two elements per lane, FP32 only; 4: two elements per lane with one metric
  * per element, FP32, chosen only when every element map is affine; 5: the slice /
  * pencil form of 4, orders 1-4; 6: the 1D contractions on the tensor cores
- * (tcgen05), FP32, orders 4-7; -1: not applicable).  For a tet matrix-free
+ * (tcgen05), FP32, orders 4-7; -1: not applicable).  A generic B^T D B operator
+ * (gh1_form_set_bdb, hex or tet) reports 7 in both: metric records per rule
+ * point, or 8: one record per element (affine elements, D per element).  For a tet matrix-free
  * operator info[5] is 6 when its FP32 apply runs both tile products on the
  * tensor cores (orders 2-4 without a mass term, kept when faster), else -1.  For a CSR operator info[4..5]
  * are the autotuned SpMV configuration in FP64 and FP32: lanes per row L, plus

@@ -58,6 +58,8 @@ SIGNATURES = {
     "gh1_form_create": [_P, _P, _P, _I, _PP],
     "gh1_form_set_coefs": [_P, _P, _P, _I],
     "gh1_form_set_tensor": [_P, _P, _I],
+    "gh1_form_set_bdb": [_P, _P, _I, _I],
+    "gh1_space_qpoints": [_P, _P, _P, _I, _P],
     "gh1_form_free": [_P],
     "gh1_assemble_csr": [_P, _PP],
     "gh1_csr_info": [_P, _P],

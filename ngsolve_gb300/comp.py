@@ -321,6 +321,118 @@ class _Product:
         raise NotImplementedError("only kappa*grad(u)*grad(v)*dx, mu*u*v*dx and f*v*dx are on the H1 path")
 
 
+def _is_vector_cf(f):
+    return isinstance(f, CoefficientFunction) and isinstance(f.values, (tuple, list)) and len(f.values) == 3
+
+
+def _is_pointwise(f):
+    """A coefficient that varies inside an element (a coordinate function or a
+    vector with such a component)."""
+    if isinstance(f, _AffineCF):
+        return True
+    return _is_vector_cf(f) and any(isinstance(c, _AffineCF) for c in f.values)
+
+
+def _bdb_needed(term):
+    """True when a bilinear term lies outside kappa grad.grad / mu u v / symmetric
+    K grad.grad: it then goes into the generic B^T D B form."""
+    if not isinstance(term, _Product):
+        return False
+    fs = term.factors
+    grads = [f for f in fs if isinstance(f, _Grad)]
+    proxies = [f for f in fs if isinstance(f, _Proxy)]
+    if any(_is_pointwise(f) or _is_vector_cf(f) for f in fs):
+        return len(grads) + len(proxies) == 2
+    if len(grads) == 1 and len(proxies) == 1:
+        return True
+    for f in fs:
+        if isinstance(f, CoefficientFunction) and f.is_tensor():
+            K = np.asarray(f.values, dtype=np.float64)
+            if np.abs(K - np.swapaxes(K, -1, -2)).max() > 1e-12 * max(np.abs(K).max(), 1e-300):
+                return True
+    return False
+
+
+def _bdb_parts(term):
+    """Splits a bilinear term into (trial, test, scalars, vector, matrix): trial /
+    test are ("val" | "grad"); raises NotImplementedError for shapes the generic
+    form does not take."""
+    trial = test = None
+    scalars, vectors, matrices, has_dx = [], [], [], False
+    for f in term.factors:
+        if isinstance(f, _Grad) or isinstance(f, _Proxy):
+            kind = "grad" if isinstance(f, _Grad) else "val"
+            is_test = (f.proxy if isinstance(f, _Grad) else f).test
+            if is_test:
+                if test is not None:
+                    raise NotImplementedError("two test functions in one term")
+                test = kind
+            else:
+                if trial is not None:
+                    raise NotImplementedError("two trial functions in one term")
+                trial = kind
+        elif isinstance(f, _Measure):
+            has_dx = True
+        elif _is_vector_cf(f):
+            vectors.append(f)
+        elif isinstance(f, CoefficientFunction) and f.is_tensor():
+            matrices.append(f)
+        elif isinstance(f, (CoefficientFunction, int, float, np.floating, np.integer)):
+            scalars.append(f)
+        else:
+            raise NotImplementedError("factor %r is not on the B^T D B path" % (f,))
+    if not has_dx:
+        raise ValueError("integrand needs * dx")
+    if trial is None or test is None:
+        raise NotImplementedError("a bilinear term needs one trial and one test function")
+    ok = {("grad", "grad"): (0, (0, 1)), ("grad", "val"): (1, (0,)), ("val", "grad"): (1, (0,)),
+          ("val", "val"): (0, (0,))}[(trial, test)]
+    if len(vectors) != ok[0] or len(matrices) not in ok[1]:
+        raise NotImplementedError("term shape (%s u, %s v) with %d vector and %d matrix factors is not a scalar "
+                                  "B^T D B integrand" % (trial, test, len(vectors), len(matrices)))
+    return trial, test, scalars, (vectors[0] if vectors else None), (matrices[0] if matrices else None)
+
+
+def _bdb_scalar(f, ne, pts, dev):
+    """Values of a scalar factor: (ne, P) with P = nq at points or 1 per element."""
+    if isinstance(f, _AffineCF):
+        return pts @ torch.tensor(f.a, dtype=torch.float64, device=dev) + f.d
+    if not isinstance(f, CoefficientFunction):  # a number or an array per element (vector components)
+        f = CoefficientFunction(f)
+    return torch.tensor(f.element_values(ne), dtype=torch.float64, device=dev)[:, None]
+
+
+def _bdb_D(terms, ne, pts, dev):
+    """Sum of the terms' D matrices in physical coordinates, rows test (v, grad v),
+    columns trial (u, grad u): (ne, P, 4, 4), P = nq when pts is given, else 1 --
+    the reference's per-(trial, test)-component evaluation of the integrand
+    (comp/matrixfree.cpp:1240-1275)."""
+    P = 1 if pts is None else pts.shape[1]
+    D = torch.zeros((ne, P, 4, 4), dtype=torch.float64, device=dev)
+    for t in terms:
+        trial, test, scalars, vec, mat = _bdb_parts(t)
+        c = torch.ones((ne, 1), dtype=torch.float64, device=dev)
+        for f in scalars:
+            c = c * _bdb_scalar(f, ne, pts, dev)
+        c = c.expand(ne, P)
+        if trial == "grad" and test == "grad":
+            if mat is None:
+                K = torch.eye(3, dtype=torch.float64, device=dev).expand(ne, 3, 3)
+            else:
+                K = torch.tensor(np.broadcast_to(np.asarray(mat.values, dtype=np.float64), (ne, 3, 3)).copy(),
+                                 dtype=torch.float64, device=dev)
+            D[:, :, 1:, 1:] += c[:, :, None, None] * K[:, None]
+        elif trial == "val" and test == "val":
+            D[:, :, 0, 0] += c
+        else:
+            b = torch.stack([_bdb_scalar(comp, ne, pts, dev).expand(ne, P) for comp in vec.values], dim=-1)
+            if trial == "grad":   # (b . grad u) v
+                D[:, :, 0, 1:] += c[:, :, None] * b
+            else:                 # u (b . grad v)
+                D[:, :, 1:, 0] += c[:, :, None] * b
+    return D
+
+
 def _coupling_mask(free, ne, et, order):
     """free without the element-interior DOFs: the last ne * n_cell DOFs in this
     numbering ((p-1)^3 per hex, (p-1)(p-2)(p-3)/6 per tet)."""
@@ -1012,6 +1124,8 @@ class BilinearForm:
         self.K6 = None  # (ne, 6) sum of the tensor diffusion terms
         self.mu = None
         self._has_laplace = False
+        self._terms = []       # every bilinear term, for the generic B^T D B form
+        self._generic = False  # a term outside kappa grad.grad / mu u v / symmetric K
         self._form = None
         self.mat = None
         if integrand is not None:
@@ -1022,7 +1136,17 @@ class BilinearForm:
             for t in term.terms:
                 self += t
             return self
+        if _bdb_needed(term):
+            if self._sfes is not self.fes:
+                raise NotImplementedError("the generic B^T D B form is on the path for scalar H1 only")
+            _bdb_parts(term)  # shape check now, values at Assemble
+            self._terms.append(term)
+            self._generic = True
+            self._form = None
+            return self
         kind, coef = term.classify(self.fes.ne)
+        if kind in ("laplace", "laplace_tensor", "mass"):
+            self._terms.append(term)
         if kind == "laplace":
             self.kappa = self.kappa + coef
             self._has_laplace = True
@@ -1044,6 +1168,26 @@ class BilinearForm:
         ctx = self.fes.ctx
         kappa = np.ascontiguousarray(self.kappa, dtype=np.float64)
         mu = None if self.mu is None else np.ascontiguousarray(self.mu, dtype=np.float64)
+        if self._form is None and self._generic:
+            # generic B^T D B: D per element, or per rule point when a coefficient
+            # varies inside the elements (gh1_form_set_bdb, gh1_space_qpoints)
+            sfes, ne = self._sfes, self._sfes.ne
+            dev = torch.device("cuda", ctx.device)
+            pts = None
+            if any(_is_pointwise(f) for t in self._terms for f in t.factors):
+                nq = ctypes.c_int()
+                ctx.check(ctx.lib.gh1_space_qpoints(sfes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(nq)))
+                pts = torch.empty((ne, nq.value, 3), dtype=torch.float64, device=dev)
+                ctx.sync_stream()
+                ctx.check(ctx.lib.gh1_space_qpoints(sfes.h, None, _ptr(pts), _lib.GH1_MEM_DEVICE, None))
+            D = _bdb_D(self._terms, ne, pts, dev).reshape(ne, -1, 16)
+            D = (D[:, 0] if pts is None else D).contiguous()
+            torch.cuda.synchronize(dev)
+            h = ctypes.c_void_p()
+            ctx.check(ctx.lib.gh1_form_create(sfes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(h)))
+            self._form = h
+            ctx.check(ctx.lib.gh1_form_set_bdb(h, _ptr(D), 0 if pts is None else 1, _lib.GH1_MEM_DEVICE))
+            return self._form
         if self._form is None:
             h = ctypes.c_void_p()
             ctx.check(ctx.lib.gh1_form_create(self._sfes.h, _np_ptr(kappa), None if mu is None else _np_ptr(mu),
@@ -1057,6 +1201,9 @@ class BilinearForm:
 
     def Assemble(self, reallocate=False):
         ctx = self.fes.ctx.sync_stream()
+        if self._generic and not self.nonassemble:
+            raise NotImplementedError("a generic B^T D B form is applied matrix-free: BilinearForm(..., "
+                                      "nonassemble=True)")
         form = self._make_form()
         h = ctypes.c_void_p()
         sfes = self._sfes

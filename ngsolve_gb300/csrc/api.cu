@@ -557,9 +557,48 @@ int gh1_form_free(gh1_form* f) {
   return GH1_OK;
 }
 
+int gh1_form_set_bdb(gh1_form* f, const double* D, int per_point, int mem) {
+  if (!f) return GH1_ERR_ARG;
+  return guard(f->sp->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    GH1_CHECK(per_point == 0 || per_point == 1, GH1_ERR_ARG, "per_point is 0 (D per element) or 1 (D per rule point)");
+    if (D) {
+      const int64_t n = (int64_t)f->sp->mesh->ne * (per_point ? space_rule_size(f->sp) : 1) * 16;
+      upload_coef(f->sp->ctx, f->d_bdb, D, mem, n, 0.0);
+      f->bdb_mode = per_point ? 2 : 1;
+    } else {
+      f->d_bdb.release();
+      f->bdb_mode = 0;
+    }
+    f->version++;
+    GH1_CUDA(cudaStreamSynchronize(f->sp->ctx->stream));
+  });
+}
+int gh1_space_qpoints(gh1_space* sp, double* ref, double* xyz, int mem, int* nq) {
+  if (!sp) return GH1_ERR_ARG;
+  return guard(sp->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    GH1_CUDA(cudaSetDevice(sp->ctx->device));
+    const int n = space_rule_size(sp);
+    if (nq) *nq = n;
+    if (ref) space_qpoints(sp, ref, nullptr);
+    if (xyz) {
+      if (mem == GH1_MEM_DEVICE) {
+        space_qpoints(sp, nullptr, xyz);
+      } else {
+        DBuf<double> d((size_t)sp->mesh->ne * n * 3);
+        space_qpoints(sp, nullptr, d.p);
+        GH1_CUDA(cudaMemcpyAsync(xyz, d.p, d.bytes(), cudaMemcpyDeviceToHost, sp->ctx->stream));
+      }
+    }
+    GH1_CUDA(cudaStreamSynchronize(sp->ctx->stream));
+  });
+}
 int gh1_assemble_csr(gh1_form* f, gh1_op** out) {
   if (!f || !out) return GH1_ERR_ARG;
   return guard(f->sp->ctx, [&] {
+    GH1_CHECK(f->bdb_mode == 0, GH1_ERR_UNSUPPORTED,
+              "a generic B^T D B form is applied matrix-free (gh1_matfree_create)");
     gh1_space* sp = f->sp;
     GH1_CUDA(cudaSetDevice(sp->ctx->device));
     if (!sp->have_graph) {
@@ -655,6 +694,10 @@ int gh1_op_info(gh1_op* op, int64_t* info) {
   info[4] = hexmf ? op->hex_gmode[0] : -1;
   info[5] = hexmf && (op->prec_mask & 2) ? op->hex_gmode[1] : -1;
   if (op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 4 && op->tet_use_tc) info[5] = 6;
+  if (op->kind == GH1_OP_MATFREE && op->bdb) {  // generic B^T D B: records per point (7) or per element (8)
+    info[4] = 6 + op->bdb;
+    info[5] = (op->prec_mask & 2) ? 6 + op->bdb : -1;
+  }
   if (op->kind == GH1_OP_CSR) {  // autotuned SpMV configuration (0 until the first SpMV)
     info[4] = op->spmv_L[0];
     info[5] = op->spmv_L[1];

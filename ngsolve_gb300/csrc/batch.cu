@@ -281,6 +281,7 @@ extern "C" int gh1_batch_create(gh1_ctx* ctx, int nprob, gh1_form* const* forms,
       for (int i = 0; i < nprob; i++) {
         GH1_CHECK(forms[i] && forms[i]->sp->ctx == ctx, GH1_ERR_ARG, "batch: form of another context");
         GH1_CHECK(forms[i]->sp->et == 8, GH1_ERR_UNSUPPORTED, "batch: hex meshes only");
+        GH1_CHECK(forms[i]->bdb_mode == 0, GH1_ERR_UNSUPPORTED, "batch: Laplace / mass forms only (a B^T D B form is set)");
         GH1_CHECK(nrhs[i] >= 1 && nrhs[i] <= 16, GH1_ERR_UNSUPPORTED, "batch: 1..16 right-hand sides per problem");
         auto* P = new gh1_batch::Prob();
         B->probs.push_back(P);

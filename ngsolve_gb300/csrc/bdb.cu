@@ -1,0 +1,331 @@
+// bdb.cu -- generic B^T D B operator: y = A x for
+//   a(u, v) = sum_e int_e (B v)^T D (B u) dx,   B w = (w, dw/dx, dw/dy, dw/dz),
+// with D a 4x4 matrix per element or per rule point: any bilinear integrand in
+// u, grad u, v, grad v (full diffusion tensors, convection b.grad(u) v and its
+// transpose u c.grad(v), reaction, non-symmetric combinations).
+//
+// Replaces the reference's fused symbolic B^T D B operator: AssembleBDBFused
+// (comp/matrixfree.cpp:1090-1330) evaluates D per element from the integrand,
+// one entry per (trial component, test component) pair, and keeps the
+// Jacobians per element (per point on curved elements); MatrixFreeBTDTB
+// (ngscuda/cuda_matrix_free_btdtb.cpp:60-310) applies B^T (J-transformed D) B
+// on the device.  Here setup folds the geometry into reference-coordinate
+// matrices
+//   Mh = s T^T D T,   T = diag(1, J^{-T}),   s = w |det J|,
+// so the kernels need no Jacobian:
+//  - hex: the sum-factorized one-element apply of hexsf.cuh with the point
+//    transform (vm, vx, vy, vz) = Mh (u, du/dxi, du/deta, du/dzeta); G mode 2
+//    streams Mh per point, G mode 3 (affine hexes, D per element) reads one
+//    16-value record per element and applies the rule weight in the kernel;
+//  - tet: tetapply.cu (same-class tiles, 16-point chunks of the degree-2p rule).
+// The rule is the one of the space: tensor Gauss with p+1 points per direction
+// on hexes, degree 2p on tets (the reference's BDB rule has order 2p as well).
+#include <cstdlib>
+#include <string>
+#include <vector>
+#include "common.cuh"
+#include "hexcore.cuh"
+#include "hexsf.cuh"
+
+namespace gh1 {
+
+// Mh[r][c] = s sum_{a,b} T[a][r] D[a][b] T[b][c] with T = diag(1, J^{-T}): the
+// physical gradient component k of a shape is sum_j Ji[3j+k] times its reference
+// component j (Ji = J^{-1}, row-major).  D and Mh are row = test, column = trial.
+__device__ __forceinline__ void bdb_transform(const double* Ji, const double* D, double s, double* M) {
+  double T[4][4];
+  for (int a = 0; a < 4; a++)
+    for (int c = 0; c < 4; c++) T[a][c] = 0;
+  T[0][0] = 1;
+  for (int k = 0; k < 3; k++)
+    for (int j = 0; j < 3; j++) T[1 + k][1 + j] = Ji[3 * j + k];
+  double DT[4][4];
+  for (int a = 0; a < 4; a++)
+    for (int c = 0; c < 4; c++) {
+      double v = 0;
+      for (int b = 0; b < 4; b++) v += D[4 * a + b] * T[b][c];
+      DT[a][c] = v;
+    }
+  for (int r = 0; r < 4; r++)
+    for (int c = 0; c < 4; c++) {
+      double v = 0;
+      for (int a = 0; a < 4; a++) v += T[a][r] * DT[a][c];
+      M[4 * r + c] = s * v;
+    }
+}
+
+// hex, per rule point: G[e*gs + m*nq + q] = Mh_m (m = 4 r + c), D per element
+// ([e][16]) or per point ([e][q][16])
+__global__ void hex_bdb_point_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
+                                     const double* __restrict__ gx, const double* __restrict__ gw,
+                                     const double* __restrict__ D, int per_point, double* G64, int gs64, float* G32,
+                                     int gs32) {
+  const int nq = nq1 * nq1 * nq1;
+  const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (int64_t)ne * nq) return;
+  const int e = (int)(id / nq), q = (int)(id % nq);
+  const int i = q / (nq1 * nq1), j = (q / nq1) % nq1, k = q % nq1;
+  int v[8];
+  for (int a = 0; a < 8; a++) v[a] = el[(size_t)e * 8 + a];
+  double J[9], Ji[9], det;
+  hex_jacobian(X, v, gx[i], gx[j], gx[k], J);
+  inv3(J, Ji, det);
+  const double* De = per_point ? D + ((size_t)e * nq + q) * 16 : D + (size_t)e * 16;
+  double M[16];
+  bdb_transform(Ji, De, gw[i] * gw[j] * gw[k] * fabs(det), M);
+  for (int m = 0; m < 16; m++) {
+    if (G64) G64[(size_t)e * gs64 + (size_t)m * nq + q] = M[m];
+    if (G32) G32[(size_t)e * gs32 + (size_t)m * nq + q] = (float)M[m];
+  }
+}
+
+// hex, one record per element (D per element): Mh without the rule weight from
+// the Jacobian at the center.  *flag = 1 when the Jacobian at a vertex of the
+// reference cube differs from the center one: that element map is not affine
+// and the caller switches to per-point records.
+__global__ void hex_bdb_elem_kernel(int ne, const double* __restrict__ X, const int* __restrict__ el,
+                                    const double* __restrict__ D, double* G64, float* G32, int* flag) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  int v[8];
+  for (int a = 0; a < 8; a++) v[a] = el[(size_t)e * 8 + a];
+  double J0[9], J[9], Ji[9], det, scale = 0, dev = 0;
+  hex_jacobian(X, v, 0.5, 0.5, 0.5, J0);
+  for (int c = 0; c < 9; c++) scale = fmax(scale, fabs(J0[c]));
+  for (int corner = 0; corner < 8; corner++) {
+    hex_jacobian(X, v, corner & 1, (corner >> 1) & 1, (corner >> 2) & 1, J);
+    for (int c = 0; c < 9; c++) dev = fmax(dev, fabs(J[c] - J0[c]));
+  }
+  if (dev > 1e-12 * scale) atomicExch(flag, 1);
+  inv3(J0, Ji, det);
+  double M[16];
+  bdb_transform(Ji, D + (size_t)e * 16, fabs(det), M);
+  for (int m = 0; m < 16; m++) {
+    if (G64) G64[(size_t)e * 16 + m] = M[m];
+    if (G32) G32[(size_t)e * 16 + m] = (float)M[m];
+  }
+}
+
+// tet, affine map x = v3 + sum_j (v_j - v3) xi_j: one record [e][16] without the
+// rule weight (D per element), or [e][q][16] with it (D per point)
+__global__ void tet_bdb_geom_kernel(int ne, int nq, const double* __restrict__ X, const int* __restrict__ el,
+                                    const double* __restrict__ rule, const double* __restrict__ D, int per_point,
+                                    double* M64, float* M32) {
+  const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nper = per_point ? nq : 1;
+  if (id >= (int64_t)ne * nper) return;
+  const int e = (int)(id / nper), q = (int)(id % nper);
+  const int* v = el + (size_t)e * 4;
+  const double* p3 = X + 3 * (size_t)v[3];
+  double J[9], Ji[9], det;
+  for (int j = 0; j < 3; j++) {
+    const double* pj = X + 3 * (size_t)v[j];
+    for (int k = 0; k < 3; k++) J[3 * k + j] = pj[k] - p3[k];
+  }
+  inv3(J, Ji, det);
+  const double s = per_point ? rule[4 * q + 3] * fabs(det) : fabs(det);
+  double M[16];
+  bdb_transform(Ji, D + (size_t)id * 16, s, M);
+  for (int m = 0; m < 16; m++) {
+    if (M64) M64[(size_t)id * 16 + m] = M[m];
+    if (M32) M32[(size_t)id * 16 + m] = (float)M[m];
+  }
+}
+
+// Diagonal of the hex operator, sum-factorized as for Laplace + mass: each of
+// the 10 symmetric component pairs (r <= s) of Mh + Mh^T is a product of 1D
+// factor pairs, BB, DD or BD per direction (D where the pair differentiates in
+// that direction), contracted direction by direction.
+__global__ void __launch_bounds__(256) hex_bdb_diag_kernel(int ne, int N, const int* __restrict__ tdof, int tstride,
+                                                            const double* __restrict__ G, int gstride, int per_elem,
+                                                            const double* __restrict__ gw, const double* __restrict__ B,
+                                                            const double* __restrict__ D, double* diag) {
+  extern __shared__ double dsm[];
+  const int N2 = N * N, N3 = N2 * N;
+  double* g = dsm;
+  double* h = dsm + 10 * N3;
+  const int pr[10] = {0, 1, 2, 3, 0, 0, 0, 1, 1, 2}, ps[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+  // factor selector of pair m in direction d (1 = x, 2 = y, 3 = z): 0 = B*B, 1 = D*D, 2 = B*D
+  auto sel = [&](int m, int d) {
+    const int c = (pr[m] == d) + (ps[m] == d);
+    return c == 0 ? 0 : (c == 2 ? 1 : 2);
+  };
+  auto fac = [&](int s, int q, int a) {
+    const double b = B[q * N + a], d = D[q * N + a];
+    return s == 0 ? b * b : (s == 1 ? d * d : b * d);
+  };
+  for (int e = blockIdx.x; e < ne; e += gridDim.x) {
+    const double* Ge = G + (size_t)e * gstride;
+    for (int t = threadIdx.x; t < 10 * N3; t += blockDim.x) {
+      const int m = t / N3, q = t % N3, r = pr[m], s = ps[m];
+      double v;
+      if (per_elem) {
+        const double w = gw[q / N2] * gw[(q / N) % N] * gw[q % N];
+        v = w * (Ge[4 * r + s] + (r != s ? Ge[4 * s + r] : 0.0));
+      } else {
+        v = Ge[(size_t)(4 * r + s) * N3 + q] + (r != s ? Ge[(size_t)(4 * s + r) * N3 + q] : 0.0);
+      }
+      g[t] = v;
+    }
+    __syncthreads();
+    // z: h[m][i][j][c] = sum_k f(k,c) g[m][i][j][k]
+    for (int t = threadIdx.x; t < 10 * N3; t += blockDim.x) {
+      const int m = t / N3, r = t % N3, ij = r / N, c = r % N, f = sel(m, 3);
+      double v = 0;
+      for (int k = 0; k < N; k++) v += fac(f, k, c) * g[m * N3 + ij * N + k];
+      h[t] = v;
+    }
+    __syncthreads();
+    // y: g[m][i][b][c] = sum_j f(j,b) h[m][i][j][c]
+    for (int t = threadIdx.x; t < 10 * N3; t += blockDim.x) {
+      const int m = t / N3, r = t % N3, i = r / N2, b = (r / N) % N, c = r % N, f = sel(m, 2);
+      double v = 0;
+      for (int j = 0; j < N; j++) v += fac(f, j, b) * h[m * N3 + (i * N + j) * N + c];
+      g[t] = v;
+    }
+    __syncthreads();
+    // x, and the sum over the pairs
+    for (int t = threadIdx.x; t < N3; t += blockDim.x) {
+      const int a = t / N2, bc = t % N2;
+      double v = 0;
+      for (int m = 0; m < 10; m++) {
+        const int f = sel(m, 1);
+        for (int i = 0; i < N; i++) v += fac(f, i, a) * g[m * N3 + i * N2 + bc];
+      }
+      atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
+    }
+    __syncthreads();
+  }
+}
+
+#define GH1_BDB_SWITCH(N, CASE)                                                                        \
+  switch (N) {                                                                                         \
+    CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)                                   \
+    default: throw Error(GH1_ERR_UNSUPPORTED, "hex order out of range");                              \
+  }
+
+template <class T>
+static int hex_bdb_occupancy(gh1_op* op, int gstride) {
+  const int tstride = op->sp->tstride;
+  int v = 0;
+#define GH1_BOCC_CASE(NN)                                                                                   \
+  case NN:                                                                                                  \
+    v = op->bdb == 2 ? hex_apply_occupancy<NN, T, true, 3>(HexSmem<NN, T>::total(gstride, tstride, 3))     \
+                     : hex_apply_occupancy<NN, T, true, 2>(HexSmem<NN, T>::total(gstride, tstride, 2));    \
+    break;
+  GH1_BDB_SWITCH(op->sp->p + 1, GH1_BOCC_CASE)
+#undef GH1_BOCC_CASE
+  return v;
+}
+
+template <class T>
+static void hex_bdb_launch(gh1_op* op, const T* x, T* y, const T* G, int gstride, double* partial,
+                           unsigned int* counter, double* energy, const int* skip) {
+#define GH1_BAPP_CASE(NN)                                                                                  \
+  case NN:                                                                                                 \
+    if (op->bdb == 2) launch_hex_apply<NN, T, true, 3>(op, x, y, G, gstride, partial, counter, energy, skip); \
+    else launch_hex_apply<NN, T, true, 2>(op, x, y, G, gstride, partial, counter, energy, skip);          \
+    break;
+  GH1_BDB_SWITCH(op->sp->p + 1, GH1_BAPP_CASE)
+#undef GH1_BAPP_CASE
+}
+
+void bdb_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  gh1_form* f = op->form;
+  cudaStream_t s = sp->ctx->stream;
+  const int ne = sp->mesh->ne;
+  const bool want32 = (op->prec_mask & 2) != 0;
+  GH1_CHECK(f->bdb_mode == 1 || f->bdb_mode == 2, GH1_ERR_ARG, "internal: not a B^T D B form");
+  op->has_mass = true;  // the value component is always interpolated
+  op->d_M64.release();
+  op->d_M32.release();
+  if (sp->et == 8) {
+    const int nq = sp->nq1 * sp->nq1 * sp->nq1;
+    // one record per element when D is per element and every element map is
+    // affine (GH1_BDB_AFFINE=0 keeps the per-point records)
+    const char* env = getenv("GH1_BDB_AFFINE");
+    bool elem = f->bdb_mode == 1 && !(env && std::string(env) == "0") && ne > 0;
+    if (elem) {
+      op->d_G64.alloc((size_t)ne * 16);
+      if (want32) op->d_G32.alloc((size_t)ne * 16); else op->d_G32.release();
+      DBuf<int> flag(1);
+      flag.zero(s);
+      hex_bdb_elem_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, f->d_bdb.p, op->d_G64.p,
+                                                           want32 ? op->d_G32.p : nullptr, flag.p);
+      check_kernel(sp->ctx, "hex_bdb_elem_kernel");
+      int h = 0;
+      GH1_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GH1_CUDA(cudaStreamSynchronize(s));
+      elem = h == 0;
+      op->gstride64 = op->gstride32 = 16;
+    }
+    if (!elem) {
+      op->gstride64 = (int)(round16((size_t)16 * nq * sizeof(double)) / sizeof(double));
+      op->gstride32 = (int)(round16((size_t)16 * nq * sizeof(float)) / sizeof(float));
+      op->d_G64.alloc((size_t)ne * op->gstride64);
+      if (want32) op->d_G32.alloc((size_t)ne * op->gstride32); else op->d_G32.release();
+      const int64_t tot = (int64_t)ne * nq;
+      if (tot > 0) {
+        hex_bdb_point_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
+            ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_bdb.p, f->bdb_mode == 2 ? 1 : 0,
+            op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
+        check_kernel(sp->ctx, "hex_bdb_point_kernel");
+      }
+    }
+    op->ncomp = 16;
+    op->bdb = elem ? 2 : 1;
+    upload_const_tables(sp);
+    op->bdb_per_sm[0] = hex_bdb_occupancy<double>(op, op->gstride64);
+    op->bdb_per_sm[1] = want32 ? hex_bdb_occupancy<float>(op, op->gstride32) : 0;
+  } else {
+    const int nq = sp->tet_nq_mass, per_point = f->bdb_mode == 2 ? 1 : 0;
+    const size_t nrec = (size_t)ne * (per_point ? nq : 1) * 16;
+    op->d_G64.alloc(nrec);
+    if (want32) op->d_G32.alloc(nrec); else op->d_G32.release();
+    const int64_t tot = (int64_t)ne * (per_point ? nq : 1);
+    if (tot > 0) {
+      tet_bdb_geom_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(ne, nq, sp->mesh->d_X.p, sp->mesh->d_el.p,
+                                                                        sp->d_tqm.p, f->d_bdb.p, per_point, op->d_G64.p,
+                                                                        want32 ? op->d_G32.p : nullptr);
+      check_kernel(sp->ctx, "tet_bdb_geom_kernel");
+    }
+    op->bdb = per_point ? 1 : 2;
+    tet_bdb_setup(op);
+  }
+  GH1_CUDA(cudaStreamSynchronize(s));
+  op->form_version = f->version;
+  op->have_diag = false;
+}
+
+void bdb_apply(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter, double* energy,
+               const int* skip) {
+  if (op->sp->et != 8) {
+    tet_bdb_apply(op, prec, x, y, partial, counter, energy, skip);
+    return;
+  }
+  if (prec == GH1_F64)
+    hex_bdb_launch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->gstride64, partial, counter, energy, skip);
+  else
+    hex_bdb_launch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->gstride32, partial, counter, energy, skip);
+}
+
+void bdb_diag(gh1_op* op, double* diag) {
+  gh1_space* sp = op->sp;
+  if (sp->et != 8) {
+    tet_bdb_diag(op, diag);
+    return;
+  }
+  const int ne = sp->mesh->ne, N = sp->p + 1;
+  if (ne == 0) return;
+  const size_t smem = (size_t)20 * N * N * N * sizeof(double);
+  if (smem > 48 * 1024)
+    GH1_CUDA(cudaFuncSetAttribute(hex_bdb_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = std::min(ne, sp->ctx->nsm * 8);
+  hex_bdb_diag_kernel<<<grid, 256, smem, sp->ctx->stream>>>(ne, N, sp->d_tdof.p, sp->tstride, op->d_G64.p, op->gstride64,
+                                                           op->bdb == 2 ? 1 : 0, sp->d_gw.p, sp->d_B64.p, sp->d_D64.p,
+                                                           diag);
+  check_kernel(sp->ctx, "hex_bdb_diag_kernel");
+}
+
+}  // namespace gh1

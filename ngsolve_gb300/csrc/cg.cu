@@ -606,6 +606,7 @@ extern "C" int gh1_adjoint_grad(gh1_form* form, const double* f, const double* u
     using namespace gh1;
     gh1_space* sp = form->sp;
     GH1_CHECK(!form->has_K6, GH1_ERR_UNSUPPORTED, "gh1_adjoint_grad: dJ/dkappa needs a scalar kappa (a tensor is set)");
+    GH1_CHECK(form->bdb_mode == 0, GH1_ERR_UNSUPPORTED, "gh1_adjoint_grad: dJ/dkappa needs a scalar kappa (a B^T D B form is set)");
     const int64_t n = sp->ndof;
     cudaStream_t s = ctx->stream;
     // the operator with FP64 and FP32 data, kept on the form between calls; the

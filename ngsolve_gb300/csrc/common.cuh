@@ -147,6 +147,12 @@ struct gh1_form {
   bool has_mu = false;
   gh1::DBuf<double> d_K6;     // ne x 6 symmetric diffusion tensors (xx yy zz xy xz yz); empty: kappa I
   bool has_K6 = false;
+  // generic B^T D B form (gh1_form_set_bdb): D in physical coordinates, row =
+  // test component (v, dv/dx, dv/dy, dv/dz), column = trial component; [ne][4][4]
+  // (bdb_mode 1) or [ne][nq][4][4] at the points of the space's rule (bdb_mode 2).
+  // While set it replaces kappa / mu / K6.
+  gh1::DBuf<double> d_bdb;
+  int bdb_mode = 0;
   int version = 0;            // bumped on coefficient change
   // references: the caller's (dropped by gh1_form_free) plus one per operator
   // made from the form (dropped when the operator is freed); the form is
@@ -192,6 +198,15 @@ struct gh1_op {
   int ncomp = 6, gstride64 = 0, gstride32 = 0;
   gh1::DBuf<double> d_M64;    // tet mass coefficient [e]
   gh1::DBuf<float> d_M32;
+  // generic B^T D B operator: 0 = none; 1 = reference-coordinate matrices
+  // Mh = w |det J| T^T D T per rule point in G (hex [e][16][nq] with gstride,
+  // tet [e][nq][16]); 2 = per-element Mh without the rule weight, [e][16] (affine
+  // elements with D per element), weighted in the kernel.  T = diag(1, J^{-T}).
+  int bdb = 0;
+  int bdb_per_sm[2] = {0, 0};                // hex: resident blocks of the B^T D B apply [FP64/FP32]
+  int tet_ncb = 0;                           // tet: 16-point chunks of the degree-2p rule
+  gh1::DBuf<double> d_tetB64, d_tetBw64;     // tet: [class][chunk][nlocp][64] value and reference-gradient
+  gh1::DBuf<float> d_tetB32, d_tetBw32;      //      rows (component*16 + point), weights [chunk*16]
   gh1::DBuf<int> d_err;       // device error flag of the pipelined apply (bounded waits)
   int hex_per_sm[2][2] = {{0, 0}, {0, 0}};  // resident blocks per SM of the hex apply [FP64/FP32][G mode]
   int hex_gmode[2] = {0, 0};                 // autotuned hex apply variant per precision: 0/1 = G tile by TMA /
@@ -255,6 +270,18 @@ void check_kernel(gh1_ctx* ctx, const char* what);
 
 // kernels / drivers (implemented in the .cu files)
 void build_tables(gh1_space* sp);                                   // tables.cu
+// values and reference gradients [class][q][i][4] at the degree-2p tet rule (tables.cu)
+void tet_mass_rule_tables(gh1_space* sp, gh1::DBuf<double>& t64, gh1::DBuf<float>& t32);
+int space_rule_size(const gh1_space* sp);                           // points of the B^T D B rule
+void space_qpoints(gh1_space* sp, double* ref /* nq x 4 or NULL */, double* xyz /* device, ne x nq x 3 or NULL */);
+void bdb_setup(gh1_op* op);                                         // bdb.cu
+void bdb_apply(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter, double* energy,
+               const int* skip);                                    // bdb.cu
+void bdb_diag(gh1_op* op, double* diag);                            // bdb.cu
+void tet_bdb_setup(gh1_op* op);                                     // tetapply.cu
+void tet_bdb_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
+                   double* energy, const int* skip);                // tetapply.cu
+void tet_bdb_diag(gh1_op* op, double* diag);                        // tetapply.cu
 void build_graph(gh1_space* sp);                                    // assemble.cu (host)
 bool build_graph_gpu(gh1_space* sp);                                // graph.cu
 void assemble_csr(gh1_form* f, double* vals);                       // assemble.cu

@@ -13,6 +13,31 @@ constexpr int tab_off(int N) { return N <= 2 ? 0 : tab_off(N - 1) + (N - 1) * (N
 constexpr int TAB_TOTAL = tab_off(MAX_HEX_ORDER + 2);
 
 // ---------------------------------------------------------------------------
+// element geometry (FP64)
+__device__ __forceinline__ void inv3(const double* J, double* Ji, double& det) {
+  det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
+  double id = 1.0 / det;
+  Ji[0] = (J[4] * J[8] - J[5] * J[7]) * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+  Ji[3] = (J[5] * J[6] - J[3] * J[8]) * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+  Ji[6] = (J[3] * J[7] - J[4] * J[6]) * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+}
+
+// J[3k+j] = d x_k / d xi_j of the trilinear hex map at (x,y,z)
+__device__ __forceinline__ void hex_jacobian(const double* X, const int* v, double x, double y, double z, double* J) {
+  const double dl[8][3] = {
+      {-(1 - y) * (1 - z), -(1 - x) * (1 - z), -(1 - x) * (1 - y)}, {(1 - y) * (1 - z), -x * (1 - z), -x * (1 - y)},
+      {y * (1 - z), x * (1 - z), -x * y},                           {-y * (1 - z), (1 - x) * (1 - z), -(1 - x) * y},
+      {-(1 - y) * z, -(1 - x) * z, (1 - x) * (1 - y)},             {(1 - y) * z, -x * z, x * (1 - y)},
+      {y * z, x * z, x * y},                                        {-y * z, (1 - x) * z, (1 - x) * y}};
+  for (int i = 0; i < 9; i++) J[i] = 0;
+  for (int a = 0; a < 8; a++) {
+    const double* pa = X + 3 * (size_t)v[a];
+    for (int k = 0; k < 3; k++)
+      for (int j = 0; j < 3; j++) J[3 * k + j] += pa[k] * dl[a][j];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // thread-group helpers
 template <int G>
 __device__ __forceinline__ void group_sync(int gid) {

@@ -193,6 +193,76 @@ void build_tables(gh1_space* sp) {
   }
 }
 
+// values and reference gradients at the degree-2p rule (the generic B^T D B
+// rule of tets; the mass table holds values only)
+void tet_mass_rule_tables(gh1_space* sp, DBuf<double>& t64, DBuf<float>& t32) {
+  cudaStream_t s = sp->ctx->stream;
+  const int nloc = sp->nloc, nqm = sp->tet_nq_mass, tot = N_TET_CLASSES * nqm;
+  t64.alloc((size_t)tot * nloc * 4);
+  t32.alloc((size_t)tot * nloc * 4);
+  DBuf<Dual3> scratch((size_t)tot * nloc);
+  tet_class_tables<<<(tot + 63) / 64, 64, 0, s>>>(sp->p, nloc, nqm, sp->d_tqm.p, t64.p, t32.p, 0, scratch.p);
+  check_kernel(sp->ctx, "tet_class_tables(2p)");
+  GH1_CUDA(cudaStreamSynchronize(s));  // scratch is released on return
+}
+
+// the rule of the generic B^T D B form: hex tensor Gauss with p+1 points per
+// direction (point q = (i*n + j)*n + k at (x_i, x_j, x_k)), tet the degree-2p rule
+int space_rule_size(const gh1_space* sp) { return sp->et == 8 ? sp->nq1 * sp->nq1 * sp->nq1 : sp->tet_nq_mass; }
+
+// physical coordinates of the rule points: hex trilinear map, tet affine map
+// x = v3 + sum_j (v_j - v3) xi_j
+__global__ void qpoints_kernel(int et, int ne, int nq, int nq1, const double* __restrict__ X, const int* __restrict__ el,
+                               const double* __restrict__ gx, const double* __restrict__ tqm, double* xyz) {
+  const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (int64_t)ne * nq) return;
+  const int e = (int)(id / nq), q = (int)(id % nq);
+  double out[3] = {0, 0, 0};
+  if (et == 8) {
+    const double x = gx[q / (nq1 * nq1)], y = gx[(q / nq1) % nq1], z = gx[q % nq1];
+    const double lam[8] = {(1 - x) * (1 - y) * (1 - z), x * (1 - y) * (1 - z), x * y * (1 - z), (1 - x) * y * (1 - z),
+                           (1 - x) * (1 - y) * z,       x * (1 - y) * z,       x * y * z,       (1 - x) * y * z};
+    for (int a = 0; a < 8; a++) {
+      const double* pa = X + 3 * (size_t)el[(size_t)e * 8 + a];
+      for (int k = 0; k < 3; k++) out[k] += lam[a] * pa[k];
+    }
+  } else {
+    const double* p3 = X + 3 * (size_t)el[(size_t)e * 4 + 3];
+    for (int k = 0; k < 3; k++) out[k] = p3[k];
+    for (int j = 0; j < 3; j++) {
+      const double* pj = X + 3 * (size_t)el[(size_t)e * 4 + j];
+      for (int k = 0; k < 3; k++) out[k] += (pj[k] - p3[k]) * tqm[4 * q + j];
+    }
+  }
+  for (int k = 0; k < 3; k++) xyz[id * 3 + k] = out[k];
+}
+
+void space_qpoints(gh1_space* sp, double* ref, double* xyz) {
+  cudaStream_t s = sp->ctx->stream;
+  const int nq = space_rule_size(sp), ne = sp->mesh->ne;
+  if (ref) {
+    if (sp->et == 8) {
+      const int n = sp->nq1;
+      for (int q = 0; q < nq; q++) {
+        const int i = q / (n * n), j = (q / n) % n, k = q % n;
+        ref[4 * q] = sp->gx[i];
+        ref[4 * q + 1] = sp->gx[j];
+        ref[4 * q + 2] = sp->gx[k];
+        ref[4 * q + 3] = sp->gw[i] * sp->gw[j] * sp->gw[k];
+      }
+    } else {
+      GH1_CUDA(cudaMemcpyAsync(ref, sp->d_tqm.p, (size_t)nq * 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GH1_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  if (xyz && ne > 0) {
+    const int64_t tot = (int64_t)ne * nq;
+    qpoints_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(sp->et, ne, nq, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p,
+                                                                 sp->d_gx.p, sp->d_tqm.p, xyz);
+    check_kernel(sp->ctx, "qpoints_kernel");
+  }
+}
+
 // ---- shape evaluation at arbitrary points (gh1_shape_eval) -------------------
 __global__ void shape_eval_kernel(int et, int p, int nloc, int v0, int v1, int v2, int v3, int v4, int v5, int v6, int v7,
                                   int npts, const double* pts, double* val, double* grad, Dual3* scratch) {

@@ -492,26 +492,14 @@ static void tet_chunk_setup(gh1_op* op, const std::vector<double>& rule, const s
   GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
 }
 
-// Class-sorted element order, tiles, tables and occupancy.  GH1_TET_KERNEL=elementwise
-// keeps the element-wise kernel (for comparisons).
-void tet_tiles_setup(gh1_op* op) {
+// counting sort of the elements by orientation class; tiles of up to TET_TE
+// elements of one class ([ntiles][4] = class, first position, count, 0)
+static void tet_class_tiles(gh1_op* op) {
   gh1_space* sp = op->sp;
-  op->tet_tiles_per_sm[0] = op->tet_tiles_per_sm[1] = 0;
-  const char* env = getenv("GH1_TET_KERNEL");
-  if (env && std::string(env) == "elementwise") return;
-  const int ne = sp->mesh->ne, nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
-  const int nlocp = (nloc + 15) / 16 * 16;
-  op->tet_chunked = false;
-  if (nlocp / 16 > TET_TI || ne == 0) return;
-  const int R = 3 * nq + (op->has_mass ? nqm : 0), Rp = (R + 15) / 16 * 16, Rs = Rp + 1;
-  const int ncls = N_TET_CLASSES;
   cudaStream_t s = sp->ctx->stream;
-  // counting sort by class, tiles of up to TET_TE elements of one class
+  const int ne = sp->mesh->ne, ncls = N_TET_CLASSES;
   std::vector<uint8_t> cls(ne);
   GH1_CUDA(cudaMemcpyAsync(cls.data(), sp->d_class.p, ne, cudaMemcpyDeviceToHost, s));
-  std::vector<double> rule(4 * (size_t)nq), rulem(4 * (size_t)nqm);
-  GH1_CUDA(cudaMemcpyAsync(rule.data(), sp->d_tq.p, rule.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-  if (nqm) GH1_CUDA(cudaMemcpyAsync(rulem.data(), sp->d_tqm.p, rulem.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
   GH1_CUDA(cudaStreamSynchronize(s));
   std::vector<int> count(ncls + 1, 0), perm(ne), tiles;
   for (int e = 0; e < ne; e++) count[cls[e] + 1]++;
@@ -528,6 +516,28 @@ void tet_tiles_setup(gh1_op* op) {
   op->d_tet_perm.upload(perm, s);
   op->d_tet_tiles.upload(tiles, s);
   op->tet_ntiles = (int)tiles.size() / 4;
+  GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+}
+
+// Class-sorted element order, tiles, tables and occupancy.  GH1_TET_KERNEL=elementwise
+// keeps the element-wise kernel (for comparisons).
+void tet_tiles_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->tet_tiles_per_sm[0] = op->tet_tiles_per_sm[1] = 0;
+  const char* env = getenv("GH1_TET_KERNEL");
+  if (env && std::string(env) == "elementwise") return;
+  const int ne = sp->mesh->ne, nloc = sp->nloc, nq = sp->tet_nq, nqm = sp->tet_nq_mass;
+  const int nlocp = (nloc + 15) / 16 * 16;
+  op->tet_chunked = false;
+  if (nlocp / 16 > TET_TI || ne == 0) return;
+  const int R = 3 * nq + (op->has_mass ? nqm : 0), Rp = (R + 15) / 16 * 16, Rs = Rp + 1;
+  const int ncls = N_TET_CLASSES;
+  cudaStream_t s = sp->ctx->stream;
+  tet_class_tiles(op);
+  std::vector<double> rule(4 * (size_t)nq), rulem(4 * (size_t)nqm);
+  GH1_CUDA(cudaMemcpyAsync(rule.data(), sp->d_tq.p, rule.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (nqm) GH1_CUDA(cudaMemcpyAsync(rulem.data(), sp->d_tqm.p, rulem.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
   const bool mass = op->has_mass;
   // the whole class table in shared memory (compiled orders), else 16-point chunks
   const TetSmem<double> full{nlocp, Rp, Rs};
@@ -665,6 +675,264 @@ bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* parti
                            op->has_mass ? op->d_M32.p : nullptr, (const float*)x, (float*)y, partial, counter,
                            energy, skip);
   return true;
+}
+
+// ---- generic B^T D B on same-class tiles (bdb.cu sets up the element records) ----
+// The degree-2p rule goes through shared memory 16 points at a time.  Per chunk
+// the table slice holds 64 rows: value, d/dxi, d/deta, d/dzeta (row comp*16 + point)
+// of every local shape; the tile products are those of the chunked kernel and the
+// point transform is the 4x4 reference-coordinate matrix Mh of the element (times
+// the rule weight; PP: one matrix per point, weight included).
+//   Tb: [class][chunk][nlocp][64];  Wb: [chunk*16] weights, zero beyond the rule
+template <class T>
+__host__ __device__ inline size_t tet_bdb_smem(int nlocp) {
+  return tet_r16((size_t)nlocp * (4 * TET_QC + 1) * sizeof(T)) +
+         ((size_t)nlocp * TET_TE + 4 * TET_QC * TET_TE + TET_TE * 17) * sizeof(T) + (size_t)nlocp * TET_TE * sizeof(int);
+}
+
+template <class T, bool PP>
+__global__ void __launch_bounds__(TET_TT)
+tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncb,
+               int nq, const int* __restrict__ eldofs, const T* __restrict__ Mh, const T* __restrict__ Tb,
+               const T* __restrict__ Wb, const T* __restrict__ x, T* __restrict__ y, double* partial,
+               unsigned int* counter, double* energy, const int* skip) {
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int RC = 4 * TET_QC, RS = RC + 1;  // rows per chunk; odd stride: conflict-free column reads
+  T* sD = (T*)smem;                                                // [nlocp][RS]
+  T* sX = (T*)(smem + tet_r16((size_t)nlocp * RS * sizeof(T)));    // [nlocp][TE]
+  T* sP = sX + (size_t)nlocp * TET_TE;                             // [64][TE]
+  T* sM = sP + (size_t)RC * TET_TE;                                // [TE][17] element records
+  int* sDof = (int*)(sM + TET_TE * 17);                            // [nlocp][TE]
+  const int tid = threadIdx.x, cg = tid & 7, rg = tid >> 3;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  const int ni = nlocp / 16;  // block-uniform
+  double acc = 0;
+  for (int t = t0; t < t1; t++) {
+    const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    __syncthreads();
+    for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {
+      const int e = k % TET_TE, i = k / TET_TE;
+      int d = 0;
+      T v = 0;
+      if (e < cnt && i < nloc) {
+        d = eldofs[(size_t)perm[start + e] * nloc + i];
+        v = x[d];
+      }
+      sDof[k] = d;
+      sX[k] = v;
+    }
+    if (!PP)
+      for (int k = tid; k < TET_TE * 16; k += TET_TT) {
+        const int e = k / 16, c = k % 16;
+        sM[e * 17 + c] = e < cnt ? Mh[(size_t)perm[start + e] * 16 + c] : T(0);
+      }
+    T b[TET_TI][4];
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    for (int cc = 0; cc < ncb; cc++) {
+      const T* src = Tb + ((size_t)cls * ncb + cc) * nlocp * RC;
+      __syncthreads();  // X, records, DOFs ready; the previous slice is consumed
+      for (int k = tid; k < nlocp * RC; k += TET_TT) sD[(k / RC) * RS + k % RC] = src[k];
+      __syncthreads();
+      // P[r][e] = sum_i D[i][r] X[i][e], rows r = rg + 16 u
+      {
+        T a[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[u][0] = a[u][1] = a[u][2] = a[u][3] = 0;
+        for (int i = 0; i < nloc; i++) {
+          T xv[4];
+          ld4(sX + i * TET_TE + 4 * cg, xv);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const T dv = sD[i * RS + rg + 16 * u];
+            a[u][0] += dv * xv[0]; a[u][1] += dv * xv[1]; a[u][2] += dv * xv[2]; a[u][3] += dv * xv[3];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) st4(sP + (size_t)(rg + 16 * u) * TET_TE + 4 * cg, a[u]);
+      }
+      __syncthreads();
+      // point transform (v, v_x, v_y, v_z) = Mh (u, u_x, u_y, u_z), in place
+      for (int k = tid; k < TET_QC * TET_TE; k += TET_TT) {
+        const int q = k / TET_TE, e = k % TET_TE, qg = cc * TET_QC + q;
+        T in[4], m[16];
+#pragma unroll
+        for (int c = 0; c < 4; c++) in[c] = sP[(size_t)(c * TET_QC + q) * TET_TE + e];
+        if (PP) {
+          const bool ok = e < cnt && qg < nq;
+          const T* mp = Mh + ((size_t)(ok ? perm[start + e] : 0) * nq + (ok ? qg : 0)) * 16;
+#pragma unroll
+          for (int c = 0; c < 16; c++) m[c] = ok ? mp[c] : T(0);
+        } else {
+          const T w = Wb[qg];
+#pragma unroll
+          for (int c = 0; c < 16; c++) m[c] = w * sM[e * 17 + c];
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const T o = m[4 * r] * in[0] + m[4 * r + 1] * in[1] + m[4 * r + 2] * in[2] + m[4 * r + 3] * in[3];
+          acc += (double)(in[r] * o);
+          sP[(size_t)(r * TET_QC + q) * TET_TE + e] = o;
+        }
+      }
+      __syncthreads();
+      // Y[i][e] += sum_r D[i][r] V[r][e], rows i = rg + 16 u
+      for (int r = 0; r < RC; r++) {
+        T pv[4];
+        ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
+#pragma unroll
+        for (int u = 0; u < TET_TI; u++)
+          if (u < ni) {
+            const T dv = sD[(rg + 16 * u) * RS + r];
+            b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
+          }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < TET_TI; u++) {
+      const int i = rg + 16 * u;
+      if (u < ni && i < nloc) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int e = 4 * cg + c;
+          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+        }
+      }
+    }
+  }
+  if (partial) block_reduce_finish(acc, partial, counter, energy);
+}
+
+// Tb[c][cc][i][r] from the values and reference gradients at the degree-2p rule
+// (t: [class][q][i][4]); zero for i >= nloc and points beyond the rule
+template <class T>
+__global__ void tet_bdb_table_kernel(int ncls, int nloc, int nlocp, int nq, int ncb, const T* __restrict__ t, T* Tb) {
+  const int64_t tot = (int64_t)ncls * ncb * nlocp * 4 * TET_QC;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(k % (4 * TET_QC)), i = (int)((k / (4 * TET_QC)) % nlocp);
+    const int64_t ccc = k / ((int64_t)4 * TET_QC * nlocp);
+    const int cc = (int)(ccc % ncb), c = (int)(ccc / ncb);
+    const int q = cc * TET_QC + r % TET_QC, comp = r / TET_QC;
+    Tb[k] = (i < nloc && q < nq) ? t[(((size_t)c * nq + q) * nloc + i) * 4 + comp] : T(0);
+  }
+}
+
+template <class T, bool PP>
+static int tet_bdb_occupancy(int nlocp) {
+  auto kern = tet_bdb_kernel<T, PP>;
+  const size_t smem = tet_bdb_smem<T>(nlocp);
+  int dev = 0, optin = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const int avail = optin - (int)fa.sharedSizeBytes;
+  GH1_CHECK((long long)smem <= avail, GH1_ERR_UNSUPPORTED, "tet B^T D B apply does not fit in shared memory");
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, avail));
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TET_TT, smem));
+  GH1_CHECK(v >= 1, GH1_ERR_UNSUPPORTED, "tet B^T D B apply does not fit on an SM");
+  return v;
+}
+
+void tet_bdb_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  cudaStream_t s = sp->ctx->stream;
+  const int nloc = sp->nloc, nq = sp->tet_nq_mass, nlocp = (nloc + 15) / 16 * 16, ncls = N_TET_CLASSES;
+  GH1_CHECK(nlocp / 16 <= TET_TI, GH1_ERR_UNSUPPORTED, "tet order too high for the B^T D B apply");
+  const int ncb = (nq + TET_QC - 1) / TET_QC;
+  op->tet_ncb = ncb;
+  tet_class_tiles(op);
+  DBuf<double> t64;
+  DBuf<float> t32;
+  tet_mass_rule_tables(sp, t64, t32);
+  const int64_t nt = (int64_t)ncls * ncb * nlocp * 4 * TET_QC;
+  const int tgrid = (int)std::min<int64_t>((nt + 255) / 256, 4096);
+  op->d_tetB64.alloc(nt);
+  tet_bdb_table_kernel<double><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, ncb, t64.p, op->d_tetB64.p);
+  check_kernel(sp->ctx, "tet_bdb_table_kernel");
+  std::vector<double> rule(4 * (size_t)nq), w((size_t)ncb * TET_QC, 0.0);
+  GH1_CUDA(cudaMemcpyAsync(rule.data(), sp->d_tqm.p, rule.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  for (int q = 0; q < nq; q++) w[q] = rule[4 * q + 3];
+  op->d_tetBw64.upload(w, s);
+  const bool pp = op->bdb == 1;
+  op->bdb_per_sm[0] = pp ? tet_bdb_occupancy<double, true>(nlocp) : tet_bdb_occupancy<double, false>(nlocp);
+  op->bdb_per_sm[1] = 0;
+  if (op->prec_mask & 2) {
+    op->d_tetB32.alloc(nt);
+    tet_bdb_table_kernel<float><<<tgrid, 256, 0, s>>>(ncls, nloc, nlocp, nq, ncb, t32.p, op->d_tetB32.p);
+    check_kernel(sp->ctx, "tet_bdb_table_kernel");
+    std::vector<float> w32(w.begin(), w.end());
+    op->d_tetBw32.upload(w32, s);
+    op->bdb_per_sm[1] = pp ? tet_bdb_occupancy<float, true>(nlocp) : tet_bdb_occupancy<float, false>(nlocp);
+  }
+  GH1_CUDA(cudaStreamSynchronize(s));  // tables and host staging go out of scope
+}
+
+template <class T>
+static void tet_bdb_launch(gh1_op* op, int per_sm, const T* Mh, const T* Tb, const T* Wb, const T* x, T* y,
+                           double* partial, unsigned int* counter, double* energy, const int* skip) {
+  gh1_space* sp = op->sp;
+  const int nlocp = (sp->nloc + 15) / 16 * 16;
+  const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
+  const size_t smem = tet_bdb_smem<T>(nlocp);
+  if (op->bdb == 1)
+    tet_bdb_kernel<T, true><<<grid, TET_TT, smem, sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,
+        sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip);
+  else
+    tet_bdb_kernel<T, false><<<grid, TET_TT, smem, sp->ctx->stream>>>(
+        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,
+        sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip);
+  check_kernel(sp->ctx, "tet_bdb_kernel");
+}
+
+void tet_bdb_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
+                   double* energy, const int* skip) {
+  if (op->tet_ntiles == 0) return;
+  if (prec == GH1_F64)
+    tet_bdb_launch<double>(op, op->bdb_per_sm[0], op->d_G64.p, op->d_tetB64.p, op->d_tetBw64.p, (const double*)x,
+                           (double*)y, partial, counter, energy, skip);
+  else {
+    GH1_CHECK(op->bdb_per_sm[1] > 0, GH1_ERR_ARG, "operator has no FP32 data (precision_mask)");
+    tet_bdb_launch<float>(op, op->bdb_per_sm[1], op->d_G32.p, op->d_tetB32.p, op->d_tetBw32.p, (const float*)x,
+                          (float*)y, partial, counter, energy, skip);
+  }
+}
+
+// diagonal: per (element, local shape) the sum over the rule points of B^T Mh B
+__global__ void tet_bdb_diag_kernel(int ne, int nloc, int nlocp, int ncb, int nq, const int* __restrict__ eldofs,
+                                    const uint8_t* __restrict__ cls, const double* __restrict__ Mh, int per_point,
+                                    const double* __restrict__ Tb, const double* __restrict__ Wb, double* diag) {
+  const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (int64_t)ne * nloc) return;
+  const int e = (int)(id / nloc), i = (int)(id % nloc), c = cls[e];
+  double s = 0;
+  for (int q = 0; q < nq; q++) {
+    const double* row = Tb + (((size_t)c * ncb + q / TET_QC) * nlocp + i) * 4 * TET_QC + q % TET_QC;
+    const double bv[4] = {row[0], row[TET_QC], row[2 * TET_QC], row[3 * TET_QC]};
+    const double* m = per_point ? Mh + ((size_t)e * nq + q) * 16 : Mh + (size_t)e * 16;
+    const double w = per_point ? 1.0 : Wb[q];
+    double t = 0;
+    for (int r = 0; r < 4; r++)
+      for (int k = 0; k < 4; k++) t += bv[r] * m[4 * r + k] * bv[k];
+    s += w * t;
+  }
+  atomicAdd(diag + eldofs[id], s);
+}
+
+void tet_bdb_diag(gh1_op* op, double* diag) {
+  gh1_space* sp = op->sp;
+  const int ne = sp->mesh->ne, nloc = sp->nloc, nlocp = (nloc + 15) / 16 * 16;
+  const int64_t tot = (int64_t)ne * nloc;
+  if (tot == 0) return;
+  tet_bdb_diag_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, sp->ctx->stream>>>(
+      ne, nloc, nlocp, op->tet_ncb, sp->tet_nq_mass, sp->d_eldofs.p, sp->d_class.p, op->d_G64.p, op->bdb == 1 ? 1 : 0,
+      op->d_tetB64.p, op->d_tetBw64.p, diag);
+  check_kernel(sp->ctx, "tet_bdb_diag_kernel");
 }
 
 }  // namespace gh1

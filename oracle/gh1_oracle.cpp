@@ -716,6 +716,79 @@ void orc_apply_mf_k6(void* h, const double* k6, const double* mu, const double* 
   apply_mf_impl(h, nullptr, k6, mu, x, y, e0, e1);
 }
 
+// Generic B^T D B: the reference's fused symbolic operator for an arbitrary
+// bilinear integrand (comp/matrixfree.cpp:1090-1330 AssembleBDBFused: D from
+// the integrand per trial/test component pair, then B^T D B per point with the
+// element Jacobian), applied element by element as ApplyElementMatrix does
+// (fem/symbolicintegrator.cpp:2959-3040):
+//   y_e = sum_q w_q |det J_q| B_q^T D_q B_q x_e,  B_q x = (u, grad u) at point q
+// in physical coordinates, D row = test component, column = trial component.
+// per_point = 0: D[e][16]; 1: D[e][q][16] at the nq points of `rule` (reference
+// x, y, z, w).  rule = NULL: the oracle's own rule of order 2p (D per element).
+// diag != NULL: the diagonal of the operator instead of y (x unused).
+static void bdb_impl(void* h, const double* D, int per_point, int nq, const double* rule, const double* x, double* y,
+                     double* diag) {
+  Space* S = (Space*)h;
+  Rule r;
+  if (rule) {
+    for (int q = 0; q < nq; q++) {
+      r.x.push_back(rule[4 * q]); r.y.push_back(rule[4 * q + 1]); r.z.push_back(rule[4 * q + 2]); r.w.push_back(rule[4 * q + 3]);
+    }
+  } else {
+    r = mass_rule(*S);
+  }
+  double* out = diag ? diag : y;
+  std::memset(out, 0, S->ndof * sizeof(double));
+  const int n = S->nloc;
+#pragma omp parallel
+  {
+    std::vector<AD> sh(n);
+    std::vector<double> xe(n), ye(n);
+#pragma omp for schedule(dynamic, 16)
+    for (int e = 0; e < S->ne; e++) {
+      const long* dn = &S->edofs[(size_t)e * n];
+      for (int i = 0; i < n; i++) { xe[i] = diag ? 0.0 : x[dn[i]]; ye[i] = 0; }
+      for (int q = 0; q < r.size(); q++) {
+        shape_ad(*S, e, r.x[q], r.y[q], r.z[q], sh.data());
+        Geo g = geometry(*S, e, r.x[q], r.y[q], r.z[q]);
+        const double* De = per_point ? D + ((size_t)e * r.size() + q) * 16 : D + (size_t)e * 16;
+        const double s = r.w[q] * std::fabs(g.det);
+        if (diag) {
+          for (int i = 0; i < n; i++) {
+            double b[4] = {sh[i].v, 0, 0, 0};
+            for (int k = 0; k < 3; k++) b[1 + k] = g.Jinv[k] * sh[i].d[0] + g.Jinv[3 + k] * sh[i].d[1] + g.Jinv[6 + k] * sh[i].d[2];
+            double t = 0;
+            for (int a = 0; a < 4; a++) for (int c = 0; c < 4; c++) t += b[a] * De[4 * a + c] * b[c];
+            ye[i] += s * t;
+          }
+          continue;
+        }
+        double in[4] = {0, 0, 0, 0}, gr[3] = {0, 0, 0};
+        for (int i = 0; i < n; i++) {
+          in[0] += sh[i].v * xe[i];
+          for (int k = 0; k < 3; k++) gr[k] += sh[i].d[k] * xe[i];
+        }
+        for (int k = 0; k < 3; k++) in[1 + k] = g.Jinv[k] * gr[0] + g.Jinv[3 + k] * gr[1] + g.Jinv[6 + k] * gr[2];
+        double o[4];
+        for (int a = 0; a < 4; a++) o[a] = s * (De[4 * a] * in[0] + De[4 * a + 1] * in[1] + De[4 * a + 2] * in[2] + De[4 * a + 3] * in[3]);
+        double ref[3];  // J^{-1} (o_x, o_y, o_z): the test gradient's coefficients in reference coordinates
+        for (int j = 0; j < 3; j++) ref[j] = g.Jinv[3 * j] * o[1] + g.Jinv[3 * j + 1] * o[2] + g.Jinv[3 * j + 2] * o[3];
+        for (int i = 0; i < n; i++) ye[i] += sh[i].v * o[0] + sh[i].d[0] * ref[0] + sh[i].d[1] * ref[1] + sh[i].d[2] * ref[2];
+      }
+      for (int i = 0; i < n; i++) {
+#pragma omp atomic
+        out[dn[i]] += ye[i];
+      }
+    }
+  }
+}
+void orc_apply_bdb(void* h, const double* D, int per_point, int nq, const double* rule, const double* x, double* y) {
+  bdb_impl(h, D, per_point, nq, rule, x, y, nullptr);
+}
+void orc_diag_bdb(void* h, const double* D, int per_point, int nq, const double* rule, double* diag) {
+  bdb_impl(h, D, per_point, nq, rule, nullptr, nullptr, diag);
+}
+
 // LinearForm f*v with f piecewise constant per element, integration order 2p
 // (SymbolicLFI, fem/symbolicintegrator.cpp:1109)
 void orc_rhs(void* h, const double* f, double* b) {

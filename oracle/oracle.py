@@ -55,6 +55,8 @@ def lib():
         L.orc_element_matrix.argtypes = [P, i, d, d, P]
         L.orc_spmv.argtypes = [l, P, P, P, d, P, P, i]
         L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
+        L.orc_apply_bdb.argtypes = [P, P, i, i, P, P, P]
+        L.orc_diag_bdb.argtypes = [P, P, i, i, P, P]
         L.orc_rhs.argtypes = [P, P, P]
         L.orc_elem_grad_dot.argtypes = [P, P, P, P]
         L.orc_shapes.argtypes = [i, i, P, i, P, P, P]
@@ -164,6 +166,29 @@ class OracleSpace:
         else:
             lib().orc_apply_mf(self.h, _p(k), _p(m), _p(x), _p(y), int(e0), int(e1))
         return y
+
+    def _bdb_args(self, D, rule):
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        per_point = 0 if D.size == self.ne * 16 else 1
+        r = None if rule is None else np.ascontiguousarray(rule, dtype=np.float64).reshape(-1, 4)
+        if per_point and (r is None or D.size != self.ne * len(r) * 16):
+            raise ValueError("a point-wise D needs the rule it is given at, D[ne][nq][16]")
+        return D, per_point, (0 if r is None else len(r)), r
+
+    def apply_bdb(self, x, D, rule=None):
+        """Generic B^T D B apply: D[ne][4][4] (or [ne][nq][4][4] at rule's points),
+        rows test (v, grad v), columns trial (u, grad u), physical coordinates."""
+        D, pp, nq, r = self._bdb_args(D, rule)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.ndof)
+        lib().orc_apply_bdb(self.h, _p(D), pp, nq, _p(r), _p(x), _p(y))
+        return y
+
+    def diag_bdb(self, D, rule=None):
+        D, pp, nq, r = self._bdb_args(D, rule)
+        d = np.zeros(self.ndof)
+        lib().orc_diag_bdb(self.h, _p(D), pp, nq, _p(r), _p(d))
+        return d
 
     def rhs(self, f_elem):
         f = np.ascontiguousarray(f_elem, dtype=np.float64)

@@ -2,6 +2,7 @@
 classification of integrands into the forms the library runs."""
 import numpy as np
 import pytest
+import torch
 
 from ngsolve_gb300 import comp as C
 
@@ -479,3 +480,42 @@ def test_integrate_rejects_bad_operands(monkeypatch):
         C.Integrate(2.0 * vf, None)
     with pytest.raises(NotImplementedError):
         C.Integrate(C.x * vf, None)
+
+
+def test_generic_bdb_terms():
+    """Terms outside kappa grad.grad / mu u v / symmetric K go into the generic
+    B^T D B matrix (rows test (v, grad v), columns trial (u, grad u)): convection
+    b . grad(u) v in row 0, its transpose u (b . grad v) in column 0, a
+    non-symmetric K in the gradient block; a coordinate factor makes D point-wise."""
+    u, v = _uv()
+    ne = 4
+    kap = np.arange(1.0, 5.0)
+    b = C.CoefficientFunction((kap, 2.0, -1.0))
+    Kn = np.array([[1.0, 0.5, 0.0], [0.0, 2.0, 0.0], [0.3, 0.0, 3.0]])
+    terms = [C.CoefficientFunction(kap) * C.grad(u) * C.grad(v) * C.dx,
+             C.InnerProduct(b, C.grad(u)) * v * C.dx,
+             3.0 * u * C.InnerProduct(C.CoefficientFunction((0.0, 1.0, 0.0)), C.grad(v)) * C.dx,
+             C.InnerProduct(C.CoefficientFunction(Kn) * C.grad(u), C.grad(v)) * C.dx,
+             2.0 * u * v * C.dx]
+    assert all(C._bdb_needed(t) for t in terms[1:4]) and not C._bdb_needed(terms[0])
+    D = C._bdb_D(terms, ne, None, torch.device("cpu"))
+    assert D.shape == (ne, 1, 4, 4)
+    D = D[:, 0].numpy()
+    assert np.allclose(D[:, 0, 0], 2.0)
+    assert np.allclose(D[:, 0, 1], kap) and np.allclose(D[:, 0, 2], 2.0) and np.allclose(D[:, 0, 3], -1.0)
+    assert np.allclose(D[:, 1:, 0], [0.0, 3.0, 0.0])
+    assert np.allclose(D[:, 1:, 1:], kap[:, None, None] * np.eye(3) + Kn)
+    # point-wise: x * u * v at two points per element
+    pts = torch.tensor(np.random.default_rng(1).uniform(size=(ne, 2, 3)))
+    Dp = C._bdb_D([C.x * u * v * C.dx], ne, pts, torch.device("cpu")).numpy()
+    assert Dp.shape == (ne, 2, 4, 4) and np.allclose(Dp[:, :, 0, 0], pts[..., 0].numpy())
+    assert C._is_pointwise(C.CoefficientFunction((C.y, 0.0, 0.0)))
+    # shapes the generic form cannot take
+    with pytest.raises(NotImplementedError):
+        C._bdb_parts(b * C.grad(u) * C.grad(v) * C.dx)   # a vector with two gradients
+    with pytest.raises(NotImplementedError):
+        C._bdb_parts(C.CoefficientFunction(Kn) * C.grad(u) * v * C.dx)
+    with pytest.raises(NotImplementedError):
+        C._bdb_parts(u * u * C.dx)
+    with pytest.raises(ValueError):
+        C._bdb_parts(u * C.grad(v))

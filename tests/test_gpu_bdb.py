@@ -1,0 +1,183 @@
+"""Generic B^T D B operator (gh1_form_set_bdb) against the oracle's element-by-
+element B^T D B apply: convection b . grad(u) v, its transpose u (c . grad v), a
+non-symmetric diffusion matrix and reaction, with D per element (the reference's
+AssembleBDBFused evaluation) or per rule point (coefficients in x, y, z).
+FP64 within 1e-12 and FP32 within 2e-5 of max |y|; the diagonal behind Jacobi
+within 1e-12; a generic form equal to kappa grad.grad + mu u v solves like it."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from ngsolve_gb300 import comp as C
+from ngsolve_gb300 import _lib
+from ngsolve_gb300.meshes import MakeStructured3DMesh, JitterInterior
+from tests.util import lognormal
+
+pytestmark = pytest.mark.gpu
+
+
+def _mesh(hexes, n, jitter, seed=61):
+    m = MakeStructured3DMesh(hexes=hexes, nx=n)
+    return JitterInterior(m, jitter / n, seed) if jitter else m
+
+
+def _terms(gpu, fes, ne, seed, pointwise):
+    """kappa grad.grad + (b . grad u) v + u (c . grad v) + (Kn grad u).grad v + r u v;
+    with pointwise, r and one convection component depend on x, y, z."""
+    rng = np.random.default_rng(seed)
+    u, v = fes.TnT()
+    kap = lognormal(ne, 0.5, seed + 1)
+    Kn = np.eye(3) * 0.5 + rng.normal(size=(3, 3)) * 0.2  # not symmetric
+    b = gpu.CoefficientFunction((rng.normal(size=ne), 0.7, gpu.y if pointwise else -0.4))
+    c = gpu.CoefficientFunction((0.3, rng.normal(size=ne), 0.2))
+    r = (1.0 + gpu.x) if pointwise else gpu.CoefficientFunction(rng.uniform(0.5, 2.0, ne))
+    return [gpu.CoefficientFunction(kap) * gpu.grad(u) * gpu.grad(v) * gpu.dx,
+            gpu.InnerProduct(b, gpu.grad(u)) * v * gpu.dx,
+            u * gpu.InnerProduct(c, gpu.grad(v)) * gpu.dx,
+            gpu.InnerProduct(gpu.CoefficientFunction(Kn) * gpu.grad(u), gpu.grad(v)) * gpu.dx,
+            r * u * v * gpu.dx]
+
+
+def _rule(gpu, fes):
+    nq = ctypes.c_int()
+    ctx = fes.ctx
+    ctx.check(ctx.lib.gh1_space_qpoints(fes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(nq)))
+    ref = np.zeros((nq.value, 4))
+    ctx.check(ctx.lib.gh1_space_qpoints(fes.h, ref.ctypes.data_as(ctypes.c_void_p), None, _lib.GH1_MEM_HOST, None))
+    xyz = torch.empty((fes.ne, nq.value, 3), dtype=torch.float64, device="cuda")
+    ctx.sync_stream()
+    ctx.check(ctx.lib.gh1_space_qpoints(fes.h, None, ctypes.c_void_p(xyz.data_ptr()), _lib.GH1_MEM_DEVICE, None))
+    torch.cuda.synchronize()
+    return ref, xyz
+
+
+def _oracle_D(terms, ne, xyz):
+    D = C._bdb_D(terms, ne, xyz, torch.device("cuda"))
+    return (D[:, 0] if xyz is None else D).reshape(ne, -1, 16).squeeze(1).cpu().numpy()
+
+
+def _apply(gpu, a, x, dtype):
+    xv = gpu.BaseVector(data=torch.tensor(x, dtype=dtype, device="cuda"))
+    yv = gpu.BaseVector(data=torch.zeros(len(x), dtype=dtype, device="cuda"))
+    a.mat.Mult(xv, yv)
+    return yv.NumPy().astype(np.float64)
+
+
+CASES = [(True, 1, 0.0, False), (True, 2, 0.0, False), (True, 4, 0.0, False), (True, 6, 0.0, False),
+         (True, 3, 0.15, False), (True, 5, 0.1, False), (True, 3, 0.0, True), (True, 4, 0.1, True),
+         (False, 1, 0.2, False), (False, 2, 0.2, False), (False, 3, 0.2, False), (False, 4, 0.2, False),
+         (False, 5, 0.2, False), (False, 6, 0.2, False), (False, 3, 0.2, True)]
+
+
+@pytest.mark.parametrize("hexes,p,jit,pointwise", CASES)
+def test_bdb_apply_parity(gpu, hexes, p, jit, pointwise):
+    m = _mesh(hexes, 3 if hexes else 2, jit)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    terms = _terms(gpu, fes, m.ne, 62 + p, pointwise)
+    a = gpu.BilinearForm(fes, nonassemble=True, precision="fp32")
+    for t in terms:
+        a += t
+    a.Assemble()
+    info = a.mat.Info()
+    affine_elem = hexes and not pointwise and jit == 0.0
+    want = 8 if (affine_elem or (not hexes and not pointwise)) else 7
+    assert info["hex_variant_fp64"] == want and info["hex_variant_fp32"] == want
+    S = O.OracleSpace(m.points, m.elements, p)
+    ref, xyz = _rule(gpu, fes)
+    D = _oracle_D(terms, m.ne, xyz if pointwise else None)
+    x = np.random.default_rng(63).normal(size=fes.ndof)
+    yo = S.apply_bdb(x, D, rule=ref if pointwise else None)
+    sc = np.abs(yo).max()
+    assert np.abs(_apply(gpu, a, x, torch.float64) - yo).max() <= 1e-12 * sc
+    assert np.abs(_apply(gpu, a, x, torch.float32) - yo).max() <= 2e-5 * sc
+
+
+@pytest.mark.parametrize("hexes,p,jit,pointwise", [(True, 4, 0.0, False), (True, 3, 0.15, True), (False, 3, 0.2, False),
+                                                   (False, 2, 0.2, True)])
+def test_bdb_diagonal(gpu, hexes, p, jit, pointwise):
+    """The Jacobi preconditioner of a generic operator inverts the oracle's diagonal."""
+    m = _mesh(hexes, 3, jit)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    terms = _terms(gpu, fes, m.ne, 64, pointwise)
+    a = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True).Assemble()
+    S = O.OracleSpace(m.points, m.elements, p)
+    ref, xyz = _rule(gpu, fes)
+    d = S.diag_bdb(_oracle_D(terms, m.ne, xyz if pointwise else None), rule=ref if pointwise else None)
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    ones = gpu.BaseVector(fes.ndof)
+    ones.data = np.ones(fes.ndof)
+    inv = gpu.BaseVector(fes.ndof)
+    pre.Mult(ones, inv)
+    free = np.asarray(fes.FreeDofs(), dtype=bool)
+    got = inv.NumPy()
+    assert np.all(got[~free] == 0)
+    assert np.abs(got[free] * d[free] - 1.0).max() <= 1e-12
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 4), (False, 3)])
+def test_bdb_variant_paths_agree(gpu, hexes, p, monkeypatch):
+    """On affine hexes the per-element records (variant 8) and the per-point
+    records (GH1_BDB_AFFINE=0, variant 7) give the same operator; a point-wise D
+    that repeats each element's matrix equals the per-element form."""
+    m = _mesh(hexes, 4, 0.0 if hexes else 0.2)
+    fes = gpu.H1(m, order=p)
+    terms = _terms(gpu, fes, m.ne, 65, False)
+    x = np.random.default_rng(66).normal(size=fes.ndof)
+    a1 = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True, precision="fp32").Assemble()
+    y1 = _apply(gpu, a1, x, torch.float64)
+    if hexes:
+        monkeypatch.setenv("GH1_BDB_AFFINE", "0")
+        a2 = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True, precision="fp32").Assemble()
+        assert a2.mat.Info()["hex_variant_fp64"] == 7
+        assert np.abs(_apply(gpu, a2, x, torch.float64) - y1).max() <= 1e-13 * np.abs(y1).max()
+        monkeypatch.delenv("GH1_BDB_AFFINE")
+    # the same D given per point through the C ABI
+    _, xyz = _rule(gpu, fes)
+    D = C._bdb_D(terms, m.ne, None, torch.device("cuda"))[:, 0].reshape(m.ne, 1, 16)
+    Dp = D.expand(m.ne, xyz.shape[1], 16).contiguous()
+    ctx = fes.ctx
+    h = ctypes.c_void_p()
+    ctx.check(ctx.lib.gh1_form_create(fes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(h)))
+    try:
+        ctx.check(ctx.lib.gh1_form_set_bdb(h, ctypes.c_void_p(Dp.data_ptr()), 1, _lib.GH1_MEM_DEVICE))
+        op = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_matfree_create(h, 1, ctypes.byref(op)))
+        mat = C.BilinearFormApplication(ctx, op, fes.ndof, fes)
+        assert mat.Info()["hex_variant_fp64"] == 7
+        xv = gpu.BaseVector(fes.ndof)
+        xv.data = x
+        yv = gpu.BaseVector(fes.ndof)
+        mat.Mult(xv, yv)
+        assert np.abs(yv.NumPy() - y1).max() <= 1e-13 * np.abs(y1).max()
+        del mat
+    finally:
+        ctx.lib.gh1_form_free(h)
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 3), (False, 2)])
+def test_bdb_symmetric_form_solves_like_laplace(gpu, hexes, p):
+    """(1 + 0 x) grad u . grad v + mu u v is the Laplace + mass operator written as
+    a point-wise generic form: the mixed-precision CG on it reaches the same
+    solution as on the standard form (1e-9), and the assembled operator rejects it."""
+    m = _mesh(hexes, 4, 0.1)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    mu = lognormal(m.ne, 0.5, 67)
+    one = 0.0 * gpu.x + 1.0
+    ag = gpu.BilinearForm(one * gpu.grad(u) * gpu.grad(v) * gpu.dx + gpu.CoefficientFunction(mu) * u * v * gpu.dx,
+                          nonassemble=True, precision="mixed").Assemble()
+    assert ag.mat.Info()["hex_variant_fp64"] == 7
+    al = gpu.BilinearForm(gpu.grad(u) * gpu.grad(v) * gpu.dx + gpu.CoefficientFunction(mu) * u * v * gpu.dx,
+                          nonassemble=True, precision="mixed").Assemble()
+    f = gpu.LinearForm(gpu.CoefficientFunction(np.random.default_rng(68).uniform(-1, 1, m.ne)) * v * gpu.dx).Assemble()
+    sols = []
+    for a in (ag, al):
+        pre = a.mat.CreateSmoother(fes.FreeDofs())
+        sols.append(gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-11, maxsteps=5000, printrates=False,
+                                   mode="mixed"))
+    assert gpu.Norm(sols[0] - sols[1]) <= 1e-9 * gpu.Norm(sols[1])
+    with pytest.raises(NotImplementedError):
+        gpu.BilinearForm(one * gpu.grad(u) * gpu.grad(v) * gpu.dx).Assemble()

@@ -406,3 +406,69 @@ def test_affine_source_identity(hexes, p):
     fi = np.zeros(S.ndof)
     fi[:m.nv] = 2 * m.points[:, 0] - m.points[:, 1] + 3
     assert abs(ones @ (M @ fi) - 3.5) < 1e-13
+
+
+def _bdb_matrix(ne, seed, sym=False):
+    """Random D per element (4x4, rows test, columns trial) with an SPD 3x3
+    diffusion block, a positive reaction and convection terms."""
+    rng = np.random.default_rng(seed)
+    D = np.zeros((ne, 4, 4))
+    L = rng.normal(size=(ne, 3, 3)) * 0.3
+    D[:, 1:, 1:] = np.einsum("eij,ekj->eik", L, L) + np.eye(3)
+    D[:, 0, 0] = rng.uniform(0.5, 2.0, ne)
+    D[:, 0, 1:] = rng.normal(size=(ne, 3))
+    D[:, 1:, 0] = D[:, 0, 1:] if sym else rng.normal(size=(ne, 3))
+    return D
+
+
+@pytest.mark.parametrize("hexes,p", [(True, 1), (True, 3), (False, 2), (False, 4)])
+def test_oracle_bdb(hexes, p):
+    """The generic B^T D B apply: D = diag(mu, K) reproduces the kappa / tensor +
+    mass operator; transposing D transposes the operator; a point-wise D that
+    repeats the element's matrix gives the same result; convection b = e_x on the
+    interpolant of x is the load vector of f = 1 (b . grad x = 1, x is in the
+    space); the diagonal matches the operator's."""
+    m = JitterInterior(MakeStructured3DMesh(hexes=hexes, nx=2), 0.05, 3) if not hexes else \
+        MakeStructured3DMesh(hexes=True, nx=2)
+    S = O.OracleSpace(m.points, m.elements, p)
+    ne = S.ne
+    rng = np.random.default_rng(11)
+    x = rng.normal(size=S.ndof)
+    Ka = _spd_tensors(ne, 5)
+    mu = lognormal(ne, 0.5, 7)
+    D = np.zeros((ne, 4, 4))
+    D[:, 0, 0] = mu
+    D[:, 1, 1], D[:, 2, 2], D[:, 3, 3] = Ka[:, 0], Ka[:, 1], Ka[:, 2]
+    D[:, 1, 2] = D[:, 2, 1] = Ka[:, 3]
+    D[:, 1, 3] = D[:, 3, 1] = Ka[:, 4]
+    D[:, 2, 3] = D[:, 3, 2] = Ka[:, 5]
+    y_ref = S.apply_mf(x, K6=Ka, mu=mu)
+    y = S.apply_bdb(x, D)
+    assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
+    # transpose
+    Dn = _bdb_matrix(ne, 12)
+    z = rng.normal(size=S.ndof)
+    a = z @ S.apply_bdb(x, Dn)
+    b = x @ S.apply_bdb(z, np.transpose(Dn, (0, 2, 1)))
+    assert abs(a - b) <= 1e-12 * max(abs(a), 1.0)
+    # point-wise D at the oracle's own rule of order 2p
+    pts, w = O.rule(4 if not hexes else 8, 2 * p)
+    rule = np.concatenate([pts, w[:, None]], axis=1)
+    Dp = np.repeat(Dn[:, None], len(w), axis=1)
+    y1, y2 = S.apply_bdb(x, Dn), S.apply_bdb(x, Dp, rule=rule)
+    assert np.abs(y1 - y2).max() <= 1e-13 * np.abs(y1).max()
+    # convection known answer
+    Dc = np.zeros((ne, 4, 4))
+    Dc[:, 0, 1] = 1.0
+    u = np.zeros(S.ndof)
+    u[:len(m.points)] = m.points[:, 0]
+    lhs = S.apply_bdb(u, Dc)
+    rhs = S.rhs(np.ones(ne))
+    assert np.abs(lhs - rhs).max() <= 1e-13 * np.abs(rhs).max()
+    # diagonal
+    d = S.diag_bdb(Dn)
+    idx = rng.choice(S.ndof, 6, replace=False)
+    for i in idx:
+        e = np.zeros(S.ndof)
+        e[i] = 1.0
+        assert abs(S.apply_bdb(e, Dn)[i] - d[i]) <= 1e-13 * max(1.0, abs(d[i]))
