@@ -48,8 +48,8 @@ def parse():
     ap.add_argument("--no-cg", action="store_true", help="skip the CG time-to-solution legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the tet CSR and adjoint legs of the default line")
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep", "link", "vector"],
+                    help="skip the tet CSR, adjoint and generic B^T D B legs of the default line")
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "sweep", "link", "vector", "bdb"],
                     help="c3 (default, the headline line); c1/c2/c4/c5 print their own measurement records")
     ap.add_argument("--c5-problems", type=int, default=256)
     ap.add_argument("--c5-pack", default="sorted", choices=["sorted", "seed"],
@@ -468,6 +468,49 @@ def leg_adjoint_c4():
             "max_abs_gradient": float(g.abs().max())}
 
 
+def leg_bdb(nx=64, order=4):
+    """The generic B^T D B apply (a convection-diffusion-reaction form: kappa
+    grad.grad + (b . grad u) v + r u v, not symmetric) on the headline mesh
+    (64^3 hex p=4, kappa lognormal(0,0.5) seed 4): D per element, one record per
+    affine element (variant 8), FP32 and FP64; r = 1 + x evaluated at every rule
+    point (variant 7, 16 coefficients per point streamed), FP32; and the tet mesh
+    of the CSR leg (32^3 Kuhn tets, jitter 0.2h) at p = 4, D per element, FP32."""
+    import torch
+    import ngsolve_gb300 as ng
+    out = {}
+
+    def run(mesh, kappa, r, label):
+        fes = ng.H1(mesh, order=order, dirichlet=".*")
+        u, v = fes.TnT()
+        b = ng.CoefficientFunction((1.0, 0.5, 0.25))
+        a = ng.BilinearForm(ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx +
+                            ng.InnerProduct(b, ng.grad(u)) * v * ng.dx + r * u * v * ng.dx,
+                            nonassemble=True, precision="fp32")
+        t_setup, _ = _timed(lambda: a.Assemble())
+        N = fes.ndof
+        res = {"ndof": N, "ne": mesh.ne, "setup_s": t_setup, "variant": a.mat.Info()["hex_variant_fp32"]}
+        for dt, name in ((torch.float32, "fp32"), (torch.float64, "fp64")):
+            x = ng.BaseVector(data=torch.rand(N, dtype=dt, device="cuda"))
+            y = ng.BaseVector(data=torch.zeros(N, dtype=dt, device="cuda"))
+            for _ in range(3):
+                a.mat.Mult(x, y)
+            t, _ = _timed(lambda: a.mat.Mult(x, y), reps=20)
+            res[name] = {"ms": t * 1e3, "gdofs": N / t / 1e9}
+        out[label] = res
+        del a
+        torch.cuda.empty_cache()
+
+    mesh = ng.MakeStructured3DMesh(hexes=True, nx=nx)
+    kappa = np.exp(np.random.default_rng(4).normal(0, 0.5, mesh.ne))
+    run(mesh, kappa, ng.CoefficientFunction(1.0), "hex_%d^3_p%d_per_element" % (nx, order))
+    run(mesh, kappa, 1.0 + ng.x, "hex_%d^3_p%d_per_point" % (nx, order))
+    tmesh = ng.JitterInterior(ng.MakeStructured3DMesh(hexes=False, nx=32), 0.2 / 32, 2)
+    tk = np.exp(np.random.default_rng(3).normal(0, 1, tmesh.ne))
+    run(tmesh, tk, ng.CoefficientFunction(1.0), "tet_32^3_p%d_per_element" % order)
+    out["form"] = "kappa grad(u).grad(v) + ((1, 0.5, 0.25) . grad u) v + r u v, D 4x4 per element or per point"
+    return out
+
+
 def workload_link(args):
     """Host link bandwidth for the end-to-end leg: pinned-host <-> device copies of
     one 64^3 p=4 FP32 vector (67.9 MB) through the copy engines, H2D and D2H
@@ -743,7 +786,8 @@ def main():
     torch.cuda.set_device(dev)
     if args.workload != "c3":
         fn = {"c1": workload_c1, "c2": workload_c2, "c4": workload_c4, "c5": workload_c5,
-              "sweep": workload_sweep, "link": workload_link, "vector": workload_vector}[args.workload]
+              "sweep": workload_sweep, "link": workload_link, "vector": workload_vector,
+              "bdb": lambda a: leg_bdb(a.nx, a.order)}[args.workload]
         rec = fn(args)
         if rank == 0:
             print(json.dumps({"record": args.workload, **rec}), flush=True)
@@ -969,7 +1013,7 @@ def main():
     # the other configurations' device legs, at full size, in the same run
     others = None
     if not args.no_extra and args.nx == NX and args.order == ORDER:
-        others = {"tet_csr": leg_spmv_c2(), "adjoint": leg_adjoint_c4()}
+        others = {"tet_csr": leg_spmv_c2(), "adjoint": leg_adjoint_c4(), "generic_bdb": leg_bdb()}
 
     peak, peak_kind = load_peaks()
     B32, F = model_bytes_flops(ne, N, args.order, 4, 4)
