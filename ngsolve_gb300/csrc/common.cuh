@@ -28,7 +28,7 @@ struct Error : std::runtime_error {
 #define GH1_LAUNCH_CHECK() GH1_CUDA(cudaGetLastError())
 
 constexpr int MAX_HEX_ORDER = 8;   // n = p+1 <= 9 per direction
-constexpr int MAX_TET_ORDER = 6;
+constexpr int MAX_TET_ORDER = 8;
 constexpr int N_TET_CLASSES = 24;  // permutations of 4 vertex ranks
 constexpr int TET_NQ_MAX = 24;     // symmetric rules of degree <= 6 (order p <= 4)
 

@@ -26,7 +26,9 @@ namespace gh1 {
 constexpr int TET_TT = 128;  // threads per block
 constexpr int TET_TE = 32;   // elements per tile
 constexpr int TET_RB = 8;    // row-tile depth of the first product (rows per thread per pass)
-constexpr int TET_TI = 6;    // maximum row-tile depth of the second product (nloc <= 96)
+constexpr int TET_TI = 12;   // maximum row-tile depth of the second product (nloc <= 192, p <= 8)
+// row-tile depth a chunked kernel is compiled for: 6 up to p = 6, else 12
+inline int tet_ti_of(int nlocp) { return nlocp / 16 <= 6 ? 6 : 12; }
 
 __host__ __device__ inline size_t tet_r16(size_t b) { return (b + 15) / 16 * 16; }
 
@@ -181,22 +183,22 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
     }
     __syncthreads();
     // Y[i][e] = sum_r D[i][r] V[r][e], rows i = rg + 16 t; scatter
-    T b[TET_TI][4];
+    T b[ni][4];
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    for (int u = 0; u < ni; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
 #pragma unroll 16
     for (int r = 0; r < Rp; r++) {
       T pv[4];
       ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
 #pragma unroll
-      for (int u = 0; u < TET_TI; u++)
+      for (int u = 0; u < ni; u++)
         if (u < ni) {
           const T dv = sD[(size_t)(rg + 16 * u) * Rs + r];
           b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
         }
     }
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) {
+    for (int u = 0; u < ni; u++) {
       const int i = rg + 16 * u;
       if (u < ni && i < nloc) {
 #pragma unroll
@@ -218,7 +220,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
 //   Dm: [class][mass chunk][nlocp][16];  Wg, Wm: rule weights, zero-padded
 constexpr int TET_QC = 16;
 
-template <class T, bool MASS>
+template <class T, bool MASS, int TI>
 __global__ void __launch_bounds__(TET_TT)
 tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncg,
                       int ncm, const int* __restrict__ eldofs, const T* __restrict__ Ge, const T* __restrict__ Me,
@@ -258,9 +260,9 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
       if (e < cnt) v = c < 6 ? Ge[(size_t)perm[start + e] * 6 + c] : (MASS ? Me[perm[start + e]] : T(0));
       sG[k] = v;
     }
-    T b[TET_TI][4];
+    T b[TI][4];
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    for (int u = 0; u < TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
     const int nchunk = ncg + (MASS ? ncm : 0);
     for (int cc = 0; cc < nchunk; cc++) {
       const bool grad = cc < ncg;
@@ -320,7 +322,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
         T pv[4];
         ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
 #pragma unroll
-        for (int u = 0; u < TET_TI; u++)
+        for (int u = 0; u < TI; u++)
           if (u < ni) {
             const T dv = sD[(rg + 16 * u) * RS + r];
             b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
@@ -328,7 +330,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
       }
     }
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) {
+    for (int u = 0; u < TI; u++) {
       const int i = rg + 16 * u;
       if (u < ni && i < nloc) {
 #pragma unroll
@@ -439,9 +441,9 @@ __global__ void tet_chunk_table_kernel(int ncls, int nloc, int nlocp, int nq, in
   }
 }
 
-template <class T, bool MASS>
-static int tet_chunk_occupancy(int nlocp) {
-  auto kern = tet_tile_chunk_kernel<T, MASS>;
+template <class T, bool MASS, int TI>
+static int tet_chunk_occupancy_ti(int nlocp) {
+  auto kern = tet_tile_chunk_kernel<T, MASS, TI>;
   const size_t smem = tet_chunk_smem<T>(nlocp);
   int dev = 0, optin = 0;
   GH1_CUDA(cudaGetDevice(&dev));
@@ -454,6 +456,11 @@ static int tet_chunk_occupancy(int nlocp) {
   int v = 0;
   GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TET_TT, smem));
   return v;
+}
+
+template <class T, bool MASS>
+static int tet_chunk_occupancy(int nlocp) {
+  return tet_ti_of(nlocp) == 6 ? tet_chunk_occupancy_ti<T, MASS, 6>(nlocp) : tet_chunk_occupancy_ti<T, MASS, 12>(nlocp);
 }
 
 // chunked tables and weights for all precisions the operator carries
@@ -635,14 +642,17 @@ static void tet_chunk_launch(gh1_op* op, int per_sm, const T* Dg, const T* Dm, c
   const int nlocp = (sp->nloc + 15) / 16 * 16;
   const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
   const size_t smem = tet_chunk_smem<T>(nlocp);
-  if (op->has_mass)
-    tet_tile_chunk_kernel<T, true><<<grid, TET_TT, smem, sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,
-        sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip);
-  else
-    tet_tile_chunk_kernel<T, false><<<grid, TET_TT, smem, sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,
-        sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip);
+#define GH1_CHUNK_LAUNCH(MASS, TI)                                                                       \
+  tet_tile_chunk_kernel<T, MASS, TI><<<grid, TET_TT, smem, sp->ctx->stream>>>(                            \
+      op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,      \
+      sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip)
+  const bool ti6 = tet_ti_of(nlocp) == 6;
+  if (op->has_mass) {
+    if (ti6) GH1_CHUNK_LAUNCH(true, 6); else GH1_CHUNK_LAUNCH(true, 12);
+  } else {
+    if (ti6) GH1_CHUNK_LAUNCH(false, 6); else GH1_CHUNK_LAUNCH(false, 12);
+  }
+#undef GH1_CHUNK_LAUNCH
   check_kernel(sp->ctx, "tet_tile_chunk_kernel");
 }
 
@@ -690,7 +700,7 @@ __host__ __device__ inline size_t tet_bdb_smem(int nlocp) {
          ((size_t)nlocp * TET_TE + 4 * TET_QC * TET_TE + TET_TE * 17) * sizeof(T) + (size_t)nlocp * TET_TE * sizeof(int);
 }
 
-template <class T, bool PP>
+template <class T, bool PP, int TI>
 __global__ void __launch_bounds__(TET_TT)
 tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncb,
                int nq, const int* __restrict__ eldofs, const T* __restrict__ Mh, const T* __restrict__ Tb,
@@ -728,9 +738,9 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
         const int e = k / 16, c = k % 16;
         sM[e * 17 + c] = e < cnt ? Mh[(size_t)perm[start + e] * 16 + c] : T(0);
       }
-    T b[TET_TI][4];
+    T b[TI][4];
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
+    for (int u = 0; u < TI; u++) b[u][0] = b[u][1] = b[u][2] = b[u][3] = 0;
     for (int cc = 0; cc < ncb; cc++) {
       const T* src = Tb + ((size_t)cls * ncb + cc) * nlocp * RC;
       __syncthreads();  // X, records, DOFs ready; the previous slice is consumed
@@ -783,7 +793,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
         T pv[4];
         ld4(sP + (size_t)r * TET_TE + 4 * cg, pv);
 #pragma unroll
-        for (int u = 0; u < TET_TI; u++)
+        for (int u = 0; u < TI; u++)
           if (u < ni) {
             const T dv = sD[(rg + 16 * u) * RS + r];
             b[u][0] += dv * pv[0]; b[u][1] += dv * pv[1]; b[u][2] += dv * pv[2]; b[u][3] += dv * pv[3];
@@ -791,7 +801,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
       }
     }
 #pragma unroll
-    for (int u = 0; u < TET_TI; u++) {
+    for (int u = 0; u < TI; u++) {
       const int i = rg + 16 * u;
       if (u < ni && i < nloc) {
 #pragma unroll
@@ -819,9 +829,9 @@ __global__ void tet_bdb_table_kernel(int ncls, int nloc, int nlocp, int nq, int 
   }
 }
 
-template <class T, bool PP>
-static int tet_bdb_occupancy(int nlocp) {
-  auto kern = tet_bdb_kernel<T, PP>;
+template <class T, bool PP, int TI>
+static int tet_bdb_occupancy_ti(int nlocp) {
+  auto kern = tet_bdb_kernel<T, PP, TI>;
   const size_t smem = tet_bdb_smem<T>(nlocp);
   int dev = 0, optin = 0;
   GH1_CUDA(cudaGetDevice(&dev));
@@ -835,6 +845,11 @@ static int tet_bdb_occupancy(int nlocp) {
   GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TET_TT, smem));
   GH1_CHECK(v >= 1, GH1_ERR_UNSUPPORTED, "tet B^T D B apply does not fit on an SM");
   return v;
+}
+
+template <class T, bool PP>
+static int tet_bdb_occupancy(int nlocp) {
+  return tet_ti_of(nlocp) == 6 ? tet_bdb_occupancy_ti<T, PP, 6>(nlocp) : tet_bdb_occupancy_ti<T, PP, 12>(nlocp);
 }
 
 void tet_bdb_setup(gh1_op* op) {
@@ -879,14 +894,17 @@ static void tet_bdb_launch(gh1_op* op, int per_sm, const T* Mh, const T* Tb, con
   const int nlocp = (sp->nloc + 15) / 16 * 16;
   const int grid = std::max(1, std::min(op->tet_ntiles, sp->ctx->nsm * per_sm));
   const size_t smem = tet_bdb_smem<T>(nlocp);
-  if (op->bdb == 1)
-    tet_bdb_kernel<T, true><<<grid, TET_TT, smem, sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,
-        sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip);
-  else
-    tet_bdb_kernel<T, false><<<grid, TET_TT, smem, sp->ctx->stream>>>(
-        op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,
-        sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip);
+#define GH1_BDB_LAUNCH(PP, TI)                                                                            \
+  tet_bdb_kernel<T, PP, TI><<<grid, TET_TT, smem, sp->ctx->stream>>>(                                     \
+      op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,  \
+      sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip)
+  const bool ti6 = tet_ti_of(nlocp) == 6;
+  if (op->bdb == 1) {
+    if (ti6) GH1_BDB_LAUNCH(true, 6); else GH1_BDB_LAUNCH(true, 12);
+  } else {
+    if (ti6) GH1_BDB_LAUNCH(false, 6); else GH1_BDB_LAUNCH(false, 12);
+  }
+#undef GH1_BDB_LAUNCH
   check_kernel(sp->ctx, "tet_bdb_kernel");
 }
 

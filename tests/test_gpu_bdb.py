@@ -69,7 +69,7 @@ def _apply(gpu, a, x, dtype):
 CASES = [(True, 1, 0.0, False), (True, 2, 0.0, False), (True, 4, 0.0, False), (True, 6, 0.0, False),
          (True, 3, 0.15, False), (True, 5, 0.1, False), (True, 3, 0.0, True), (True, 4, 0.1, True),
          (False, 1, 0.2, False), (False, 2, 0.2, False), (False, 3, 0.2, False), (False, 4, 0.2, False),
-         (False, 5, 0.2, False), (False, 6, 0.2, False), (False, 3, 0.2, True)]
+         (False, 5, 0.2, False), (False, 6, 0.2, False), (False, 7, 0.2, False), (False, 3, 0.2, True)]
 
 
 @pytest.mark.parametrize("hexes,p,jit,pointwise", CASES)

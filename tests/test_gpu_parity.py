@@ -19,7 +19,7 @@ def _mesh(kind, n, jitter, seed=11, permute=False):
     return m
 
 
-@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7, 8])
 def test_shapes_tet(gpu, p):
     rng = np.random.default_rng(p)
     pts = rng.dirichlet(np.ones(4), size=7)[:, :3]
@@ -53,7 +53,8 @@ def test_p1_mass_golden(gpu, cube_vol, golden):
 
 @pytest.mark.parametrize("kind,p,jit,perm", [("hex", 1, 0.1, False), ("hex", 2, 0.1, False), ("hex", 3, 0.15, False),
                                              ("hex", 4, 0.1, False), ("tet", 1, 0.2, True), ("tet", 2, 0.2, False),
-                                             ("tet", 3, 0.2, True), ("tet", 4, 0.2, True), ("tet", 5, 0.0, True)])
+                                             ("tet", 3, 0.2, True), ("tet", 4, 0.2, True), ("tet", 5, 0.0, True),
+                                             ("tet", 7, 0.2, True), ("tet", 8, 0.0, False)])
 def test_assemble_parity(gpu, kind, p, jit, perm):
     """Pattern bit-exact and entries within 1e-12 (row-scaled) of the oracle's Assemble."""
     m = _mesh(kind, 3, jit, permute=perm)

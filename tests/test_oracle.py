@@ -35,7 +35,7 @@ def test_dof_and_nnz_counts(golden):
     assert S.ndof == c["kuhn32_p2"]["ndof"] and len(S.graph()[1]) == c["kuhn32_p2"]["nnz"]
 
 
-@pytest.mark.parametrize("et,p", [(4, p) for p in range(1, 7)] + [(8, p) for p in range(1, 6)])
+@pytest.mark.parametrize("et,p", [(4, p) for p in range(1, 9)] + [(8, p) for p in range(1, 6)])
 def test_element_ndof(et, p):
     """GetFE(el).ndof == len(GetDofNrs(el)) (tests/pytest/test_fespaces.py:55-100)."""
     m = MakeStructured3DMesh(hexes=(et == 8), nx=2)

