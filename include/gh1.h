@@ -191,8 +191,39 @@ int gh1_op_block_create(gh1_op* op, int nblocks, gh1_op** block);
  * (linalg/jacobi.cpp:40-110): invdiag = 1/A_ii on free DOFs, 0 elsewhere.
  * freedofs: NULL = the space's free DOFs.                                */
 int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** pre);
+/* y = s*C*x (accumulate=0) or y += s*C*x for any preconditioner below. */
 int gh1_pre_apply(gh1_pre* pre, double s, const void* x, void* y, int precision, int accumulate);
 int gh1_pre_free(gh1_pre* pre);
+
+/* Additive Schwarz: block Jacobi plus an exact low-order solve, the reference's
+ * tutorial preconditioner jac + loemb @ loinv @ loemb.T
+ * (docs/i-tutorials/unit-5.5-cuda/poisson_cuda.ipynb cells 9-13).
+ * Smoothing blocks of H1HighOrderFESpace::CreateSmoothingBlocks
+ * (comp/h1hofespace.cpp:1477-1600), only free DOFs, empty blocks dropped:
+ * blocktype 4 = VE + F + I (each vertex with the DOFs of the edges at it, each
+ * face, each element's interior), 3 = V + E + F + I.  First call with offsets /
+ * dofs NULL for the sizes; then offsets[nblocks+1] and dofs[nentries] (host). */
+int gh1_space_smoothing_blocks(gh1_space* space, int blocktype, int64_t* nblocks, int64_t* nentries, int64_t* offsets,
+                               int32_t* dofs);
+/* BlockJacobiPrecond (linalg/blockjacobi.cpp; device apply DevBlockJacobiMatrix,
+ * ngscuda/dev_blockjacobi.cpp:49-137): the dense diagonal blocks of an assembled
+ * SPD matrix (gh1_assemble_csr / gh1_csr_import), inverted on the GPU;
+ * y = s sum_b E_b A_b^{-1} E_b^T x.  Blocks: offsets[nblocks+1] into dofs,
+ * host or device per mem; up to 4096 DOFs a block. */
+int gh1_blockjacobi_create(gh1_op* csr, int64_t nblocks, const int64_t* offsets, const int32_t* dofs, int mem,
+                           gh1_pre** pre);
+/* Exact low-order solve P A_c^{-1} P^T: csr is the low-order matrix (the p = 1
+ * form, a.loform; in the hierarchical basis its DOFs are the first DOFs of the
+ * high-order space, embed = NULL), embed[i] the fine DOF of coarse DOF i,
+ * freedofs the coarse free DOFs (NULL: all); the matrix on the free coarse DOFs
+ * is inverted on the GPU (the reference factorizes it with its sparse Cholesky,
+ * ngscuda/dev_sparsecholesky.cpp); up to 8192 free coarse DOFs. */
+int gh1_coarse_create(gh1_op* csr, int64_t nfine, const int32_t* embed, const uint8_t* freedofs, int mem,
+                      gh1_pre** pre);
+/* y = s (A + B) x (SumMatrix); a and b are borrowed and must outlive the sum.
+ * gh1_cg takes any of these preconditioners; other than Jacobi they run as
+ * their own kernels inside the device-side CG loop. */
+int gh1_pre_sum(gh1_pre* a, gh1_pre* b, gh1_pre** sum);
 
 /* ---- projector ----------------------------------------------------------------
  * Projector(mask, range) (linalg/diagonalmatrix.cpp:13-110; the reference's GPU

@@ -74,6 +74,10 @@ SIGNATURES = {
     "gh1_jacobi_create": [_P, _P, _I, _PP],
     "gh1_pre_apply": [_P, _D, _P, _P, _I, _I],
     "gh1_pre_free": [_P],
+    "gh1_space_smoothing_blocks": [_P, _I, _P, _P, _P, _P],
+    "gh1_blockjacobi_create": [_P, _L, _P, _P, _I, _PP],
+    "gh1_coarse_create": [_P, _L, _P, _P, _I, _PP],
+    "gh1_pre_sum": [_P, _P, _PP],
     "gh1_rhs_elementwise": [_P, _P, _I, _P],
     "gh1_cg": [_P, _P, _P, _P, ctypes.POINTER(CGOpts), ctypes.POINTER(CGResult)],
     "gh1_elem_grad_dot": [_P, _P, _P, _P],

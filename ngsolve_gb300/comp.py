@@ -537,6 +537,37 @@ class H1:
         self.ctx.check(self.ctx.lib.gh1_space_info(h, _np_ptr(info)))
         self.ndof, self.nloc, self.nedges, self.nfaces, self.nfree, self.ne = (int(v) for v in info)
         self._dofs = None
+        self._dirichlet = dirichlet
+        self._lospace = None
+
+    @property
+    def lospace(self):
+        """The low-order (p = 1) space of the hierarchical basis on the same mesh
+        and Dirichlet boundary; its DOFs are the first (vertex) DOFs of this space."""
+        if self.order == 1:
+            return self
+        if self._lospace is None:
+            self._lospace = H1(self.mesh, order=1, dirichlet=self._dirichlet)
+        return self._lospace
+
+    @property
+    def loembedding(self):
+        """The embedding of lospace into this space (identity on the vertex DOFs)."""
+        return _Embedding(self)
+
+    def CreateSmoothingBlocks(self, blocktype=4, **flags):
+        """CreateSmoothingBlocks (comp/h1hofespace.cpp:1477-1600): blocktype 4 =
+        VE + F + I, 3 = V + E + F + I; free DOFs only."""
+        if isinstance(blocktype, str):
+            blocktype = {"vertexedge": 4, "vertex": 3}.get(blocktype, blocktype)
+        nb, ntot = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.gh1_space_smoothing_blocks(self.h, int(blocktype), ctypes.byref(nb),
+                                                               ctypes.byref(ntot), None, None))
+        off = np.zeros(nb.value + 1, dtype=np.int64)
+        dofs = np.zeros(max(ntot.value, 1), dtype=np.int32)
+        self.ctx.check(self.ctx.lib.gh1_space_smoothing_blocks(self.h, int(blocktype), ctypes.byref(nb),
+                                                               ctypes.byref(ntot), _np_ptr(off), _np_ptr(dofs)))
+        return SmoothingBlocks(off, dofs[:ntot.value])
 
     def __del__(self):
         try:
@@ -875,6 +906,12 @@ class BaseMatrix:
     def CreateSmoother(self, freedofs=None):
         return JacobiPrecond(self, freedofs)
 
+    def CreateBlockSmoother(self, blocks, **kwargs):
+        """BlockJacobiPrecond of an assembled matrix over SmoothingBlocks."""
+        if not isinstance(self, SparseMatrix):
+            raise NotImplementedError("the block smoother needs the assembled matrix (BilinearForm without nonassemble)")
+        return BlockJacobiPrecond(self, blocks)
+
     def Inverse(self, freedofs=None, inverse=None, tol=1e-12, maxsteps=100000):
         """A^{-1} on the free DOFs, for a.mat.Inverse(fes.FreeDofs()).  The
         reference factorizes (sparsecholesky, umfpack, pardiso ...); this path has
@@ -884,6 +921,10 @@ class BaseMatrix:
         the reference.  freedofs=None: the space's free DOFs."""
         if inverse not in _INVERSE_NAMES:
             raise ValueError("unknown inverse %r" % (inverse,))
+        if inverse == "sparsecholesky" and isinstance(self, SparseMatrix):
+            fd = np.ones(self.height, dtype=bool) if freedofs is None else np.asarray(freedofs, dtype=bool)
+            if int(fd.sum()) <= ExactInverse.MAX_FREE:
+                return ExactInverse(self, fd)
         return InverseOperator(self, freedofs, tol, maxsteps)
 
     def __del__(self):
@@ -1002,7 +1043,171 @@ class BlockMatrix(BaseMatrix):
         self.inner = inner
 
 
-class JacobiPrecond(BaseMatrix):
+class _PreBase(BaseMatrix):
+    """A gh1 preconditioner handle used as an operator (Mult), summed with `+`
+    (the reference's SumMatrix) and passed to CGSolver."""
+
+    def _apply(self, s, x, y, acc):
+        x, y = _as_vec(x), _as_vec(y)
+        if x.t.dtype != y.t.dtype or x.t.numel() != self.height or y.t.numel() != self.height:
+            raise ValueError("vectors must match the preconditioner in size and precision")
+        prec = _lib.GH1_F64 if x.t.dtype == torch.float64 else _lib.GH1_F32
+        self.ctx.sync_stream()
+        self.ctx.check(self.ctx.lib.gh1_pre_apply(self.h, float(s), _ptr(x.t), _ptr(y.t), prec, int(acc)))
+
+    def __add__(self, other):
+        if isinstance(other, _EmbComposed):
+            other = other.solver()
+        if not isinstance(other, _PreBase):
+            return NotImplemented
+        return SumPrecond(self, other)
+
+    __radd__ = __add__
+
+    def Info(self):  # the handle is a preconditioner, not an operator
+        return {"kind": type(self).__name__, "nrows": self.height}
+
+    def Inverse(self, *args, **kwargs):
+        raise NotImplementedError("Inverse of a preconditioner")
+
+    def __del__(self):
+        try:
+            self.ctx.lib.gh1_pre_free(self.h)
+        except Exception:
+            pass
+
+
+class SmoothingBlocks:
+    """The Table of DOF blocks of CreateSmoothingBlocks: len(), blocks[i] (a
+    list of DOFs), iteration; offsets / dofs as arrays."""
+
+    def __init__(self, offsets, dofs):
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+
+    def __len__(self):
+        return len(self.offsets) - 1
+
+    def __getitem__(self, i):
+        return self.dofs[self.offsets[i]:self.offsets[i + 1]].tolist()
+
+    def __iter__(self):
+        for i in range(len(self)):
+            yield self[i]
+
+
+class BlockJacobiPrecond(_PreBase):
+    """BlockJacobiPrecond (linalg/blockjacobi.cpp; device DevBlockJacobiMatrix,
+    ngscuda/dev_blockjacobi.cpp:49-137): sum_b E_b A_b^{-1} E_b^T."""
+
+    def __init__(self, mat, blocks):
+        if not isinstance(blocks, SmoothingBlocks):
+            rows = [np.asarray(b, dtype=np.int32) for b in blocks]
+            off = np.concatenate([[0], np.cumsum([len(b) for b in rows])]).astype(np.int64)
+            blocks = SmoothingBlocks(off, np.concatenate(rows) if rows else np.zeros(0, dtype=np.int32))
+        h = ctypes.c_void_p()
+        mat.ctx.sync_stream()
+        mat.ctx.check(mat.ctx.lib.gh1_blockjacobi_create(mat.h, len(blocks), _np_ptr(blocks.offsets),
+                                                          _np_ptr(blocks.dofs), _lib.GH1_MEM_HOST, ctypes.byref(h)))
+        self.ctx, self.h, self.height, self.width, self.fes = mat.ctx, h, mat.height, mat.height, mat.fes
+        self.blocks, self.mat = blocks, mat
+
+    def GetOperatorInfo(self):
+        return "BlockJacobiPrecond (%d blocks), h = %d, w = %d\n" % (len(self.blocks), self.height, self.width)
+
+
+class ExactInverse(_PreBase):
+    """A^{-1} on the free DOFs of an assembled matrix, inverted on the GPU: the
+    role of Inverse(inverse="sparsecholesky") for matrices with up to MAX_FREE
+    free DOFs (larger ones get the Jacobi-PCG InverseOperator).  With `nfine`,
+    the inverse of a low-order matrix embedded into the first DOFs of a larger
+    space (loemb @ loinv @ loemb.T)."""
+    MAX_FREE = 8192
+
+    def __init__(self, mat, freedofs, nfine=None):
+        fd = np.ascontiguousarray(np.asarray(freedofs, dtype=bool).astype(np.uint8))
+        if fd.shape != (mat.height,):
+            raise ValueError("freedofs size does not match the matrix")
+        n = mat.height if nfine is None else int(nfine)
+        h = ctypes.c_void_p()
+        mat.ctx.sync_stream()
+        mat.ctx.check(mat.ctx.lib.gh1_coarse_create(mat.h, n, None, _np_ptr(fd), _lib.GH1_MEM_HOST, ctypes.byref(h)))
+        self.ctx, self.h, self.height, self.width, self.fes = mat.ctx, h, n, n, mat.fes
+        self.mat, self._fd = mat, fd
+
+    def GetOperatorInfo(self):
+        return "ExactInverse (dense, %d free DOFs), h = %d, w = %d\n" % (int(self._fd.sum()), self.height, self.width)
+
+
+class SumPrecond(_PreBase):
+    """a + b of two preconditioners (SumMatrix); keeps both alive."""
+
+    def __init__(self, a, b):
+        if a.height != b.height:
+            raise ValueError("the two preconditioners differ in size")
+        h = ctypes.c_void_p()
+        a.ctx.check(a.ctx.lib.gh1_pre_sum(a.h, b.h, ctypes.byref(h)))
+        self.ctx, self.h, self.height, self.width, self.fes = a.ctx, h, a.height, a.height, a.fes
+        self.a, self.b = a, b
+
+    def GetOperatorInfo(self):
+        return "SumMatrix, h = %d, w = %d\n  %s  %s" % (self.height, self.width, self.a.GetOperatorInfo(),
+                                                         self.b.GetOperatorInfo())
+
+
+class _Embedding:
+    """fes.loembedding: the low-order space's DOFs are the first DOFs of the
+    high-order space (identity there); E @ inv @ E.T is the embedded solve."""
+
+    def __init__(self, fes, transposed=False):
+        self.fes, self.transposed = fes, transposed
+
+    @property
+    def T(self):
+        return _Embedding(self.fes, not self.transposed)
+
+    def __matmul__(self, other):
+        if self.transposed:
+            raise NotImplementedError("loembedding.T only on the right of loembedding @ loinv")
+        return _EmbComposed(self.fes, other)
+
+
+class _EmbComposed:
+    """loembedding @ loinv (@ loembedding.T): becomes an ExactInverse of the
+    low-order matrix acting on the vertex DOFs of the high-order space."""
+
+    def __init__(self, fes, inner, closed=False):
+        self.fes, self.inner, self.closed = fes, inner, closed
+        self._solver = None
+
+    def __matmul__(self, other):
+        if not (isinstance(other, _Embedding) and other.transposed and not self.closed):
+            raise NotImplementedError("loembedding @ loinv @ loembedding.T")
+        return _EmbComposed(self.fes, self.inner, closed=True)
+
+    def solver(self):
+        if not self.closed:
+            raise NotImplementedError("loembedding @ loinv needs @ loembedding.T")
+        if self._solver is None:
+            inv = self.inner
+            if not isinstance(inv, ExactInverse):
+                raise NotImplementedError("loinv = a.loform.mat.Inverse(inverse='sparsecholesky', freedofs=...)")
+            self._solver = ExactInverse(inv.mat, inv._fd.astype(bool), nfine=self.fes.ndof)
+        return self._solver
+
+    def __add__(self, other):
+        return self.solver() + other
+
+    __radd__ = __add__
+
+    def Mult(self, x, y):
+        self.solver().Mult(x, y)
+
+    def GetOperatorInfo(self):
+        return self.solver().GetOperatorInfo()
+
+
+class JacobiPrecond(_PreBase):
     """JacobiPrecond (linalg/jacobi.cpp:40-110): invdiag on free DOFs, 0 elsewhere."""
 
     def __init__(self, mat, freedofs=None):
@@ -1225,6 +1430,19 @@ class BilinearForm:
         if self.mat is None:
             self.Assemble()
         self.mat.Mult(x, y)
+
+    @property
+    def loform(self):
+        """The same integrand on fes.lospace, assembled (the reference's
+        low-order bilinear form of an H1 high-order space)."""
+        if self._generic or self._sfes is not self.fes:
+            raise NotImplementedError("the low-order form is built for scalar H1 Laplace / mass / tensor forms")
+        if getattr(self, "_loform", None) is None:
+            lo = BilinearForm(self.fes.lospace)
+            for t in self._terms:
+                lo += t
+            self._loform = lo.Assemble()
+        return self._loform
 
     def __del__(self):
         try:

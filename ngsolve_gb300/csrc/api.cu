@@ -766,7 +766,7 @@ int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** ou
     GH1_CUDA(cudaSetDevice(op->ctx->device));
     cudaStream_t st = op->ctx->stream;
     gh1_pre* pr = new gh1_pre();
-    pr->op = op; pr->n = op->nrows;
+    pr->op = op; pr->ctx = op->ctx; pr->n = op->nrows;
     try {
       pr->d_free.alloc(op->nrows);
       if (freedofs) {
@@ -792,12 +792,112 @@ int gh1_jacobi_create(gh1_op* op, const uint8_t* freedofs, int mem, gh1_pre** ou
 
 int gh1_pre_apply(gh1_pre* pr, double s, const void* x, void* y, int prec, int accumulate) {
   if (!pr || !x || !y) return GH1_ERR_ARG;
-  return guard(pr->op->ctx, [&] {
-    jacobi_apply(pr->op->ctx, pr->n, s, pr->d_inv64.p, pr->d_inv32.p, x, y, prec, accumulate);
+  return guard(pr->ctx, [&] {
+    GH1_CHECK(prec == GH1_F64 || prec == GH1_F32, GH1_ERR_ARG, "precision must be GH1_F64 or GH1_F32");
+    pre_prepare(pr);
+    pre_apply_any(pr, s, x, y, prec, accumulate);
   });
 }
 
 int gh1_pre_free(gh1_pre* pr) { delete pr; return GH1_OK; }
+
+
+int gh1_space_smoothing_blocks(gh1_space* sp, int blocktype, int64_t* nblocks, int64_t* nentries, int64_t* offsets,
+                               int32_t* dofs) {
+  if (!sp || !nblocks || !nentries) return GH1_ERR_ARG;
+  return guard(sp->ctx, [&] {
+    std::vector<int64_t> off;
+    std::vector<int32_t> d;
+    smoothing_blocks(sp, blocktype, off, d);
+    *nblocks = (int64_t)off.size() - 1;
+    *nentries = (int64_t)d.size();
+    if (offsets) std::copy(off.begin(), off.end(), offsets);
+    if (dofs) std::copy(d.begin(), d.end(), dofs);
+  });
+}
+
+int gh1_blockjacobi_create(gh1_op* csr, int64_t nblocks, const int64_t* offsets, const int32_t* dofs, int mem,
+                           gh1_pre** out) {
+  if (!csr || !out || nblocks < 0 || (nblocks > 0 && (!offsets || !dofs))) return GH1_ERR_ARG;
+  return guard(csr->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    GH1_CUDA(cudaSetDevice(csr->ctx->device));
+    cudaStream_t st = csr->ctx->stream;
+    const auto kind = mem == GH1_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    std::vector<int64_t> off(nblocks + 1, 0);
+    if (nblocks > 0) GH1_CUDA(cudaMemcpy(off.data(), offsets, (nblocks + 1) * sizeof(int64_t), kind));
+    GH1_CHECK(off[0] == 0, GH1_ERR_ARG, "offsets[0] must be 0");
+    for (int64_t b = 0; b < nblocks; b++) GH1_CHECK(off[b + 1] >= off[b], GH1_ERR_ARG, "offsets must not decrease");
+    std::vector<int32_t> d(off[nblocks]);
+    if (!d.empty()) GH1_CUDA(cudaMemcpy(d.data(), dofs, d.size() * sizeof(int32_t), kind));
+    gh1_pre* pr = new gh1_pre();
+    pr->ctx = csr->ctx;
+    pr->n = csr->nrows;
+    try {
+      block_jacobi_setup(pr, csr, nblocks, off, d);
+      // free mask: the DOFs some block covers
+      std::vector<uint8_t> mask(csr->nrows, 0);
+      for (int32_t x : d) mask[x] = 1;
+      pr->d_free.upload(mask, st);
+      GH1_CUDA(cudaStreamSynchronize(st));
+    } catch (...) { delete pr; throw; }
+    *out = pr;
+  });
+}
+
+int gh1_coarse_create(gh1_op* csr, int64_t nfine, const int32_t* embed, const uint8_t* freedofs, int mem,
+                      gh1_pre** out) {
+  if (!csr || !out || nfine <= 0) return GH1_ERR_ARG;
+  return guard(csr->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    GH1_CUDA(cudaSetDevice(csr->ctx->device));
+    cudaStream_t st = csr->ctx->stream;
+    const auto kind = mem == GH1_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    const int64_t nco = csr->nrows;
+    GH1_CHECK(embed || nco <= nfine, GH1_ERR_ARG, "the identity embedding needs nfine >= the coarse size");
+    std::vector<int32_t> emb(nco);
+    if (embed) GH1_CUDA(cudaMemcpy(emb.data(), embed, nco * sizeof(int32_t), kind));
+    else for (int64_t i = 0; i < nco; i++) emb[i] = (int32_t)i;
+    std::vector<uint8_t> cf(nco, 1);
+    if (freedofs) GH1_CUDA(cudaMemcpy(cf.data(), freedofs, nco, kind));
+    gh1_pre* pr = new gh1_pre();
+    pr->ctx = csr->ctx;
+    pr->n = nfine;
+    try {
+      coarse_setup(pr, csr, nfine, emb, cf);
+      std::vector<uint8_t> mask(nfine, 0);
+      for (int64_t i = 0; i < nco; i++)
+        if (cf[i]) mask[emb[i]] = 1;
+      pr->d_free.upload(mask, st);
+      GH1_CUDA(cudaStreamSynchronize(st));
+    } catch (...) { delete pr; throw; }
+    *out = pr;
+  });
+}
+
+int gh1_pre_sum(gh1_pre* a, gh1_pre* b, gh1_pre** out) {
+  if (!a || !b || !out) return GH1_ERR_ARG;
+  return guard(a->ctx, [&] {
+    GH1_CHECK(a->n == b->n && a->ctx == b->ctx, GH1_ERR_ARG, "the two preconditioners differ in size or context");
+    gh1_pre* pr = new gh1_pre();
+    pr->ctx = a->ctx;
+    pr->n = a->n;
+    pr->kind = 3;
+    pr->a = a;
+    pr->b = b;
+    try {
+      // free mask: the union of the parts'
+      pr->d_free.alloc(pr->n);
+      std::vector<uint8_t> ma(pr->n), mb(pr->n);
+      GH1_CUDA(cudaMemcpy(ma.data(), a->d_free.p, pr->n, cudaMemcpyDeviceToHost));
+      GH1_CUDA(cudaMemcpy(mb.data(), b->d_free.p, pr->n, cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < pr->n; i++) ma[i] |= mb[i];
+      pr->d_free.upload(ma, a->ctx->stream);
+      GH1_CUDA(cudaStreamSynchronize(a->ctx->stream));
+    } catch (...) { delete pr; throw; }
+    *out = pr;
+  });
+}
 
 int gh1_rhs_elementwise(gh1_space* sp, const double* f, int mem, double* b) {
   if (!sp || !f || !b) return GH1_ERR_ARG;
@@ -814,7 +914,7 @@ int gh1_cg(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_op
   int status = GH1_OK;
   int rc = guard(op->ctx, [&] {
     GH1_CHECK(o->mode == GH1_CG_FP64 || o->mode == GH1_CG_MIXED, GH1_ERR_ARG, "unknown CG mode");
-    GH1_CHECK(o->mode == GH1_CG_FP64 || pre, GH1_ERR_ARG, "mixed-precision CG needs the Jacobi preconditioner");
+    GH1_CHECK(o->mode == GH1_CG_FP64 || pre, GH1_ERR_ARG, "mixed-precision CG needs a preconditioner");
     GH1_CHECK(o->maxit > 0 && o->tol >= 0, GH1_ERR_ARG, "maxit must be positive and tol non-negative");
     op_refresh_any(op);
     status = cg_solve(op, pre, b, x, o, r);

@@ -157,6 +157,93 @@ __global__ void __launch_bounds__(RED_BLOCK) cg_update_kernel(int64_t n, int64_t
   }
 }
 
+// A preconditioner other than Jacobi (block Jacobi, low-order solve, their sum)
+// runs as its own kernels between these: the state starts from w = C d and d,
+// the update leaves w.d to cg_wd_kernel, which runs after w = C d.
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_init_gen_kernel(int64_t n, const uint8_t* __restrict__ fr,
+                                                                const T* __restrict__ d, const T* __restrict__ w,
+                                                                T* __restrict__ s, CGState* st, double tol, double* hist,
+                                                                double* partial, unsigned int* counter) {
+  T a0 = 0, a1 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T di = d[i], wi = w[i];
+    s[i] = wi;
+    a0 += wi * di;
+    if (fr[i]) a1 += di * di;
+  }
+  double v[2] = {(double)a0, (double)a1}, tot[2];
+  if (grid_reduce<2>(v, partial, counter, tot) && threadIdx.x == 0) {
+    st->wdn = tot[0];
+    st->wd = tot[0];
+    st->dd = tot[1];
+    double r = st->rule == GH1_STOP_TRUE ? sqrt(tot[1]) : sqrt(fabs(tot[0]));
+    st->res0 = r;
+    st->res = r;
+    st->stop = st->rule == GH1_STOP_TRUE ? tol * sqrt(st->bb) : tol * r;
+    st->it = 1;
+    if (hist) hist[0] = r;
+    st->status = GH1_OK;
+    st->done = (r <= st->stop || st->maxit <= 1 || tot[0] == 0.0) ? 1 : 0;
+    if (st->done && !(r <= st->stop) && tot[0] != 0.0) st->status = GH1_MAXITER;
+  }
+}
+
+// d -= alpha y; y = 0 on [0, zero_end); |d_free|^2 into st->dd
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_update_gen_kernel(int64_t n, int64_t zero_end, const uint8_t* __restrict__ fr,
+                                                                  T* __restrict__ d, T* __restrict__ y, CGState* st,
+                                                                  double* partial, unsigned int* counter) {
+  if (*(volatile int*)&st->done) return;
+  const double wd = st->wd, en = st->energy;
+  if (!(en > 0.0) || wd == 0.0 || !isfinite(en)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->done = 1;
+      st->status = (en == 0.0 || wd == 0.0) ? GH1_OK : GH1_BREAKDOWN;
+    }
+    return;
+  }
+  const T alpha = (T)(wd / en);
+  T a1 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T di = d[i] - alpha * y[i];
+    d[i] = di;
+    if (i < zero_end) y[i] = (T)0;
+    if (fr[i]) a1 += di * di;
+  }
+  double v[1] = {(double)a1}, tot[1];
+  if (grid_reduce<1>(v, partial, counter, tot) && threadIdx.x == 0) {
+    st->alpha = wd / en;
+    st->dd = tot[0];
+  }
+}
+
+// w.d for the new w = C d, then the step's state as cg_update_kernel ends it
+template <class T>
+__global__ void __launch_bounds__(RED_BLOCK) cg_wd_kernel(int64_t n, const T* __restrict__ d, const T* __restrict__ w,
+                                                          CGState* st, double* hist, double* partial,
+                                                          unsigned int* counter) {
+  if (*(volatile int*)&st->done) return;
+  T a0 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a0 += w[i] * d[i];
+  double v[1] = {(double)a0}, tot[1];
+  if (grid_reduce<1>(v, partial, counter, tot) && threadIdx.x == 0) {
+    const double wdn = tot[0], wd = st->wd;
+    const double r = st->rule == GH1_STOP_TRUE ? sqrt(st->dd) : sqrt(fabs(wdn));
+    st->res = r;
+    if (hist) hist[st->it] = r;
+    st->it += 1;
+    st->beta = wdn / wd;
+    st->wdn = wdn;
+    st->wd = wdn;
+    if (!isfinite(r)) { st->done = 1; st->status = GH1_BREAKDOWN; }
+    else if (r <= st->stop) { st->done = 1; st->status = GH1_OK; }
+    else if (st->it >= st->maxit) { st->done = 1; st->status = GH1_MAXITER; }
+    st->xpend = st->done;
+  }
+}
+
 // tail of the WHILE body: count the body launches and keep looping while the
 // solve is not done and the launch bound ctl[1] is not reached
 __global__ void cg_loop_kernel(const CGState* st, int* ctl, cudaGraphConditionalHandle h) {
@@ -332,6 +419,8 @@ struct PCG {
   int chunk;
   int* ctl;              // [2]: body launches so far, bound on body launches
   int64_t zero_end;      // the apply writes (does not accumulate) y from here on
+  gh1_pre* gpre = nullptr;       // a preconditioner other than Jacobi (inv unused then)
+  const uint8_t* fr = nullptr;   // its free-DOF mask
   int applies = 0;
 
   void launch_iteration(cudaStream_t cs) {
@@ -343,8 +432,16 @@ struct PCG {
       dot_energy_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, s, y, &st->energy, partial + 2 * ctx->nsm * 64, counters + 1, &st->done);
       check_kernel(ctx, "dot_energy_kernel");
     }
-    cg_update_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, zero_end, inv, d, w, y, st, hist, partial, counters + 2);
-    check_kernel(ctx, "cg_update_kernel");
+    if (gpre) {
+      cg_update_gen_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, zero_end, fr, d, y, st, partial, counters + 2);
+      check_kernel(ctx, "cg_update_gen_kernel");
+      pre_apply_any(gpre, 1.0, d, w, prec, 0);
+      cg_wd_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, d, w, st, hist, partial, counters + 4);
+      check_kernel(ctx, "cg_wd_kernel");
+    } else {
+      cg_update_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, zero_end, inv, d, w, y, st, hist, partial, counters + 2);
+      check_kernel(ctx, "cg_update_kernel");
+    }
     cg_dir_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, w, s, x, st);
     check_kernel(ctx, "cg_dir_kernel");
   }
@@ -358,8 +455,15 @@ struct PCG {
     GH1_CUDA(cudaMemcpyAsync(st, &h, sizeof(CGState), cudaMemcpyHostToDevice, cs));
     GH1_CUDA(cudaMemsetAsync(y, 0, n * sizeof(T), cs));
     int g = red_grid(ctx, n);
-    cg_init_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, d, w, s, st, tol, hist, partial, counters + 0);
-    check_kernel(ctx, "cg_init_kernel");
+    if (gpre) {
+      pre_prepare(gpre);
+      pre_apply_any(gpre, 1.0, d, w, prec, 0);
+      cg_init_gen_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, fr, d, w, s, st, tol, hist, partial, counters + 0);
+      check_kernel(ctx, "cg_init_gen_kernel");
+    } else {
+      cg_init_kernel<T><<<g, RED_BLOCK, 0, cs>>>(n, inv, d, w, s, st, tol, hist, partial, counters + 0);
+      check_kernel(ctx, "cg_init_kernel");
+    }
     CGState* hs = (CGState*)ctx->h_pinned;
     // one WHILE node whose body is `chunk` iterations plus the loop condition,
     // built once per solve shape
@@ -454,7 +558,9 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
       freemask = ones.p;
     }
     DBuf<double> inv_ident;
-    const double* inv64 = pre ? pre->d_inv64.p : nullptr;
+    gh1_pre* gpre = (pre && pre->kind != 0) ? pre : nullptr;  // a preconditioner run as its own kernels
+    GH1_CHECK(!pre || pre->n == n, GH1_ERR_ARG, "the preconditioner's size differs from the operator's");
+    const double* inv64 = (pre && !gpre) ? pre->d_inv64.p : nullptr;
     if (!inv64) {
       std::vector<double> one(n, 1.0);
       inv_ident.upload(one, cs);
@@ -498,7 +604,7 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
     double final_rr = 0.0;  // |b - A x|^2 on free DOFs for the returned x
     if (o->mode == GH1_CG_FP64) {
       PCG<double> P{op, ctx, n, inv64, x, W.d64.p, W.w64.p, W.s64.p, W.y64.p, GH1_F64, st.p, partial.p, counters.p, hist.p, chunk,
-                    ctl.p, zero_end};
+                    ctl.p, zero_end, gpre, freemask};
       GH1_CUDA(cudaMemsetAsync(W.y64.p, 0, n * sizeof(double), cs));
       CGState res = P.run(o->tol, o->maxit, o->stop_rule, bb, cs, &exec64, &ch64);
       execs.push_back(exec64);
@@ -553,8 +659,8 @@ int cg_solve(gh1_op* op, gh1_pre* pre, const double* b, double* x, const gh1_cg_
         scale_to_f32_kernel<<<grid_for(ctx, n, 256), 256, 0, cs>>>(n, W.r64.p, norm2.p, W.d32.p);
         check_kernel(ctx, "scale_to_f32_kernel");
         GH1_CUDA(cudaMemsetAsync(W.x32.p, 0, n * sizeof(float), cs));
-        PCG<float> P{op, ctx, n, pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32, st.p, partial.p,
-                     counters.p, nullptr, chunk, ctl.p, zero_end};
+        PCG<float> P{op, ctx, n, gpre ? nullptr : pre->d_inv32.p, W.x32.p, W.d32.p, W.w32.p, W.s32.p, W.y32.p, GH1_F32,
+                     st.p, partial.p, counters.p, nullptr, chunk, ctl.p, zero_end, gpre, freemask};
         CGState res = P.run(tol_k, std::max(2, o->maxit - total_inner), GH1_STOP_PRECOND, 0.0, cs, &exec32, &ch32);
         total_inner += res.it;
         r->applies32 += P.applies;

@@ -253,11 +253,27 @@ struct gh1_op {
 };
 
 struct gh1_pre {
-  gh1_op* op = nullptr;
+  gh1_op* op = nullptr;        // Jacobi: the operator of the diagonal (NULL otherwise)
+  gh1_ctx* ctx = nullptr;
   int64_t n = 0;
-  gh1::DBuf<double> d_inv64;
+  int kind = 0;                // 0 Jacobi, 1 block Jacobi, 2 exact low-order solve, 3 sum a + b
+  gh1::DBuf<double> d_inv64;   // Jacobi: 1/A_ii on free DOFs, 0 elsewhere
   gh1::DBuf<float> d_inv32;
-  gh1::DBuf<uint8_t> d_free;
+  gh1::DBuf<uint8_t> d_free;   // free-DOF mask (the true-residual norm of CG)
+  // block Jacobi: block b holds bdofs[boff[b] .. boff[b+1]), its inverse (row-major) at binv[moff[b]]
+  int64_t nblocks = 0;
+  int smax = 0;
+  gh1::DBuf<int64_t> d_boff, d_moff;
+  gh1::DBuf<int32_t> d_bdofs;
+  gh1::DBuf<double> d_binv64;
+  gh1::DBuf<float> d_binv32;
+  // low-order solve: dense inverse of the coarse matrix on its nc free DOFs, cfine[a] = fine DOF of coarse DOF a
+  int nc = 0;
+  gh1::DBuf<int32_t> d_cfine;
+  gh1::DBuf<double> d_cinv64;
+  gh1::DBuf<float> d_cinv32;
+  gh1_pre* a = nullptr;        // sum: the two parts (borrowed)
+  gh1_pre* b = nullptr;
 };
 
 namespace gh1 {
@@ -329,6 +345,15 @@ int hex_tc_occupancy(gh1_op* op);
 void hex_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                   const int* skip);
 void spmv_prepare(gh1_op* op, int prec);                            // spmv.cu (call before capture)
+// preconditioners (precond.cu): block Jacobi, exact low-order solve, their sum;
+// pre_apply_any launches kernels only (capturable), pre_prepare before capture
+void block_jacobi_setup(gh1_pre* pr, gh1_op* csr, int64_t nblocks, const std::vector<int64_t>& off,
+                        const std::vector<int32_t>& dofs);
+void coarse_setup(gh1_pre* pr, gh1_op* csr, int64_t nfine, const std::vector<int32_t>& embed,
+                  const std::vector<uint8_t>& cfreemask);
+void pre_apply_any(gh1_pre* pr, double s, const void* x, void* y, int prec, int accumulate);
+void pre_prepare(gh1_pre* pr);
+void smoothing_blocks(gh1_space* sp, int blocktype, std::vector<int64_t>& off, std::vector<int32_t>& dofs);
 // any operator kind (api.cu): y = A x into a y the call zeroes first where the kind
 // needs it; skip as for the CG graph kernels; prepare / refresh before capture
 void op_apply_any(gh1_op* op, const void* x, void* y, int prec, const int* skip);

@@ -308,6 +308,7 @@ struct Space {
   std::vector<double> X;       // nv*3
   std::vector<int> el;         // ne*nvert
   std::vector<int> el_edges, el_faces;  // global ids per element (local order)
+  std::vector<std::array<int, 2>> edges;  // vertex pair of each global edge
   std::vector<long> edofs;     // ne*nloc (as long for safety)
   std::vector<unsigned char> freedof;
   // Dirichlet on these boundary faces only (sorted vertex numbers, padded with
@@ -335,6 +336,7 @@ void build_space(Space& S) {
   std::vector<std::array<int, 2>> Eu = E;
   std::sort(Eu.begin(), Eu.end()); Eu.erase(std::unique(Eu.begin(), Eu.end()), Eu.end());
   S.ned = (int)Eu.size();
+  S.edges = Eu;
   S.el_edges.resize(E.size());
   for (size_t k = 0; k < E.size(); k++) S.el_edges[k] = int(std::lower_bound(Eu.begin(), Eu.end(), E[k]) - Eu.begin());
   // faces: unique sorted vertex tuples, numbered in lexicographic order
@@ -787,6 +789,60 @@ void orc_apply_bdb(void* h, const double* D, int per_point, int nq, const double
 }
 void orc_diag_bdb(void* h, const double* D, int per_point, int nq, const double* rule, double* diag) {
   bdb_impl(h, D, per_point, nq, rule, nullptr, nullptr, diag);
+}
+
+// H1HighOrderFESpace::CreateSmoothingBlocks (comp/h1hofespace.cpp:1477-1600)
+// through a FilteredTableCreator (only free DOFs enter): blocktype 4 "VE + F + I"
+// -- row v holds vertex v and the DOFs of every edge at v, then one row per
+// face, one per element interior; 3 "V + E + F + I".  Empty rows are dropped
+// and each row is sorted (the block's matrix and inverse do not depend on the
+// order).  Returns the number of rows; offsets / dofs may be NULL (sizes only:
+// *nentries gets the total).
+long orc_smoothing_blocks(void* h, int blocktype, long* nentries, long* offsets, int* dofs) {
+  Space* S = (Space*)h;
+  std::vector<std::vector<int>> rows;
+  const int ned = S->n_edge_dofs;
+  if (blocktype == 4) {
+    std::vector<std::vector<int>> vb(S->nv);
+    for (int v = 0; v < S->nv; v++) vb[v].push_back(v);
+    for (int g = 0; g < S->ned; g++)
+      for (int k = 0; k < ned; k++) {
+        const int d = (int)(S->first_edge + (long)g * ned + k);
+        vb[S->edges[g][0]].push_back(d);
+        vb[S->edges[g][1]].push_back(d);
+      }
+    for (auto& r : vb) rows.push_back(r);
+  } else {
+    for (int v = 0; v < S->nv; v++) rows.push_back({v});
+    for (int g = 0; g < S->ned; g++) {
+      std::vector<int> r;
+      for (int k = 0; k < ned; k++) r.push_back((int)(S->first_edge + (long)g * ned + k));
+      rows.push_back(r);
+    }
+  }
+  for (int f = 0; f < S->nfa; f++) {
+    std::vector<int> r;
+    for (int k = 0; k < S->n_face_dofs; k++) r.push_back((int)(S->first_face + (long)f * S->n_face_dofs + k));
+    rows.push_back(r);
+  }
+  for (int e = 0; e < S->ne; e++) {
+    std::vector<int> r;
+    for (int k = 0; k < S->n_cell_dofs; k++) r.push_back((int)(S->first_cell + (long)e * S->n_cell_dofs + k));
+    rows.push_back(r);
+  }
+  long nb = 0, nt = 0;
+  if (offsets) offsets[0] = 0;
+  for (auto& r : rows) {
+    std::vector<int> f;
+    for (int d : r) if (S->freedof[d]) f.push_back(d);
+    if (f.empty()) continue;
+    std::sort(f.begin(), f.end());
+    for (int d : f) { if (dofs) dofs[nt] = d; nt++; }
+    nb++;
+    if (offsets) offsets[nb] = nt;
+  }
+  if (nentries) *nentries = nt;
+  return nb;
 }
 
 // LinearForm f*v with f piecewise constant per element, integration order 2p

@@ -56,6 +56,8 @@ def lib():
         L.orc_spmv.argtypes = [l, P, P, P, d, P, P, i]
         L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
         L.orc_apply_bdb.argtypes = [P, P, i, i, P, P, P]
+        L.orc_smoothing_blocks.argtypes = [P, i, P, P, P]
+        L.orc_smoothing_blocks.restype = l
         L.orc_diag_bdb.argtypes = [P, P, i, i, P, P]
         L.orc_rhs.argtypes = [P, P, P]
         L.orc_elem_grad_dot.argtypes = [P, P, P, P]
@@ -189,6 +191,15 @@ class OracleSpace:
         d = np.zeros(self.ndof)
         lib().orc_diag_bdb(self.h, _p(D), pp, nq, _p(r), _p(d))
         return d
+
+    def smoothing_blocks(self, blocktype=4):
+        """CreateSmoothingBlocks: (offsets int64, dofs int32), rows sorted, empty rows dropped."""
+        nt = np.zeros(1, dtype=np.int64)
+        nb = lib().orc_smoothing_blocks(self.h, int(blocktype), _p(nt), None, None)
+        off = np.zeros(nb + 1, dtype=np.int64)
+        dofs = np.zeros(max(int(nt[0]), 1), dtype=np.int32)
+        lib().orc_smoothing_blocks(self.h, int(blocktype), _p(nt), _p(off), _p(dofs))
+        return off, dofs[:int(nt[0])]
 
     def rhs(self, f_elem):
         f = np.ascontiguousarray(f_elem, dtype=np.float64)
