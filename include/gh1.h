@@ -118,8 +118,9 @@ int gh1_form_set_tensor(gh1_form* form, const double* K6, int mem);
  * (gh1_space_qpoints: hex tensor Gauss with p+1 points per direction, tet the
  * degree-2p rule).  Host or device per mem; NULL returns the form to kappa / mu /
  * K6, which a set D replaces.  Such a form gives matrix-free operators
- * (gh1_matfree_create, FP64 and FP32, with their diagonal for Jacobi);
- * gh1_assemble_csr, gh1_adjoint_grad and gh1_batch_create reject it. */
+ * (gh1_matfree_create, FP64 and FP32, with their diagonal for Jacobi) and CSR
+ * matrices (gh1_assemble_csr, not symmetric when D is not);
+ * gh1_adjoint_grad and gh1_batch_create reject it. */
 int gh1_form_set_bdb(gh1_form* form, const double* D, int per_point, int mem);
 /* The rule the generic form integrates with: *nq points per element; ref (host,
  * may be NULL): nq x 4 reference coordinates and weight; xyz (may be NULL):

@@ -1406,9 +1406,6 @@ class BilinearForm:
 
     def Assemble(self, reallocate=False):
         ctx = self.fes.ctx.sync_stream()
-        if self._generic and not self.nonassemble:
-            raise NotImplementedError("a generic B^T D B form is applied matrix-free: BilinearForm(..., "
-                                      "nonassemble=True)")
         form = self._make_form()
         h = ctypes.c_void_p()
         sfes = self._sfes

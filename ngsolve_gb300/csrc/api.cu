@@ -597,8 +597,6 @@ int gh1_space_qpoints(gh1_space* sp, double* ref, double* xyz, int mem, int* nq)
 int gh1_assemble_csr(gh1_form* f, gh1_op** out) {
   if (!f || !out) return GH1_ERR_ARG;
   return guard(f->sp->ctx, [&] {
-    GH1_CHECK(f->bdb_mode == 0, GH1_ERR_UNSUPPORTED,
-              "a generic B^T D B form is applied matrix-free (gh1_matfree_create)");
     gh1_space* sp = f->sp;
     GH1_CUDA(cudaSetDevice(sp->ctx->device));
     if (!sp->have_graph) {

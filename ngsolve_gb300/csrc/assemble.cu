@@ -107,8 +107,10 @@ __global__ void tet_assemble_kernel(int ne, int nloc, const int* __restrict__ el
 }
 
 // hex: one thread per (element, t, t'), tensor indices with signs
+// bdb != 0: the generic B^T D B form, Gq = [16][N3] reference-coordinate
+// matrices per point (row = test component, column = trial component)
 __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof, int tstride, const double* __restrict__ Gq,
-                                    int gstride, int mass, const double* __restrict__ B, const double* __restrict__ D,
+                                    int gstride, int mass, int bdb, const double* __restrict__ B, const double* __restrict__ D,
                                     const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind, double* vals,
                                     int* bad) {
   const int N3 = N * N * N;
@@ -129,6 +131,12 @@ __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof,
           int q = (i * N + j) * N + k;
           double x1 = Da * Bb * Bc, y1 = Ba * Db * Bc, z1 = Ba * Bb * Dc;
           double x2 = Da2 * Bb2 * Bc2, y2 = Ba2 * Db2 * Bc2, z2 = Ba2 * Bb2 * Dc2;
+          if (bdb) {
+            const double b1[4] = {Ba * Bb * Bc, x1, y1, z1}, b2[4] = {Ba2 * Bb2 * Bc2, x2, y2, z2};
+            for (int r = 0; r < 4; r++)
+              for (int cc = 0; cc < 4; cc++) s += b1[r] * Ge[(4 * r + cc) * N3 + q] * b2[cc];
+            continue;
+          }
           double gxx = Ge[q], gyy = Ge[N3 + q], gzz = Ge[2 * N3 + q], gxy = Ge[3 * N3 + q], gxz = Ge[4 * N3 + q],
                  gyz = Ge[5 * N3 + q];
           s += x1 * (gxx * x2 + gxy * y2 + gxz * z2) + y1 * (gxy * x2 + gyy * y2 + gyz * z2) + z1 * (gxz * x2 + gyz * y2 + gzz * z2);
@@ -154,7 +162,7 @@ __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof,
 //   K[aa'][bb'][cc'] = sum_v sum_i X^v_a(i) X^v_a'(i) C_v[i][bb'][cc']  4 N^7 FMAs
 // (N = 4: ~1.2e5 FMAs per element instead of ~5e6 for the entry-by-entry sum).
 __global__ void __launch_bounds__(256) hex_assemble_sf_kernel(int ne, int N, const int* __restrict__ tdof, int tstride,
-                                                              const double* __restrict__ Gq, int gstride, int mass,
+                                                              const double* __restrict__ Gq, int gstride, int mass, int bdb,
                                                               const double* __restrict__ Btab,
                                                               const double* __restrict__ Dtab,
                                                               const int64_t* __restrict__ rowptr,
@@ -163,22 +171,31 @@ __global__ void __launch_bounds__(256) hex_assemble_sf_kernel(int ne, int N, con
   const int N2 = N * N, N3 = N2 * N, N4 = N2 * N2, N5 = N4 * N, N6 = N3 * N3;
   double* sB = sfm;             // [q][a]
   double* sD = sB + N2;         // [q][a]
-  double* sG = sD + N2;         // [7][N3]
-  double* sA = sG + 7 * N3;     // [i][j][c][c']
+  double* sG = sD + N2;         // [7][N3] (B^T D B: [16][N3])
+  double* sA = sG + (bdb ? 16 : 7) * N3;  // [i][j][c][c']
   double* sC = sA + N4;         // [4][i][b][b'][c][c']
   int* sT = (int*)(sC + 4 * N5);  // DOF row of the element
   for (int k = threadIdx.x; k < N2; k += blockDim.x) { sB[k] = Btab[k]; sD[k] = Dtab[k]; }
   for (int e = blockIdx.x; e < ne; e += gridDim.x) {
     __syncthreads();
     const double* Ge = Gq + (size_t)e * gstride;
-    for (int k = threadIdx.x; k < (mass ? 7 : 6) * N3; k += blockDim.x) sG[k] = Ge[k];
+    for (int k = threadIdx.x; k < (bdb ? 16 : (mass ? 7 : 6)) * N3; k += blockDim.x) sG[k] = Ge[k];
     for (int k = threadIdx.x; k < N3; k += blockDim.x) sT[k] = tdof[(size_t)e * tstride + k];
     for (int k = threadIdx.x; k < 4 * N5; k += blockDim.x) sC[k] = 0;
-    const int nterm = mass ? 10 : 9;
+    const int nterm = bdb ? 16 : (mass ? 10 : 9);
     for (int term = 0; term < nterm; term++) {
-      // term < 9: (m, n) = (term / 3, term % 3); term 9: mass
-      const int m = term < 9 ? term / 3 : -1, n = term < 9 ? term % 3 : -1;
-      const int gc = term == 9 ? 6 : (m == n ? m : 3 + m + n - 1);  // xy -> 3, xz -> 4, yz -> 5
+      // term < 9: (m, n) = (term / 3, term % 3); term 9: mass.  B^T D B: (m, n) =
+      // (term / 4 - 1, term % 4 - 1) with -1 the value (all factors B), weight G_term
+      int m, n, gc;
+      if (bdb) {
+        m = term / 4 - 1;
+        n = term % 4 - 1;
+        gc = term;
+      } else {
+        m = term < 9 ? term / 3 : -1;
+        n = term < 9 ? term % 3 : -1;
+        gc = term == 9 ? 6 : (m == n ? m : 3 + m + n - 1);  // xy -> 3, xz -> 4, yz -> 5
+      }
       const double* Zm = m == 2 ? sD : sB;
       const double* Zn = n == 2 ? sD : sB;
       const double* Ym = m == 1 ? sD : sB;
@@ -221,9 +238,9 @@ __global__ void __launch_bounds__(256) hex_assemble_sf_kernel(int ne, int N, con
   }
 }
 
-static size_t hex_assemble_sf_smem(int N) {
+static size_t hex_assemble_sf_smem(int N, bool bdb) {
   const size_t N2 = N * N, N3 = N2 * N, N4 = N2 * N2, N5 = N4 * N;
-  return (2 * N2 + 7 * N3 + N4 + 4 * N5) * sizeof(double) + N3 * sizeof(int);
+  return (2 * N2 + (bdb ? 16 : 7) * N3 + N4 + 4 * N5) * sizeof(double) + N3 * sizeof(int);
 }
 
 void assemble_csr(gh1_form* f, double* vals) {
@@ -233,12 +250,16 @@ void assemble_csr(gh1_form* f, double* vals) {
   // geometry (G, M) in FP64 through a temporary matrix-free operator
   gh1_op geo;
   geo.ctx = ctx; geo.kind = GH1_OP_MATFREE; geo.form = f; geo.sp = sp; geo.nrows = sp->ndof; geo.prec_mask = 1;
+  geo.bdb_points_only = true;  // B^T D B on hexes: matrices per point, the layout the kernels read
   matfree_setup(&geo);
+  const int bdb = geo.bdb ? 1 : 0;
   GH1_CUDA(cudaMemsetAsync(vals, 0, sp->nnz * sizeof(double), s));
   DBuf<int> bad(1);
   bad.zero(s);
   const int ne = sp->mesh->ne;
-  if (sp->et == 4) {
+  if (sp->et == 4 && bdb) {
+    tet_bdb_assemble(&geo, sp->d_rowptr.p, sp->d_colind.p, vals, bad.p);
+  } else if (sp->et == 4) {
     int64_t tot = (int64_t)ne * sp->nloc * sp->nloc;
     int grid = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)ctx->nsm * 32);
     tet_assemble_kernel<<<grid, 256, 0, s>>>(ne, sp->nloc, sp->d_eldofs.p, sp->d_class.p, geo.d_G64.p,
@@ -247,7 +268,7 @@ void assemble_csr(gh1_form* f, double* vals) {
     check_kernel(ctx, "tet_assemble_kernel");
   } else if (sp->p + 1 <= 5 && !getenv("GH1_HEX_ASSEMBLE_ENTRYWISE")) {
     const int N = sp->p + 1;
-    const size_t smem = hex_assemble_sf_smem(N);
+    const size_t smem = hex_assemble_sf_smem(N, bdb);
     static bool attr = false;
     if (!attr) {
       GH1_CUDA(cudaFuncSetAttribute(hex_assemble_sf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
@@ -255,7 +276,7 @@ void assemble_csr(gh1_form* f, double* vals) {
     }
     const int grid = std::max(1, std::min(ne, ctx->nsm * 8));
     hex_assemble_sf_kernel<<<grid, 256, smem, s>>>(ne, N, sp->d_tdof.p, sp->tstride, geo.d_G64.p, geo.gstride64,
-                                                   geo.has_mass ? 1 : 0, sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p,
+                                                   geo.has_mass ? 1 : 0, bdb, sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p,
                                                    sp->d_colind.p, vals, bad.p);
     check_kernel(ctx, "hex_assemble_sf_kernel");
   } else {
@@ -263,7 +284,7 @@ void assemble_csr(gh1_form* f, double* vals) {
     int64_t tot = (int64_t)ne * N * N * N * N * N * N;
     int grid = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)ctx->nsm * 32);
     hex_assemble_kernel<<<grid, 256, 0, s>>>(ne, N, sp->d_tdof.p, sp->tstride, geo.d_G64.p, geo.gstride64,
-                                             geo.has_mass ? 1 : 0, sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p, sp->d_colind.p,
+                                             geo.has_mass ? 1 : 0, bdb, sp->d_B64.p, sp->d_D64.p, sp->d_rowptr.p, sp->d_colind.p,
                                              vals, bad.p);
     check_kernel(ctx, "hex_assemble_kernel");
   }

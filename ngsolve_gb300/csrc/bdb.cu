@@ -245,7 +245,7 @@ void bdb_setup(gh1_op* op) {
     // one record per element when D is per element and every element map is
     // affine (GH1_BDB_AFFINE=0 keeps the per-point records)
     const char* env = getenv("GH1_BDB_AFFINE");
-    bool elem = f->bdb_mode == 1 && !(env && std::string(env) == "0") && ne > 0;
+    bool elem = f->bdb_mode == 1 && !(env && std::string(env) == "0") && ne > 0 && !op->bdb_points_only;
     if (elem) {
       op->d_G64.alloc((size_t)ne * 16);
       if (want32) op->d_G32.alloc((size_t)ne * 16); else op->d_G32.release();

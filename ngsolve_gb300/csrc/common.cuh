@@ -204,6 +204,7 @@ struct gh1_op {
   // elements with D per element), weighted in the kernel.  T = diag(1, J^{-T}).
   int bdb = 0;
   int bdb_per_sm[2] = {0, 0};                // hex: resident blocks of the B^T D B apply [FP64/FP32]
+  bool bdb_points_only = false;              // hex: per-point records even for affine elements (assembly)
   int tet_ncb = 0;                           // tet: 16-point chunks of the degree-2p rule
   gh1::DBuf<double> d_tetB64, d_tetBw64;     // tet: [class][chunk][nlocp][64] value and reference-gradient
   gh1::DBuf<float> d_tetB32, d_tetBw32;      //      rows (component*16 + point), weights [chunk*16]
@@ -298,6 +299,7 @@ void tet_bdb_setup(gh1_op* op);                                     // tetapply.
 void tet_bdb_apply(gh1_op* op, int prec, const void* x, void* y, double* partial, unsigned int* counter,
                    double* energy, const int* skip);                // tetapply.cu
 void tet_bdb_diag(gh1_op* op, double* diag);                        // tetapply.cu
+void tet_bdb_assemble(gh1_op* op, const int64_t* rowptr, const int32_t* colind, double* vals, int* bad);  // tetapply.cu
 void build_graph(gh1_space* sp);                                    // assemble.cu (host)
 bool build_graph_gpu(gh1_space* sp);                                // graph.cu
 void assemble_csr(gh1_form* f, double* vals);                       // assemble.cu

@@ -953,4 +953,53 @@ void tet_bdb_diag(gh1_op* op, double* diag) {
   check_kernel(sp->ctx, "tet_bdb_diag_kernel");
 }
 
+// element matrices of the generic form on tets, one thread per (element, i, j):
+// K_ij = sum_q sum_rc B_r(i,q) Mh_rc(q) B_c(j,q) (B from the chunked value /
+// reference-gradient table, Mh per point or w_q times the element's record),
+// scattered into the CSR pattern as the other assemblies do
+__global__ void tet_bdb_assemble_kernel(int ne, int nloc, int nlocp, int ncb, int nq, const int* __restrict__ eldofs,
+                                        const uint8_t* __restrict__ cls, const double* __restrict__ Mh, int per_point,
+                                        const double* __restrict__ Tb, const double* __restrict__ Wb,
+                                        const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                                        double* vals, int* bad) {
+  const int64_t per = (int64_t)nloc * nloc;
+  for (int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; id < (int64_t)ne * per;
+       id += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(id / per), ij = (int)(id % per), i = ij / nloc, j = ij % nloc, c = cls[e];
+    double k = 0;
+    for (int q = 0; q < nq; q++) {
+      const double* ri = Tb + (((size_t)c * ncb + q / TET_QC) * nlocp + i) * 4 * TET_QC + q % TET_QC;
+      const double* rj = Tb + (((size_t)c * ncb + q / TET_QC) * nlocp + j) * 4 * TET_QC + q % TET_QC;
+      const double bi[4] = {ri[0], ri[TET_QC], ri[2 * TET_QC], ri[3 * TET_QC]};
+      const double bj[4] = {rj[0], rj[TET_QC], rj[2 * TET_QC], rj[3 * TET_QC]};
+      const double* m = per_point ? Mh + ((size_t)e * nq + q) * 16 : Mh + (size_t)e * 16;
+      double t = 0;
+      for (int r = 0; r < 4; r++)
+        for (int cc = 0; cc < 4; cc++) t += bi[r] * m[4 * r + cc] * bj[cc];
+      k += (per_point ? 1.0 : Wb[q]) * t;
+    }
+    const int row = eldofs[(size_t)e * nloc + i], col = eldofs[(size_t)e * nloc + j];
+    int64_t lo = rowptr[row], hi = rowptr[row + 1] - 1, pos = -1;
+    while (lo <= hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (colind[mid] == col) { pos = mid; break; }
+      if (colind[mid] < col) lo = mid + 1; else hi = mid - 1;
+    }
+    if (pos < 0) { atomicExch(bad, 1); continue; }
+    atomicAdd(vals + pos, k);
+  }
+}
+
+void tet_bdb_assemble(gh1_op* op, const int64_t* rowptr, const int32_t* colind, double* vals, int* bad) {
+  gh1_space* sp = op->sp;
+  const int ne = sp->mesh->ne, nloc = sp->nloc, nlocp = (nloc + 15) / 16 * 16;
+  const int64_t tot = (int64_t)ne * nloc * nloc;
+  if (tot == 0) return;
+  const int grid = (int)std::min<int64_t>((tot + 255) / 256, (int64_t)sp->ctx->nsm * 32);
+  tet_bdb_assemble_kernel<<<grid, 256, 0, sp->ctx->stream>>>(ne, nloc, nlocp, op->tet_ncb, sp->tet_nq_mass, sp->d_eldofs.p,
+                                                             sp->d_class.p, op->d_G64.p, op->bdb == 1 ? 1 : 0,
+                                                             op->d_tetB64.p, op->d_tetBw64.p, rowptr, colind, vals, bad);
+  check_kernel(sp->ctx, "tet_bdb_assemble_kernel");
+}
+
 }  // namespace gh1

@@ -161,7 +161,7 @@ def test_bdb_variant_paths_agree(gpu, hexes, p, monkeypatch):
 def test_bdb_symmetric_form_solves_like_laplace(gpu, hexes, p):
     """(1 + 0 x) grad u . grad v + mu u v is the Laplace + mass operator written as
     a point-wise generic form: the mixed-precision CG on it reaches the same
-    solution as on the standard form (1e-9), and the assembled operator rejects it."""
+    solution as on the standard form (1e-9)."""
     m = _mesh(hexes, 4, 0.1)
     fes = gpu.H1(m, order=p, dirichlet=".*")
     u, v = fes.TnT()
@@ -179,5 +179,32 @@ def test_bdb_symmetric_form_solves_like_laplace(gpu, hexes, p):
         sols.append(gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-11, maxsteps=5000, printrates=False,
                                    mode="mixed"))
     assert gpu.Norm(sols[0] - sols[1]) <= 1e-9 * gpu.Norm(sols[1])
-    with pytest.raises(NotImplementedError):
-        gpu.BilinearForm(one * gpu.grad(u) * gpu.grad(v) * gpu.dx).Assemble()
+
+
+@pytest.mark.parametrize("hexes,p,jit,pointwise", [(True, 2, 0.0, False), (True, 3, 0.15, True), (True, 5, 0.0, False),
+                                                   (False, 2, 0.2, False), (False, 3, 0.2, True), (False, 4, 0.2, False)])
+def test_bdb_assembled(gpu, hexes, p, jit, pointwise):
+    """BilinearForm(generic).Assemble(): the CSR pattern is the space's
+    MatrixGraph, A x matches the oracle's B^T D B apply (1e-12) and the
+    matrix-free operator of the same form; transposing D transposes A."""
+    m = _mesh(hexes, 3 if hexes else 2, jit)
+    fes = gpu.H1(m, order=p)
+    terms = _terms(gpu, fes, m.ne, 69 + p, pointwise)
+    a = gpu.BilinearForm(sum(terms[1:], terms[0])).Assemble()
+    rp, ci, va = a.mat.CSR()
+    S = O.OracleSpace(m.points, m.elements, p)
+    orp, oci = S.graph()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    ref, xyz = _rule(gpu, fes)
+    D = _oracle_D(terms, m.ne, xyz if pointwise else None)
+    x = np.random.default_rng(70).normal(size=fes.ndof)
+    yo = S.apply_bdb(x, D, rule=ref if pointwise else None)
+    sc = np.abs(yo).max()
+    assert np.abs(O.spmv(rp, ci, va, x) - yo).max() <= 1e-12 * sc
+    amf = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True).Assemble()
+    assert np.abs(_apply(gpu, amf, x, torch.float64) - O.spmv(rp, ci, va, x)).max() <= 1e-12 * sc
+    z = np.random.default_rng(71).normal(size=fes.ndof)
+    Dt = np.ascontiguousarray(np.swapaxes(D.reshape(D.shape[:-1] + (4, 4)), -1, -2).reshape(D.shape))
+    Ax = O.spmv(rp, ci, va, x)
+    lhs, rhs = z @ Ax, x @ S.apply_bdb(z, Dt, rule=ref if pointwise else None)
+    assert abs(lhs - rhs) <= 1e-11 * np.linalg.norm(z) * np.linalg.norm(Ax)
