@@ -48,7 +48,9 @@ void gauss01(int n, std::vector<double>& x, std::vector<double>& w) {
 }
 
 // tet rule of a given order: tabulated symmetric rules up to degree 6 (the point
-// counts of fem/intrule.cpp:2596-2812), collapsed tensor Gauss rule above.
+// counts of fem/intrule.cpp:2596-2812), a 46-point symmetric rule for degrees 7
+// and 8 (gen_tet_rules.py; the reference's collapsed rule there has 216 points),
+// collapsed tensor Gauss rule above.
 void tet_rule(int order, std::vector<double>& r /* x,y,z,w per point */) {
   r.clear();
   auto add = [&](const double (*t)[4], int n) { for (int i = 0; i < n; i++) for (int k = 0; k < 4; k++) r.push_back(t[i][k]); };
@@ -56,6 +58,7 @@ void tet_rule(int order, std::vector<double>& r /* x,y,z,w per point */) {
   else if (order == 2) add(TET_RULE_D2, 4);
   else if (order <= 5) add(TET_RULE_D5, 14);
   else if (order == 6) add(TET_RULE_D6, 24);
+  else if (order <= 8) add(TET_RULE_D8, 46);
   else {
     int n = order / 2 + 2;
     std::vector<double> g, gw;

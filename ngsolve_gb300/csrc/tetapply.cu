@@ -38,7 +38,7 @@ template <int P>
 struct TetDims {
   static constexpr int NLOC = (P + 1) * (P + 2) * (P + 3) / 6;
   static constexpr int NQ = P == 1 ? 1 : P == 2 ? 4 : P == 3 ? 14 : 24;
-  static constexpr int NQM = P == 1 ? 4 : P == 2 ? 14 : P == 3 ? 24 : 216;
+  static constexpr int NQM = P == 1 ? 4 : P == 2 ? 14 : P == 3 ? 24 : 46;
   static constexpr int NLOCP = (NLOC + 15) / 16 * 16;
   template <bool MASS>
   static constexpr int R() { return 3 * NQ + (MASS ? NQM : 0); }

@@ -140,7 +140,7 @@ def test_abi_argument_checks(gpu):
     with pytest.raises(GH1Error, match="order"):
         gpu.H1(m, order=9)
     with pytest.raises(GH1Error, match="order"):
-        gpu.H1(MakeStructured3DMesh(hexes=False, nx=1), order=7)
+        gpu.H1(MakeStructured3DMesh(hexes=False, nx=1), order=9)
     bad = m.elements.copy()
     bad[3, 5] = m.points.shape[0]
     with pytest.raises(ValueError, match="out of range"):  # the host-side mesh check

@@ -53,8 +53,8 @@ def _form(gpu, fes, kappa, mu, kernel):
 @pytest.mark.parametrize("mass", [False, True])
 @pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7, 8])
 def test_tet_apply_parity(gpu, p, mass, kernel):
-    if kernel == "elementwise" and (p >= 5 or (mass and p >= 4)):
-        pytest.skip("the element-wise kernel supports rules up to 128 points (p=4 mass: 216, p=5: 216, p=6: 343)")
+    if kernel == "elementwise" and (p >= 6 or (mass and p >= 5)):
+        pytest.skip("the element-wise kernel supports rules up to 128 points (p=5 mass: 343, p=6: 343)")
     if p >= 7 and mass and kernel is None:
         pytest.skip("p = 7, 8 run without the mass term here; the B^T D B tests cover reaction at p = 7")
     m = _mesh(3, 21 + p)

@@ -472,3 +472,36 @@ def test_oracle_bdb(hexes, p):
         e = np.zeros(S.ndof)
         e[i] = 1.0
         assert abs(S.apply_bdb(e, Dn)[i] - d[i]) <= 1e-13 * max(1.0, abs(d[i]))
+
+
+def _tet_rules_inc():
+    """The symmetric tet rules the library compiles in (csrc/tet_rules.inc):
+    {degree: (points (n, 3), weights (n,))}."""
+    import os
+    import re
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ngsolve_gb300", "csrc",
+                        "tet_rules.inc")
+    text = open(path).read()
+    out = {}
+    for m in re.finditer(r"TET_RULE_D(\d+)\[(\d+)\]\[4\] = \{(.*?)\};", text, re.S):
+        rows = re.findall(r"\{([^{}]*)\}", m.group(3))
+        arr = np.array([[float(v) for v in r.split(",") if v.strip()] for r in rows])
+        assert arr.shape == (int(m.group(2)), 4)
+        out[int(m.group(1))] = (arr[:, :3], arr[:, 3])
+    return out
+
+
+def test_tet_rules_exact():
+    """Every compiled tet rule integrates all monomials x^i y^j z^k of total
+    degree <= its degree exactly (i! j! k! / (i+j+k+3)!, relative 1e-14), with
+    positive weights and interior points; degree 8 has 46 points."""
+    rules = _tet_rules_inc()
+    assert sorted(rules) == [1, 2, 5, 6, 8] and len(rules[8][1]) == 46
+    for deg, (P, W) in rules.items():
+        assert np.all(W > 0) and np.all(P > 0) and np.all(P.sum(1) < 1)
+        for i in range(deg + 1):
+            for j in range(deg + 1 - i):
+                for k in range(deg + 1 - i - j):
+                    ex = math.factorial(i) * math.factorial(j) * math.factorial(k) / math.factorial(i + j + k + 3)
+                    got = np.sum(W * P[:, 0] ** i * P[:, 1] ** j * P[:, 2] ** k)
+                    assert abs(got - ex) <= 1e-14 * ex, (deg, i, j, k)
