@@ -127,6 +127,17 @@ int gh1_form_set_bdb(gh1_form* form, const double* D, int per_point, int mem);
  * ne x nq x 3 physical coordinates, host or device per mem.  A point-wise D of
  * gh1_form_set_bdb follows this point order. */
 int gh1_space_qpoints(gh1_space* space, double* ref, double* xyz, int mem, int* nq);
+/* Curved elements: MeshAccess::SetDeformation (comp/meshaccess.cpp:1573-1580,
+ * ALE_ElementTransformation :240-340).  d: 3 * ndof(space) values, the x, y and z
+ * components of a displacement field in the H1 space `space` of this mesh one
+ * after the other (VectorH1 numbering), host or device per mem.  Element maps
+ * become x(xi) + d(xi), Jacobians J(xi) + grad d(xi), at every rule point.
+ * Forms, operators, load vectors and rule points made while it is set use the
+ * deformed elements (made before: the mesh as it was); on tets the operators
+ * then take the per-point B^T D B path, and the element contraction of
+ * gh1_adjoint_grad is not available.  d = NULL removes the deformation; freeing
+ * `space` removes it too. */
+int gh1_mesh_set_deformation(gh1_mesh* mesh, gh1_space* space, const double* d, int mem);
 /* Releases the caller's handle.  Operators made from the form (gh1_assemble_csr,
  * gh1_matfree_create, gh1_batch_create) keep it alive, as the reference's
  * BilinearFormApplication holds its BilinearForm: its memory goes when the last

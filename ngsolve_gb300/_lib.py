@@ -48,6 +48,7 @@ SIGNATURES = {
     "gh1_version": [],
     "gh1_mesh_upload": [_P, _I, _P, _I, _I, _P, _PP],
     "gh1_mesh_free": [_P],
+    "gh1_mesh_set_deformation": [_P, _P, _P, _I],
     "gh1_space_h1": [_P, _I, _I, _PP],
     "gh1_space_h1_bnd": [_P, _I, _L, _P, _PP],
     "gh1_space_free": [_P],

@@ -90,6 +90,24 @@ class Mesh:
     def nv(self):
         return self.raw.nv
 
+    def SetDeformation(self, gf):
+        """MeshAccess::SetDeformation (comp/meshaccess.cpp:1573-1580): gf is a
+        GridFunction of VectorH1(mesh, order=k) whose values displace the mesh;
+        forms assembled afterwards integrate over the deformed (curved) elements."""
+        fes = gf.fes
+        if not isinstance(fes, VectorH1) or fes.dim != 3 or fes.mesh is not self:
+            raise ValueError("SetDeformation needs a GridFunction of VectorH1(mesh, dim=3) on this mesh")
+        v = gf.vec.t
+        if v.dtype != torch.float64 or not v.is_cuda or not v.is_contiguous() or v.numel() != fes.ndof:
+            raise TypeError("the deformation vector must be a contiguous CUDA float64 vector of the space's size")
+        self.ctx.sync_stream()
+        # the values are copied; the library borrows the field's space, so the
+        # deformation lasts while the GridFunction's space does
+        self.ctx.check(self.ctx.lib.gh1_mesh_set_deformation(self.h, fes.scalar.h, _ptr(v), _lib.GH1_MEM_DEVICE))
+
+    def UnsetDeformation(self):
+        self.ctx.check(self.ctx.lib.gh1_mesh_set_deformation(self.h, None, None, _lib.GH1_MEM_HOST))
+
     def __del__(self):
         try:
             self.ctx.lib.gh1_mesh_free(self.h)

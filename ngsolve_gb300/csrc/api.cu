@@ -425,7 +425,29 @@ int gh1_mesh_upload(gh1_ctx* ctx, int nv, const double* coords, int ne, int et, 
   });
 }
 
-int gh1_mesh_free(gh1_mesh* m) { delete m; return GH1_OK; }
+int gh1_mesh_free(gh1_mesh* m) {
+  if (m && m->def_space) m->def_space->def_of = nullptr;  // the two may be freed in either order
+  delete m;
+  return GH1_OK;
+}
+
+static void upload_coef(gh1_ctx* ctx, DBuf<double>& dst, const double* src, int mem, int64_t n, double dflt);
+int gh1_mesh_set_deformation(gh1_mesh* m, gh1_space* sp, const double* d, int mem) {
+  if (!m) return GH1_ERR_ARG;
+  return guard(m->ctx, [&] {
+    GH1_CHECK(mem == GH1_MEM_HOST || mem == GH1_MEM_DEVICE, GH1_ERR_ARG, "mem must be GH1_MEM_HOST or GH1_MEM_DEVICE");
+    if (m->def_space) m->def_space->def_of = nullptr;
+    m->def_space = nullptr;
+    m->d_def.release();
+    if (!d) return;
+    GH1_CHECK(sp && sp->mesh == m, GH1_ERR_ARG, "the deformation lives in an H1 space of this mesh");
+    GH1_CHECK(m->et == 8 || sp->p <= MAX_TET_ORDER, GH1_ERR_UNSUPPORTED, "deformation order out of range");
+    upload_coef(m->ctx, m->d_def, d, mem, 3 * sp->ndof, 0.0);
+    m->def_space = sp;
+    sp->def_of = m;
+    GH1_CUDA(cudaStreamSynchronize(m->ctx->stream));
+  });
+}
 
 int gh1_space_h1(gh1_mesh* m, int order, int dirichlet, gh1_space** out) {
   if (!m || !out) return GH1_ERR_ARG;
@@ -476,7 +498,14 @@ int gh1_space_h1_bnd(gh1_mesh* m, int order, int64_t nbf, const int32_t* faces, 
   });
 }
 
-int gh1_space_free(gh1_space* sp) { delete sp; return GH1_OK; }
+int gh1_space_free(gh1_space* sp) {
+  if (sp && sp->def_of) {  // the mesh's deformation lived in this space
+    sp->def_of->def_space = nullptr;
+    sp->def_of->d_def.release();
+  }
+  delete sp;
+  return GH1_OK;
+}
 
 int gh1_space_info(gh1_space* sp, int64_t* info) {
   if (!sp || !info) return GH1_ERR_ARG;

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 #include "common.cuh"
+#include "deform.cuh"
 
 namespace gh1 {
 
@@ -296,7 +297,8 @@ void assemble_csr(gh1_form* f, double* vals) {
 
 // ---- LinearForm f*v, f piecewise constant ---------------------------------------
 __global__ void hex_wdet_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
-                                const double* __restrict__ gx, const double* __restrict__ gw, double* wdet) {
+                                const double* __restrict__ gx, const double* __restrict__ gw, double* wdet,
+                                DeformView dv) {
   const int nq = nq1 * nq1 * nq1;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -314,6 +316,7 @@ __global__ void hex_wdet_kernel(int ne, int nq1, const double* __restrict__ X, c
     for (int r = 0; r < 3; r++)
       for (int c = 0; c < 3; c++) J[3 * r + c] += pa[r] * dl[a][c];
   }
+  deform_add(dv, e, x, y, z, J, nullptr);
   double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
   wdet[id] = gw[i] * gw[j] * gw[k] * fabs(det);
 }
@@ -355,9 +358,11 @@ __global__ void __launch_bounds__(128) hex_rhs_kernel(int ne, int N, const int* 
   }
 }
 
+// deformed meshes: |det J| per rule point (the Jacobian gains the field's gradient)
 __global__ void tet_rhs_kernel(int ne, int nloc, int nqm, const int* __restrict__ eldofs, const uint8_t* __restrict__ cls,
                                const double* __restrict__ X, const int* __restrict__ el, const double* __restrict__ tabm,
-                               const double* __restrict__ rulem, const double* __restrict__ f, double* b) {
+                               const double* __restrict__ rulem, const double* __restrict__ f, double* b,
+                               DeformView dv) {
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nloc) return;
   int e = (int)(id / nloc), i = (int)(id % nloc);
@@ -369,6 +374,18 @@ __global__ void tet_rhs_kernel(int ne, int nloc, int nqm, const int* __restrict_
   double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
   const double* tc = tabm + (size_t)cls[e] * nqm * nloc;
   double s = 0;
+  if (dv.d) {
+    for (int q = 0; q < nqm; q++) {
+      double Jq[9];
+      for (int c = 0; c < 9; c++) Jq[c] = J[c];
+      deform_add(dv, e, rulem[4 * q], rulem[4 * q + 1], rulem[4 * q + 2], Jq, nullptr);
+      const double dq = Jq[0] * (Jq[4] * Jq[8] - Jq[5] * Jq[7]) - Jq[1] * (Jq[3] * Jq[8] - Jq[5] * Jq[6]) +
+                        Jq[2] * (Jq[3] * Jq[7] - Jq[4] * Jq[6]);
+      s += rulem[4 * q + 3] * fabs(dq) * tc[(size_t)q * nloc + i];
+    }
+    atomicAdd(b + eldofs[id], f[e] * s);
+    return;
+  }
   for (int q = 0; q < nqm; q++) s += rulem[4 * q + 3] * tc[(size_t)q * nloc + i];
   atomicAdd(b + eldofs[id], f[e] * fabs(det) * s);
 }
@@ -383,7 +400,7 @@ void rhs_elementwise(gh1_space* sp, const double* f, double* b) {
     DBuf<double> wdet((size_t)ne * nq);
     int64_t tot = (int64_t)ne * nq;
     hex_wdet_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p,
-                                                                   sp->d_gw.p, wdet.p);
+                                                                   sp->d_gw.p, wdet.p, deform_view(sp->mesh));
     check_kernel(ctx, "hex_wdet_kernel");
     hex_rhs_kernel<<<std::min(ne, ctx->nsm * 16), 128, 2 * (size_t)N * N * N * sizeof(double), s>>>(
         ne, N, sp->d_tdof.p, sp->tstride, wdet.p, sp->d_B64.p, f, b);
@@ -393,7 +410,7 @@ void rhs_elementwise(gh1_space* sp, const double* f, double* b) {
     int64_t tot = (int64_t)ne * sp->nloc;
     tet_rhs_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, sp->nloc, sp->tet_nq_mass, sp->d_eldofs.p, sp->d_class.p,
                                                                   sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_tabm64.p,
-                                                                  sp->d_tqm.p, f, b);
+                                                                  sp->d_tqm.p, f, b, deform_view(sp->mesh));
     check_kernel(ctx, "tet_rhs_kernel");
   }
 }

@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "hexcore.cuh"
 #include "hexsf.cuh"
+#include "deform.cuh"
 
 namespace gh1 {
 
@@ -59,7 +60,7 @@ __device__ __forceinline__ void bdb_transform(const double* Ji, const double* D,
 __global__ void hex_bdb_point_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
                                      const double* __restrict__ gx, const double* __restrict__ gw,
                                      const double* __restrict__ D, int per_point, double* G64, int gs64, float* G32,
-                                     int gs32) {
+                                     int gs32, DeformView dv) {
   const int nq = nq1 * nq1 * nq1;
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -69,6 +70,7 @@ __global__ void hex_bdb_point_kernel(int ne, int nq1, const double* __restrict__
   for (int a = 0; a < 8; a++) v[a] = el[(size_t)e * 8 + a];
   double J[9], Ji[9], det;
   hex_jacobian(X, v, gx[i], gx[j], gx[k], J);
+  deform_add(dv, e, gx[i], gx[j], gx[k], J, nullptr);
   inv3(J, Ji, det);
   const double* De = per_point ? D + ((size_t)e * nq + q) * 16 : D + (size_t)e * 16;
   double M[16];
@@ -106,13 +108,14 @@ __global__ void hex_bdb_elem_kernel(int ne, const double* __restrict__ X, const 
   }
 }
 
-// tet, affine map x = v3 + sum_j (v_j - v3) xi_j: one record [e][16] without the
-// rule weight (D per element), or [e][q][16] with it (D per point)
+// tet, map x = v3 + sum_j (v_j - v3) xi_j (+ the deformation): one record
+// [e][16] without the rule weight (out_pp = 0: affine element, D per element), or
+// [e][q][16] with it (out_pp = 1); D per element or per point (d_pp)
 __global__ void tet_bdb_geom_kernel(int ne, int nq, const double* __restrict__ X, const int* __restrict__ el,
-                                    const double* __restrict__ rule, const double* __restrict__ D, int per_point,
-                                    double* M64, float* M32) {
+                                    const double* __restrict__ rule, const double* __restrict__ D, int d_pp, int out_pp,
+                                    double* M64, float* M32, DeformView dv) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int nper = per_point ? nq : 1;
+  const int nper = out_pp ? nq : 1;
   if (id >= (int64_t)ne * nper) return;
   const int e = (int)(id / nper), q = (int)(id % nper);
   const int* v = el + (size_t)e * 4;
@@ -122,10 +125,11 @@ __global__ void tet_bdb_geom_kernel(int ne, int nq, const double* __restrict__ X
     const double* pj = X + 3 * (size_t)v[j];
     for (int k = 0; k < 3; k++) J[3 * k + j] = pj[k] - p3[k];
   }
+  if (out_pp) deform_add(dv, e, rule[4 * q], rule[4 * q + 1], rule[4 * q + 2], J, nullptr);
   inv3(J, Ji, det);
-  const double s = per_point ? rule[4 * q + 3] * fabs(det) : fabs(det);
+  const double s = out_pp ? rule[4 * q + 3] * fabs(det) : fabs(det);
   double M[16];
-  bdb_transform(Ji, D + (size_t)id * 16, s, M);
+  bdb_transform(Ji, D + (d_pp ? (size_t)id : (size_t)e) * 16, s, M);
   for (int m = 0; m < 16; m++) {
     if (M64) M64[(size_t)id * 16 + m] = M[m];
     if (M32) M32[(size_t)id * 16 + m] = (float)M[m];
@@ -198,6 +202,26 @@ __global__ void __launch_bounds__(256) hex_bdb_diag_kernel(int ne, int N, const 
   }
 }
 
+// D per element of the form kappa grad.grad + mu u v (or K grad.grad + mu u v):
+// the B^T D B path of curved tets takes the standard forms this way
+__global__ void coef_bdb_kernel(int ne, const double* __restrict__ kappa, const double* __restrict__ K6,
+                                const double* __restrict__ mu, double* D) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double* d = D + (size_t)e * 16;
+  for (int c = 0; c < 16; c++) d[c] = 0;
+  d[0] = mu ? mu[e] : 0.0;
+  if (K6) {
+    const double* k = K6 + (size_t)e * 6;
+    d[5] = k[0]; d[10] = k[1]; d[15] = k[2];
+    d[6] = d[9] = k[3];
+    d[7] = d[13] = k[4];
+    d[11] = d[14] = k[5];
+  } else {
+    d[5] = d[10] = d[15] = kappa[e];
+  }
+}
+
 #define GH1_BDB_SWITCH(N, CASE)                                                                        \
   switch (N) {                                                                                         \
     CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)                                   \
@@ -236,7 +260,23 @@ void bdb_setup(gh1_op* op) {
   cudaStream_t s = sp->ctx->stream;
   const int ne = sp->mesh->ne;
   const bool want32 = (op->prec_mask & 2) != 0;
-  GH1_CHECK(f->bdb_mode == 1 || f->bdb_mode == 2, GH1_ERR_ARG, "internal: not a B^T D B form");
+  const bool deformed = sp->mesh->def_space != nullptr;
+  const DeformView dv = deform_view(sp->mesh);
+  // D: the form's generic matrices, or (a standard form on a curved tet mesh)
+  // diag(mu, kappa I or K) per element
+  int dmode = f->bdb_mode;
+  const double* Dsrc = f->d_bdb.p;
+  DBuf<double> Dcoef;
+  if (dmode == 0) {
+    Dcoef.alloc((size_t)std::max(ne, 1) * 16);
+    if (ne > 0) {
+      coef_bdb_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, f->d_kappa.p, f->has_K6 ? f->d_K6.p : nullptr,
+                                                      f->has_mu ? f->d_mu.p : nullptr, Dcoef.p);
+      check_kernel(sp->ctx, "coef_bdb_kernel");
+    }
+    Dsrc = Dcoef.p;
+    dmode = 1;
+  }
   op->has_mass = true;  // the value component is always interpolated
   op->d_M64.release();
   op->d_M32.release();
@@ -245,13 +285,13 @@ void bdb_setup(gh1_op* op) {
     // one record per element when D is per element and every element map is
     // affine (GH1_BDB_AFFINE=0 keeps the per-point records)
     const char* env = getenv("GH1_BDB_AFFINE");
-    bool elem = f->bdb_mode == 1 && !(env && std::string(env) == "0") && ne > 0 && !op->bdb_points_only;
+    bool elem = dmode == 1 && !(env && std::string(env) == "0") && ne > 0 && !op->bdb_points_only && !deformed;
     if (elem) {
       op->d_G64.alloc((size_t)ne * 16);
       if (want32) op->d_G32.alloc((size_t)ne * 16); else op->d_G32.release();
       DBuf<int> flag(1);
       flag.zero(s);
-      hex_bdb_elem_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, f->d_bdb.p, op->d_G64.p,
+      hex_bdb_elem_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, Dsrc, op->d_G64.p,
                                                            want32 ? op->d_G32.p : nullptr, flag.p);
       check_kernel(sp->ctx, "hex_bdb_elem_kernel");
       int h = 0;
@@ -268,8 +308,8 @@ void bdb_setup(gh1_op* op) {
       const int64_t tot = (int64_t)ne * nq;
       if (tot > 0) {
         hex_bdb_point_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
-            ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_bdb.p, f->bdb_mode == 2 ? 1 : 0,
-            op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
+            ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, Dsrc, dmode == 2 ? 1 : 0,
+            op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32, dv);
         check_kernel(sp->ctx, "hex_bdb_point_kernel");
       }
     }
@@ -279,15 +319,15 @@ void bdb_setup(gh1_op* op) {
     op->bdb_per_sm[0] = hex_bdb_occupancy<double>(op, op->gstride64);
     op->bdb_per_sm[1] = want32 ? hex_bdb_occupancy<float>(op, op->gstride32) : 0;
   } else {
-    const int nq = sp->tet_nq_mass, per_point = f->bdb_mode == 2 ? 1 : 0;
+    const int nq = sp->tet_nq_mass, d_pp = dmode == 2 ? 1 : 0, per_point = (d_pp || deformed) ? 1 : 0;
     const size_t nrec = (size_t)ne * (per_point ? nq : 1) * 16;
     op->d_G64.alloc(nrec);
     if (want32) op->d_G32.alloc(nrec); else op->d_G32.release();
     const int64_t tot = (int64_t)ne * (per_point ? nq : 1);
     if (tot > 0) {
       tet_bdb_geom_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, s>>>(ne, nq, sp->mesh->d_X.p, sp->mesh->d_el.p,
-                                                                        sp->d_tqm.p, f->d_bdb.p, per_point, op->d_G64.p,
-                                                                        want32 ? op->d_G32.p : nullptr);
+                                                                        sp->d_tqm.p, Dsrc, d_pp, per_point, op->d_G64.p,
+                                                                        want32 ? op->d_G32.p : nullptr, dv);
       check_kernel(sp->ctx, "tet_bdb_geom_kernel");
     }
     op->bdb = per_point ? 1 : 2;

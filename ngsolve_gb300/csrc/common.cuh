@@ -81,6 +81,11 @@ struct gh1_mesh {
   std::vector<int32_t> el;
   gh1::DBuf<double> d_X;
   gh1::DBuf<int32_t> d_el;
+  // deformation field (gh1_mesh_set_deformation): [3][ndof] in the H1 space
+  // def_space (borrowed) of this mesh; operators made while it is set see the
+  // deformed, curved elements
+  gh1_space* def_space = nullptr;
+  gh1::DBuf<double> d_def;
 };
 
 struct gh1_space {
@@ -123,6 +128,7 @@ struct gh1_space {
   int64_t nnz = 0;
   gh1::DBuf<int64_t> d_rowptr;
   gh1::DBuf<int32_t> d_colind;
+  gh1_mesh* def_of = nullptr;     // the mesh whose deformation field lives in this space
 };
 
 // G = s * Ji K Ji^T for the symmetric tensor K = (xx yy zz xy xz yz), written

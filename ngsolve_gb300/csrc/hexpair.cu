@@ -1069,7 +1069,7 @@ void hex_affine_setup(gh1_op* op) {
   op->all_affine = false;
   op->d_Ga32.release();
   const char* env = getenv("GH1_HEX_AFFINE");
-  if ((env && env[0] == '0') || !hex_pair_supported(sp->p + 1)) return;
+  if ((env && env[0] == '0') || !hex_pair_supported(sp->p + 1) || sp->mesh->def_space) return;  // curved: per point
   const int ne = sp->mesh->ne;
   cudaStream_t s = sp->ctx->stream;
   op->d_Ga32.alloc((size_t)ne * 8);

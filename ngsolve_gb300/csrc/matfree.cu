@@ -30,6 +30,7 @@
 #include "basis.cuh"
 #include "hexcore.cuh"
 #include "hexsf.cuh"
+#include "deform.cuh"
 
 namespace gh1 {
 
@@ -40,7 +41,8 @@ namespace gh1 {
 __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, const int* __restrict__ el,
                                 const double* __restrict__ gx, const double* __restrict__ gw,
                                 const double* __restrict__ kappa, const double* __restrict__ K6,
-                                const double* __restrict__ mu, double* G64, int gs64, float* G32, int gs32) {
+                                const double* __restrict__ mu, double* G64, int gs64, float* G32, int gs32,
+                                DeformView dv) {
   const int nq = nq1 * nq1 * nq1;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -50,6 +52,7 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
   for (int a = 0; a < 8; a++) v[a] = el[(size_t)e * 8 + a];
   double J[9], Ji[9], det;
   hex_jacobian(X, v, gx[i], gx[j], gx[k], J);
+  deform_add(dv, e, gx[i], gx[j], gx[k], J, nullptr);
   inv3(J, Ji, det);
   double wdet = gw[i] * gw[j] * gw[k] * fabs(det);
   double g[7];
@@ -690,7 +693,9 @@ void matfree_setup(gh1_op* op) {
     op->d_err.zero(s);
   }
   op->bdb = 0;
-  if (f->bdb_mode) {  // generic B^T D B form (bdb.cu)
+  // generic B^T D B form (bdb.cu); on a deformed tet mesh every form goes this
+  // way, its metrics per rule point (the tet kernels assume affine elements)
+  if (f->bdb_mode || (sp->et == 4 && sp->mesh->def_space)) {
     bdb_setup(op);
     return;
   }
@@ -705,7 +710,8 @@ void matfree_setup(gh1_op* op) {
     int64_t tot = (int64_t)ne * nq;
     hex_geom_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
         ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_kappa.p,
-        f->has_K6 ? f->d_K6.p : nullptr, op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32);
+        f->has_K6 ? f->d_K6.p : nullptr, op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32,
+        deform_view(sp->mesh));
     check_kernel(sp->ctx, "hex_geom_kernel");
     upload_const_tables(sp);
     op->hex_per_sm[0][0] = hex_occupancy_dispatch<double, 0>(op, op->gstride64);
@@ -850,6 +856,8 @@ void elem_grad_dot(gh1_space* sp, const double* u, const double* w, double* out)
 
 void elem_grad_dot_with(gh1_op* op, const double* u, const double* w, double* out) {
   gh1_space* sp = op->sp;
+  GH1_CHECK(!(sp->et == 4 && sp->mesh->def_space), GH1_ERR_UNSUPPORTED,
+            "the element contraction on tets needs affine elements (the mesh is deformed)");
   const double* kappa = op->form->d_kappa.p;
   if (sp->et == 8) {
 #define GH1_GD_CASE(NN) \

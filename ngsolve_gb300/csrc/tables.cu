@@ -20,6 +20,7 @@
 #include "common.cuh"
 #include "basis.cuh"
 #include "tet_rules.inc"
+#include "deform.cuh"
 
 namespace gh1 {
 
@@ -216,13 +217,14 @@ int space_rule_size(const gh1_space* sp) { return sp->et == 8 ? sp->nq1 * sp->nq
 // physical coordinates of the rule points: hex trilinear map, tet affine map
 // x = v3 + sum_j (v_j - v3) xi_j
 __global__ void qpoints_kernel(int et, int ne, int nq, int nq1, const double* __restrict__ X, const int* __restrict__ el,
-                               const double* __restrict__ gx, const double* __restrict__ tqm, double* xyz) {
+                               const double* __restrict__ gx, const double* __restrict__ tqm, double* xyz, DeformView dv) {
   const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
   const int e = (int)(id / nq), q = (int)(id % nq);
-  double out[3] = {0, 0, 0};
+  double out[3] = {0, 0, 0}, Jd[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (et == 8) {
     const double x = gx[q / (nq1 * nq1)], y = gx[(q / nq1) % nq1], z = gx[q % nq1];
+    deform_add(dv, e, x, y, z, Jd, out);  // the displacement (Jd unused)
     const double lam[8] = {(1 - x) * (1 - y) * (1 - z), x * (1 - y) * (1 - z), x * y * (1 - z), (1 - x) * y * (1 - z),
                            (1 - x) * (1 - y) * z,       x * (1 - y) * z,       x * y * z,       (1 - x) * y * z};
     for (int a = 0; a < 8; a++) {
@@ -231,7 +233,8 @@ __global__ void qpoints_kernel(int et, int ne, int nq, int nq1, const double* __
     }
   } else {
     const double* p3 = X + 3 * (size_t)el[(size_t)e * 4 + 3];
-    for (int k = 0; k < 3; k++) out[k] = p3[k];
+    deform_add(dv, e, tqm[4 * q], tqm[4 * q + 1], tqm[4 * q + 2], Jd, out);
+    for (int k = 0; k < 3; k++) out[k] += p3[k];
     for (int j = 0; j < 3; j++) {
       const double* pj = X + 3 * (size_t)el[(size_t)e * 4 + j];
       for (int k = 0; k < 3; k++) out[k] += (pj[k] - p3[k]) * tqm[4 * q + j];
@@ -261,7 +264,7 @@ void space_qpoints(gh1_space* sp, double* ref, double* xyz) {
   if (xyz && ne > 0) {
     const int64_t tot = (int64_t)ne * nq;
     qpoints_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(sp->et, ne, nq, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p,
-                                                                 sp->d_gx.p, sp->d_tqm.p, xyz);
+                                                                 sp->d_gx.p, sp->d_tqm.p, xyz, deform_view(sp->mesh));
     check_kernel(sp->ctx, "qpoints_kernel");
   }
 }

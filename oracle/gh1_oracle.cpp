@@ -309,6 +309,10 @@ struct Space {
   std::vector<int> el;         // ne*nvert
   std::vector<int> el_edges, el_faces;  // global ids per element (local order)
   std::vector<std::array<int, 2>> edges;  // vertex pair of each global edge
+  // deformation (MeshAccess::SetDeformation): a field in the H1 space `def` of
+  // the same mesh, [3][def->ndof] component-major
+  const struct Space* def = nullptr;
+  std::vector<double> defvec;
   std::vector<long> edofs;     // ne*nloc (as long for safety)
   std::vector<unsigned char> freedof;
   // Dirichlet on these boundary faces only (sorted vertex numbers, padded with
@@ -419,6 +423,7 @@ inline void invert3(const double* J, double* Ji, double& det) {
 // tet: x = v3 + sum_j (v_j - v3) xi_j  (comp/meshaccess.cpp:541-552)
 // hex: trilinear map from the 8 vertices with the hex vertex functions of
 // h1hofe_impl.hpp:826-827 (netgen's own element map is not in the tree).
+void add_deformation(const Space& S, int e, double x, double y, double z, double* J);
 Geo geometry(const Space& S, int e, double x, double y, double z) {
   Geo g; const int* v = &S.el[(size_t)e * S.nvert];
   if (S.et == 4) {
@@ -433,6 +438,7 @@ Geo geometry(const Space& S, int e, double x, double y, double z) {
     for (int i = 0; i < 9; i++) g.J[i] = 0;
     for (int a = 0; a < 8; a++) { const double* pa = &S.X[3 * (size_t)v[a]]; for (int k = 0; k < 3; k++) for (int j = 0; j < 3; j++) g.J[3 * k + j] += pa[k] * dl[a][j]; }
   }
+  add_deformation(S, e, x, y, z, g.J);
   invert3(g.J, g.Jinv, g.det);
   return g;
 }
@@ -441,6 +447,21 @@ int shape_ad(const Space& S, int e, double x, double y, double z, AD* sh) {
   const int* vn = &S.el[(size_t)e * S.nvert];
   AD X = AD::var(x, 0), Y = AD::var(y, 1), Z = AD::var(z, 2);
   return S.et == 4 ? tet_shape<AD>(S.p, vn, X, Y, Z, sh) : hex_shape<AD>(S.p, vn, X, Y, Z, sh);
+}
+
+// ALE_ElementTransformation::CalcJacobian (comp/meshaccess.cpp:318-330): the
+// mesh Jacobian plus the reference gradient of the deformation field
+void add_deformation(const Space& S, int e, double x, double y, double z, double* J) {
+  if (!S.def) return;
+  const Space& D = *S.def;
+  std::vector<AD> sh(D.nloc);
+  shape_ad(D, e, x, y, z, sh.data());
+  const long* dn = &D.edofs[(size_t)e * D.nloc];
+  for (int i = 0; i < D.nloc; i++)
+    for (int r = 0; r < 3; r++) {
+      const double dr = S.defvec[(size_t)r * D.ndof + dn[i]];
+      for (int c = 0; c < 3; c++) J[3 * r + c] += dr * sh[i].d[c];
+    }
 }
 
 Rule bilinear_rule(const Space& S) {
@@ -847,10 +868,29 @@ long orc_smoothing_blocks(void* h, int blocktype, long* nentries, long* offsets,
 
 // LinearForm f*v with f piecewise constant per element, integration order 2p
 // (SymbolicLFI, fem/symbolicintegrator.cpp:1109)
+// deformation: d[3][ndof of hdef] on the space hdef (same mesh); d = NULL removes it
+void orc_space_set_deformation(void* h, void* hdef, const double* d) {
+  Space* S = (Space*)h;
+  if (!d) { S->def = nullptr; S->defvec.clear(); return; }
+  S->def = (Space*)hdef;
+  S->defvec.assign(d, d + 3 * (size_t)S->def->ndof);
+}
+
+static void rhs_impl(Space* S, const Rule& r, const double* f, double* b);
 void orc_rhs(void* h, const double* f, double* b) {
   Space* S = (Space*)h;
+  rhs_impl(S, mass_rule(*S), f, b);
+}
+// the same at a caller's rule (nq points: reference x, y, z, weight)
+void orc_rhs_rule(void* h, const double* f, int nq, const double* rule, double* b) {
+  Rule r;
+  for (int q = 0; q < nq; q++) {
+    r.x.push_back(rule[4 * q]); r.y.push_back(rule[4 * q + 1]); r.z.push_back(rule[4 * q + 2]); r.w.push_back(rule[4 * q + 3]);
+  }
+  rhs_impl((Space*)h, r, f, b);
+}
+static void rhs_impl(Space* S, const Rule& r, const double* f, double* b) {
   std::memset(b, 0, S->ndof * sizeof(double));
-  Rule r = mass_rule(*S);
   const int n = S->nloc;
 #pragma omp parallel
   {

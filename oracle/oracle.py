@@ -57,6 +57,8 @@ def lib():
         L.orc_apply_mf.argtypes = [P, P, P, P, P, i, i]
         L.orc_apply_bdb.argtypes = [P, P, i, i, P, P, P]
         L.orc_smoothing_blocks.argtypes = [P, i, P, P, P]
+        L.orc_space_set_deformation.argtypes = [P, P, P]
+        L.orc_rhs_rule.argtypes = [P, P, i, P, P]
         L.orc_smoothing_blocks.restype = l
         L.orc_diag_bdb.argtypes = [P, P, i, i, P, P]
         L.orc_rhs.argtypes = [P, P, P]
@@ -201,11 +203,26 @@ class OracleSpace:
         lib().orc_smoothing_blocks(self.h, int(blocktype), _p(nt), _p(off), _p(dofs))
         return off, dofs[:int(nt[0])]
 
-    def rhs(self, f_elem):
+    def rhs(self, f_elem, rule=None):
         f = np.ascontiguousarray(f_elem, dtype=np.float64)
         b = np.zeros(self.ndof)
-        lib().orc_rhs(self.h, _p(f), _p(b))
+        if rule is None:
+            lib().orc_rhs(self.h, _p(f), _p(b))
+        else:
+            r = np.ascontiguousarray(rule, dtype=np.float64).reshape(-1, 4)
+            lib().orc_rhs_rule(self.h, _p(f), len(r), _p(r), _p(b))
         return b
+
+    def set_deformation(self, def_space, d):
+        """Curved elements: d = [3 * def_space.ndof] displacement in def_space (same mesh), None removes it."""
+        if d is None:
+            lib().orc_space_set_deformation(self.h, None, None)
+            self._def = None
+            return
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        assert d.size == 3 * def_space.ndof
+        self._def = (def_space, d)  # keeps the field's space alive
+        lib().orc_space_set_deformation(self.h, def_space.h, _p(d))
 
     def elem_grad_dot(self, u, w):
         u = np.ascontiguousarray(u, dtype=np.float64)
