@@ -497,13 +497,15 @@ def leg_bdb(nx=64, order=4):
     import ngsolve_gb300 as ng
     out = {}
 
-    def run(mesh, kappa, r, label):
+    def run(mesh, kappa, r, label, convection=True):
         fes = ng.H1(mesh, order=order, dirichlet=".*")
         u, v = fes.TnT()
         b = ng.CoefficientFunction((1.0, 0.5, 0.25))
-        a = ng.BilinearForm(ng.CoefficientFunction(kappa) * ng.grad(u) * ng.grad(v) * ng.dx +
-                            ng.InnerProduct(b, ng.grad(u)) * v * ng.dx + r * u * v * ng.dx,
-                            nonassemble=True, precision="fp32")
+        integrand = (ng.CoefficientFunction(kappa) if not isinstance(kappa, ng.comp._AffineCF) else kappa) * \
+            ng.grad(u) * ng.grad(v) * ng.dx + r * u * v * ng.dx
+        if convection:
+            integrand = integrand + ng.InnerProduct(b, ng.grad(u)) * v * ng.dx
+        a = ng.BilinearForm(integrand, nonassemble=True, precision="fp32")
         t_setup, _ = _timed(lambda: a.Assemble())
         N = fes.ndof
         res = {"ndof": N, "ne": mesh.ne, "setup_s": t_setup, "variant": a.mat.Info()["hex_variant_fp32"]}
@@ -522,10 +524,15 @@ def leg_bdb(nx=64, order=4):
     kappa = np.exp(np.random.default_rng(4).normal(0, 0.5, mesh.ne))
     run(mesh, kappa, ng.CoefficientFunction(1.0), "hex_%d^3_p%d_per_element" % (nx, order))
     run(mesh, kappa, 1.0 + ng.x, "hex_%d^3_p%d_per_point" % (nx, order))
+    # a form of Laplace type with a coefficient in x, (1 + x) grad.grad + u v:
+    # routed to the standard per-point-metric kernels
+    run(mesh, 1.0 + ng.x, ng.CoefficientFunction(1.0), "hex_%d^3_p%d_laplace_type_per_point" % (nx, order),
+        convection=False)
     tmesh = ng.JitterInterior(ng.MakeStructured3DMesh(hexes=False, nx=32), 0.2 / 32, 2)
     tk = np.exp(np.random.default_rng(3).normal(0, 1, tmesh.ne))
     run(tmesh, tk, ng.CoefficientFunction(1.0), "tet_32^3_p%d_per_element" % order)
-    out["form"] = "kappa grad(u).grad(v) + ((1, 0.5, 0.25) . grad u) v + r u v, D 4x4 per element or per point"
+    out["form"] = ("kappa grad(u).grad(v) + ((1, 0.5, 0.25) . grad u) v + r u v, D 4x4 per element or per point; "
+                   "laplace_type: (1 + x) grad(u).grad(v) + u v")
     return out
 
 

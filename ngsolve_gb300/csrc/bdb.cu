@@ -222,6 +222,75 @@ __global__ void coef_bdb_kernel(int ne, const double* __restrict__ kappa, const 
   }
 }
 
+// structure of D records: flags[0] = a value-gradient coupling is non-zero,
+// flags[1] = the gradient block is not symmetric, flags[2] = the value entry is
+// non-zero somewhere
+__global__ void bdb_structure_kernel(int64_t nrec, const double* __restrict__ D, int* flags) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += (int64_t)gridDim.x * blockDim.x) {
+    const double* d = D + r * 16;
+    if (d[1] != 0.0 || d[2] != 0.0 || d[3] != 0.0 || d[4] != 0.0 || d[8] != 0.0 || d[12] != 0.0) atomicOr(flags, 1);
+    double sc = 0;
+    for (int c = 5; c < 16; c++) sc = fmax(sc, fabs(d[c]));
+    const double tol = 1e-14 * sc;
+    if (fabs(d[6] - d[9]) > tol || fabs(d[7] - d[13]) > tol || fabs(d[11] - d[14]) > tol) atomicOr(flags + 1, 1);
+    if (d[0] != 0.0) atomicOr(flags + 2, 1);
+  }
+}
+
+// per-element D of Laplace type -> K6 (xx yy zz xy xz yz) and mu
+__global__ void bdb_to_k6_kernel(int ne, const double* __restrict__ D, double* K6, double* mu) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double* d = D + (size_t)e * 16;
+  double* k = K6 + (size_t)e * 6;
+  k[0] = d[5]; k[1] = d[10]; k[2] = d[15];
+  k[3] = 0.5 * (d[6] + d[9]); k[4] = 0.5 * (d[7] + d[13]); k[5] = 0.5 * (d[11] + d[14]);
+  if (mu) mu[e] = d[0];
+}
+
+// A generic form on hexes whose D is diag(mu, K) with K symmetric (diffusion
+// with any tensor, reaction; no convection) is the standard operator with
+// per-element or per-point coefficients: it takes the standard kernels (all
+// autotuned variants, the per-element metric on affine meshes) instead of the
+// 16-coefficient B^T D B kernel.  GH1_BDB_STANDARD=0 keeps the B^T D B kernel.
+bool bdb_laplace_route(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  gh1_form* f = op->form;
+  op->lap_ov = false;
+  op->lap_pp = nullptr;
+  op->d_ovK6.release();
+  op->d_ovmu.release();
+  const char* env = getenv("GH1_BDB_STANDARD");
+  if (sp->et != 8 || !f->bdb_mode || (env && std::string(env) == "0")) return false;
+  cudaStream_t s = sp->ctx->stream;
+  const int ne = sp->mesh->ne, nq = sp->nq1 * sp->nq1 * sp->nq1;
+  const int64_t nrec = (int64_t)ne * (f->bdb_mode == 2 ? nq : 1);
+  DBuf<int> flags(3);
+  flags.zero(s);
+  if (nrec > 0) {
+    bdb_structure_kernel<<<grid_for(sp->ctx, nrec, 256), 256, 0, s>>>(nrec, f->d_bdb.p, flags.p);
+    check_kernel(sp->ctx, "bdb_structure_kernel");
+  }
+  int h[3] = {0, 0, 0};
+  GH1_CUDA(cudaMemcpyAsync(h, flags.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  if (h[0] || h[1]) return false;
+  op->lap_ov = true;
+  op->has_mass = h[2] != 0;
+  if (f->bdb_mode == 2) {
+    op->lap_pp = f->d_bdb.p;
+  } else {
+    op->d_ovK6.alloc((size_t)std::max(ne, 1) * 6);
+    if (op->has_mass) op->d_ovmu.alloc(std::max(ne, 1));
+    if (ne > 0) {
+      bdb_to_k6_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, f->d_bdb.p, op->d_ovK6.p, op->has_mass ? op->d_ovmu.p : nullptr);
+      check_kernel(sp->ctx, "bdb_to_k6_kernel");
+    }
+    GH1_CUDA(cudaStreamSynchronize(s));
+  }
+  return true;
+}
+
 #define GH1_BDB_SWITCH(N, CASE)                                                                        \
   switch (N) {                                                                                         \
     CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)                                   \

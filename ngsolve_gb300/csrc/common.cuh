@@ -211,6 +211,12 @@ struct gh1_op {
   int bdb = 0;
   int bdb_per_sm[2] = {0, 0};                // hex: resident blocks of the B^T D B apply [FP64/FP32]
   bool bdb_points_only = false;              // hex: per-point records even for affine elements (assembly)
+  // a generic form of Laplace type on hexes (D = diag(mu, K), K symmetric) runs on
+  // the standard kernels: per element through these coefficient arrays, per point
+  // through lap_pp (the form's D, read by the metric kernel)
+  bool lap_ov = false;
+  gh1::DBuf<double> d_ovK6, d_ovmu;
+  const double* lap_pp = nullptr;
   int tet_ncb = 0;                           // tet: 16-point chunks of the degree-2p rule
   gh1::DBuf<double> d_tetB64, d_tetBw64;     // tet: [class][chunk][nlocp][64] value and reference-gradient
   gh1::DBuf<float> d_tetB32, d_tetBw32;      //      rows (component*16 + point), weights [chunk*16]
@@ -298,6 +304,7 @@ void tet_mass_rule_tables(gh1_space* sp, gh1::DBuf<double>& t64, gh1::DBuf<float
 int space_rule_size(const gh1_space* sp);                           // points of the B^T D B rule
 void space_qpoints(gh1_space* sp, double* ref /* nq x 4 or NULL */, double* xyz /* device, ne x nq x 3 or NULL */);
 void bdb_setup(gh1_op* op);                                         // bdb.cu
+bool bdb_laplace_route(gh1_op* op);                                 // bdb.cu: hex generic form of Laplace type?
 void bdb_apply(gh1_op* op, const void* x, void* y, int prec, double* partial, unsigned int* counter, double* energy,
                const int* skip);                                    // bdb.cu
 void bdb_diag(gh1_op* op, double* diag);                            // bdb.cu

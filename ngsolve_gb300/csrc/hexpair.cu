@@ -1069,14 +1069,18 @@ void hex_affine_setup(gh1_op* op) {
   op->all_affine = false;
   op->d_Ga32.release();
   const char* env = getenv("GH1_HEX_AFFINE");
-  if ((env && env[0] == '0') || !hex_pair_supported(sp->p + 1) || sp->mesh->def_space) return;  // curved: per point
+  // curved elements or coefficients per point: per-point metrics only
+  if ((env && env[0] == '0') || !hex_pair_supported(sp->p + 1) || sp->mesh->def_space || op->lap_pp) return;
   const int ne = sp->mesh->ne;
   cudaStream_t s = sp->ctx->stream;
   op->d_Ga32.alloc((size_t)ne * 8);
   DBuf<int> flag(1);
   flag.zero(s);
-  hex_affine_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, op->form->d_kappa.p,
-                                                     op->form->has_K6 ? op->form->d_K6.p : nullptr, op->has_mass ? op->form->d_mu.p : nullptr, op->d_Ga32.p, flag.p);
+  const gh1_form* f = op->form;
+  const double* K6 = op->lap_ov ? op->d_ovK6.p : (f->has_K6 ? f->d_K6.p : nullptr);
+  const double* mu = !op->has_mass ? nullptr : (op->lap_ov ? op->d_ovmu.p : f->d_mu.p);
+  hex_affine_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->mesh->d_X.p, sp->mesh->d_el.p, f->d_kappa.p, K6, mu,
+                                                     op->d_Ga32.p, flag.p);
   check_kernel(sp->ctx, "hex_affine_kernel");
   int h = 1;
   GH1_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));

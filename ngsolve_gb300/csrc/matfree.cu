@@ -42,7 +42,7 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
                                 const double* __restrict__ gx, const double* __restrict__ gw,
                                 const double* __restrict__ kappa, const double* __restrict__ K6,
                                 const double* __restrict__ mu, double* G64, int gs64, float* G32, int gs32,
-                                DeformView dv) {
+                                DeformView dv, const double* __restrict__ Dpp) {
   const int nq = nq1 * nq1 * nq1;
   int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (int64_t)ne * nq) return;
@@ -56,6 +56,18 @@ __global__ void hex_geom_kernel(int ne, int nq1, const double* __restrict__ X, c
   inv3(J, Ji, det);
   double wdet = gw[i] * gw[j] * gw[k] * fabs(det);
   double g[7];
+  if (Dpp) {  // a generic form of Laplace type with D per point: K = the gradient block, mu = the value entry
+    const double* d = Dpp + ((size_t)e * nq + q) * 16;
+    const double K[6] = {d[5], d[10], d[15], 0.5 * (d[6] + d[9]), 0.5 * (d[7] + d[13]), 0.5 * (d[11] + d[14])};
+    tensor_metric(Ji, K, wdet, g);
+    g[6] = d[0] * wdet;
+    const int nc = mu ? 7 : 6;
+    for (int c = 0; c < nc; c++) {
+      if (G64) G64[(size_t)e * gs64 + c * nq + q] = g[c];
+      if (G32) G32[(size_t)e * gs32 + c * nq + q] = (float)g[c];
+    }
+    return;
+  }
   if (K6) {
     tensor_metric(Ji, K6 + 6 * (size_t)e, wdet, g);
   } else {
@@ -695,12 +707,18 @@ void matfree_setup(gh1_op* op) {
   op->bdb = 0;
   // generic B^T D B form (bdb.cu); on a deformed tet mesh every form goes this
   // way, its metrics per rule point (the tet kernels assume affine elements)
-  if (f->bdb_mode || (sp->et == 4 && sp->mesh->def_space)) {
+  // (a hex form of Laplace type takes the standard kernels with its coefficients)
+  const bool lap = bdb_laplace_route(op);
+  if ((f->bdb_mode && !lap) || (sp->et == 4 && sp->mesh->def_space)) {
     bdb_setup(op);
     return;
   }
-  op->has_mass = f->has_mu;
+  if (!lap) op->has_mass = f->has_mu;
   if (sp->et == 8) {
+    // coefficients: the form's, or those of a generic form of Laplace type
+    const double* kap = f->d_kappa.p;
+    const double* K6 = lap ? op->d_ovK6.p : (f->has_K6 ? f->d_K6.p : nullptr);
+    const double* mu = !op->has_mass ? nullptr : (lap ? op->d_ovmu.p : f->d_mu.p);
     const int nq = sp->nq1 * sp->nq1 * sp->nq1;
     op->ncomp = op->has_mass ? 7 : 6;
     op->gstride64 = pad16(op->ncomp * nq, 8);
@@ -709,9 +727,9 @@ void matfree_setup(gh1_op* op) {
     if (want32) op->d_G32.alloc((size_t)ne * op->gstride32); else op->d_G32.release();
     int64_t tot = (int64_t)ne * nq;
     hex_geom_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
-        ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, f->d_kappa.p,
-        f->has_K6 ? f->d_K6.p : nullptr, op->has_mass ? f->d_mu.p : nullptr, op->d_G64.p, op->gstride64, want32 ? op->d_G32.p : nullptr, op->gstride32,
-        deform_view(sp->mesh));
+        ne, sp->nq1, sp->mesh->d_X.p, sp->mesh->d_el.p, sp->d_gx.p, sp->d_gw.p, kap, K6,
+        op->lap_pp ? (op->has_mass ? op->lap_pp : nullptr) : mu, op->d_G64.p, op->gstride64,
+        want32 ? op->d_G32.p : nullptr, op->gstride32, deform_view(sp->mesh), op->lap_pp);
     check_kernel(sp->ctx, "hex_geom_kernel");
     upload_const_tables(sp);
     op->hex_per_sm[0][0] = hex_occupancy_dispatch<double, 0>(op, op->gstride64);

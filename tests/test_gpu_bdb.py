@@ -169,7 +169,9 @@ def test_bdb_symmetric_form_solves_like_laplace(gpu, hexes, p):
     one = 0.0 * gpu.x + 1.0
     ag = gpu.BilinearForm(one * gpu.grad(u) * gpu.grad(v) * gpu.dx + gpu.CoefficientFunction(mu) * u * v * gpu.dx,
                           nonassemble=True, precision="mixed").Assemble()
-    assert ag.mat.Info()["hex_variant_fp64"] == 7
+    # hexes: a form of Laplace type takes the standard kernels (per-point metric
+    # variants 0-3 or the tensor-core form); tets keep the B^T D B kernel
+    assert (ag.mat.Info()["hex_variant_fp64"] in (0, 1)) if hexes else ag.mat.Info()["hex_variant_fp64"] == 7
     al = gpu.BilinearForm(gpu.grad(u) * gpu.grad(v) * gpu.dx + gpu.CoefficientFunction(mu) * u * v * gpu.dx,
                           nonassemble=True, precision="mixed").Assemble()
     f = gpu.LinearForm(gpu.CoefficientFunction(np.random.default_rng(68).uniform(-1, 1, m.ne)) * v * gpu.dx).Assemble()
@@ -208,3 +210,55 @@ def test_bdb_assembled(gpu, hexes, p, jit, pointwise):
     Ax = O.spmv(rp, ci, va, x)
     lhs, rhs = z @ Ax, x @ S.apply_bdb(z, Dt, rule=ref if pointwise else None)
     assert abs(lhs - rhs) <= 1e-11 * np.linalg.norm(z) * np.linalg.norm(Ax)
+
+
+@pytest.mark.parametrize("pointwise,p", [(False, 3), (True, 3), (True, 5)])
+def test_bdb_laplace_type_takes_standard_kernels(gpu, pointwise, p, monkeypatch):
+    """A generic hex form whose D is diag(mu, K) with K symmetric runs on the
+    standard kernels (the autotuned variants; per-element records on affine
+    meshes when D is per element) and matches the oracle's B^T D B apply and the
+    B^T D B kernel itself (GH1_BDB_STANDARD=0).  Per point: (1 + x) grad.grad +
+    K grad.grad + r u v from the front end; per element: D set through the C ABI."""
+    m = _mesh(True, 3, 0.0)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    u, v = fes.TnT()
+    rng = np.random.default_rng(90)
+    A = rng.normal(size=(3, 3)) * 0.2
+    Ks = np.eye(3) + A @ A.T
+    kap = (1.0 + gpu.x) if pointwise else gpu.CoefficientFunction(lognormal(m.ne, 0.5, 91))
+    terms = [kap * gpu.grad(u) * gpu.grad(v) * gpu.dx,
+             gpu.InnerProduct(gpu.CoefficientFunction(Ks) * gpu.grad(u), gpu.grad(v)) * gpu.dx,
+             gpu.CoefficientFunction(rng.uniform(0.5, 2.0, m.ne)) * u * v * gpu.dx]
+    ref, xyz = _rule(gpu, fes)
+    D = _oracle_D(terms, m.ne, xyz if pointwise else None)
+    S = O.OracleSpace(m.points, m.elements, p)
+    x = np.random.default_rng(92).normal(size=fes.ndof)
+    yo = S.apply_bdb(x, D, rule=ref if pointwise else None)
+    sc = np.abs(yo).max()
+
+    def make():
+        if pointwise:
+            return gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True, precision="fp32").Assemble().mat, None
+        ctx = fes.ctx
+        h = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_form_create(fes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(h)))
+        Dc = np.ascontiguousarray(D, dtype=np.float64)
+        ctx.check(ctx.lib.gh1_form_set_bdb(h, Dc.ctypes.data_as(ctypes.c_void_p), 0, _lib.GH1_MEM_HOST))
+        op = ctypes.c_void_p()
+        ctx.check(ctx.lib.gh1_matfree_create(h, 3, ctypes.byref(op)))
+        ctx.lib.gh1_form_free(h)  # the operator keeps the form alive
+        return C.BilinearFormApplication(ctx, op, fes.ndof, fes), None
+
+    class _A:
+        pass
+    for standard in (True, False):
+        if not standard:
+            monkeypatch.setenv("GH1_BDB_STANDARD", "0")
+        mat, _ = make()
+        a = _A()
+        a.mat = mat
+        info = mat.Info()["hex_variant_fp64"]
+        assert (info in (0, 1)) if standard else (info in (7, 8))
+        assert np.abs(_apply(gpu, a, x, torch.float64) - yo).max() <= 1e-12 * sc
+        assert np.abs(_apply(gpu, a, x, torch.float32) - yo).max() <= 2e-5 * sc
+    monkeypatch.delenv("GH1_BDB_STANDARD")
