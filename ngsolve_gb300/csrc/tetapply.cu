@@ -104,7 +104,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
   const size_t dsize = (size_t)nlocp * Rs;
   for (int r = tid; r < Rp; r += TET_TT) sW[r] = W[r];
   int loaded = -1;
-  double acc = 0;  // energy x^T A x of this thread's quadrature terms
+  T acc = 0;  // energy x^T A x of this thread's quadrature terms (working precision: FP64 is scarce)
   for (int t = t0; t < t1; t++) {
     const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
     __syncthreads();  // the previous tile is done with the shared arrays
@@ -169,7 +169,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
       const T vx = w * (g[0] * ux + g[3] * uy + g[4] * uz);
       const T vy = w * (g[3] * ux + g[1] * uy + g[5] * uz);
       const T vz = w * (g[4] * ux + g[5] * uy + g[2] * uz);
-      acc += (double)(ux * vx + uy * vy + uz * vz);
+      if (partial) acc += ux * vx + uy * vy + uz * vz;
       *px = vx; *py = vy; *pz = vz;
     }
     if (MASS) {
@@ -177,7 +177,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
         const int q = k / TET_TE, e = k % TET_TE;
         T* pm = sP + (size_t)(3 * nq + q) * TET_TE + e;
         const T u = *pm, vm = sW[3 * nq + q] * sG[e * 7 + 6] * u;
-        acc += (double)(u * vm);
+        if (partial) acc += u * vm;
         *pm = vm;
       }
     }
@@ -209,7 +209,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
       }
     }
   }
-  if (partial) block_reduce_finish(acc, partial, counter, energy);
+  if (partial) block_reduce_finish((double)acc, partial, counter, energy);
 }
 
 // ---- chunked variant (orders whose whole class table does not fit in shared memory)
@@ -239,7 +239,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
   const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
   const int ni = nlocp / 16;  // block-uniform
-  double acc = 0;
+  T acc = 0;  // energy of this thread's quadrature terms, in the working precision
   for (int t = t0; t < t1; t++) {
     const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
     __syncthreads();
@@ -304,7 +304,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
           const T vx = w * (g[0] * ux + g[3] * uy + g[4] * uz);
           const T vy = w * (g[3] * ux + g[1] * uy + g[5] * uz);
           const T vz = w * (g[4] * ux + g[5] * uy + g[2] * uz);
-          acc += (double)(ux * vx + uy * vy + uz * vz);
+          if (partial) acc += ux * vx + uy * vy + uz * vz;
           *px = vx; *py = vy; *pz = vz;
         }
       } else {
@@ -312,7 +312,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
           const int q = k / TET_TE, e = k % TET_TE;
           T* pm = sP + (size_t)q * TET_TE + e;
           const T u = *pm, vm = Wm[(cc - ncg) * TET_QC + q] * sG[e * 7 + 6] * u;
-          acc += (double)(u * vm);
+          if (partial) acc += u * vm;
           *pm = vm;
         }
       }
@@ -341,7 +341,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
       }
     }
   }
-  if (partial) block_reduce_finish(acc, partial, counter, energy);
+  if (partial) block_reduce_finish((double)acc, partial, counter, energy);
 }
 
 template <class T>
@@ -718,7 +718,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
   const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
   const int ni = nlocp / 16;  // block-uniform
-  double acc = 0;
+  T acc = 0;  // energy of this thread's quadrature terms, in the working precision
   for (int t = t0; t < t1; t++) {
     const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
     __syncthreads();
@@ -783,7 +783,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
 #pragma unroll
         for (int r = 0; r < 4; r++) {
           const T o = m[4 * r] * in[0] + m[4 * r + 1] * in[1] + m[4 * r + 2] * in[2] + m[4 * r + 3] * in[3];
-          acc += (double)(in[r] * o);
+          if (partial) acc += in[r] * o;
           sP[(size_t)(r * TET_QC + q) * TET_TE + e] = o;
         }
       }
@@ -812,7 +812,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
       }
     }
   }
-  if (partial) block_reduce_finish(acc, partial, counter, energy);
+  if (partial) block_reduce_finish((double)acc, partial, counter, energy);
 }
 
 // Tb[c][cc][i][r] from the values and reference gradients at the degree-2p rule
