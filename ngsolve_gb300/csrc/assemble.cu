@@ -103,7 +103,7 @@ __global__ void tet_assemble_kernel(int ne, int nloc, const int* __restrict__ el
     int row = eldofs[(size_t)e * nloc + i], col = eldofs[(size_t)e * nloc + j];
     int64_t pos = find_col(rowptr, colind, row, col);
     if (pos < 0) { atomicExch(bad, 1); continue; }
-    atomicAdd(vals + pos, k);
+    red_add(vals + pos, k);
   }
 }
 
@@ -149,7 +149,7 @@ __global__ void hex_assemble_kernel(int ne, int N, const int* __restrict__ tdof,
     if ((dt < 0) != (du < 0)) s = -s;
     int64_t pos = find_col(rowptr, colind, dt & 0x7fffffff, du & 0x7fffffff);
     if (pos < 0) { atomicExch(bad, 1); continue; }
-    atomicAdd(vals + pos, s);
+    red_add(vals + pos, s);
   }
 }
 
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) hex_assemble_sf_kernel(int ne, int N, con
       if ((dt < 0) != (du < 0)) s = -s;
       const int64_t pos = find_col(rowptr, colind, dt & 0x7fffffff, du & 0x7fffffff);
       if (pos < 0) { atomicExch(bad, 1); continue; }
-      atomicAdd(vals + pos, s);
+      red_add(vals + pos, s);
     }
   }
 }
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(128) hex_rhs_kernel(int ne, int N, const int* 
       for (int i = 0; i < N; i++) s += B[i * N + a] * u[i * N2 + bc];
       s *= f[e];
       const int d = tdof[(size_t)e * tstride + t];
-      atomicAdd(b + (d & 0x7fffffff), d < 0 ? -s : s);
+      red_add(b + (d & 0x7fffffff), d < 0 ? -s : s);
     }
     __syncthreads();
   }
@@ -383,11 +383,11 @@ __global__ void tet_rhs_kernel(int ne, int nloc, int nqm, const int* __restrict_
                         Jq[2] * (Jq[3] * Jq[7] - Jq[4] * Jq[6]);
       s += rulem[4 * q + 3] * fabs(dq) * tc[(size_t)q * nloc + i];
     }
-    atomicAdd(b + eldofs[id], f[e] * s);
+    red_add(b + eldofs[id], f[e] * s);
     return;
   }
   for (int q = 0; q < nqm; q++) s += rulem[4 * q + 3] * tc[(size_t)q * nloc + i];
-  atomicAdd(b + eldofs[id], f[e] * fabs(det) * s);
+  red_add(b + eldofs[id], f[e] * fabs(det) * s);
 }
 
 void rhs_elementwise(gh1_space* sp, const double* f, double* b) {

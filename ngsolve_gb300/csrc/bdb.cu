@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) hex_bdb_diag_kernel(int ne, int N, const 
         const int f = sel(m, 1);
         for (int i = 0; i < N; i++) v += fac(f, i, a) * g[m * N3 + i * N2 + bc];
       }
-      atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
+      red_add(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
     }
     __syncthreads();
   }

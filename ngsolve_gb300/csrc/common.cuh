@@ -290,6 +290,15 @@ struct gh1_pre {
 };
 
 namespace gh1 {
+// *p += v as a reduction (red.global: nothing is returned, the add completes in
+// L2 without a round trip to the SM): the scatter of every apply, assembly and
+// diagonal kernel.  atomicAdd with its result unused measured slower here.
+__device__ __forceinline__ void red_add(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void red_add(double* p, double v) {
+  asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
 // form references held by operators (api.cu)
 void form_retain(gh1_form* f);
 void form_release(gh1_form* f);

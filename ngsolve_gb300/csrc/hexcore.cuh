@@ -46,7 +46,7 @@ __device__ __forceinline__ void group_sync(int gid) {
 }
 
 template <class T>
-__device__ __forceinline__ void atomic_add_t(T* p, T v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_t(T* p, T v) { red_add(p, v); }
 
 // End-of-kernel reduction of one double per thread into partial[blockIdx.x];
 // the last block to finish sums all partials into *out and resets the counter.

@@ -486,7 +486,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
             const int dof = d & 0x7fffffff;
             const float v = __int_as_float(__float_as_int(h ? v1 : v0) ^ (d & (int)0x80000000));
             if (dof >= first_cell) y[dof] = v;  // element-interior DOF: single writer
-            else atomicAdd(y + dof, v);
+            else red_add(y + dof, v);
           }
         }
       }
@@ -652,8 +652,8 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
           ya[dof] = wa;
           if (rb >= 0) yb[dof] = wb;
         } else {
-          atomicAdd(ya + dof, wa);
-          if (rb >= 0) atomicAdd(yb + dof, wb);
+          red_add(ya + dof, wa);
+          if (rb >= 0) red_add(yb + dof, wb);
         }
       }
       group_sync<G>(gid);
@@ -975,13 +975,13 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
             const int dof = d0[j] & 0x7fffffff;
             const float v = __int_as_float(__float_as_int(o0) ^ (d0[j] & (int)0x80000000));
             if (dof >= first_cell) y[dof] = v;
-            else atomicAdd(y + dof, v);
+            else red_add(y + dof, v);
           }
           if (d1[j] != -1) {
             const int dof = d1[j] & 0x7fffffff;
             const float v = __int_as_float(__float_as_int(o1) ^ (d1[j] & (int)0x80000000));
             if (dof >= first_cell) y[dof] = v;
-            else atomicAdd(y + dof, v);
+            else red_add(y + dof, v);
           }
         }
       }

@@ -331,7 +331,7 @@ hex_apply_tc_kernel(int ne, const int* __restrict__ tdof, int tstride, const flo
       const int dof = d & 0x7fffffff;
       const float val = d < 0 ? -obuf[i] : obuf[i];
       if (dof >= first_cell) y[dof] = val;
-      else atomicAdd(y + dof, val);
+      else red_add(y + dof, val);
     }
     __syncthreads();  // idx / obuf / A0 are rewritten by the next tile
   }

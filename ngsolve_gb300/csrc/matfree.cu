@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) hex_diag_kernel(int ne, int N, const int*
       double v = 0;
       for (int m = 0; m < nc; m++)
         for (int i = 0; i < N; i++) v += wi[m] * fac(fi[m], i, a) * g[m * N3 + i * N2 + bc];
-      atomicAdd(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
+      red_add(diag + (tdof[(size_t)e * tstride + t] & 0x7fffffff), v);
     }
     __syncthreads();
   }
@@ -447,7 +447,7 @@ tet_apply_kernel(int ne, int nloc, int nq, int nqm, const int* __restrict__ eldo
         const double* tm = tabm + (size_t)c * nqm * nloc;
         for (int q = 0; q < nqm && q < 128; q++) r += (T)(tm[(size_t)q * nloc + i] * (double)sv[w][4 * q + 3]);
       }
-      atomicAdd(y + dn[i], r);
+      red_add(y + dn[i], r);
     }
     __syncwarp();
   }
@@ -466,7 +466,7 @@ __global__ void tet_diag_kernel(int ne, int nloc, const int* __restrict__ eldofs
   double s = 0;
   for (int b = 0; b < 6; b++) s += Ge[(size_t)e * 6 + b] * Sc[((size_t)b * nloc + i) * nloc + i];
   if (Me) s += Me[e] * Sc[((size_t)6 * nloc + i) * nloc + i];
-  atomicAdd(diag + eldofs[id], s);
+  red_add(diag + eldofs[id], s);
 }
 
 __global__ void tet_graddot_kernel(int ne, int nloc, int nq, const int* __restrict__ eldofs, const uint8_t* __restrict__ cls,

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) block_apply_kernel(int64_t nblocks, int s
       T acc = 0;
       if (r < n)
         for (int c = 0; c < n; c++) acc += M[(size_t)c * n + r] * xs[c];
-      if (r < n) atomicAdd(y + dofs[o + r], s * acc);
+      if (r < n) red_add(y + dofs[o + r], s * acc);
     }
     __syncwarp();
   }

@@ -204,7 +204,7 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
 #pragma unroll
         for (int c = 0; c < 4; c++) {
           const int e = 4 * cg + c;
-          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+          if (e < cnt) red_add(y + sDof[i * TET_TE + e], b[u][c]);
         }
       }
     }
@@ -336,7 +336,7 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
 #pragma unroll
         for (int c = 0; c < 4; c++) {
           const int e = 4 * cg + c;
-          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+          if (e < cnt) red_add(y + sDof[i * TET_TE + e], b[u][c]);
         }
       }
     }
@@ -807,7 +807,7 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
 #pragma unroll
         for (int c = 0; c < 4; c++) {
           const int e = 4 * cg + c;
-          if (e < cnt) atomicAdd(y + sDof[i * TET_TE + e], b[u][c]);
+          if (e < cnt) red_add(y + sDof[i * TET_TE + e], b[u][c]);
         }
       }
     }
@@ -939,7 +939,7 @@ __global__ void tet_bdb_diag_kernel(int ne, int nloc, int nlocp, int ncb, int nq
       for (int k = 0; k < 4; k++) t += bv[r] * m[4 * r + k] * bv[k];
     s += w * t;
   }
-  atomicAdd(diag + eldofs[id], s);
+  red_add(diag + eldofs[id], s);
 }
 
 void tet_bdb_diag(gh1_op* op, double* diag) {
@@ -986,7 +986,7 @@ __global__ void tet_bdb_assemble_kernel(int ne, int nloc, int nlocp, int ncb, in
       if (colind[mid] < col) lo = mid + 1; else hi = mid - 1;
     }
     if (pos < 0) { atomicExch(bad, 1); continue; }
-    atomicAdd(vals + pos, k);
+    red_add(vals + pos, k);
   }
 }
 

@@ -21,6 +21,7 @@
 // product is hi*hi + lo*hi + hi*lo (3xTF32), accumulated in FP32 in tensor memory.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 #include "common.cuh"
 #include "hexcore.cuh"
@@ -38,12 +39,16 @@ struct TetTcCfg {
   static constexpr int N2 = (NLOC + 15) / 16 * 16; // backward N
   static constexpr int C2 = N1;                     // TMEM column of the backward accumulator
   static constexpr int TCOLS = (N1 + N2) <= 32 ? 32 : (N1 + N2) <= 64 ? 64 : (N1 + N2) <= 128 ? 128 : 256;
-  // float offsets in dynamic shared memory; A1 and A2 share their space (A1 is
-  // read by the first product, which completes before A2 is written, and A2 by
-  // the second, which completes before the next tile's A1)
+  // the backward product runs in two K chunks of V (columns [0, KA) and
+  // [KA, K2)), so its operand needs no more room than the forward one: two
+  // CTAs fit on an SM and one's products overlap the other's gather / scatter
+  static constexpr int KA = K2 <= K1 ? K2 : K1;     // first chunk (a multiple of 8)
+  static constexpr int KB = K2 - KA;                // second chunk (0: one chunk)
+  // float offsets in dynamic shared memory; A1 and the A2 chunks share their
+  // space (each is read by its product, which completes before the next is written)
   static constexpr int A1 = 0;                      // [hi, lo][128][K1]
-  static constexpr int A2 = 0;                      // [hi, lo][128][K2]
-  static constexpr int AW = 2 * 128 * (K1 > K2 ? K1 : K2);
+  static constexpr int A2 = 0;                      // [hi, lo][128][KA] and then [hi, lo][128][KB]
+  static constexpr int AW = 2 * 128 * (K1 > KA ? K1 : KA);
   static constexpr int T1 = AW;                     // [hi, lo][N1][K1]
   static constexpr int T2 = T1 + 2 * N1 * K1;       // [hi, lo][N2][K2]
   static constexpr int W = T2 + 2 * N2 * K2;        // weights [R] (padded to 4)
@@ -72,18 +77,20 @@ __device__ __forceinline__ void tt_mma(uint32_t d, uint64_t a, uint64_t b, uint3
                "l"(a), "l"(b), "r"(idesc), "r"(acc)
                : "memory");
 }
-// D = A * T^T over K (K/8 steps of 8), 3xTF32: A, T are [hi][rows][K] then [lo]
-template <int K, int N, int ROWS_T>
+// D (+)= A * T^T over the K columns [K0, K0 + KC) of T (KC/8 steps of 8),
+// 3xTF32: A is [hi][128][KC] then [lo], T is [hi][ROWS_T][KT] then [lo];
+// ACC: add to D from the first step on
+template <int KC, int KT, int K0, int N, int ROWS_T, bool ACC>
 __device__ __forceinline__ void tt_gemm(uint32_t d, const float* A, const float* T) {
   const uint32_t idesc = tt_idesc<N>();
-  const float* Al = A + 128 * K;
-  const float* Tl = T + ROWS_T * K;
+  const float* Al = A + 128 * KC;
+  const float* Tl = T + ROWS_T * KT;
 #pragma unroll
-  for (int s = 0; s < K / 8; s++) {
-    const int o = s * 64;  // two core matrices (2 x 32 floats) per K step of 8
-    tt_mma(d, tt_desc<K>(A + o), tt_desc<K>(T + o), idesc, s > 0 ? 1u : 0u);
-    tt_mma(d, tt_desc<K>(Al + o), tt_desc<K>(T + o), idesc, 1u);
-    tt_mma(d, tt_desc<K>(A + o), tt_desc<K>(Tl + o), idesc, 1u);
+  for (int s = 0; s < KC / 8; s++) {
+    const int o = s * 64, ot = (K0 / 8 + s) * 64;  // two core matrices (2 x 32 floats) per K step of 8
+    tt_mma(d, tt_desc<KC>(A + o), tt_desc<KT>(T + ot), idesc, (ACC || s > 0) ? 1u : 0u);
+    tt_mma(d, tt_desc<KC>(Al + o), tt_desc<KT>(T + ot), idesc, 1u);
+    tt_mma(d, tt_desc<KC>(A + o), tt_desc<KT>(Tl + ot), idesc, 1u);
   }
 }
 __device__ __forceinline__ void tt_ld16(uint32_t taddr, float* v) {
@@ -111,7 +118,7 @@ __device__ __forceinline__ void tt_put4(float* A, int r, int k, const float* v) 
 constexpr int TT_THREADS = 256;
 
 template <int P>
-__global__ void __launch_bounds__(TT_THREADS)
+__global__ void __launch_bounds__(TT_THREADS, 2)
 tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
               const float* __restrict__ Ge, const double* __restrict__ D64, int nlocp, int Rs,
               const double* __restrict__ W64, const float* __restrict__ x, float* __restrict__ y, double* partial,
@@ -208,25 +215,26 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
 #pragma unroll
     for (int j = 0; j < H1; j += 4) tt_put4<K1>(sA1, m, half * H1 + j, xv + j);
     // ---- P = X D_c ------------------------------------------------------------------
-    issue_stage([&] { tt_gemm<K1, N1, N1>(tmem, sA1, sT1); });
+    issue_stage([&] { tt_gemm<K1, K1, 0, N1, N1, false>(tmem, sA1, sT1); });
     if (!(ok = wait_stage())) break;
     float pv[N1];
 #pragma unroll
     for (int c = 0; c < N1; c += 16) tt_ld16(tl + c, pv + c);
-    // ---- metric at the points, into row m of A2: this half writes the column
-    // groups [4j, 4j+4) with j = half (mod 2); column r = component * nq + point
-    {
-      float g[6];
+    // ---- metric at the points, into row m of the A2 chunk: this half writes the
+    // column groups [4j, 4j+4) with j = half (mod 2); column r = component * nq + point
+    float g[6];
 #pragma unroll
-      for (int c = 0; c < 6; c++) g[c] = act ? __ldg(Ge + (size_t)e * 6 + c) : 0.f;
-      float en = 0.f;
+    for (int c = 0; c < 6; c++) g[c] = act ? __ldg(Ge + (size_t)e * 6 + c) : 0.f;
+    float en = 0.f;
+    auto transform = [&](auto k0c, auto kcc) {  // columns [K0, K0 + KC) into an operand with KC columns
+      constexpr int K0 = decltype(k0c)::value, KC = decltype(kcc)::value;
 #pragma unroll
-      for (int j = 0; j < K2 / 4; j++) {
-        if ((j & 1) != half) continue;
+      for (int j = 0; j < KC / 4; j++) {
+        if (((K0 / 4 + j) & 1) != half) continue;
         float vv[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          const int r = 4 * j + k;
+          const int r = K0 + 4 * j + k;
           float v = 0.f;
           if (r < R) {
             const int q = r % NQ, c = r / NQ;
@@ -235,16 +243,23 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
             const float gy = c == 0 ? g[3] : c == 1 ? g[1] : g[5];
             const float gz = c == 0 ? g[4] : c == 1 ? g[5] : g[2];
             v = sW[q] * (gx * ux + gy * uy + gz * uz);
-            en += pv[r] * v;
+            if (partial) en += pv[r] * v;
           }
           vv[k] = v;
         }
-        tt_put4<K2>(sA2, m, 4 * j, vv);
+        tt_put4<KC>(sA2, m, 4 * j, vv);
       }
-      acc += (double)en;
+    };
+    // ---- Y = V D_c^T in its K chunks (the next tile's gather overlaps the last),
+    // then the scatter ----------------------------------------------------------------
+    transform(std::integral_constant<int, 0>(), std::integral_constant<int, C::KA>());
+    issue_stage([&] { tt_gemm<C::KA, K2, 0, N2, N2, false>(tmem + C::C2, sA2, sT2); });
+    if constexpr (C::KB > 0) {
+      if (!(ok = wait_stage())) break;
+      transform(std::integral_constant<int, C::KA>(), std::integral_constant<int, C::KB>());
+      issue_stage([&] { tt_gemm<C::KB, K2, C::KA, N2, N2, true>(tmem + C::C2, sA2, sT2); });
     }
-    // ---- Y = V D_c^T (the next tile's gather overlaps it), then the scatter ----------
-    issue_stage([&] { tt_gemm<K2, N2, N2>(tmem + C::C2, sA2, sT2); });
+    if (partial) acc += (double)en;
     if (tile + (int)gridDim.x < ntiles) gather(tile + gridDim.x);
     if (!(ok = wait_stage())) break;
     float yv[N2];
@@ -254,10 +269,10 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
       constexpr int HS = (NLOC + 1) / 2;
       if (half == 0) {
 #pragma unroll
-        for (int i = 0; i < HS; i++) atomicAdd(y + __ldg(ed + i), yv[i]);
+        for (int i = 0; i < HS; i++) red_add(y + __ldg(ed + i), yv[i]);
       } else {
 #pragma unroll
-        for (int i = HS; i < NLOC; i++) atomicAdd(y + __ldg(ed + i), yv[i]);
+        for (int i = HS; i < NLOC; i++) red_add(y + __ldg(ed + i), yv[i]);
       }
     }
   }
