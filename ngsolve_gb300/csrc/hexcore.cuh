@@ -3,6 +3,8 @@
 // group barriers and votes, the end-of-kernel energy reduction, and the bulk-copy
 // (TMA) / mbarrier helpers of the pipelined element loops.
 #pragma once
+#include <algorithm>
+#include <cmath>
 #include "common.cuh"
 
 namespace gh1 {
@@ -11,6 +13,36 @@ namespace gh1 {
 // tables of every order
 constexpr int tab_off(int N) { return N <= 2 ? 0 : tab_off(N - 1) + (N - 1) * (N - 1); }
 constexpr int TAB_TOTAL = tab_off(MAX_HEX_ORDER + 2);
+// offset of the N per-point entries of order p = N-1 in the tables of every order
+// that hold one value per 1D point (rule weights, even-odd coefficients)
+constexpr int eo_off(int N) { return N * (N - 1) / 2 - 1; }
+
+// Even-odd coefficients of the vertex pair of the N x N tables B = psi_a(x_q),
+// D = psi_a'(x_q): eo[0..3][q] = (B[q][0] + B[q][1]) / 2, (B[q][0] - B[q][1]) / 2,
+// (D[q][0] + D[q][1]) / 2, (D[q][0] - D[q][1]) / 2.  Returns the largest
+// deviation from the reflection symmetry the even-odd contractions rely on
+// (psi_0 <-> psi_1 and psi_c -> (-1)^c psi_c under x -> 1-x), relative to the
+// tables' scale.
+inline double hex_eo_coefficients(const double* B, const double* D, int N, double eo[4][16]) {
+  double scale = 0, dev = 0;
+  for (int q = 0; q < N; q++)
+    for (int c = 0; c < N; c++) {
+      const int qr = N - 1 - q, cr = c < 2 ? 1 - c : c;
+      const double sg = c < 2 ? 1.0 : ((c % 2) ? -1.0 : 1.0);
+      scale = std::max(scale, std::max(std::fabs(B[q * N + c]), std::fabs(D[q * N + c])));
+      dev = std::max(dev, std::fabs(B[qr * N + c] - sg * B[q * N + cr]));
+      dev = std::max(dev, std::fabs(D[qr * N + c] + sg * D[q * N + cr]));
+    }
+  for (int k = 0; k < 4; k++)
+    for (int q = 0; q < 16; q++) eo[k][q] = 0.0;
+  for (int q = 0; q < N; q++) {
+    eo[0][q] = 0.5 * (B[q * N] + B[q * N + 1]);
+    eo[1][q] = 0.5 * (B[q * N] - B[q * N + 1]);
+    eo[2][q] = 0.5 * (D[q * N] + D[q * N + 1]);
+    eo[3][q] = 0.5 * (D[q * N] - D[q * N + 1]);
+  }
+  return scale > 0 ? dev / scale : dev;
+}
 
 // ---------------------------------------------------------------------------
 // element geometry (FP64)

@@ -80,17 +80,112 @@ __device__ __forceinline__ f2 bcast(float t) {
   asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(t));
   return r;
 }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// t (+)= c x: the first term of an unrolled sum starts it with a multiply
+__device__ __forceinline__ f2 mac2(bool first, float c, f2 x, f2 t) { return first ? mul2(bcast(c), x) : fma2(bcast(c), x, t); }
 
-// resident 128-thread blocks per SM the register allocation must allow: the
-// largest count each variant compiles to without spills (p=4: 4 blocks = 128
-// registers with the G tile in shared memory, 5 blocks = 96 with direct G loads)
+// Even-odd coefficients of the vertex pair, (B[q][0] +- B[q][1]) / 2 and
+// (D[q][0] +- D[q][1]) / 2 at offset eo_off(N): the packed contractions below use
+// the reflection symmetry of the 1D tables on the Gauss points (psi_0 <-> psi_1,
+// psi_c -> (-1)^c psi_c under x -> 1-x; checked when the tables are uploaded), so
+// B u at the points q and N-1-q is (even part) +- (odd part) and every 1D
+// contraction takes about a third fewer packed FMAs at N = 5.
+__constant__ float c_EOp[4][64];
+
+// ob[q] = sum_c B[q][c] u[c], od[q] = sum_c D[q][c] u[c] (either may be skipped)
+template <int N, bool WB, bool WD>
+__device__ __forceinline__ void eo2_fwd(const f2* u, f2* ob, f2* od) {
+  constexpr int O = tab_off(N), W = eo_off(N), M = N / 2;
+  const f2 s = add2(u[0], u[1]), d = sub2(u[0], u[1]);
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    f2 eb = 0, obb = 0, ed = 0, odd = 0;
+    if (WB) { eb = mul2(bcast(c_EOp[0][W + q]), s); obb = mul2(bcast(c_EOp[1][W + q]), d); }
+    if (WD) { ed = mul2(bcast(c_EOp[2][W + q]), s); odd = mul2(bcast(c_EOp[3][W + q]), d); }
+#pragma unroll
+    for (int c = 2; c < N; c++) {
+      if (c % 2 == 0) {
+        if (WB) eb = fma2(bcast(c_Bp[O + q * N + c]), u[c], eb);
+        if (WD) ed = fma2(bcast(c_Dp[O + q * N + c]), u[c], ed);
+      } else {
+        if (WB) obb = fma2(bcast(c_Bp[O + q * N + c]), u[c], obb);
+        if (WD) odd = fma2(bcast(c_Dp[O + q * N + c]), u[c], odd);
+      }
+    }
+    if (WB) { ob[q] = add2(eb, obb); ob[N - 1 - q] = sub2(eb, obb); }
+    if (WD) { od[q] = add2(ed, odd); od[N - 1 - q] = sub2(odd, ed); }
+  }
+  if (N % 2 == 1) {  // middle point: B keeps its even part, D its odd part
+    constexpr int q = M;
+    f2 eb = 0, odd = 0;
+    if (WB) eb = mul2(bcast(c_EOp[0][W + q]), s);
+    if (WD) odd = mul2(bcast(c_EOp[3][W + q]), d);
+#pragma unroll
+    for (int c = 2; c < N; c++) {
+      if (c % 2 == 0) { if (WB) eb = fma2(bcast(c_Bp[O + q * N + c]), u[c], eb); }
+      else { if (WD) odd = fma2(bcast(c_Dp[O + q * N + c]), u[c], odd); }
+    }
+    if (WB) ob[q] = eb;
+    if (WD) od[q] = odd;
+  }
+}
+
+// out[a] (+)= sum_q B[q][a] v[q] (WANT_D false) or sum_q D[q][a] v[q] (WANT_D true)
+template <int N, bool WANT_D, bool ACC>
+__device__ __forceinline__ void eo2_bwd(const f2* v, f2* out) {
+  constexpr int O = tab_off(N), W = eo_off(N), M = N / 2;
+  f2 vs[M > 0 ? M : 1], vd[M > 0 ? M : 1];
+#pragma unroll
+  for (int k = 0; k < M; k++) { vs[k] = add2(v[k], v[N - 1 - k]); vd[k] = sub2(v[k], v[N - 1 - k]); }
+  // a = 0, 1: out[0] = P + Q, out[1] = P - Q
+  f2 P = 0, Q = 0;
+#pragma unroll
+  for (int k = 0; k < M; k++) {
+    if (!WANT_D) { P = mac2(k == 0, c_EOp[0][W + k], vs[k], P); Q = mac2(k == 0, c_EOp[1][W + k], vd[k], Q); }
+    else { P = mac2(k == 0, c_EOp[2][W + k], vd[k], P); Q = mac2(k == 0, c_EOp[3][W + k], vs[k], Q); }
+  }
+  if (N % 2 == 1) {
+    if (!WANT_D) P = mac2(M == 0, c_Bp[O + M * N], v[M], P);
+    else Q = mac2(M == 0, c_Dp[O + M * N], v[M], Q);
+  }
+  out[0] = ACC ? add2(out[0], add2(P, Q)) : add2(P, Q);
+  out[1] = ACC ? add2(out[1], sub2(P, Q)) : sub2(P, Q);
+#pragma unroll
+  for (int a = 2; a < N; a++) {
+    // B: even a takes vs (and the middle point), odd a takes vd; D: the reverse
+    const bool sym = WANT_D ? (a % 2 == 1) : (a % 2 == 0);
+    f2 t = ACC ? out[a] : (f2)0;
+#pragma unroll
+    for (int k = 0; k < M; k++)
+      t = mac2(!ACC && k == 0, WANT_D ? c_Dp[O + k * N + a] : c_Bp[O + k * N + a], sym ? vs[k] : vd[k], t);
+    if (N % 2 == 1 && sym) t = mac2(!ACC && M == 0, WANT_D ? c_Dp[O + M * N + a] : c_Bp[O + M * N + a], v[M], t);
+    out[a] = t;
+  }
+}
+
+// resident blocks per SM the register allocation must allow, measured per
+// variant (p=4: 4 blocks = 128 registers with the G tile in shared memory or a
+// metric per element, 5 blocks = 96 with direct G loads; p=6: 3 blocks = 168)
 constexpr int pair_min_blocks(int N, bool mass, int gm) {
   return N == 2   ? 6
          : N == 3 ? (mass ? (gm ? 5 : 4) : (gm ? 6 : 5))
          : N == 4 ? (mass ? (gm ? 5 : 4) : 5)
-         : N == 5 ? (mass ? (gm ? 4 : 3) : (gm ? 5 : 4))
+         : N == 5 ? (mass ? (gm ? 4 : 3) : (gm == 1 ? 5 : 4))
          : N == 6 ? 2
-                  : 2;
+                  : (mass && gm == 0 ? 2 : 3);
+}
+
+// Even-odd (reflection) form of the 1D contractions, per order and metric mode,
+// as measured on the 1-16 M DOF operators: it takes about a third fewer packed
+// FMAs and pays where the kernel is issue-bound (p=4 with a metric per element
+// or a staged G tile, p >= 5); the per-point metric loaded directly at p <= 4 runs
+// faster with the plain form.
+constexpr bool pair_eo(int N, int GM) {
+  return N == 3 ? GM == 0 : N == 4 ? GM != 2 : N == 5 ? GM != 1 : true;
 }
 
 // Work-array layouts.  Element index (a,b,c) sits at a*SA + b*SB + c in the s
@@ -136,8 +231,8 @@ struct PairCfg {
 
 // forward chain on packed pairs (see hex_forward in matfree.cu): coefficients in
 // su[(a*N+b)*N+c] -> reference gradient at the points of lane (j,k).  (pa, pk):
-// this lane's stage-2 pair.
-template <int N, bool WANT_U>
+// this lane's stage-2 pair.  EO: the 1D contractions in even-odd form.
+template <int N, bool WANT_U, bool EO>
 __device__ __forceinline__ void pair_forward(int pl, int pa, int pk, bool active, int gid, const f2* su, f2* s1, f2* s2,
                                              f2* t1, f2* t2, f2* t3, f2* gx, f2* gy, f2* gz, f2* uq) {
   constexpr int G = HexCfg<N>::G, O = tab_off(N);
@@ -147,16 +242,26 @@ __device__ __forceinline__ void pair_forward(int pl, int pa, int pk, bool active
     f2 u[N];
 #pragma unroll
     for (int c = 0; c < N; c++) u[c] = su[(a * N + b) * N + c];
+    if constexpr (EO) {
+      f2 ub[N], ud[N];
+      eo2_fwd<N, true, true>(u, ub, ud);
 #pragma unroll
-    for (int k = 0; k < N; k++) {
-      f2 ub = mul2(bcast(c_Bp[O + k * N]), u[0]), ud = mul2(bcast(c_Dp[O + k * N]), u[0]);
-#pragma unroll
-      for (int c = 1; c < N; c++) {
-        ub = fma2(bcast(c_Bp[O + k * N + c]), u[c], ub);
-        ud = fma2(bcast(c_Dp[O + k * N + c]), u[c], ud);
+      for (int k = 0; k < N; k++) {
+        s1[a * L::SA + b * L::SB + k] = ub[k];
+        s2[a * L::SA + b * L::SB + k] = ud[k];
       }
-      s1[a * L::SA + b * L::SB + k] = ub;
-      s2[a * L::SA + b * L::SB + k] = ud;
+    } else {
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        f2 ub = mul2(bcast(c_Bp[O + k * N]), u[0]), ud = mul2(bcast(c_Dp[O + k * N]), u[0]);
+#pragma unroll
+        for (int c = 1; c < N; c++) {
+          ub = fma2(bcast(c_Bp[O + k * N + c]), u[c], ub);
+          ud = fma2(bcast(c_Dp[O + k * N + c]), u[c], ud);
+        }
+        s1[a * L::SA + b * L::SB + k] = ub;
+        s2[a * L::SA + b * L::SB + k] = ud;
+      }
     }
   }
   group_sync<G>(gid);
@@ -165,18 +270,30 @@ __device__ __forceinline__ void pair_forward(int pl, int pa, int pk, bool active
     f2 v1[N], v2[N];
 #pragma unroll
     for (int b = 0; b < N; b++) { v1[b] = s1[a * L::SA + b * L::SB + k]; v2[b] = s2[a * L::SA + b * L::SB + k]; }
+    if constexpr (EO) {
+      f2 bb[N], db[N], bd[N];
+      eo2_fwd<N, true, true>(v1, bb, db);
+      eo2_fwd<N, true, false>(v2, bd, nullptr);
 #pragma unroll
-    for (int j = 0; j < N; j++) {
-      f2 bb = mul2(bcast(c_Bp[O + j * N]), v1[0]), db = mul2(bcast(c_Dp[O + j * N]), v1[0]), bd = mul2(bcast(c_Bp[O + j * N]), v2[0]);
-#pragma unroll
-      for (int b = 1; b < N; b++) {
-        bb = fma2(bcast(c_Bp[O + j * N + b]), v1[b], bb);
-        db = fma2(bcast(c_Dp[O + j * N + b]), v1[b], db);
-        bd = fma2(bcast(c_Bp[O + j * N + b]), v2[b], bd);
+      for (int j = 0; j < N; j++) {
+        t1[a * L::TA + j * L::TB + k] = bb[j];
+        t2[a * L::TA + j * L::TB + k] = db[j];
+        t3[a * L::TA + j * L::TB + k] = bd[j];
       }
-      t1[a * L::TA + j * L::TB + k] = bb;
-      t2[a * L::TA + j * L::TB + k] = db;
-      t3[a * L::TA + j * L::TB + k] = bd;
+    } else {
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        f2 bb = mul2(bcast(c_Bp[O + j * N]), v1[0]), db = mul2(bcast(c_Dp[O + j * N]), v1[0]), bd = mul2(bcast(c_Bp[O + j * N]), v2[0]);
+#pragma unroll
+        for (int b = 1; b < N; b++) {
+          bb = fma2(bcast(c_Bp[O + j * N + b]), v1[b], bb);
+          db = fma2(bcast(c_Dp[O + j * N + b]), v1[b], db);
+          bd = fma2(bcast(c_Bp[O + j * N + b]), v2[b], bd);
+        }
+        t1[a * L::TA + j * L::TB + k] = bb;
+        t2[a * L::TA + j * L::TB + k] = db;
+        t3[a * L::TA + j * L::TB + k] = bd;
+      }
     }
   }
   group_sync<G>(gid);
@@ -189,27 +306,33 @@ __device__ __forceinline__ void pair_forward(int pl, int pa, int pk, bool active
       w2[a] = t2[a * L::TA + j * L::TB + k];
       w3[a] = t3[a * L::TA + j * L::TB + k];
     }
+    if constexpr (EO) {
+      eo2_fwd<N, WANT_U, true>(w1, uq, gx);
+      eo2_fwd<N, true, false>(w2, gy, nullptr);
+      eo2_fwd<N, true, false>(w3, gz, nullptr);
+    } else {
 #pragma unroll
-    for (int i = 0; i < N; i++) {
-      f2 x = mul2(bcast(c_Dp[O + i * N]), w1[0]), y = mul2(bcast(c_Bp[O + i * N]), w2[0]), z = mul2(bcast(c_Bp[O + i * N]), w3[0]);
-      f2 uu = 0;
-      if (WANT_U) uu = mul2(bcast(c_Bp[O + i * N]), w1[0]);
+      for (int i = 0; i < N; i++) {
+        f2 x = mul2(bcast(c_Dp[O + i * N]), w1[0]), y = mul2(bcast(c_Bp[O + i * N]), w2[0]), z = mul2(bcast(c_Bp[O + i * N]), w3[0]);
+        f2 uu = 0;
+        if (WANT_U) uu = mul2(bcast(c_Bp[O + i * N]), w1[0]);
 #pragma unroll
-      for (int a = 1; a < N; a++) {
-        x = fma2(bcast(c_Dp[O + i * N + a]), w1[a], x);
-        y = fma2(bcast(c_Bp[O + i * N + a]), w2[a], y);
-        z = fma2(bcast(c_Bp[O + i * N + a]), w3[a], z);
-        if (WANT_U) uu = fma2(bcast(c_Bp[O + i * N + a]), w1[a], uu);
+        for (int a = 1; a < N; a++) {
+          x = fma2(bcast(c_Dp[O + i * N + a]), w1[a], x);
+          y = fma2(bcast(c_Bp[O + i * N + a]), w2[a], y);
+          z = fma2(bcast(c_Bp[O + i * N + a]), w3[a], z);
+          if (WANT_U) uu = fma2(bcast(c_Bp[O + i * N + a]), w1[a], uu);
+        }
+        gx[i] = x; gy[i] = y; gz[i] = z;
+        if (WANT_U) uq[i] = uu;
       }
-      gx[i] = x; gy[i] = y; gz[i] = z;
-      if (WANT_U) uq[i] = uu;
     }
   }
   group_sync<G>(gid);
 }
 
 // transposed chain on packed pairs (see hex_backward in matfree.cu)
-template <int N, bool WANT_M>
+template <int N, bool WANT_M, bool EO>
 __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool active, int gid, f2* su, f2* s1, f2* s2,
                                               f2* t1, f2* t2, f2* t3, const f2* vx, const f2* vy, const f2* vz,
                                               const f2* vm) {
@@ -217,20 +340,34 @@ __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool activ
   using L = PairLayout<N>;
   if (active) {
     const int j = pl / N, k = pl % N;
+    if constexpr (EO) {
+      f2 w[N];
+      eo2_bwd<N, true, false>(vx, w);
+      if (WANT_M) eo2_bwd<N, false, true>(vm, w);
 #pragma unroll
-    for (int a = 0; a < N; a++) {
-      f2 w1 = mul2(bcast(c_Dp[O + a]), vx[0]), w2 = mul2(bcast(c_Bp[O + a]), vy[0]), w3 = mul2(bcast(c_Bp[O + a]), vz[0]);
-      if (WANT_M) w1 = fma2(bcast(c_Bp[O + a]), vm[0], w1);
+      for (int a = 0; a < N; a++) t1[a * L::TA + j * L::TB + k] = w[a];
+      eo2_bwd<N, false, false>(vy, w);
 #pragma unroll
-      for (int i = 1; i < N; i++) {
-        w1 = fma2(bcast(c_Dp[O + i * N + a]), vx[i], w1);
-        if (WANT_M) w1 = fma2(bcast(c_Bp[O + i * N + a]), vm[i], w1);
-        w2 = fma2(bcast(c_Bp[O + i * N + a]), vy[i], w2);
-        w3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], w3);
+      for (int a = 0; a < N; a++) t2[a * L::TA + j * L::TB + k] = w[a];
+      eo2_bwd<N, false, false>(vz, w);
+#pragma unroll
+      for (int a = 0; a < N; a++) t3[a * L::TA + j * L::TB + k] = w[a];
+    } else {
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        f2 w1 = mul2(bcast(c_Dp[O + a]), vx[0]), w2 = mul2(bcast(c_Bp[O + a]), vy[0]), w3 = mul2(bcast(c_Bp[O + a]), vz[0]);
+        if (WANT_M) w1 = fma2(bcast(c_Bp[O + a]), vm[0], w1);
+#pragma unroll
+        for (int i = 1; i < N; i++) {
+          w1 = fma2(bcast(c_Dp[O + i * N + a]), vx[i], w1);
+          if (WANT_M) w1 = fma2(bcast(c_Bp[O + i * N + a]), vm[i], w1);
+          w2 = fma2(bcast(c_Bp[O + i * N + a]), vy[i], w2);
+          w3 = fma2(bcast(c_Bp[O + i * N + a]), vz[i], w3);
+        }
+        t1[a * L::TA + j * L::TB + k] = w1;
+        t2[a * L::TA + j * L::TB + k] = w2;
+        t3[a * L::TA + j * L::TB + k] = w3;
       }
-      t1[a * L::TA + j * L::TB + k] = w1;
-      t2[a * L::TA + j * L::TB + k] = w2;
-      t3[a * L::TA + j * L::TB + k] = w3;
     }
   }
   group_sync<G>(gid);
@@ -243,18 +380,29 @@ __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool activ
       r2[j] = t2[a * L::TA + j * L::TB + k];
       r3[j] = t3[a * L::TA + j * L::TB + k];
     }
+    if constexpr (EO) {
+      f2 v[N];
+      eo2_bwd<N, false, false>(r1, v);
+      eo2_bwd<N, true, true>(r2, v);
 #pragma unroll
-    for (int b = 0; b < N; b++) {
-      f2 v1 = mul2(bcast(c_Bp[O + b]), r1[0]), v2 = mul2(bcast(c_Bp[O + b]), r3[0]);
-      v1 = fma2(bcast(c_Dp[O + b]), r2[0], v1);
+      for (int b = 0; b < N; b++) s1[a * L::SA + b * L::SB + k] = v[b];
+      eo2_bwd<N, false, false>(r3, v);
 #pragma unroll
-      for (int j = 1; j < N; j++) {
-        v1 = fma2(bcast(c_Bp[O + j * N + b]), r1[j], v1);
-        v1 = fma2(bcast(c_Dp[O + j * N + b]), r2[j], v1);
-        v2 = fma2(bcast(c_Bp[O + j * N + b]), r3[j], v2);
+      for (int b = 0; b < N; b++) s2[a * L::SA + b * L::SB + k] = v[b];
+    } else {
+#pragma unroll
+      for (int b = 0; b < N; b++) {
+        f2 v1 = mul2(bcast(c_Bp[O + b]), r1[0]), v2 = mul2(bcast(c_Bp[O + b]), r3[0]);
+        v1 = fma2(bcast(c_Dp[O + b]), r2[0], v1);
+#pragma unroll
+        for (int j = 1; j < N; j++) {
+          v1 = fma2(bcast(c_Bp[O + j * N + b]), r1[j], v1);
+          v1 = fma2(bcast(c_Dp[O + j * N + b]), r2[j], v1);
+          v2 = fma2(bcast(c_Bp[O + j * N + b]), r3[j], v2);
+        }
+        s1[a * L::SA + b * L::SB + k] = v1;
+        s2[a * L::SA + b * L::SB + k] = v2;
       }
-      s1[a * L::SA + b * L::SB + k] = v1;
-      s2[a * L::SA + b * L::SB + k] = v2;
     }
   }
   group_sync<G>(gid);
@@ -263,16 +411,24 @@ __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool activ
     f2 r1[N], r2[N];
 #pragma unroll
     for (int k = 0; k < N; k++) { r1[k] = s1[a * L::SA + b * L::SB + k]; r2[k] = s2[a * L::SA + b * L::SB + k]; }
+    if constexpr (EO) {
+      f2 v[N];
+      eo2_bwd<N, false, false>(r1, v);
+      eo2_bwd<N, true, true>(r2, v);
 #pragma unroll
-    for (int c = 0; c < N; c++) {
-      f2 v = mul2(bcast(c_Bp[O + c]), r1[0]);
-      v = fma2(bcast(c_Dp[O + c]), r2[0], v);
+      for (int c = 0; c < N; c++) su[(a * N + b) * N + c] = v[c];
+    } else {
 #pragma unroll
-      for (int k = 1; k < N; k++) {
-        v = fma2(bcast(c_Bp[O + k * N + c]), r1[k], v);
-        v = fma2(bcast(c_Dp[O + k * N + c]), r2[k], v);
+      for (int c = 0; c < N; c++) {
+        f2 v = mul2(bcast(c_Bp[O + c]), r1[0]);
+        v = fma2(bcast(c_Dp[O + c]), r2[0], v);
+#pragma unroll
+        for (int k = 1; k < N; k++) {
+          v = fma2(bcast(c_Bp[O + k * N + c]), r1[k], v);
+          v = fma2(bcast(c_Dp[O + k * N + c]), r2[k], v);
+        }
+        su[(a * N + b) * N + c] = v;
       }
-      su[(a * N + b) * N + c] = v;
     }
   }
   group_sync<G>(gid);
@@ -398,7 +554,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     if (has_next) t_issued++;
     group_sync<G>(gid);
     f2 gx[N], gy[N], gz[N], uq[N];
-    pair_forward<N, MASS>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
+    pair_forward<N, MASS, pair_eo(N, GM)>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
     if (has_next) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
       if (!ok) break;
@@ -469,7 +625,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
       }
       if (has_next) g_issued++;
     }
-    pair_backward<N, MASS>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
+    pair_backward<N, MASS, pair_eo(N, GM)>(pl, pa, pk, active, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
     const int* td = tbuf(b);
     const int nrow = rows_of(ch);
 #pragma unroll
@@ -609,7 +765,7 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
       }
       group_sync<G>(gid);
       f2 gx[N], gy[N], gz[N], uq[N];
-      pair_forward<N, MASS>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
+      pair_forward<N, MASS, true>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, gx, gy, gz, uq);
       f2 vx[N], vy[N], vz[N], vm[N];
       f2 en = 0;
       if (act_el) {
@@ -638,7 +794,7 @@ hex_apply_multi_pair_kernel(int ne, int64_t n, int R, const int* __restrict__ ph
         atomicAdd(&sacc[gid][ra], ea);
         if (rb >= 0) atomicAdd(&sacc[gid][rb], eb);
       }
-      pair_backward<N, MASS>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
+      pair_backward<N, MASS, true>(pl, pa, pk, act_el, gid, su, s1, s2, t1, t2, t3, vx, vy, vz, vm);
       float* ya = y + (size_t)ra * n;
       float* yb = y + (size_t)(rb >= 0 ? rb : ra) * n;
       for (int t = lane; t < SN3; t += G) {
@@ -1008,7 +1164,18 @@ void upload_pair_tables(gh1_space* sp) {
   std::vector<float> w(sp->gw.begin(), sp->gw.end());
   GH1_CUDA(cudaMemcpyToSymbolAsync(c_Wp, w.data(), N * sizeof(float), (N * (N - 1) / 2 - 1) * sizeof(float),
                                    cudaMemcpyHostToDevice, s));
-  GH1_CUDA(cudaStreamSynchronize(s));  // the host staging vector goes out of scope
+  std::vector<double> B(N * N), D(N * N);
+  GH1_CUDA(cudaMemcpyAsync(B.data(), sp->d_B64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaMemcpyAsync(D.data(), sp->d_D64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));  // the host staging vectors go out of scope
+  double eo[4][16];
+  GH1_CHECK(hex_eo_coefficients(B.data(), D.data(), N, eo) <= 1e-12, GH1_ERR_ARG,
+            "internal: 1D hex tables lack the reflection symmetry");
+  for (int k = 0; k < 4; k++) {
+    float e32[16];
+    for (int q = 0; q < 16; q++) e32[q] = (float)eo[k][q];
+    GH1_CUDA(cudaMemcpyToSymbol(c_EOp, e32, N * sizeof(float), (k * 64 + eo_off(N)) * sizeof(float)));
+  }
 }
 
 // Per-element metric of an affine hex (x = P0 + J xi: J[3k+j] = d x_k / d xi_j

@@ -45,7 +45,6 @@ template <> struct CTab<double> {
   static __device__ __forceinline__ double EO(int k, int i) { return c_EO64[k][i]; }
   static __device__ __forceinline__ double W(int i) { return c_W64[i]; }
 };
-constexpr int eo_off(int N) { return N * (N - 1) / 2 - 1; }
 
 static void upload_const_tables(gh1_space* sp) {
   const int N = sp->p + 1, off = tab_off(N);
@@ -59,25 +58,12 @@ static void upload_const_tables(gh1_space* sp) {
   GH1_CUDA(cudaMemcpyAsync(B.data(), sp->d_B64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
   GH1_CUDA(cudaMemcpyAsync(D.data(), sp->d_D64.p, N * N * sizeof(double), cudaMemcpyDeviceToHost, s));
   GH1_CUDA(cudaStreamSynchronize(s));
-  double scale = 0, dev = 0;
-  for (int q = 0; q < N; q++)
-    for (int c = 0; c < N; c++) {
-      const int qr = N - 1 - q, cr = c < 2 ? 1 - c : c;
-      const double sg = c < 2 ? 1.0 : ((c % 2) ? -1.0 : 1.0);
-      scale = std::max(scale, std::max(std::fabs(B[q * N + c]), std::fabs(D[q * N + c])));
-      dev = std::max(dev, std::fabs(B[qr * N + c] - sg * B[q * N + cr]));
-      dev = std::max(dev, std::fabs(D[qr * N + c] + sg * D[q * N + cr]));
-    }
-  GH1_CHECK(dev <= 1e-12 * scale, GH1_ERR_ARG, "internal: 1D hex tables lack the reflection symmetry");
-  double eo[4][16] = {};
-  float eo32[4][16] = {};
-  for (int q = 0; q < N; q++) {
-    eo[0][q] = 0.5 * (B[q * N] + B[q * N + 1]);
-    eo[1][q] = 0.5 * (B[q * N] - B[q * N + 1]);
-    eo[2][q] = 0.5 * (D[q * N] + D[q * N + 1]);
-    eo[3][q] = 0.5 * (D[q * N] - D[q * N + 1]);
-    for (int k = 0; k < 4; k++) eo32[k][q] = (float)eo[k][q];
-  }
+  double eo[4][16];
+  GH1_CHECK(hex_eo_coefficients(B.data(), D.data(), N, eo) <= 1e-12, GH1_ERR_ARG,
+            "internal: 1D hex tables lack the reflection symmetry");
+  float eo32[4][16];
+  for (int k = 0; k < 4; k++)
+    for (int q = 0; q < 16; q++) eo32[k][q] = (float)eo[k][q];
   for (int k = 0; k < 4; k++) {
     GH1_CUDA(cudaMemcpyToSymbol(c_EO64, eo[k], N * sizeof(double), (k * 64 + eo_off(N)) * sizeof(double)));
     GH1_CUDA(cudaMemcpyToSymbol(c_EO32, eo32[k], N * sizeof(float), (k * 64 + eo_off(N)) * sizeof(float)));
