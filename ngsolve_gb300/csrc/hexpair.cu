@@ -490,37 +490,44 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
   };
   // gathered pairs of the chunk: position t = s*N3 + l -> (element 2s, 2s+1; local DOF l).
   // Plain loads only: nothing consumes them until the chunk starts (put_x), so the
-  // gather latency overlaps the rest of the current chunk.
-  auto gather = [&](int c, const int* tn, f2* xr) {
+  // gather latency overlaps the rest of the current chunk.  The shape signs (bit 31
+  // of the DOF rows) go to sg: bits 2j and 2j+1 for the two halves of position j.
+  auto gather = [&](int c, const int* tn, f2* xr, unsigned& sg) {
     const int nrow = rows_of(c);
+    sg = 0u;
 #pragma unroll
     for (int j = 0; j < NG; j++) {
       const int t = lane + j * G;
       float v0 = 0.f, v1 = 0.f;
       if (t < SN3) {
         const int s = t / N3, l = t % N3;
-        if (2 * s < nrow) v0 = __ldg(x + (tn[(2 * s) * rowt + l] & 0x7fffffff));
-        if (2 * s + 1 < nrow) v1 = __ldg(x + (tn[(2 * s + 1) * rowt + l] & 0x7fffffff));
+        if (2 * s < nrow) {
+          const unsigned d = (unsigned)tn[(2 * s) * rowt + l];
+          v0 = __ldg(x + (d & 0x7fffffffu));
+          sg |= (d >> 31) << (2 * j);
+        }
+        if (2 * s + 1 < nrow) {
+          const unsigned d = (unsigned)tn[(2 * s + 1) * rowt + l];
+          v1 = __ldg(x + (d & 0x7fffffffu));
+          sg |= (d >> 31) << (2 * j + 1);
+        }
       }
       xr[j] = pack2(v0, v1);
     }
   };
-  // signed coefficients into the work array (shape signs: bit 31 of the DOF rows)
-  auto put_x = [&](int c, const int* tn, const f2* xr) {
-    const int nrow = rows_of(c);
+  // signed coefficients into the work array
+  auto put_x = [&](const f2* xr, unsigned sg) {
 #pragma unroll
     for (int j = 0; j < NG; j++) {
       const int t = lane + j * G;
-      if (t < SN3) {
-        const int s = t / N3, l = t % N3;
-        const unsigned d0 = 2 * s < nrow ? (unsigned)tn[(2 * s) * rowt + l] : 0u;
-        const unsigned d1 = 2 * s + 1 < nrow ? (unsigned)tn[(2 * s + 1) * rowt + l] : 0u;
-        work[t] = xr[j] ^ (((f2)(d1 & 0x80000000u) << 32) | (f2)(d0 & 0x80000000u));
-      }
+      if (t < SN3)
+        work[t] = xr[j] ^ (((f2)((sg >> (2 * j + 1)) & 1u) << 63) | ((f2)((sg >> (2 * j)) & 1u) << 31));
     }
   };
   f2 xr[NG];
+  unsigned xs = 0u;
   f2 acc = 0;  // per-lane energy of both elements (working precision)
+  const bool want_e = partial != nullptr;
   int t_issued = 0, t_waited = 0, g_issued = 0, g_waited = 0;
   bool ok = true;
   if (ch < nch) {
@@ -535,7 +542,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     ok = group_all<G>(gid, mbar_wait_polls(&mbar[0], 0, g_first_wait_polls));
     if (ok) {
       t_waited = 1;  // a wait counts only once it succeeded: the drain covers the rest
-      gather(ch, tbuf(0), xr);
+      gather(ch, tbuf(0), xr, xs);
     }
   }
   for (int k = 0; ok && ch < nch; ch += stride, k++) {
@@ -544,7 +551,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     const int e0 = ch * E + 2 * slot;  // first element of this lane's pair
     const bool active = slot < S && e0 < ne;
     const bool second = active && e0 + 1 < ne;
-    put_x(ch, tbuf(b), xr);
+    put_x(xr, xs);
     if (lane == 0 && has_next) {
       fence_proxy_async();
       issue_t(ch + stride, b ^ 1);
@@ -559,7 +566,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[b ^ 1], ((k + 1) >> 1) & 1));
       if (!ok) break;
       t_waited++;
-      gather(ch + stride, tbuf(b ^ 1), xr);
+      gather(ch + stride, tbuf(b ^ 1), xr, xs);
     }
     if (GM == 0) {
       ok = group_all<G>(gid, mbar_wait_bounded(&mbar[2], k & 1));
@@ -608,13 +615,15 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
           vy[i] = fma2(gyz, gz[i], fma2(gyy, gy[i], mul2(gxy, gx[i])));
           vz[i] = fma2(gzz, gz[i], fma2(gyz, gy[i], mul2(gxz, gx[i])));
         }
-        f2 en = fma2(gz[i], vz[i], fma2(gy[i], vy[i], mul2(gx[i], vx[i])));
         if (MASS) {
           if (GM == 2) vm[i] = mul2(mul2(bcast(c_Wp[WO + i] * wjk), ea[6]), uq[i]);
           else vm[i] = mul2(ld(6), uq[i]);
-          en = fma2(uq[i], vm[i], en);
         }
-        acc = add2(acc, en);
+        if (want_e) {  // x^T A x only for a caller that asks for it (CG)
+          f2 en = fma2(gz[i], vz[i], fma2(gy[i], vy[i], mul2(gx[i], vx[i])));
+          if (MASS) en = fma2(uq[i], vm[i], en);
+          acc = add2(acc, en);
+        }
       }
     }
     if (GM == 0) {
@@ -926,6 +935,7 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
   const int ss = p * SPU + t * SUA;         // slice-phase staging offset of this lane (a = t)
   const int nch = (ne + 2 * P - 1) / (2 * P);
   f2 acc = 0;
+  const bool want_e = partial != nullptr;
   for (int ch = blockIdx.x * C::WARPS + warp; ch < nch; ch += gridDim.x * C::WARPS) {
     const int eb = ch * 2 * P, nrow = min(2 * P, ne - eb);
     const int e0 = eb + 2 * p;
@@ -1053,12 +1063,12 @@ hex_apply_slice_kernel(int ne, const int* __restrict__ tdof, int tstride, const 
           vx[i] = fma2(ea[4], sz, fma2(ea[3], sy, mul2(ea[0], sx)));
           vy[i] = fma2(ea[5], sz, fma2(ea[1], sy, mul2(ea[3], sx)));
           vz[i] = fma2(ea[2], sz, fma2(ea[5], sy, mul2(ea[4], sx)));
-          f2 en = fma2(gz, vz[i], fma2(gy, vy[i], mul2(gx, vx[i])));
-          if (MASS) {
-            vm[i] = mul2(mul2(wq, ea[6]), uq);
-            en = fma2(uq, vm[i], en);
+          if (MASS) vm[i] = mul2(mul2(wq, ea[6]), uq);
+          if (want_e) {  // x^T A x only for a caller that asks for it (CG)
+            f2 en = fma2(gz, vz[i], fma2(gy, vy[i], mul2(gx, vx[i])));
+            if (MASS) en = fma2(uq, vm[i], en);
+            acc = add2(acc, en);
           }
-          acc = add2(acc, en);
         }
 #pragma unroll
         for (int a = 0; a < N; a++) {
