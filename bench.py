@@ -903,6 +903,8 @@ def main():
         Bg, _ = model_bytes_flops(ne, N, args.order, 4, 4)
         general = {"variant": gvar, "ms": tg * 1e3, "gdofs": N / tg / 1e9, "achieved_gbs": Bg / tg / 1e9,
                    "frac": Bg / tg / 1e9 / load_peaks()[0]}
+        if gvar == 2 and args.order == ORDER and args.nx == NX:
+            general["traffic"] = load_traffic("hex_apply_pair_fp32_c3.md")
         del ag
         torch.cuda.empty_cache()
 
@@ -1049,10 +1051,10 @@ def main():
               "hex_apply_pair_kernel<%d, 0, %d>" % (nn, variant - 2))
     traffic = None
     if args.order == ORDER and args.nx == NX:  # the committed profiles cover the benchmark configuration
-        # variant 5 (the slice form) has no capture at this configuration: the
-        # autotuner has not picked it at p=4, so its traffic stays null
+        # variants 3 and 5 have no capture at this configuration: the autotuner
+        # has not picked them at p=4, so their traffic stays null
         prof = {0: "hex_apply_fp32_c3.md", 1: "hex_apply_fp32_c3.md", 2: "hex_apply_pair_fp32_c3.md",
-                3: "hex_apply_pair_fp32_c3.md", 4: "hex_apply_pair_affine_fp32_c3.md"}.get(variant)
+                4: "hex_apply_pair_affine_fp32_c3.md"}.get(variant)
         traffic = load_traffic(prof) if prof else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": peak_kind,

@@ -65,6 +65,40 @@ def test_fp32_variant_parity(gpu, mode, p, mass):
         assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
 
 
+def _renumbered(m, seed):
+    """The same mesh with its vertices numbered in a random order: the edge and
+    face orientations, which follow the global vertex numbers, then take every
+    class (reversed edges; transposed and reflected faces)."""
+    perm = np.random.default_rng(seed).permutation(len(m.points))
+    pts = np.empty_like(m.points)
+    pts[perm] = m.points
+    return RawMesh(pts, perm[m.elements])
+
+
+@pytest.mark.parametrize("mass", [False, True])
+@pytest.mark.parametrize("p", [3, 4, 5, 6])
+@pytest.mark.parametrize("mode", [2, 3])
+def test_fp32_paired_all_orientations(gpu, mode, p, mass):
+    """The paired kernels read every DOF and shape sign from the signed tensor
+    table.  On jittered meshes with randomly renumbered vertices (all edge and
+    face orientation classes; 27 and 8 elements) the apply is within 2e-5 of
+    the oracle."""
+    for nx in (3, 2):
+        m = _renumbered(JitterInterior(MakeStructured3DMesh(hexes=True, nx=nx), 0.1 / nx, 11), 20 + nx)
+        kappa = lognormal(m.ne, 1.0, 5)
+        mu = lognormal(m.ne, 0.5, 6) if mass else None
+        fes = gpu.H1(m, order=p, dirichlet=".*")
+        a = _form(gpu, fes, kappa, mu, mode)
+        assert a.mat.Info()["hex_variant_fp32"] == mode
+        S = O.OracleSpace(m.points, m.elements, p)
+        x = np.random.default_rng(7).normal(size=fes.ndof)
+        yo = S.apply_mf(x, kappa=kappa, mu=mu)
+        x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        a.mat.Mult(x32, y32)
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+
+
 def _sheared(nx):
     """Structured hexes under a general affine map: every element is the same
     parallelepiped, so the metric is one full symmetric 3x3 per element."""
