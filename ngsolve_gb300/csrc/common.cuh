@@ -250,6 +250,8 @@ struct gh1_op {
   int tet_tc_per_sm = 0;                     // resident CTAs of the tensor-core FP32 tet apply (0: not available)
   int tet_tc_ntiles = 0;                     // its tiles of up to 128 same-class elements
   gh1::DBuf<int> d_tet_tc_tiles;             // [ntiles][4] = class, first position, count, 0
+  gh1::DBuf<float> d_tet_tc_tab;             // per class: both B operands, TF32 hi / lo parts, in the
+                                             // kernel's shared-memory layout (copied as is)
   bool tet_use_tc = false;                   // FP32 tet apply on the tensor cores (timed at setup)
   int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
   gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights

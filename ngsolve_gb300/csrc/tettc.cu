@@ -54,6 +54,7 @@ struct TetTcCfg {
   static constexpr int W = T2 + 2 * N2 * K2;        // weights [R] (padded to 4)
   static constexpr int BAR = W + (R + 3) / 4 * 4;   // mbarrier (8 B) + TMEM base (4 B)
   static constexpr size_t smem = (size_t)(BAR + 4) * sizeof(float);
+  static constexpr int TAB = 2 * N1 * K1 + 2 * N2 * K2;  // floats of one class's operands (T1, T2)
 };
 
 // element (row r, column k) of a K-major operand with K columns
@@ -120,9 +121,9 @@ constexpr int TT_THREADS = 256;
 template <int P>
 __global__ void __launch_bounds__(TT_THREADS, 2)
 tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
-              const float* __restrict__ Ge, const double* __restrict__ D64, int nlocp, int Rs,
-              const double* __restrict__ W64, const float* __restrict__ x, float* __restrict__ y, double* partial,
-              unsigned int* counter, double* energy, const int* skip, int* err) {
+              const float* __restrict__ Ge, const float* __restrict__ tab, const double* __restrict__ W64,
+              const float* __restrict__ x, float* __restrict__ y, double* partial, unsigned int* counter,
+              double* energy, const int* skip, int* err) {
   using C = TetTcCfg<P>;
   constexpr int NLOC = C::NLOC, NQ = C::NQ, R = C::R, K1 = C::K1, N1 = C::N1, K2 = C::K2, N2 = C::N2;
   if (skip && *(volatile const int*)skip) return;
@@ -187,25 +188,18 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
       xv[j] = (a && i < NLOC) ? __ldg(x + __ldg(edn + i)) : 0.f;
     }
   };
-  if (blockIdx.x < ntiles) gather(blockIdx.x);
-  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+  // a contiguous range of the class-sorted tiles per CTA: consecutive tiles
+  // share their class, so the class operands are copied only where it changes
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  if (t0 < t1) gather(t0);
+  for (int tile = t0; ok && tile < t1; tile++) {
     const int cls = tiles[4 * tile], start = tiles[4 * tile + 1], cnt = tiles[4 * tile + 2];
-    if (cls != loaded) {  // the class table as both B operands, split hi / lo from FP64
-      const double* Dc = D64 + (size_t)cls * nlocp * Rs;
-      for (int k = t; k < N1 * K1; k += TT_THREADS) {
-        const int n = k / K1, i = k % K1;
-        const double v = (n < R && i < NLOC) ? Dc[(size_t)i * Rs + n] : 0.0;
-        const float h = tt_hi((float)v);
-        sT1[tt_off<K1>(n, i)] = h;
-        sT1[N1 * K1 + tt_off<K1>(n, i)] = (float)(v - (double)h);
-      }
-      for (int k = t; k < N2 * K2; k += TT_THREADS) {
-        const int i = k / K2, r = k % K2;
-        const double v = (i < NLOC && r < R) ? Dc[(size_t)i * Rs + r] : 0.0;
-        const float h = tt_hi((float)v);
-        sT2[tt_off<K2>(i, r)] = h;
-        sT2[N2 * K2 + tt_off<K2>(i, r)] = (float)(v - (double)h);
-      }
+    if (cls != loaded) {  // both B operands of the class (TF32 hi / lo, final layout)
+      __syncthreads();    // the previous tile's products have completed (its last wait)
+      const float4* src = (const float4*)(tab + (size_t)cls * C::TAB);
+      float4* dst = (float4*)sT1;
+      for (int k = t; k < C::TAB / 4; k += TT_THREADS) dst[k] = __ldg(src + k);
       loaded = cls;
     }
     // ---- the gathered half of this row's element into A1 ---------------------------
@@ -260,7 +254,7 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
       issue_stage([&] { tt_gemm<C::KB, K2, C::KA, N2, N2, true>(tmem + C::C2, sA2, sT2); });
     }
     if (partial) acc += (double)en;
-    if (tile + (int)gridDim.x < ntiles) gather(tile + gridDim.x);
+    if (tile + 1 < t1) gather(tile + 1);
     if (!(ok = wait_stage())) break;
     float yv[N2];
 #pragma unroll
@@ -304,6 +298,46 @@ static int tet_tc_occupancy_p() {
   return std::min(v, 512 / TetTcCfg<P>::TCOLS);
 }
 
+// per class: the table D_c as the B operand of both products, split into TF32
+// high and low parts from FP64, in the kernel's shared-memory layout
+// ([hi, lo][N1][K1] then [hi, lo][N2][K2]; zero padding)
+template <int P>
+__global__ void tet_tc_table_kernel(int ncls, const double* __restrict__ D64, int nlocp, int Rs, float* __restrict__ tab) {
+  using C = TetTcCfg<P>;
+  constexpr int NLOC = C::NLOC, R = C::R, K1 = C::K1, N1 = C::N1, K2 = C::K2, N2 = C::N2;
+  const int64_t tot = (int64_t)ncls * (N1 * K1 + N2 * K2);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int cls = (int)(k / (N1 * K1 + N2 * K2)), j = (int)(k % (N1 * K1 + N2 * K2));
+    const double* Dc = D64 + (size_t)cls * nlocp * Rs;
+    float* T1 = tab + (size_t)cls * C::TAB;
+    float* T2 = T1 + 2 * N1 * K1;
+    if (j < N1 * K1) {
+      const int n = j / K1, i = j % K1;
+      const double v = (n < R && i < NLOC) ? Dc[(size_t)i * Rs + n] : 0.0;
+      const float h = tt_hi((float)v);
+      T1[tt_off<K1>(n, i)] = h;
+      T1[N1 * K1 + tt_off<K1>(n, i)] = (float)(v - (double)h);
+    } else {
+      const int jj = j - N1 * K1, i = jj / K2, r = jj % K2;
+      const double v = (i < NLOC && r < R) ? Dc[(size_t)i * Rs + r] : 0.0;
+      const float h = tt_hi((float)v);
+      T2[tt_off<K2>(i, r)] = h;
+      T2[N2 * K2 + tt_off<K2>(i, r)] = (float)(v - (double)h);
+    }
+  }
+}
+
+template <int P>
+static void tet_tc_table_p(gh1_op* op) {
+  using C = TetTcCfg<P>;
+  gh1_space* sp = op->sp;
+  op->d_tet_tc_tab.alloc((size_t)N_TET_CLASSES * C::TAB);
+  const int64_t tot = (int64_t)N_TET_CLASSES * (C::N1 * C::K1 + C::N2 * C::K2);
+  tet_tc_table_kernel<P><<<(unsigned)((tot + 255) / 256), 256, 0, sp->ctx->stream>>>(
+      N_TET_CLASSES, op->d_tetD64.p, (sp->nloc + 15) / 16 * 16, op->tet_Rs, op->d_tet_tc_tab.p);
+  check_kernel(sp->ctx, "tet_tc_table_kernel");
+}
+
 // tiles of up to 128 same-class elements over the class-sorted order of the
 // tiled apply, and the CTAs per SM (0: not available: order, mass term,
 // GH1_TET_TC=0)
@@ -331,9 +365,9 @@ void tet_tc_setup(gh1_op* op) {
   op->d_tet_tc_tiles.upload(tiles, s);
   op->tet_tc_ntiles = (int)tiles.size() / 4;
   switch (sp->p) {
-    case 2: op->tet_tc_per_sm = tet_tc_occupancy_p<2>(); break;
-    case 3: op->tet_tc_per_sm = tet_tc_occupancy_p<3>(); break;
-    case 4: op->tet_tc_per_sm = tet_tc_occupancy_p<4>(); break;
+    case 2: op->tet_tc_per_sm = tet_tc_occupancy_p<2>(); tet_tc_table_p<2>(op); break;
+    case 3: op->tet_tc_per_sm = tet_tc_occupancy_p<3>(); tet_tc_table_p<3>(op); break;
+    case 4: op->tet_tc_per_sm = tet_tc_occupancy_p<4>(); tet_tc_table_p<4>(op); break;
     default: break;
   }
   GH1_CUDA(cudaStreamSynchronize(s));
@@ -345,8 +379,8 @@ static void tet_tc_launch_p(gh1_op* op, const float* x, float* y, double* partia
   gh1_space* sp = op->sp;
   const int grid = std::max(1, std::min(op->tet_tc_ntiles, sp->ctx->nsm * op->tet_tc_per_sm));
   tet_tc_kernel<P><<<grid, TT_THREADS, TetTcCfg<P>::smem, sp->ctx->stream>>>(
-      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_G32.p, op->d_tetD64.p,
-      (sp->nloc + 15) / 16 * 16, op->tet_Rs, op->d_tetw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_G32.p, op->d_tet_tc_tab.p,
+      op->d_tetw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
   check_kernel(sp->ctx, "tet_tc_kernel");
 }
 
