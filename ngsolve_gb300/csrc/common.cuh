@@ -252,6 +252,8 @@ struct gh1_op {
   gh1::DBuf<int> d_tet_tc_tiles;             // [ntiles][4] = class, first position, count, 0
   gh1::DBuf<float> d_tet_tc_tab;             // per class: both B operands, TF32 hi / lo parts, in the
                                              // kernel's shared-memory layout (copied as is)
+  gh1::DBuf<int> d_tet_tc_dofs;              // [tile][nloc][128]: DOF of local DOF i of tile row m
+                                             // (0 past the tile's count), coalesced per i
   bool tet_use_tc = false;                   // FP32 tet apply on the tensor cores (timed at setup)
   int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
   gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights

@@ -120,7 +120,7 @@ constexpr int TT_THREADS = 256;
 
 template <int P>
 __global__ void __launch_bounds__(TT_THREADS, 2)
-tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
+tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ tdofs,
               const float* __restrict__ Ge, const float* __restrict__ tab, const double* __restrict__ W64,
               const float* __restrict__ x, float* __restrict__ y, double* partial, unsigned int* counter,
               double* energy, const int* skip, int* err) {
@@ -178,14 +178,15 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
   // while the current tile's second product runs
   constexpr int H1 = K1 / 2;  // a multiple of 4
   float xv[H1];
+  // DOF of local DOF i of this thread's row in tile tl_ (tile-major table: the
+  // 32 rows of a warp read 128 consecutive bytes)
+  auto dof_of = [&](int tl_, int i) { return __ldg(tdofs + ((size_t)tl_ * NLOC + i) * 128 + m); };
   auto gather = [&](int tl_) {
-    const int st = tiles[4 * tl_ + 1], n = tiles[4 * tl_ + 2];
-    const bool a = m < n;
-    const int* edn = eldofs + (size_t)(a ? perm[st + m] : 0) * NLOC;
+    const bool a = m < tiles[4 * tl_ + 2];
 #pragma unroll
     for (int j = 0; j < H1; j++) {
       const int i = half * H1 + j;
-      xv[j] = (a && i < NLOC) ? __ldg(x + __ldg(edn + i)) : 0.f;
+      xv[j] = (a && i < NLOC) ? __ldg(x + dof_of(tl_, i)) : 0.f;
     }
   };
   // a contiguous range of the class-sorted tiles per CTA: consecutive tiles
@@ -205,7 +206,6 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
     // ---- the gathered half of this row's element into A1 ---------------------------
     const bool act = m < cnt;
     const int e = act ? perm[start + m] : 0;
-    const int* ed = eldofs + (size_t)e * NLOC;
 #pragma unroll
     for (int j = 0; j < H1; j += 4) tt_put4<K1>(sA1, m, half * H1 + j, xv + j);
     // ---- P = X D_c ------------------------------------------------------------------
@@ -263,10 +263,10 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
       constexpr int HS = (NLOC + 1) / 2;
       if (half == 0) {
 #pragma unroll
-        for (int i = 0; i < HS; i++) red_add(y + __ldg(ed + i), yv[i]);
+        for (int i = 0; i < HS; i++) red_add(y + dof_of(tile, i), yv[i]);
       } else {
 #pragma unroll
-        for (int i = HS; i < NLOC; i++) red_add(y + __ldg(ed + i), yv[i]);
+        for (int i = HS; i < NLOC; i++) red_add(y + dof_of(tile, i), yv[i]);
       }
     }
   }
@@ -338,6 +338,18 @@ static void tet_tc_table_p(gh1_op* op) {
   check_kernel(sp->ctx, "tet_tc_table_kernel");
 }
 
+// tile-major DOF table: tdofs[(t * nloc + i) * 128 + m] = DOF i of the element in
+// row m of tile t (0 past the tile's count)
+__global__ void tet_tc_dofs_kernel(int ntiles, int nloc, const int* __restrict__ tiles, const int* __restrict__ perm,
+                                   const int* __restrict__ eldofs, int* __restrict__ tdofs) {
+  const int64_t tot = (int64_t)ntiles * nloc * 128;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(k % 128), i = (int)((k / 128) % nloc), t = (int)(k / (128 * (int64_t)nloc));
+    const int st = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    tdofs[k] = m < cnt ? eldofs[(size_t)perm[st + m] * nloc + i] : 0;
+  }
+}
+
 // tiles of up to 128 same-class elements over the class-sorted order of the
 // tiled apply, and the CTAs per SM (0: not available: order, mass term,
 // GH1_TET_TC=0)
@@ -364,6 +376,13 @@ void tet_tc_setup(gh1_op* op) {
   }
   op->d_tet_tc_tiles.upload(tiles, s);
   op->tet_tc_ntiles = (int)tiles.size() / 4;
+  op->d_tet_tc_dofs.alloc((size_t)op->tet_tc_ntiles * sp->nloc * 128);
+  {
+    const int64_t tot = (int64_t)op->tet_tc_ntiles * sp->nloc * 128;
+    tet_tc_dofs_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(
+        op->tet_tc_ntiles, sp->nloc, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_tet_tc_dofs.p);
+    check_kernel(sp->ctx, "tet_tc_dofs_kernel");
+  }
   switch (sp->p) {
     case 2: op->tet_tc_per_sm = tet_tc_occupancy_p<2>(); tet_tc_table_p<2>(op); break;
     case 3: op->tet_tc_per_sm = tet_tc_occupancy_p<3>(); tet_tc_table_p<3>(op); break;
@@ -379,7 +398,7 @@ static void tet_tc_launch_p(gh1_op* op, const float* x, float* y, double* partia
   gh1_space* sp = op->sp;
   const int grid = std::max(1, std::min(op->tet_tc_ntiles, sp->ctx->nsm * op->tet_tc_per_sm));
   tet_tc_kernel<P><<<grid, TT_THREADS, TetTcCfg<P>::smem, sp->ctx->stream>>>(
-      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_G32.p, op->d_tet_tc_tab.p,
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, op->d_tet_tc_dofs.p, op->d_G32.p, op->d_tet_tc_tab.p,
       op->d_tetw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
   check_kernel(sp->ctx, "tet_tc_kernel");
 }
