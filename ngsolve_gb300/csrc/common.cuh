@@ -254,6 +254,8 @@ struct gh1_op {
                                              // kernel's shared-memory layout (copied as is)
   gh1::DBuf<int> d_tet_tc_dofs;              // [tile][nloc][128]: DOF of local DOF i of tile row m
                                              // (0 past the tile's count), coalesced per i
+  gh1::DBuf<float> d_tet_tc_G;               // [tile][6][128]: the FP32 metric of tile row m (rebuilt
+                                             // with the metric)
   bool tet_use_tc = false;                   // FP32 tet apply on the tensor cores (timed at setup)
   int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
   gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights

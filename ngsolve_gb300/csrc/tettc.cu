@@ -120,8 +120,8 @@ constexpr int TT_THREADS = 256;
 
 template <int P>
 __global__ void __launch_bounds__(TT_THREADS, 2)
-tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ tdofs,
-              const float* __restrict__ Ge, const float* __restrict__ tab, const double* __restrict__ W64,
+tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ tdofs, const float* __restrict__ Gt,
+              const float* __restrict__ tab, const double* __restrict__ W64,
               const float* __restrict__ x, float* __restrict__ y, double* partial, unsigned int* counter,
               double* energy, const int* skip, int* err) {
   using C = TetTcCfg<P>;
@@ -195,7 +195,7 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
   const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
   if (t0 < t1) gather(t0);
   for (int tile = t0; ok && tile < t1; tile++) {
-    const int cls = tiles[4 * tile], start = tiles[4 * tile + 1], cnt = tiles[4 * tile + 2];
+    const int cls = tiles[4 * tile], cnt = tiles[4 * tile + 2];
     if (cls != loaded) {  // both B operands of the class (TF32 hi / lo, final layout)
       __syncthreads();    // the previous tile's products have completed (its last wait)
       const float4* src = (const float4*)(tab + (size_t)cls * C::TAB);
@@ -205,7 +205,6 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
     }
     // ---- the gathered half of this row's element into A1 ---------------------------
     const bool act = m < cnt;
-    const int e = act ? perm[start + m] : 0;
 #pragma unroll
     for (int j = 0; j < H1; j += 4) tt_put4<K1>(sA1, m, half * H1 + j, xv + j);
     // ---- P = X D_c ------------------------------------------------------------------
@@ -218,7 +217,7 @@ tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__
     // column groups [4j, 4j+4) with j = half (mod 2); column r = component * nq + point
     float g[6];
 #pragma unroll
-    for (int c = 0; c < 6; c++) g[c] = act ? __ldg(Ge + (size_t)e * 6 + c) : 0.f;
+    for (int c = 0; c < 6; c++) g[c] = act ? __ldg(Gt + ((size_t)tile * 6 + c) * 128 + m) : 0.f;
     float en = 0.f;
     auto transform = [&](auto k0c, auto kcc) {  // columns [K0, K0 + KC) into an operand with KC columns
       constexpr int K0 = decltype(k0c)::value, KC = decltype(kcc)::value;
@@ -350,6 +349,18 @@ __global__ void tet_tc_dofs_kernel(int ntiles, int nloc, const int* __restrict__
   }
 }
 
+// tile-major metric: Gt[(t * 6 + c) * 128 + m] = component c of the FP32 metric
+// of the element in row m of tile t (0 past the tile's count)
+__global__ void tet_tc_g_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm,
+                                const float* __restrict__ G, float* __restrict__ Gt) {
+  const int64_t tot = (int64_t)ntiles * 6 * 128;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(k % 128), c = (int)((k / 128) % 6), t = (int)(k / (128 * 6));
+    const int st = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    Gt[k] = m < cnt ? G[(size_t)perm[st + m] * 6 + c] : 0.f;
+  }
+}
+
 // tiles of up to 128 same-class elements over the class-sorted order of the
 // tiled apply, and the CTAs per SM (0: not available: order, mass term,
 // GH1_TET_TC=0)
@@ -382,6 +393,11 @@ void tet_tc_setup(gh1_op* op) {
     tet_tc_dofs_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(
         op->tet_tc_ntiles, sp->nloc, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_tet_tc_dofs.p);
     check_kernel(sp->ctx, "tet_tc_dofs_kernel");
+    op->d_tet_tc_G.alloc((size_t)op->tet_tc_ntiles * 6 * 128);
+    const int64_t tg = (int64_t)op->tet_tc_ntiles * 6 * 128;
+    tet_tc_g_kernel<<<(unsigned)std::min<int64_t>((tg + 255) / 256, 65535), 256, 0, s>>>(
+        op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, op->d_G32.p, op->d_tet_tc_G.p);
+    check_kernel(sp->ctx, "tet_tc_g_kernel");
   }
   switch (sp->p) {
     case 2: op->tet_tc_per_sm = tet_tc_occupancy_p<2>(); tet_tc_table_p<2>(op); break;
@@ -398,7 +414,7 @@ static void tet_tc_launch_p(gh1_op* op, const float* x, float* y, double* partia
   gh1_space* sp = op->sp;
   const int grid = std::max(1, std::min(op->tet_tc_ntiles, sp->ctx->nsm * op->tet_tc_per_sm));
   tet_tc_kernel<P><<<grid, TT_THREADS, TetTcCfg<P>::smem, sp->ctx->stream>>>(
-      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, op->d_tet_tc_dofs.p, op->d_G32.p, op->d_tet_tc_tab.p,
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_tc_dofs.p, op->d_tet_tc_G.p, op->d_tet_tc_tab.p,
       op->d_tetw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
   check_kernel(sp->ctx, "tet_tc_kernel");
 }
