@@ -9,6 +9,8 @@
 // gathers are in flight per lane; shuffle reduction.  L and U are autotuned per
 // matrix (L = 4..32).
 #include <algorithm>
+#include <cstdlib>
+#include <iterator>
 #include "common.cuh"
 
 namespace gh1 {
@@ -107,7 +109,14 @@ static int spmv_tune(gh1_op* op, int prec) {
   GH1_CUDA(cudaEventCreate(&b));
   float best = 1e30f;
   int bestL = 32;
-  for (int cand : {4, 8, 16, 32, 104, 108, 116, 132}) {
+  // GH1_SPMV_L forces one of the candidates (tests run every form this way)
+  const char* env = getenv("GH1_SPMV_L");
+  const int cands[] = {4, 8, 16, 32, 104, 108, 116, 132};
+  if (env && std::find(std::begin(cands), std::end(cands), atoi(env)) != std::end(cands)) {
+    L = atoi(env);
+    return L;
+  }
+  for (int cand : cands) {
     for (int rep = 0; rep < 2; rep++) {  // 3 warm-up launches, then 5 timed
       if (rep == 1) GH1_CUDA(cudaEventRecord(a, s));
       for (int k = 0; k < 3 + 2 * rep; k++) {

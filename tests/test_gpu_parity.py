@@ -130,6 +130,36 @@ def test_spmv_parity(gpu, kind, p):
     assert np.abs(yv.NumPy() - yo).max() <= 1e-13 * np.abs(yo).max()
 
 
+@pytest.mark.parametrize("form", [4, 8, 16, 32, 104, 108, 116, 132])
+@pytest.mark.parametrize("kind,p", [("hex", 1), ("tet", 2), ("tet", 4)])
+def test_spmv_every_form(gpu, monkeypatch, kind, p, form):
+    """Every SpMV form the autotuner may pick (GH1_SPMV_L: sub-warp width L,
+    +100 eight nonzeros in flight per lane) against the oracle's CSR product,
+    in FP64 (1e-13) and FP32 (2e-5, as the FP32 applies), on rows of 8 to 100+
+    nonzeros that start at every residue mod 4."""
+    monkeypatch.setenv("GH1_SPMV_L", str(form))
+    m = _mesh(kind, 3, 0.1)
+    kappa = lognormal(m.ne, 1.0, 8)
+    fes = gpu.H1(m, order=p)
+    u, v = fes.TnT()
+    a = gpu.BilinearForm(fes)
+    a += gpu.CoefficientFunction(kappa) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    a.Assemble()
+    rp, ci, va = a.mat.CSR()
+    assert set(np.asarray(rp[:-1]) % 4) == {0, 1, 2, 3}
+    x = np.random.default_rng(9).normal(size=fes.ndof)
+    yo = O.spmv(rp, ci, va, x)
+    xv = gpu.BaseVector(fes.ndof)
+    xv.data = x
+    yv = gpu.BaseVector(fes.ndof)
+    yv.data = a.mat * xv
+    assert np.abs(yv.NumPy() - yo).max() <= 1e-13 * np.abs(yo).max()
+    x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+    a.mat.Mult(x32, y32)
+    assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+
+
 @pytest.mark.parametrize("kind,p", [("hex", 2), ("hex", 3), ("tet", 3)])
 def test_rhs_parity(gpu, kind, p):
     m = _mesh(kind, 3, 0.1)
