@@ -132,6 +132,32 @@ def test_tet_tensor_core_apply(gpu, p):
     assert b.mat.Info()["hex_variant_fp32"] != 6
 
 
+@pytest.mark.parametrize("p", [2, 4])
+def test_tet_tensor_core_coefficient_update(gpu, p):
+    """The tensor-core tet apply keeps its metric tile-major; a new kappa set on
+    the form (gh1_form_set_coefs) rebuilds it before the next apply, which then
+    matches the oracle with the new coefficient (FP32 2e-5)."""
+    from ngsolve_gb300 import _lib
+    m = _mesh(6, 40 + p)
+    k1, k2 = lognormal(m.ne, 1.0, 5), lognormal(m.ne, 1.0, 6)
+    fes = gpu.H1(m, order=p, dirichlet=".*")
+    a = _form(gpu, fes, k1, None, "tc")
+    assert a.mat.Info()["hex_variant_fp32"] == 6
+    S = O.OracleSpace(m.points, m.elements, p)
+    x = np.random.default_rng(7).normal(size=fes.ndof)
+    x32 = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float32, device="cuda"))
+    for kappa in (k1, k2):
+        if kappa is k2:
+            kk = np.ascontiguousarray(k2, dtype=np.float64)
+            fes.ctx.check(fes.ctx.lib.gh1_form_set_coefs(a._form, kk.ctypes.data, None, _lib.GH1_MEM_HOST))
+        yo = S.apply_mf(x, kappa=kappa)
+        y32 = gpu.BaseVector(data=torch.zeros(fes.ndof, dtype=torch.float32, device="cuda"))
+        with tet_kernel("tc"):  # the rebuild keeps the tensor-core kernel
+            a.mat.Mult(x32, y32)
+        assert a.mat.Info()["hex_variant_fp32"] == 6
+        assert np.abs(y32.NumPy().astype(np.float64) - yo).max() <= 2e-5 * np.abs(yo).max()
+
+
 def test_tet_mixed_cg_tensor_core(gpu):
     """Mixed CG whose inner FP32 applies run on the tensor cores (with the fused
     energy x^T A x) reaches 1e-11 and matches the FP64 solution."""
