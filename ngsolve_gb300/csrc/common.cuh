@@ -242,6 +242,8 @@ struct gh1_op {
   // up to 32 same-class elements, per-class GEMM tables
   gh1::DBuf<int> d_tet_perm;                 // class-sorted element order
   gh1::DBuf<int> d_tet_tiles;                // [ntiles][4] = class, first position, count, 0
+  gh1::DBuf<int> d_tet_tdofs;                // [ntiles][nlocp][TET_TE]: DOF of local DOF i of tile
+                                             // element e (-1 past the tile's count or nloc)
   int tet_ntiles = 0, tet_R = 0, tet_Rp = 0, tet_Rs = 0;
   gh1::DBuf<double> d_tetD64, d_tetw64;      // [class][nloc][Rs] table rows, per-row weights [Rp]
   gh1::DBuf<float> d_tetD32, d_tetw32;

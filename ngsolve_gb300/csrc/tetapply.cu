@@ -82,7 +82,7 @@ __device__ __forceinline__ void st4(double* p, const double* v) {
 // Shared X and DOF rows are [i][element], P is [row][element].
 template <class T, bool MASS, int P>
 __global__ void __launch_bounds__(TET_TT)
-tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ eldofs,
+tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, const int* __restrict__ tdofs,
                 const T* __restrict__ Ge, const T* __restrict__ Me, const T* __restrict__ D, const T* __restrict__ W,
                 const T* __restrict__ x, T* __restrict__ y, double* partial, unsigned int* counter, double* energy,
                 const int* skip) {
@@ -113,16 +113,12 @@ tet_tile_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict
       for (size_t k = tid; k < dsize; k += TET_TT) sD[k] = src[k];
       loaded = cls;
     }
-    for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {  // element index fastest: conflict-free [i][e] stores
-      const int e = k % TET_TE, i = k / TET_TE;
-      int d = 0;
-      T v = 0;
-      if (e < cnt && i < nloc) {
-        d = eldofs[(size_t)perm[start + e] * nloc + i];
-        v = x[d];
-      }
-      sDof[k] = d;
-      sX[k] = v;
+    // the tile's DOFs in tile-major order (element index fastest): entry
+    // k = i * TET_TE + e is read coalesced and stored conflict-free
+    for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {
+      const int d = tdofs[(size_t)t * TET_TE * nlocp + k];
+      sDof[k] = d < 0 ? 0 : d;
+      sX[k] = d < 0 ? T(0) : x[d];
     }
     for (int k = tid; k < TET_TE * 7; k += TET_TT) {
       const int e = k / 7, c = k % 7;
@@ -223,7 +219,7 @@ constexpr int TET_QC = 16;
 template <class T, bool MASS, int TI>
 __global__ void __launch_bounds__(TET_TT)
 tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncg,
-                      int ncm, const int* __restrict__ eldofs, const T* __restrict__ Ge, const T* __restrict__ Me,
+                      int ncm, const int* __restrict__ tdofs, const T* __restrict__ Ge, const T* __restrict__ Me,
                       const T* __restrict__ Dg, const T* __restrict__ Dm, const T* __restrict__ Wg,
                       const T* __restrict__ Wm, const T* __restrict__ x, T* __restrict__ y, double* partial,
                       unsigned int* counter, double* energy, const int* skip) {
@@ -243,16 +239,11 @@ tet_tile_chunk_kernel(int ntiles, const int* __restrict__ tiles, const int* __re
   for (int t = t0; t < t1; t++) {
     const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
     __syncthreads();
+    // the tile's DOFs in tile-major order: entry k = i * TET_TE + e is read coalesced
     for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {
-      const int e = k % TET_TE, i = k / TET_TE;
-      int d = 0;
-      T v = 0;
-      if (e < cnt && i < nloc) {
-        d = eldofs[(size_t)perm[start + e] * nloc + i];
-        v = x[d];
-      }
-      sDof[k] = d;
-      sX[k] = v;
+      const int d = tdofs[(size_t)t * TET_TE * nlocp + k];
+      sDof[k] = d < 0 ? 0 : d;
+      sX[k] = d < 0 ? T(0) : x[d];
     }
     for (int k = tid; k < TET_TE * 7; k += TET_TT) {
       const int e = k / 7, c = k % 7;
@@ -499,6 +490,18 @@ static void tet_chunk_setup(gh1_op* op, const std::vector<double>& rule, const s
   GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
 }
 
+// tile-major DOF table of the 32-element tiles: tdofs[(t * nlocp + i) * TET_TE + e]
+// = DOF i of element e of tile t, -1 past the tile's count or nloc
+__global__ void tet_tile_dofs_kernel(int ntiles, int nloc, int nlocp, const int* __restrict__ tiles,
+                                     const int* __restrict__ perm, const int* __restrict__ eldofs, int* __restrict__ tdofs) {
+  const int64_t tot = (int64_t)ntiles * nlocp * TET_TE;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(k % TET_TE), i = (int)((k / TET_TE) % nlocp), t = (int)(k / ((int64_t)TET_TE * nlocp));
+    const int st = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    tdofs[k] = (e < cnt && i < nloc) ? eldofs[(size_t)perm[st + e] * nloc + i] : -1;
+  }
+}
+
 // counting sort of the elements by orientation class; tiles of up to TET_TE
 // elements of one class ([ntiles][4] = class, first position, count, 0)
 static void tet_class_tiles(gh1_op* op) {
@@ -523,6 +526,12 @@ static void tet_class_tiles(gh1_op* op) {
   op->d_tet_perm.upload(perm, s);
   op->d_tet_tiles.upload(tiles, s);
   op->tet_ntiles = (int)tiles.size() / 4;
+  const int nloc = sp->nloc, nlocp = (nloc + 15) / 16 * 16;
+  op->d_tet_tdofs.alloc((size_t)op->tet_ntiles * nlocp * TET_TE);
+  const int64_t tot = (int64_t)op->tet_ntiles * nlocp * TET_TE;
+  tet_tile_dofs_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(
+      op->tet_ntiles, nloc, nlocp, op->d_tet_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_tet_tdofs.p);
+  check_kernel(sp->ctx, "tet_tile_dofs_kernel");
   GH1_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
 }
 
@@ -614,7 +623,7 @@ static void tet_tile_launch_p(gh1_op* op, int grid, const T* D, const T* W, cons
   const TetSmem<T> L{Dm::NLOCP, Dm::template RP<MASS>(), Dm::template RP<MASS>() + 1};
   gh1_space* sp = op->sp;
   tet_tile_kernel<T, MASS, P><<<grid, TET_TT, L.total(), sp->ctx->stream>>>(
-      op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, G, M, D, W, x, y, partial, counter, energy,
+      op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, op->d_tet_tdofs.p, G, M, D, W, x, y, partial, counter, energy,
       skip);
   check_kernel(sp->ctx, "tet_tile_kernel");
 }
@@ -645,7 +654,7 @@ static void tet_chunk_launch(gh1_op* op, int per_sm, const T* Dg, const T* Dm, c
 #define GH1_CHUNK_LAUNCH(MASS, TI)                                                                       \
   tet_tile_chunk_kernel<T, MASS, TI><<<grid, TET_TT, smem, sp->ctx->stream>>>(                            \
       op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncg, op->tet_ncm,      \
-      sp->d_eldofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip)
+      op->d_tet_tdofs.p, G, M, Dg, Dm, Wg, Wm, x, y, partial, counter, energy, skip)
   const bool ti6 = tet_ti_of(nlocp) == 6;
   if (op->has_mass) {
     if (ti6) GH1_CHUNK_LAUNCH(true, 6); else GH1_CHUNK_LAUNCH(true, 12);
@@ -703,7 +712,7 @@ __host__ __device__ inline size_t tet_bdb_smem(int nlocp) {
 template <class T, bool PP, int TI>
 __global__ void __launch_bounds__(TET_TT)
 tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm, int nloc, int nlocp, int ncb,
-               int nq, const int* __restrict__ eldofs, const T* __restrict__ Mh, const T* __restrict__ Tb,
+               int nq, const int* __restrict__ tdofs, const T* __restrict__ Mh, const T* __restrict__ Tb,
                const T* __restrict__ Wb, const T* __restrict__ x, T* __restrict__ y, double* partial,
                unsigned int* counter, double* energy, const int* skip) {
   if (skip && *(volatile const int*)skip) return;
@@ -722,16 +731,11 @@ tet_bdb_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict_
   for (int t = t0; t < t1; t++) {
     const int cls = tiles[4 * t], start = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
     __syncthreads();
+    // the tile's DOFs in tile-major order: entry k = i * TET_TE + e is read coalesced
     for (int k = tid; k < TET_TE * nlocp; k += TET_TT) {
-      const int e = k % TET_TE, i = k / TET_TE;
-      int d = 0;
-      T v = 0;
-      if (e < cnt && i < nloc) {
-        d = eldofs[(size_t)perm[start + e] * nloc + i];
-        v = x[d];
-      }
-      sDof[k] = d;
-      sX[k] = v;
+      const int d = tdofs[(size_t)t * TET_TE * nlocp + k];
+      sDof[k] = d < 0 ? 0 : d;
+      sX[k] = d < 0 ? T(0) : x[d];
     }
     if (!PP)
       for (int k = tid; k < TET_TE * 16; k += TET_TT) {
@@ -897,7 +901,7 @@ static void tet_bdb_launch(gh1_op* op, int per_sm, const T* Mh, const T* Tb, con
 #define GH1_BDB_LAUNCH(PP, TI)                                                                            \
   tet_bdb_kernel<T, PP, TI><<<grid, TET_TT, smem, sp->ctx->stream>>>(                                     \
       op->tet_ntiles, op->d_tet_tiles.p, op->d_tet_perm.p, sp->nloc, nlocp, op->tet_ncb, sp->tet_nq_mass,  \
-      sp->d_eldofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip)
+      op->d_tet_tdofs.p, Mh, Tb, Wb, x, y, partial, counter, energy, skip)
   const bool ti6 = tet_ti_of(nlocp) == 6;
   if (op->bdb == 1) {
     if (ti6) GH1_BDB_LAUNCH(true, 6); else GH1_BDB_LAUNCH(true, 12);
