@@ -1,5 +1,5 @@
 // cg.cu -- Jacobi preconditioner, preconditioned CG (FP64 and FP32-inner with
-// FP64 iterative refinement) and the adjoint gradient driver.
+// FP64 iterative refinement) and the adjoint gradient entry point.
 //
 // CG follows CGSolver._SolveImpl (python/krylovspace.py:263-291) step by step:
 //   d = b - A x; w = P d; s = w; wdn = w.d; check sqrt|wdn|
