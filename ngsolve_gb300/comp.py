@@ -19,6 +19,7 @@ python/krylovspace.py (solvers.CG).  Coefficients are per-element constants
 numerical call goes to libgh1.so on the GPU; there is no CPU path.
 """
 import ctypes
+import weakref
 
 import numpy as np
 import torch
@@ -891,22 +892,37 @@ class BaseMatrix:
     def MultAdd(self, s, x, y):
         self._apply(s, x, y, 1)
 
-    # Every operator on this path is symmetric: sum_e B^T G B with a symmetric G
-    # (scalar kappa, a symmetric tensor, the mass term), the Jacobi diagonal and
-    # the projectors.  So the transpose products apply the same operator.
+    # The operators of the Laplace / mass / tensor forms, the Jacobi diagonal and
+    # the projectors are symmetric (sum_e B^T G B with a symmetric G), so their
+    # transpose products apply the operator itself.  A generic B^T D B form with
+    # a non-symmetric D (convection b.grad(u) v, for example) carries a factory
+    # `_transposer` for the operator of the transposed form, D^T (built on first use).
+    def _transpose_op(self):
+        back = getattr(self, "_transpose_of", None)  # this is the transposed operator of another
+        if back is not None and back() is not None:
+            return back()
+        f = getattr(self, "_transposer", None)
+        if f is None:
+            return self
+        if getattr(self, "_transposed", None) is None:
+            self._transposed = f()
+            self._transposed._transpose_of = weakref.ref(self)
+        return self._transposed
+
     def MultTrans(self, value, x, y):
         """y = A^T x.  As in the reference binding (linalg/python_linalg.cpp:1074),
         y is cleared and A^T x added; `value` is accepted and not applied."""
-        self._apply(1.0, x, y, 0)
+        self._transpose_op()._apply(1.0, x, y, 0)
 
     def MultTransAdd(self, value, x, y):
         """y += value * A^T x (linalg/python_linalg.cpp:1075)."""
-        self._apply(value, x, y, 1)
+        self._transpose_op()._apply(value, x, y, 1)
 
     @property
     def T(self):
-        """The transpose: this operator itself (it is symmetric)."""
-        return self
+        """The transpose: this operator itself where it is symmetric, else the
+        operator of the transposed form."""
+        return self._transpose_op()
 
     def CreateDeviceMatrix(self):
         """The operator already lives on the device (BaseMatrix.CreateDeviceMatrix)."""
@@ -1410,6 +1426,11 @@ class BilinearForm:
             ctx.check(ctx.lib.gh1_form_create(sfes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(h)))
             self._form = h
             ctx.check(ctx.lib.gh1_form_set_bdb(h, _ptr(D), 0 if pts is None else 1, _lib.GH1_MEM_DEVICE))
+            # the transposed form's D, kept while it differs from D
+            Dm = D.reshape(*D.shape[:-1], 4, 4)
+            DT = Dm.transpose(-1, -2).reshape(D.shape).contiguous()
+            sym = float((DT - D).abs().max()) <= 1e-14 * max(float(D.abs().max()), 1e-300)
+            self._bdb_T = None if sym else (DT, pts is not None)
             return self._form
         if self._form is None:
             h = ctypes.c_void_p()
@@ -1434,12 +1455,36 @@ class BilinearForm:
         else:
             ctx.check(ctx.lib.gh1_assemble_csr(form, ctypes.byref(h)))
             mat = SparseMatrix(ctx, h, sfes)
+        if self._generic and getattr(self, "_bdb_T", None) is not None:
+            mat._transposer = self._transposer(*self._bdb_T)
         if sfes is not self.fes:  # VectorH1: the scalar operator once per component
             hb = ctypes.c_void_p()
             ctx.check(ctx.lib.gh1_op_block_create(mat.h, self.fes.dim, ctypes.byref(hb)))
             mat = BlockMatrix(ctx, hb, self.fes, mat)
         self.mat = mat
         return self
+
+    def _transposer(self, DT, per_point):
+        """Factory of the operator of the transposed B^T D B form (D^T), of the
+        same kind as this form's (matrix-free with the same precisions, or CSR)."""
+        ctx, sfes, nonassemble, precision = self.fes.ctx, self._sfes, self.nonassemble, self.precision
+
+        def make():
+            ctx.sync_stream()
+            hf = ctypes.c_void_p()
+            ctx.check(ctx.lib.gh1_form_create(sfes.h, None, None, _lib.GH1_MEM_HOST, ctypes.byref(hf)))
+            try:
+                ctx.check(ctx.lib.gh1_form_set_bdb(hf, _ptr(DT), 1 if per_point else 0, _lib.GH1_MEM_DEVICE))
+                h = ctypes.c_void_p()
+                if nonassemble:
+                    mask = 1 | (2 if precision in ("fp32", "mixed") else 0)
+                    ctx.check(ctx.lib.gh1_matfree_create(hf, mask, ctypes.byref(h)))
+                    return BilinearFormApplication(ctx, h, sfes.ndof, sfes)
+                ctx.check(ctx.lib.gh1_assemble_csr(hf, ctypes.byref(h)))
+                return SparseMatrix(ctx, h, sfes)
+            finally:
+                ctx.lib.gh1_form_free(hf)  # the operator keeps its form alive
+        return make
 
     def Apply(self, x, y):
         if self.mat is None:

@@ -212,6 +212,51 @@ def test_bdb_assembled(gpu, hexes, p, jit, pointwise):
     assert abs(lhs - rhs) <= 1e-11 * np.linalg.norm(z) * np.linalg.norm(Ax)
 
 
+def _csr_T_apply(rp, ci, va, x):
+    """(CSR)^T x on the host."""
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    y = np.zeros(len(rp) - 1)
+    np.add.at(y, ci, np.asarray(va) * x[rows])
+    return y
+
+
+@pytest.mark.parametrize("hexes,p,pointwise", [(True, 3, False), (True, 2, True), (False, 3, False), (False, 2, True)])
+def test_bdb_transpose_products(gpu, hexes, p, pointwise):
+    """A non-symmetric B^T D B form: MultTrans, MultTransAdd and .T of the
+    matrix-free and the assembled operator apply A^T (the form with D^T),
+    checked against the transpose of the assembled CSR (1e-12); .T.T is A.  A
+    symmetric form's transpose is the operator itself."""
+    m = _mesh(hexes, 3 if hexes else 2, 0.1)
+    fes = gpu.H1(m, order=p)
+    terms = _terms(gpu, fes, m.ne, 80 + p, pointwise)
+    form = sum(terms[1:], terms[0])
+    acsr = gpu.BilinearForm(form).Assemble()
+    rp, ci, va = acsr.mat.CSR()
+    x = np.random.default_rng(81).normal(size=fes.ndof)
+    yT = _csr_T_apply(rp, ci, va, x)
+    yA = O.spmv(rp, ci, va, x)
+    sc = np.abs(yT).max()
+    assert np.abs(yT - yA).max() > 1e-3 * sc  # the form is not symmetric
+    amf = gpu.BilinearForm(form, nonassemble=True).Assemble()
+    for mat in (amf.mat, acsr.mat):
+        xv = gpu.BaseVector(data=torch.tensor(x, dtype=torch.float64, device="cuda"))
+        yv = gpu.BaseVector(fes.ndof)
+        mat.MultTrans(1.0, xv, yv)
+        assert np.abs(yv.NumPy() - yT).max() <= 1e-12 * sc
+        yv.data = x
+        mat.MultTransAdd(2.0, xv, yv)
+        assert np.abs(yv.NumPy() - (x + 2.0 * yT)).max() <= 1e-12 * (sc + np.abs(x).max())
+        yv2 = gpu.BaseVector(fes.ndof)
+        mat.T.Mult(xv, yv2)
+        assert np.abs(yv2.NumPy() - yT).max() <= 1e-12 * sc
+        assert mat.T.T is mat
+    u, v = fes.TnT()
+    sym = gpu.BilinearForm(fes, nonassemble=True)
+    sym += gpu.CoefficientFunction(lognormal(m.ne, 0.5, 3)) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+    sym.Assemble()
+    assert sym.mat.T is sym.mat
+
+
 @pytest.mark.parametrize("pointwise,p", [(False, 3), (True, 3), (True, 5)])
 def test_bdb_laplace_type_takes_standard_kernels(gpu, pointwise, p, monkeypatch):
     """A generic hex form whose D is diag(mu, K) with K symmetric runs on the
