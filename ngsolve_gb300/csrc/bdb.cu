@@ -323,6 +323,43 @@ static void hex_bdb_launch(gh1_op* op, const T* x, T* y, const T* G, int gstride
 #undef GH1_BAPP_CASE
 }
 
+// FP32, one record per affine element: the paired kernel (two elements per lane,
+// G mode 3 of hexpair.cu) or the one-element kernel, whichever is faster on this
+// operator's mesh (GH1_BDB_PAIR=0/1 forces one)
+static bool bdb_pair_choice(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->bdb_pair = false;
+  op->pair_per_sm[3] = 0;
+  if (!(op->prec_mask & 2) || op->bdb != 2 || !hex_pair_supported(sp->p + 1)) return false;
+  set_first_wait_polls();
+  upload_pair_tables(sp);
+  op->pair_per_sm[3] = hex_pair_occupancy(op, 3);
+  if (op->pair_per_sm[3] <= 0) return false;
+  const char* env = getenv("GH1_BDB_PAIR");
+  if (env) return env[0] == '1';
+  if (sp->mesh->ne < 4096) return false;
+  cudaStream_t s = sp->ctx->stream;
+  DBuf<float> xs(op->nrows), ys(op->nrows);
+  xs.zero(s);
+  cudaEvent_t a, b;
+  GH1_CUDA(cudaEventCreate(&a));
+  GH1_CUDA(cudaEventCreate(&b));
+  float ms[2];
+  for (int v = 0; v < 2; v++) {
+    for (int r = 0; r < 5; r++) {
+      if (r == 2) GH1_CUDA(cudaEventRecord(a, s));
+      if (v == 0) hex_bdb_launch<float>(op, xs.p, ys.p, op->d_G32.p, op->gstride32, nullptr, nullptr, nullptr, nullptr);
+      else hex_pair_apply(op, 3, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+    }
+    GH1_CUDA(cudaEventRecord(b, s));
+    GH1_CUDA(cudaEventSynchronize(b));
+    GH1_CUDA(cudaEventElapsedTime(&ms[v], a, b));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms[1] < ms[0];
+}
+
 void bdb_setup(gh1_op* op) {
   gh1_space* sp = op->sp;
   gh1_form* f = op->form;
@@ -387,6 +424,7 @@ void bdb_setup(gh1_op* op) {
     upload_const_tables(sp);
     op->bdb_per_sm[0] = hex_bdb_occupancy<double>(op, op->gstride64);
     op->bdb_per_sm[1] = want32 ? hex_bdb_occupancy<float>(op, op->gstride32) : 0;
+    op->bdb_pair = bdb_pair_choice(op);
   } else {
     const int nq = sp->tet_nq_mass, d_pp = dmode == 2 ? 1 : 0, per_point = (d_pp || deformed) ? 1 : 0;
     const size_t nrec = (size_t)ne * (per_point ? nq : 1) * 16;
@@ -415,6 +453,8 @@ void bdb_apply(gh1_op* op, const void* x, void* y, int prec, double* partial, un
   }
   if (prec == GH1_F64)
     hex_bdb_launch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->gstride64, partial, counter, energy, skip);
+  else if (op->bdb_pair)
+    hex_pair_apply(op, 3, (const float*)x, (float*)y, partial, counter, energy, skip);
   else
     hex_bdb_launch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->gstride32, partial, counter, energy, skip);
 }

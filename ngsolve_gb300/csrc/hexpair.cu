@@ -171,7 +171,8 @@ __device__ __forceinline__ void eo2_bwd(const f2* v, f2* out) {
 // variant (p=4: 4 blocks = 128 registers with the G tile in shared memory or a
 // metric per element, 5 blocks = 96 with direct G loads; p=6: 3 blocks = 168)
 constexpr int pair_min_blocks(int N, bool mass, int gm) {
-  return N == 2   ? 6
+  return gm == 3 ? (N <= 4 ? 4 : N == 5 ? 3 : 2)  // B^T D B records: 16 packed coefficients in registers
+         : N == 2 ? 6
          : N == 3 ? (mass ? (gm ? 5 : 4) : (gm ? 6 : 5))
          : N == 4 ? (mass ? (gm ? 5 : 4) : 5)
          : N == 5 ? (mass ? (gm ? 4 : 3) : (gm == 1 ? 5 : 4))
@@ -434,6 +435,12 @@ __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool activ
   group_sync<G>(gid);
 }
 
+// GM: 0 = per-point G tile bulk-copied into shared memory, 1 = per-point G rows
+// loaded directly (after a bulk L2 prefetch), 2 = one metric record per affine
+// element (8 floats: G and the mass coefficient), 3 = the generic B^T D B form
+// with one 16-float record per affine element (the reference-coordinate 4x4
+// matrix Mh of bdb.cu, row = test component (v, d/dxi, d/deta, d/dzeta), column =
+// trial component; MASS = true), the rule weight applied in the kernel.
 template <int N, bool MASS, int GM>
 __global__ void __launch_bounds__(PairCfg<N>::BLOCK, pair_min_blocks(N, MASS, GM))
 hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const float* __restrict__ Gq, int gstride,
@@ -579,7 +586,30 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     const float* Ga = GM == 0 ? gbuf + (size_t)r0 * rowg : Gq + ((size_t)ch * E + r0) * gstride;
     const float* Gb = GM == 0 ? gbuf + (size_t)r1 * rowg : Gq + ((size_t)ch * E + r1) * gstride;
     f2 vx[N], vy[N], vz[N], vm[N];
-    if (active) {
+    if (GM == 3 && active) {
+      // (vm, vx, vy, vz) = w_i w_j w_k Mh (uq, gx, gy, gz) with one Mh per element
+      constexpr int WO = N * (N - 1) / 2 - 1;
+      f2 em[16];
+      const float4* Ea = (const float4*)(Gq + ((size_t)ch * E + r0) * 16);
+      const float4* Eb = (const float4*)(Gq + ((size_t)ch * E + r1) * 16);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float4 a = __ldg(Ea + q), b = __ldg(Eb + q);
+        em[4 * q] = pack2(a.x, b.x); em[4 * q + 1] = pack2(a.y, b.y);
+        em[4 * q + 2] = pack2(a.z, b.z); em[4 * q + 3] = pack2(a.w, b.w);
+      }
+      const float wjk = c_Wp[WO + pl / N] * c_Wp[WO + pl % N];
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        const f2 w = bcast(c_Wp[WO + i] * wjk);
+        const f2 a0 = mul2(w, uq[i]), a1 = mul2(w, gx[i]), a2 = mul2(w, gy[i]), a3 = mul2(w, gz[i]);
+        vm[i] = fma2(em[3], a3, fma2(em[2], a2, fma2(em[1], a1, mul2(em[0], a0))));
+        vx[i] = fma2(em[7], a3, fma2(em[6], a2, fma2(em[5], a1, mul2(em[4], a0))));
+        vy[i] = fma2(em[11], a3, fma2(em[10], a2, fma2(em[9], a1, mul2(em[8], a0))));
+        vz[i] = fma2(em[15], a3, fma2(em[14], a2, fma2(em[13], a1, mul2(em[12], a0))));
+        if (want_e) acc = add2(acc, fma2(uq[i], vm[i], fma2(gz[i], vz[i], fma2(gy[i], vy[i], mul2(gx[i], vx[i])))));
+      }
+    } else if (active) {
       // G mode 2 (every element affine): one metric per element, records of 8
       // floats (xx yy zz xy xz yz, mass, pad), times the rule weight w_i w_j w_k
       constexpr int WO = N * (N - 1) / 2 - 1;
@@ -1319,8 +1349,9 @@ int hex_pair_occupancy(gh1_op* op, int gm) {
                           : pair_occupancy<NN, false, 0>(PairCfg<NN>::total(gs, ts, 0));                      \
     else if (gm == 1) v = mass ? pair_occupancy<NN, true, 1>(PairCfg<NN>::total(gs, ts, 1))                   \
                                : pair_occupancy<NN, false, 1>(PairCfg<NN>::total(gs, ts, 1));                 \
-    else v = mass ? pair_occupancy<NN, true, 2>(PairCfg<NN>::total(8, ts, 2))                                 \
-                  : pair_occupancy<NN, false, 2>(PairCfg<NN>::total(8, ts, 2));                               \
+    else if (gm == 2) v = mass ? pair_occupancy<NN, true, 2>(PairCfg<NN>::total(8, ts, 2))                    \
+                               : pair_occupancy<NN, false, 2>(PairCfg<NN>::total(8, ts, 2));                  \
+    else v = pair_occupancy<NN, true, 3>(PairCfg<NN>::total(16, ts, 3));                                      \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_OCC)
 #undef GH1_PAIR_OCC
@@ -1338,9 +1369,11 @@ void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partia
     } else if (gm == 1) {                                                                       \
       if (mass) pair_launch<NN, true, 1>(op, x, y, partial, counter, energy, skip);             \
       else pair_launch<NN, false, 1>(op, x, y, partial, counter, energy, skip);                 \
-    } else {                                                                                    \
+    } else if (gm == 2) {                                                                       \
       if (mass) pair_launch<NN, true, 2>(op, x, y, partial, counter, energy, skip);             \
       else pair_launch<NN, false, 2>(op, x, y, partial, counter, energy, skip);                 \
+    } else {                                                                                    \
+      pair_launch<NN, true, 3>(op, x, y, partial, counter, energy, skip);                       \
     }                                                                                           \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)

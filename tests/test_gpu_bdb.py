@@ -157,6 +157,60 @@ def test_bdb_variant_paths_agree(gpu, hexes, p, monkeypatch):
         ctx.lib.gh1_form_free(h)
 
 
+def _affine_hexes(nx):
+    """Structured hexes under a general affine map (every element the same
+    parallelepiped): one record per element applies."""
+    from ngsolve_gb300.meshes import Mesh as RawMesh
+    m = MakeStructured3DMesh(hexes=True, nx=nx)
+    A = np.array([[1.0, 0.3, -0.2], [0.1, 0.8, 0.25], [-0.15, 0.2, 1.3]])
+    return RawMesh(m.points @ A.T + np.array([0.5, -1.0, 2.0]), m.elements)
+
+
+@pytest.mark.parametrize("pair", ["0", "1"])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
+def test_bdb_paired_records(gpu, monkeypatch, p, pair):
+    """FP32 B^T D B with one record per affine element, on the paired kernel
+    (two elements per lane; GH1_BDB_PAIR=1, variant 9) and on the one-element
+    kernel (GH1_BDB_PAIR=0, variant 8): within 2e-5 of the oracle, with 27 and 8
+    elements (the odd count leaves the last pair half empty)."""
+    monkeypatch.setenv("GH1_BDB_PAIR", pair)
+    for nx in (3, 2):
+        m = _affine_hexes(nx)
+        fes = gpu.H1(m, order=p)
+        terms = _terms(gpu, fes, m.ne, 90 + p, False)
+        a = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True, precision="fp32").Assemble()
+        assert a.mat.Info()["hex_variant_fp32"] == (9 if pair == "1" else 8)
+        D = _oracle_D(terms, m.ne, None)
+        x = np.random.default_rng(91).normal(size=fes.ndof)
+        yo = O.OracleSpace(m.points, m.elements, p).apply_bdb(x, D)
+        assert np.abs(_apply(gpu, a, x, torch.float32) - yo).max() <= 2e-5 * np.abs(yo).max()
+        assert np.abs(_apply(gpu, a, x, torch.float64) - yo).max() <= 1e-12 * np.abs(yo).max()
+
+
+def test_bdb_paired_records_mixed_cg(gpu, monkeypatch):
+    """A symmetric generic form outside the Laplace type (value-gradient coupling
+    u (c . grad v) + (c . grad u) v) on the paired record kernel: the mixed CG,
+    which uses the kernel's fused energy, reaches the FP64 CG's solution (1e-8)."""
+    monkeypatch.setenv("GH1_BDB_PAIR", "1")
+    m = _affine_hexes(4)
+    fes = gpu.H1(m, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+    c = gpu.CoefficientFunction((0.2, -0.1, 0.15))
+    form = (gpu.CoefficientFunction(lognormal(m.ne, 0.5, 92)) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+            + gpu.InnerProduct(c, gpu.grad(u)) * v * gpu.dx + u * gpu.InnerProduct(c, gpu.grad(v)) * gpu.dx
+            + gpu.CoefficientFunction(2.0) * u * v * gpu.dx)
+    a = gpu.BilinearForm(form, nonassemble=True, precision="mixed").Assemble()
+    assert a.mat.Info()["hex_variant_fp32"] == 9
+    f = gpu.LinearForm(gpu.CoefficientFunction(np.random.default_rng(93).uniform(-1, 1, m.ne)) * v * gpu.dx).Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    xm = gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-11, maxsteps=5000, printrates=False,
+                        mode="mixed").NumPy().copy()
+    assert gpu.solvers.CG.last_solver.result.applies32 > 0
+    x6 = gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-12, maxsteps=5000, printrates=False,
+                        mode="fp64").NumPy()
+    assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
+
+
 @pytest.mark.parametrize("hexes,p", [(True, 3), (False, 2)])
 def test_bdb_symmetric_form_solves_like_laplace(gpu, hexes, p):
     """(1 + 0 x) grad u . grad v + mu u v is the Laplace + mass operator written as
