@@ -261,6 +261,10 @@ struct gh1_op {
   gh1::DBuf<float> d_tet_tc_G;               // [tile][6][128]: the FP32 metric of tile row m (rebuilt
                                              // with the metric)
   bool tet_use_tc = false;                   // FP32 tet apply on the tensor cores (timed at setup)
+  bool tet_bdb_tc = false;                   // FP32 tet B^T D B (records per element) on the tensor cores
+  int tet_bdb_tc_per_sm = 0;                 // its resident CTAs (0: not available)
+  gh1::DBuf<float> d_tet_bdb_tab;            // its class operands (TF32 hi / lo, shared-memory layout)
+  gh1::DBuf<float> d_tet_bdb_M;              // its element records tile-major [tile][16][128]
   int tet_ncg = 0, tet_ncm = 0;              // gradient / mass-rule chunks
   gh1::DBuf<double> d_tetDm64, d_tetwm64;    // chunked mass-rule tables and weights
   gh1::DBuf<float> d_tetDm32, d_tetwm32;
@@ -371,6 +375,11 @@ void hex_slice_apply(gh1_op* op, const float* x, float* y, double* partial, unsi
 // FP32 tet apply with both tile products on the tensor cores (tettc.cu)
 bool tet_tc_supported(int p);
 void tet_tc_setup(gh1_op* op);
+// tensor-core tet B^T D B (tettc.cu): setup from the degree-2p tables [class][q][i][4]
+// (t64, FP64), after the class tiles and the element records; apply
+void tet_bdb_tc_setup(gh1_op* op, const double* t64);
+void tet_bdb_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                      const int* skip);
 void tet_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                   const int* skip);
 // FP32 hex apply with the 1D contractions on the tensor cores (hextc.cu)

@@ -888,6 +888,8 @@ void tet_bdb_setup(gh1_op* op) {
     op->d_tetBw32.upload(w32, s);
     op->bdb_per_sm[1] = pp ? tet_bdb_occupancy<float, true>(nlocp) : tet_bdb_occupancy<float, false>(nlocp);
   }
+  GH1_CUDA(cudaStreamSynchronize(s));
+  tet_bdb_tc_setup(op, t64.p);         // FP32, records per element: the tensor-core form where faster
   GH1_CUDA(cudaStreamSynchronize(s));  // tables and host staging go out of scope
 }
 
@@ -918,7 +920,9 @@ void tet_bdb_apply(gh1_op* op, int prec, const void* x, void* y, double* partial
   if (prec == GH1_F64)
     tet_bdb_launch<double>(op, op->bdb_per_sm[0], op->d_G64.p, op->d_tetB64.p, op->d_tetBw64.p, (const double*)x,
                            (double*)y, partial, counter, energy, skip);
-  else {
+  else if (op->tet_bdb_tc) {
+    tet_bdb_tc_apply(op, (const float*)x, (float*)y, partial, counter, energy, skip);
+  } else {
     GH1_CHECK(op->bdb_per_sm[1] > 0, GH1_ERR_ARG, "operator has no FP32 data (precision_mask)");
     tet_bdb_launch<float>(op, op->bdb_per_sm[1], op->d_G32.p, op->d_tetB32.p, op->d_tetBw32.p, (const float*)x,
                           (float*)y, partial, counter, energy, skip);

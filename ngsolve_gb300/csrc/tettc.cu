@@ -361,21 +361,15 @@ __global__ void tet_tc_g_kernel(int ntiles, const int* __restrict__ tiles, const
   }
 }
 
-// tiles of up to 128 same-class elements over the class-sorted order of the
-// tiled apply, and the CTAs per SM (0: not available: order, mass term,
-// GH1_TET_TC=0)
-void tet_tc_setup(gh1_op* op) {
+// tiles of up to 128 same-class elements (consecutive 32-element tiles of the
+// class-sorted order merged) and their tile-major DOF table
+static void tet_tc_build_tiles(gh1_op* op) {
   gh1_space* sp = op->sp;
-  op->tet_tc_per_sm = 0;
-  const char* env = getenv("GH1_TET_TC");
-  if (!tet_tc_supported(sp->p) || op->has_mass || !(op->prec_mask & 2) || op->tet_ntiles == 0 || op->tet_chunked ||
-      (env && env[0] == '0'))
-    return;
   cudaStream_t s = sp->ctx->stream;
   std::vector<int> small(4 * (size_t)op->tet_ntiles);
   GH1_CUDA(cudaMemcpyAsync(small.data(), op->d_tet_tiles.p, small.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
   GH1_CUDA(cudaStreamSynchronize(s));
-  std::vector<int> tiles;  // merge consecutive 32-element tiles of one class into tiles of up to 128
+  std::vector<int> tiles;
   for (int k = 0; k < op->tet_ntiles; k++) {
     const int c = small[4 * k], a = small[4 * k + 1], n = small[4 * k + 2];
     const size_t m = tiles.size();
@@ -388,11 +382,26 @@ void tet_tc_setup(gh1_op* op) {
   op->d_tet_tc_tiles.upload(tiles, s);
   op->tet_tc_ntiles = (int)tiles.size() / 4;
   op->d_tet_tc_dofs.alloc((size_t)op->tet_tc_ntiles * sp->nloc * 128);
+  const int64_t tot = (int64_t)op->tet_tc_ntiles * sp->nloc * 128;
+  tet_tc_dofs_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(
+      op->tet_tc_ntiles, sp->nloc, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_tet_tc_dofs.p);
+  check_kernel(sp->ctx, "tet_tc_dofs_kernel");
+  GH1_CUDA(cudaStreamSynchronize(s));  // host staging goes out of scope
+}
+
+// tiles of up to 128 same-class elements over the class-sorted order of the
+// tiled apply, and the CTAs per SM (0: not available: order, mass term,
+// GH1_TET_TC=0)
+void tet_tc_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->tet_tc_per_sm = 0;
+  const char* env = getenv("GH1_TET_TC");
+  if (!tet_tc_supported(sp->p) || op->has_mass || !(op->prec_mask & 2) || op->tet_ntiles == 0 || op->tet_chunked ||
+      (env && env[0] == '0'))
+    return;
+  cudaStream_t s = sp->ctx->stream;
+  tet_tc_build_tiles(op);
   {
-    const int64_t tot = (int64_t)op->tet_tc_ntiles * sp->nloc * 128;
-    tet_tc_dofs_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, s>>>(
-        op->tet_tc_ntiles, sp->nloc, op->d_tet_tc_tiles.p, op->d_tet_perm.p, sp->d_eldofs.p, op->d_tet_tc_dofs.p);
-    check_kernel(sp->ctx, "tet_tc_dofs_kernel");
     op->d_tet_tc_G.alloc((size_t)op->tet_tc_ntiles * 6 * 128);
     const int64_t tg = (int64_t)op->tet_tc_ntiles * 6 * 128;
     tet_tc_g_kernel<<<(unsigned)std::min<int64_t>((tg + 255) / 256, 65535), 256, 0, s>>>(
@@ -428,6 +437,365 @@ void tet_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigne
     case 4: tet_tc_launch_p<4>(op, x, y, partial, counter, energy, skip); break;
     default: throw Error(GH1_ERR_UNSUPPORTED, "tensor-core tet apply: order out of range");
   }
+}
+
+
+// ---- generic B^T D B on the tensor cores (records per element) -------------------
+// The same machinery for a(u, v) = sum_e int_e (B v)^T D_e (B u), B w = (w, grad w),
+// on affine tets with one reference-coordinate record Mh_e per element (bdb.cu):
+//   P[m][r] = sum_i X[m][i] T_c[i][r]     r = 4 q + comp: value and the three
+//                                         reference derivatives at point q of the
+//                                         degree-2p rule (point-major columns)
+//   V[m][4q + .] = w_q Mh_m P[m][4q + .]  (per element and point, registers)
+//   Y[m][i] = sum_r V[m][r] T_c[i][r]
+// Point-major columns make every chunk of KC = 40 columns (10 points) of V
+// self-contained, so the second product runs in chunks through two
+// shared-memory buffers: the transform of chunk j fills one while the product of
+// chunk j-1 reads the other (two mbarriers, one product in flight on each).
+template <int P>
+struct TetBdbTcCfg {
+  static constexpr int NLOC = (P + 1) * (P + 2) * (P + 3) / 6;
+  static constexpr int NQ = P == 2 ? 14 : P == 3 ? 24 : 46;  // degree-2p rule points (tables.cu tet_rule)
+  static constexpr int R = 4 * NQ;
+  static constexpr int K1 = (NLOC + 7) / 8 * 8;    // forward K (local DOFs)
+  static constexpr int N1 = (R + 15) / 16 * 16;    // forward N = backward K
+  static constexpr int N2 = (NLOC + 15) / 16 * 16; // backward N
+  static constexpr int KC = 40;                     // chunk of V columns (10 points; a multiple of 8)
+  static constexpr int NCH = (N1 + KC - 1) / KC;
+  static constexpr int LW = N1 - (NCH - 1) * KC;    // width of the last chunk (a multiple of 8)
+  static constexpr int C2 = N1;                     // TMEM column of the backward accumulator
+  static constexpr int TCOLS = (N1 + N2) <= 128 ? 128 : 256;
+  static constexpr int ABUF = 2 * 128 * KC;         // floats of one operand buffer (hi, lo)
+  static constexpr int T1 = 2 * ABUF;               // [hi, lo][N1][K1]
+  static constexpr int T2 = T1 + 2 * N1 * K1;       // [hi, lo][N2][N1]
+  static constexpr int W = T2 + 2 * N2 * N1;        // rule weights [NQ] (padded to 4)
+  static constexpr int BAR = W + (NQ + 3) / 4 * 4;  // two mbarriers (16 B) + TMEM base (4 B)
+  static constexpr size_t smem = (size_t)(BAR + 6) * sizeof(float);
+  static constexpr int TAB = 2 * N1 * K1 + 2 * N2 * N1;  // floats of one class's operands
+  static_assert(K1 <= KC && LW % 8 == 0 && (LW / 2) % 4 == 0, "chunk layout");
+  static_assert(N1 + N2 <= 256, "tensor memory columns");
+};
+
+// W consecutive accumulator columns of this thread's row (W = 4, 8, 12, 16, 20)
+template <int W>
+__device__ __forceinline__ void tt_ldw(uint32_t taddr, float* v) {
+  uint32_t r[20];
+  if constexpr (W >= 16) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+  }
+  constexpr int O8 = W >= 16 ? 16 : 0;
+  if constexpr ((W - O8) >= 8) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[O8]), "=r"(r[O8 + 1]), "=r"(r[O8 + 2]), "=r"(r[O8 + 3]), "=r"(r[O8 + 4]), "=r"(r[O8 + 5]),
+                   "=r"(r[O8 + 6]), "=r"(r[O8 + 7])
+                 : "r"(taddr + O8));
+  }
+  constexpr int O4 = O8 + ((W - O8) >= 8 ? 8 : 0);
+  if constexpr ((W - O4) >= 4) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[O4]), "=r"(r[O4 + 1]), "=r"(r[O4 + 2]), "=r"(r[O4 + 3])
+                 : "r"(taddr + O4));
+  }
+  static_assert(W % 4 == 0 && W <= 20, "column count");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < W; i++) v[i] = __uint_as_float(r[i]);
+}
+
+template <int P>
+__global__ void __launch_bounds__(TT_THREADS, 1)
+tet_bdb_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ tdofs, const float* __restrict__ Mt,
+                  const float* __restrict__ tab, const double* __restrict__ W64, const float* __restrict__ x,
+                  float* __restrict__ y, double* partial, unsigned int* counter, double* energy, const int* skip,
+                  int* err) {
+  using C = TetBdbTcCfg<P>;
+  constexpr int NLOC = C::NLOC, NQ = C::NQ, K1 = C::K1, N1 = C::N1, N2 = C::N2, KC = C::KC, NCH = C::NCH;
+  if (skip && *(volatile const int*)skip) return;
+  extern __shared__ __align__(1024) float ts[];
+  float* sA = ts;  // buffer 0: X (K = K1), then V chunks alternate between buffers 0 and 1
+  float* sT1 = ts + C::T1;
+  float* sT2 = ts + C::T2;
+  float* sW = ts + C::W;
+  uint64_t* bar = (uint64_t*)(ts + C::BAR);  // [0], [1]
+  uint32_t* tslot = (uint32_t*)(ts + C::BAR + 4);
+  const int t = threadIdx.x, warp = t >> 5, m = t & 127, half = t >> 7;
+  for (int i = t; i < 2 * C::ABUF; i += TT_THREADS) ts[i] = 0.f;
+  for (int i = t; i < NQ; i += TT_THREADS) sW[i] = (float)W64[i];
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(C::TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // lanes of row m
+  uint32_t ph[2] = {0u, 0u};
+  int pend[2] = {0, 0};  // commits issued on each barrier and not yet waited for (0 or 1)
+  bool ok = true;
+  double acc = 0.0;
+  int loaded = -1;
+  auto issue_on = [&](int b, auto&& issue) {  // operands visible to the tensor core, issue, commit to bar[b]
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      issue();
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&bar[b]))
+                   : "memory");
+    }
+    pend[b] = 1;
+  };
+  auto wait_on = [&](int b) {
+    const bool got = mbar_wait_bounded(&bar[b], ph[b]);
+    if (got) {
+      ph[b] ^= 1u;
+      pend[b] = 0;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return __syncthreads_and(got) != 0;
+  };
+  constexpr int H1 = K1 / 2;
+  float xv[H1];
+  auto dof_of = [&](int tl_, int i) { return __ldg(tdofs + ((size_t)tl_ * NLOC + i) * 128 + m); };
+  auto gather = [&](int tl_) {
+    const bool a = m < tiles[4 * tl_ + 2];
+#pragma unroll
+    for (int j = 0; j < H1; j++) {
+      const int i = half * H1 + j;
+      xv[j] = (a && i < NLOC) ? __ldg(x + dof_of(tl_, i)) : 0.f;
+    }
+  };
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  if (t0 < t1) gather(t0);
+  for (int tile = t0; ok && tile < t1; tile++) {
+    const int cls = tiles[4 * tile], cnt = tiles[4 * tile + 2];
+    if (cls != loaded) {  // both B operands of the class (TF32 hi / lo, final layout)
+      __syncthreads();
+      const float4* src = (const float4*)(tab + (size_t)cls * C::TAB);
+      float4* dst = (float4*)sT1;
+      for (int k = t; k < C::TAB / 4; k += TT_THREADS) dst[k] = __ldg(src + k);
+      loaded = cls;
+    }
+    const bool act = m < cnt;
+#pragma unroll
+    for (int j = 0; j < H1; j += 4) tt_put4<K1>(sA, m, half * H1 + j, xv + j);
+    float mh[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) mh[c] = act ? __ldg(Mt + ((size_t)tile * 16 + c) * 128 + m) : 0.f;
+    // ---- P = X T_c ------------------------------------------------------------------
+    issue_on(1, [&] { tt_gemm<K1, K1, 0, N1, N1, false>(tmem, sA, sT1); });
+    if (!(ok = wait_on(1))) break;
+    // ---- V chunk by chunk, Y += V_j T_c[:, chunk j]^T -----------------------------------
+    float en = 0.f;
+    auto chunk = [&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      constexpr int KCJ = J < NCH - 1 ? KC : C::LW, K0 = J * KC, HW = KCJ / 2;
+      float* buf = sA + (J & 1) * C::ABUF;
+      if (J >= 2 && ok) ok = wait_on(J & 1);  // the product of chunk J-2 has read this buffer
+      if (!ok) return;
+      float pv[HW];
+      tt_ldw<HW>(tl + K0 + half * HW, pv);
+#pragma unroll
+      for (int pt = 0; pt < HW / 4; pt++) {
+        const int q = (K0 + half * HW) / 4 + pt;
+        float o[4];
+        const float w = q < NQ ? sW[q < NQ ? q : 0] : 0.f;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          o[r] = w * (mh[4 * r] * pv[4 * pt] + mh[4 * r + 1] * pv[4 * pt + 1] + mh[4 * r + 2] * pv[4 * pt + 2] +
+                      mh[4 * r + 3] * pv[4 * pt + 3]);
+          if (partial) en += pv[4 * pt + r] * o[r];
+        }
+        tt_put4<KCJ>(buf, m, half * HW + 4 * pt, o);
+      }
+      issue_on(J & 1, [&] { tt_gemm<KCJ, N1, K0, N2, N2, (J > 0)>(tmem + C::C2, buf, sT2); });
+    };
+    static_assert(NCH <= 5, "chunk count");
+    chunk(std::integral_constant<int, 0>());
+    if constexpr (NCH > 1) chunk(std::integral_constant<int, 1>());
+    if constexpr (NCH > 2) chunk(std::integral_constant<int, 2>());
+    if constexpr (NCH > 3) chunk(std::integral_constant<int, 3>());
+    if constexpr (NCH > 4) chunk(std::integral_constant<int, 4>());
+    if (!ok) break;
+    if (partial) acc += (double)en;
+    if (tile + 1 < t1) gather(tile + 1);
+    // the last two products (each barrier has at most one in flight)
+    if (NCH >= 2 && pend[(NCH - 2) & 1]) {
+      if (!(ok = wait_on((NCH - 2) & 1))) break;
+    }
+    if (!(ok = wait_on((NCH - 1) & 1))) break;
+    float yv[N2];
+#pragma unroll
+    for (int c = 0; c < N2; c += 16) tt_ld16(tl + C::C2 + c, yv + c);
+    if (act) {
+      constexpr int HS = (NLOC + 1) / 2;
+      if (half == 0) {
+#pragma unroll
+        for (int i = 0; i < HS; i++) red_add(y + dof_of(tile, i), yv[i]);
+      } else {
+#pragma unroll
+        for (int i = HS; i < NLOC; i++) red_add(y + dof_of(tile, i), yv[i]);
+      }
+    }
+  }
+  if (!ok && t == 0) {
+    atomicExch(err, 1);
+    for (int b = 0; b < 2; b++)
+      if (pend[b]) mbar_wait_bounded(&bar[b], ph[b]);  // the commits still in flight
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TCOLS) : "memory");
+  if (partial) block_reduce_finish(acc, partial, counter, energy);
+}
+
+// per class: T_c as the B operand of both products (TF32 hi / lo from FP64), from
+// the degree-2p tables t64[class][q][i][4]: T1[r][i] and T2[i][r] with r = 4q + comp
+template <int P>
+__global__ void tet_bdb_tc_table_kernel(int ncls, const double* __restrict__ t64, float* __restrict__ tab) {
+  using C = TetBdbTcCfg<P>;
+  constexpr int NLOC = C::NLOC, NQ = C::NQ, R = C::R, K1 = C::K1, N1 = C::N1, N2 = C::N2;
+  const int64_t per = (int64_t)N1 * K1 + (int64_t)N2 * N1, tot = (int64_t)ncls * per;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int cls = (int)(k / per);
+    const int64_t j = k % per;
+    float* T1 = tab + (size_t)cls * C::TAB;
+    float* T2 = T1 + 2 * N1 * K1;
+    int r, i;
+    if (j < (int64_t)N1 * K1) { r = (int)(j / K1); i = (int)(j % K1); }
+    else { i = (int)((j - (int64_t)N1 * K1) / N1); r = (int)((j - (int64_t)N1 * K1) % N1); }
+    const int q = r / 4, comp = r % 4;
+    const double v = (r < R && i < NLOC && q < NQ) ? t64[(((size_t)cls * NQ + q) * NLOC + i) * 4 + comp] : 0.0;
+    const float h = tt_hi((float)v);
+    if (j < (int64_t)N1 * K1) {
+      T1[tt_off<K1>(r, i)] = h;
+      T1[N1 * K1 + tt_off<K1>(r, i)] = (float)(v - (double)h);
+    } else {
+      T2[tt_off<N1>(i, r)] = h;
+      T2[N2 * N1 + tt_off<N1>(i, r)] = (float)(v - (double)h);
+    }
+  }
+}
+
+// tile-major element records: Mt[(t * 16 + c) * 128 + m] (0 past the tile's count)
+__global__ void tet_bdb_tc_rec_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ perm,
+                                      const float* __restrict__ M, float* __restrict__ Mt) {
+  const int64_t tot = (int64_t)ntiles * 16 * 128;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < tot; k += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(k % 128), c = (int)((k / 128) % 16), t = (int)(k / (128 * 16));
+    const int st = tiles[4 * t + 1], cnt = tiles[4 * t + 2];
+    Mt[k] = m < cnt ? M[(size_t)perm[st + m] * 16 + c] : 0.f;
+  }
+}
+
+template <int P>
+static int tet_bdb_tc_prepare_p(gh1_op* op, const double* t64) {
+  using C = TetBdbTcCfg<P>;
+  gh1_space* sp = op->sp;
+  GH1_CHECK(sp->tet_nq_mass == C::NQ, GH1_ERR_ARG, "internal: tet B^T D B rule size");
+  auto kern = tet_bdb_tc_kernel<P>;
+  int dev = 0, optin = 0;
+  GH1_CUDA(cudaGetDevice(&dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
+  if ((size_t)optin < C::smem + fa.sharedSizeBytes) return 0;
+  GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem));
+  int v = 0;
+  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TT_THREADS, C::smem));
+  if (v <= 0) return 0;
+  op->d_tet_bdb_tab.alloc((size_t)N_TET_CLASSES * C::TAB);
+  const int64_t tot = (int64_t)N_TET_CLASSES * ((int64_t)C::N1 * C::K1 + (int64_t)C::N2 * C::N1);
+  tet_bdb_tc_table_kernel<P><<<(unsigned)std::min<int64_t>((tot + 255) / 256, 65535), 256, 0, sp->ctx->stream>>>(
+      N_TET_CLASSES, t64, op->d_tet_bdb_tab.p);
+  check_kernel(sp->ctx, "tet_bdb_tc_table_kernel");
+  return std::min(v, 512 / C::TCOLS);
+}
+
+template <int P>
+static void tet_bdb_tc_launch_p(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter,
+                                double* energy, const int* skip) {
+  gh1_space* sp = op->sp;
+  const int grid = std::max(1, std::min(op->tet_tc_ntiles, sp->ctx->nsm * op->tet_bdb_tc_per_sm));
+  tet_bdb_tc_kernel<P><<<grid, TT_THREADS, TetBdbTcCfg<P>::smem, sp->ctx->stream>>>(
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_tc_dofs.p, op->d_tet_bdb_M.p, op->d_tet_bdb_tab.p,
+      op->d_tetBw64.p, x, y, partial, counter, energy, skip, op->d_err.p);
+  check_kernel(sp->ctx, "tet_bdb_tc_kernel");
+}
+
+void tet_bdb_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
+                      const int* skip) {
+  GH1_CHECK(op->tet_bdb_tc_per_sm > 0, GH1_ERR_ARG, "internal: tensor-core tet B^T D B apply not prepared");
+  switch (op->sp->p) {
+    case 2: tet_bdb_tc_launch_p<2>(op, x, y, partial, counter, energy, skip); break;
+    case 3: tet_bdb_tc_launch_p<3>(op, x, y, partial, counter, energy, skip); break;
+    case 4: tet_bdb_tc_launch_p<4>(op, x, y, partial, counter, energy, skip); break;
+    default: throw Error(GH1_ERR_UNSUPPORTED, "tensor-core tet B^T D B apply: order out of range");
+  }
+}
+
+// FP32, records per element, p = 2..4: the tensor-core form, kept when the setup's
+// timing finds it faster than the class-tiled kernel (GH1_TET_BDB_TC=0/1 forces)
+void tet_bdb_tc_setup(gh1_op* op, const double* t64) {
+  gh1_space* sp = op->sp;
+  op->tet_bdb_tc = false;
+  op->tet_bdb_tc_per_sm = 0;
+  const char* env = getenv("GH1_TET_BDB_TC");
+  if (!(op->prec_mask & 2) || op->bdb != 2 || sp->p < 2 || sp->p > 4 || op->tet_ntiles == 0 ||
+      (env && env[0] == '0'))
+    return;
+  cudaStream_t s = sp->ctx->stream;
+  switch (sp->p) {
+    case 2: op->tet_bdb_tc_per_sm = tet_bdb_tc_prepare_p<2>(op, t64); break;
+    case 3: op->tet_bdb_tc_per_sm = tet_bdb_tc_prepare_p<3>(op, t64); break;
+    default: op->tet_bdb_tc_per_sm = tet_bdb_tc_prepare_p<4>(op, t64); break;
+  }
+  if (op->tet_bdb_tc_per_sm <= 0) return;
+  tet_tc_build_tiles(op);
+  op->d_tet_bdb_M.alloc((size_t)op->tet_tc_ntiles * 16 * 128);
+  const int64_t tm = (int64_t)op->tet_tc_ntiles * 16 * 128;
+  tet_bdb_tc_rec_kernel<<<(unsigned)std::min<int64_t>((tm + 255) / 256, 65535), 256, 0, s>>>(
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, op->d_G32.p, op->d_tet_bdb_M.p);
+  check_kernel(sp->ctx, "tet_bdb_tc_rec_kernel");
+  GH1_CUDA(cudaStreamSynchronize(s));
+  if (env && env[0] == '1') {
+    op->tet_bdb_tc = true;
+    return;
+  }
+  if (sp->mesh->ne < 4096) return;
+  DBuf<float> xs(op->nrows), ys(op->nrows);
+  xs.zero(s);
+  cudaEvent_t a, b;
+  GH1_CUDA(cudaEventCreate(&a));
+  GH1_CUDA(cudaEventCreate(&b));
+  float ms[2];
+  for (int v = 0; v < 2; v++) {
+    op->tet_bdb_tc = v == 1;
+    for (int r = 0; r < 5; r++) {
+      if (r == 2) GH1_CUDA(cudaEventRecord(a, s));
+      tet_bdb_apply(op, GH1_F32, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+    }
+    GH1_CUDA(cudaEventRecord(b, s));
+    GH1_CUDA(cudaEventSynchronize(b));
+    GH1_CUDA(cudaEventElapsedTime(&ms[v], a, b));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  op->tet_bdb_tc = ms[1] < ms[0];
 }
 
 }  // namespace gh1

@@ -187,6 +187,55 @@ def test_bdb_paired_records(gpu, monkeypatch, p, pair):
         assert np.abs(_apply(gpu, a, x, torch.float64) - yo).max() <= 1e-12 * np.abs(yo).max()
 
 
+@pytest.mark.parametrize("tc", ["0", "1"])
+@pytest.mark.parametrize("p", [2, 3, 4])
+def test_bdb_tet_tensor_core(gpu, monkeypatch, p, tc):
+    """FP32 B^T D B on tets with one record per element, both products of a
+    same-class tile of up to 128 elements on the tensor cores (GH1_TET_BDB_TC=1,
+    variant 10) or on the FP32 pipe (=0, variant 8): within 2e-5 of the oracle on
+    meshes with all 24 orientation classes, 162 and 3,072 tets (one partial tile
+    per class, several tiles)."""
+    from tests.util import permute_tets
+    from ngsolve_gb300.meshes import Mesh as RawMesh
+    monkeypatch.setenv("GH1_TET_BDB_TC", tc)
+    for n in (3, 8):
+        m0 = _mesh(False, n, 0.2)
+        m = RawMesh(m0.points, permute_tets(m0.elements, 95 + n))
+        fes = gpu.H1(m, order=p)
+        terms = _terms(gpu, fes, m.ne, 96 + p, False)
+        a = gpu.BilinearForm(sum(terms[1:], terms[0]), nonassemble=True, precision="fp32").Assemble()
+        assert a.mat.Info()["hex_variant_fp32"] == (10 if tc == "1" else 8)
+        D = _oracle_D(terms, m.ne, None)
+        x = np.random.default_rng(97).normal(size=fes.ndof)
+        yo = O.OracleSpace(m.points, m.elements, p).apply_bdb(x, D)
+        assert np.abs(_apply(gpu, a, x, torch.float32) - yo).max() <= 2e-5 * np.abs(yo).max()
+        assert np.abs(_apply(gpu, a, x, torch.float64) - yo).max() <= 1e-12 * np.abs(yo).max()
+
+
+def test_bdb_tet_tensor_core_mixed_cg(gpu, monkeypatch):
+    """A symmetric generic tet form (value-gradient coupling in both directions)
+    with its FP32 applies on the tensor cores: the mixed CG, which uses the
+    kernel's fused energy, reaches the FP64 CG's solution (1e-8)."""
+    monkeypatch.setenv("GH1_TET_BDB_TC", "1")
+    m = _mesh(False, 5, 0.2)
+    fes = gpu.H1(m, order=3, dirichlet=".*")
+    u, v = fes.TnT()
+    c = gpu.CoefficientFunction((0.2, -0.1, 0.15))
+    form = (gpu.CoefficientFunction(lognormal(m.ne, 0.5, 98)) * gpu.grad(u) * gpu.grad(v) * gpu.dx
+            + gpu.InnerProduct(c, gpu.grad(u)) * v * gpu.dx + u * gpu.InnerProduct(c, gpu.grad(v)) * gpu.dx
+            + gpu.CoefficientFunction(2.0) * u * v * gpu.dx)
+    a = gpu.BilinearForm(form, nonassemble=True, precision="mixed").Assemble()
+    assert a.mat.Info()["hex_variant_fp32"] == 10
+    f = gpu.LinearForm(gpu.CoefficientFunction(np.random.default_rng(99).uniform(-1, 1, m.ne)) * v * gpu.dx).Assemble()
+    pre = a.mat.CreateSmoother(fes.FreeDofs())
+    xm = gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-11, maxsteps=5000, printrates=False,
+                        mode="mixed").NumPy().copy()
+    assert gpu.solvers.CG.last_solver.result.applies32 > 0
+    x6 = gpu.solvers.CG(mat=a.mat, rhs=f.vec, pre=pre, tol=1e-12, maxsteps=5000, printrates=False,
+                        mode="fp64").NumPy()
+    assert np.abs(xm - x6).max() <= 1e-8 * np.abs(x6).max()
+
+
 def test_bdb_paired_records_mixed_cg(gpu, monkeypatch):
     """A symmetric generic form outside the Laplace type (value-gradient coupling
     u (c . grad v) + (c . grad u) v) on the paired record kernel: the mixed CG,
