@@ -323,6 +323,25 @@ static void hex_bdb_launch(gh1_op* op, const T* x, T* y, const T* G, int gstride
 #undef GH1_BAPP_CASE
 }
 
+// FP32 records Mh = |det J| T^T D T per element (reference coordinates, no rule
+// weight) of a standard tet form, D = diag(mu, kappa I or K): the input of the
+// tensor-core B^T D B kernel for stiffness + mass forms
+void tet_standard_records(gh1_op* op, float* M32) {
+  gh1_space* sp = op->sp;
+  gh1_form* f = op->form;
+  const int ne = sp->mesh->ne;
+  if (ne == 0) return;
+  cudaStream_t s = sp->ctx->stream;
+  DBuf<double> D((size_t)ne * 16), M64((size_t)ne * 16);
+  coef_bdb_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, f->d_kappa.p, f->has_K6 ? f->d_K6.p : nullptr,
+                                                  op->has_mass ? f->d_mu.p : nullptr, D.p);
+  check_kernel(sp->ctx, "coef_bdb_kernel");
+  tet_bdb_geom_kernel<<<(ne + 127) / 128, 128, 0, s>>>(ne, sp->tet_nq_mass, sp->mesh->d_X.p, sp->mesh->d_el.p,
+                                                       sp->d_tqm.p, D.p, 0, 0, M64.p, M32, deform_view(sp->mesh));
+  check_kernel(sp->ctx, "tet_bdb_geom_kernel");
+  GH1_CUDA(cudaStreamSynchronize(s));  // D and M64 go out of scope
+}
+
 // FP32, one record per affine element: the paired kernel (two elements per lane,
 // G mode 3 of hexpair.cu) or the one-element kernel, whichever is faster on this
 // operator's mesh (GH1_BDB_PAIR=0/1 forces one)

@@ -378,6 +378,11 @@ void tet_tc_setup(gh1_op* op);
 // tensor-core tet B^T D B (tettc.cu): setup from the degree-2p tables [class][q][i][4]
 // (t64, FP64), after the class tiles and the element records; apply
 void tet_bdb_tc_setup(gh1_op* op, const double* t64);
+// the same kernel for standard FP32 tet forms with a mass term (records from
+// kappa / K and mu, bdb.cu tet_standard_records), kept when faster than the tiles
+void tet_mass_tc_setup(gh1_op* op);
+void tet_standard_records(gh1_op* op, float* M32);  // bdb.cu
+void tet_mass_rule_tables(gh1_space* sp, gh1::DBuf<double>& t64, gh1::DBuf<float>& t32);  // tables.cu
 void tet_bdb_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,
                       const int* skip);
 void tet_tc_apply(gh1_op* op, const float* x, float* y, double* partial, unsigned int* counter, double* energy,

@@ -614,6 +614,7 @@ void tet_tiles_setup(gh1_op* op) {
       op->tet_use_tc = ms[1] < ms[0];
     }
   }
+  tet_mass_tc_setup(op);  // FP32 with a mass term: the tensor-core B^T D B kernel where faster
 }
 
 template <class T, bool MASS, int P>
@@ -683,6 +684,10 @@ bool tet_tiles_apply(gh1_op* op, int prec, const void* x, void* y, double* parti
   }
   if (prec == GH1_F32 && op->tet_use_tc) {
     tet_tc_apply(op, (const float*)x, (float*)y, partial, counter, energy, skip);
+    return true;
+  }
+  if (prec == GH1_F32 && op->tet_bdb_tc) {  // stiffness + mass on the tensor cores
+    tet_bdb_tc_apply(op, (const float*)x, (float*)y, partial, counter, energy, skip);
     return true;
   }
   if (prec == GH1_F64)

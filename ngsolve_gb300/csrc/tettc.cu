@@ -750,6 +750,8 @@ void tet_bdb_tc_apply(gh1_op* op, const float* x, float* y, double* partial, uns
 
 // FP32, records per element, p = 2..4: the tensor-core form, kept when the setup's
 // timing finds it faster than the class-tiled kernel (GH1_TET_BDB_TC=0/1 forces)
+static void tet_bdb_tc_prepare(gh1_op* op, const double* t64, const float* rec32, const char* env);
+
 void tet_bdb_tc_setup(gh1_op* op, const double* t64) {
   gh1_space* sp = op->sp;
   op->tet_bdb_tc = false;
@@ -758,6 +760,39 @@ void tet_bdb_tc_setup(gh1_op* op, const double* t64) {
   if (!(op->prec_mask & 2) || op->bdb != 2 || sp->p < 2 || sp->p > 4 || op->tet_ntiles == 0 ||
       (env && env[0] == '0'))
     return;
+  tet_bdb_tc_prepare(op, t64, op->d_G32.p, env);
+}
+
+// FP32 stiffness + mass tet forms (p = 2..4, affine): the tensor-core B^T D B
+// kernel on the records of D = diag(mu, kappa I or K) and the degree-2p rule,
+// which integrates both terms exactly; GH1_TET_BDB_TC=0/1 forces as for the
+// generic forms
+void tet_mass_tc_setup(gh1_op* op) {
+  gh1_space* sp = op->sp;
+  op->tet_bdb_tc = false;
+  op->tet_bdb_tc_per_sm = 0;
+  const char* env = getenv("GH1_TET_BDB_TC");
+  if (!(op->prec_mask & 2) || op->bdb || !op->has_mass || sp->p < 2 || sp->p > 4 || op->tet_ntiles == 0 ||
+      op->tet_chunked || sp->mesh->def_space || (env && env[0] == '0'))
+    return;
+  cudaStream_t s = sp->ctx->stream;
+  DBuf<double> t64;
+  DBuf<float> t32;
+  tet_mass_rule_tables(sp, t64, t32);
+  DBuf<float> rec((size_t)std::max(sp->mesh->ne, 1) * 16);
+  tet_standard_records(op, rec.p);
+  // rule weights of the degree-2p rule
+  std::vector<double> rule(4 * (size_t)sp->tet_nq_mass), w((size_t)sp->tet_nq_mass);
+  GH1_CUDA(cudaMemcpyAsync(rule.data(), sp->d_tqm.p, rule.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GH1_CUDA(cudaStreamSynchronize(s));
+  for (int q = 0; q < sp->tet_nq_mass; q++) w[q] = rule[4 * q + 3];
+  op->d_tetBw64.upload(w, s);
+  tet_bdb_tc_prepare(op, t64.p, rec.p, env);
+  GH1_CUDA(cudaStreamSynchronize(s));  // tables and records go out of scope
+}
+
+static void tet_bdb_tc_prepare(gh1_op* op, const double* t64, const float* rec32, const char* env) {
+  gh1_space* sp = op->sp;
   cudaStream_t s = sp->ctx->stream;
   switch (sp->p) {
     case 2: op->tet_bdb_tc_per_sm = tet_bdb_tc_prepare_p<2>(op, t64); break;
@@ -769,7 +804,7 @@ void tet_bdb_tc_setup(gh1_op* op, const double* t64) {
   op->d_tet_bdb_M.alloc((size_t)op->tet_tc_ntiles * 16 * 128);
   const int64_t tm = (int64_t)op->tet_tc_ntiles * 16 * 128;
   tet_bdb_tc_rec_kernel<<<(unsigned)std::min<int64_t>((tm + 255) / 256, 65535), 256, 0, s>>>(
-      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, op->d_G32.p, op->d_tet_bdb_M.p);
+      op->tet_tc_ntiles, op->d_tet_tc_tiles.p, op->d_tet_perm.p, rec32, op->d_tet_bdb_M.p);
   check_kernel(sp->ctx, "tet_bdb_tc_rec_kernel");
   GH1_CUDA(cudaStreamSynchronize(s));
   if (env && env[0] == '1') {
@@ -787,7 +822,8 @@ void tet_bdb_tc_setup(gh1_op* op, const double* t64) {
     op->tet_bdb_tc = v == 1;
     for (int r = 0; r < 5; r++) {
       if (r == 2) GH1_CUDA(cudaEventRecord(a, s));
-      tet_bdb_apply(op, GH1_F32, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+      if (op->bdb) tet_bdb_apply(op, GH1_F32, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+      else tet_tiles_apply(op, GH1_F32, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
     }
     GH1_CUDA(cudaEventRecord(b, s));
     GH1_CUDA(cudaEventSynchronize(b));
