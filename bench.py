@@ -490,8 +490,9 @@ def leg_bdb(nx=64, order=4):
     """The generic B^T D B apply (a convection-diffusion-reaction form: kappa
     grad.grad + (b . grad u) v + r u v, not symmetric) on the headline mesh
     (64^3 hex p=4, kappa lognormal(0,0.5) seed 4): D per element, one record per
-    affine element (variant 8), FP32 and FP64; r = 1 + x evaluated at every rule
-    point (variant 7, 16 coefficients per point streamed), FP32; and the tet mesh
+    affine element (variant 8, or 9 on the paired kernel), FP32 and FP64; r = 1 + x
+    evaluated at every rule point (variant 7, or 11 on the paired kernel: 16
+    coefficients per point streamed), FP32; and the tet mesh
     of the CSR leg (32^3 Kuhn tets, jitter 0.2h) at p = 4, D per element, FP32."""
     import torch
     import ngsolve_gb300 as ng

@@ -171,9 +171,13 @@ int gh1_op_apply(gh1_op* op, double s, const void* x, void* y, int precision, in
  * pencil form of 4, orders 1-4; 6: the 1D contractions on the tensor cores
  * (tcgen05), FP32, orders 4-7; -1: not applicable).  A generic B^T D B operator
  * (gh1_form_set_bdb, hex or tet) reports 7 in both: metric records per rule
- * point, or 8: one record per element (affine elements, D per element).  For a tet matrix-free
- * operator info[5] is 6 when its FP32 apply runs both tile products on the
- * tensor cores (orders 2-4 without a mass term, kept when faster), else -1.  For a CSR operator info[4..5]
+ * point, or 8: one record per element (affine elements, D per element); in FP32
+ * a hex one reports 9 / 11 when the two-elements-per-lane kernel runs it (records
+ * per element / per point), a tet one 10 when both tile products run on the
+ * tensor cores (records per element, orders 2-4), each kept only when faster.
+ * For a tet matrix-free operator info[5] is 6 when its FP32 apply runs both tile
+ * products on the tensor cores (orders 2-4 without a mass term), 10 with a mass
+ * term (the B^T D B tensor-core kernel), kept when faster, else -1.  For a CSR operator info[4..5]
  * are the autotuned SpMV configuration in FP64 and FP32: lanes per row L, plus
  * 100 when each lane keeps 8 instead of 4 nonzeros in flight (0: not tuned yet). */
 int gh1_op_info(gh1_op* op, int64_t* info);

@@ -723,8 +723,10 @@ int gh1_op_info(gh1_op* op, int64_t* info) {
   if (op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 4 && op->tet_use_tc) info[5] = 6;
   if (op->kind == GH1_OP_MATFREE && op->sp && op->sp->et == 4 && !op->bdb && op->tet_bdb_tc) info[5] = 10;
   if (op->kind == GH1_OP_MATFREE && op->bdb) {  // generic B^T D B: records per point (7) or per element (8;
-    info[4] = 6 + op->bdb;                       // FP32 9: hex paired kernel, 10: tet tensor cores)
-    info[5] = (op->prec_mask & 2) ? (op->bdb_pair ? 9 : op->tet_bdb_tc ? 10 : 6 + op->bdb) : -1;
+    info[4] = 6 + op->bdb;                       // FP32 9 / 11: hex paired kernel, per element / per
+                                                 // point; 10: tet tensor cores)
+    info[5] = (op->prec_mask & 2) ? (op->bdb_pair ? (op->bdb == 2 ? 9 : 11) : op->tet_bdb_tc ? 10 : 6 + op->bdb)
+                                  : -1;
   }
   if (op->kind == GH1_OP_CSR) {  // autotuned SpMV configuration (0 until the first SpMV)
     info[4] = op->spmv_L[0];

@@ -342,18 +342,21 @@ void tet_standard_records(gh1_op* op, float* M32) {
   GH1_CUDA(cudaStreamSynchronize(s));  // D and M64 go out of scope
 }
 
-// FP32, one record per affine element: the paired kernel (two elements per lane,
-// G mode 3 of hexpair.cu) or the one-element kernel, whichever is faster on this
-// operator's mesh (GH1_BDB_PAIR=0/1 forces one)
+// FP32: the paired kernel (two elements per lane; G mode 3 of hexpair.cu with one
+// record per affine element, 4 with records per point) or the one-element
+// kernel, whichever is faster on this operator's mesh (GH1_BDB_PAIR=0/1 forces one)
+static int bdb_pair_mode(const gh1_op* op) { return op->bdb == 2 ? 3 : 4; }
+
 static bool bdb_pair_choice(gh1_op* op) {
   gh1_space* sp = op->sp;
   op->bdb_pair = false;
-  op->pair_per_sm[3] = 0;
-  if (!(op->prec_mask & 2) || op->bdb != 2 || !hex_pair_supported(sp->p + 1)) return false;
+  op->pair_per_sm[3] = op->pair_per_sm[4] = 0;
+  if (!(op->prec_mask & 2) || !op->bdb || !hex_pair_supported(sp->p + 1)) return false;
   set_first_wait_polls();
   upload_pair_tables(sp);
-  op->pair_per_sm[3] = hex_pair_occupancy(op, 3);
-  if (op->pair_per_sm[3] <= 0) return false;
+  const int gm = bdb_pair_mode(op);
+  op->pair_per_sm[gm] = hex_pair_occupancy(op, gm);
+  if (op->pair_per_sm[gm] <= 0) return false;
   const char* env = getenv("GH1_BDB_PAIR");
   if (env) return env[0] == '1';
   if (sp->mesh->ne < 4096) return false;
@@ -368,7 +371,7 @@ static bool bdb_pair_choice(gh1_op* op) {
     for (int r = 0; r < 5; r++) {
       if (r == 2) GH1_CUDA(cudaEventRecord(a, s));
       if (v == 0) hex_bdb_launch<float>(op, xs.p, ys.p, op->d_G32.p, op->gstride32, nullptr, nullptr, nullptr, nullptr);
-      else hex_pair_apply(op, 3, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
+      else hex_pair_apply(op, gm, xs.p, ys.p, nullptr, nullptr, nullptr, nullptr);
     }
     GH1_CUDA(cudaEventRecord(b, s));
     GH1_CUDA(cudaEventSynchronize(b));
@@ -473,7 +476,7 @@ void bdb_apply(gh1_op* op, const void* x, void* y, int prec, double* partial, un
   if (prec == GH1_F64)
     hex_bdb_launch<double>(op, (const double*)x, (double*)y, op->d_G64.p, op->gstride64, partial, counter, energy, skip);
   else if (op->bdb_pair)
-    hex_pair_apply(op, 3, (const float*)x, (float*)y, partial, counter, energy, skip);
+    hex_pair_apply(op, bdb_pair_mode(op), (const float*)x, (float*)y, partial, counter, energy, skip);
   else
     hex_bdb_launch<float>(op, (const float*)x, (float*)y, op->d_G32.p, op->gstride32, partial, counter, energy, skip);
 }

@@ -210,8 +210,9 @@ struct gh1_op {
   // elements with D per element), weighted in the kernel.  T = diag(1, J^{-T}).
   int bdb = 0;
   int bdb_per_sm[2] = {0, 0};                // hex: resident blocks of the B^T D B apply [FP64/FP32]
-  bool bdb_pair = false;                     // hex, records per element: the FP32 apply on the paired
-                                             // kernel (G mode 3 of hexpair.cu), timed against the other
+  bool bdb_pair = false;                     // hex: the FP32 apply on the paired kernel (G mode 3 of
+                                             // hexpair.cu with records per element, 4 per point), timed
+                                             // against the one-element kernel
   bool bdb_points_only = false;              // hex: per-point records even for affine elements (assembly)
   // a generic form of Laplace type on hexes (D = diag(mu, K), K symmetric) runs on
   // the standard kernels: per element through these coefficient arrays, per point
@@ -229,7 +230,7 @@ struct gh1_op {
                                              // 4 = two elements per lane with per-element (affine) metrics,
                                              // 5 = slice / pencil form of 4 (hexpair.cu),
                                              // 6 = 1D contractions on the tensor cores (hextc.cu)
-  int pair_per_sm[4] = {0, 0, 0, 0};         // resident blocks per SM of the paired FP32 apply [G mode]
+  int pair_per_sm[5] = {0, 0, 0, 0, 0};      // resident blocks per SM of the paired FP32 apply [G mode]
   int slice_per_sm = 0;                      // ... of the slice-form FP32 apply (0: not available)
   int tc_per_sm = 0;                         // ... of the tensor-core FP32 apply (0: not available)
   bool all_affine = false;                   // hex: every element map affine (G mode 2 available)

@@ -171,7 +171,7 @@ __device__ __forceinline__ void eo2_bwd(const f2* v, f2* out) {
 // variant (p=4: 4 blocks = 128 registers with the G tile in shared memory or a
 // metric per element, 5 blocks = 96 with direct G loads; p=6: 3 blocks = 168)
 constexpr int pair_min_blocks(int N, bool mass, int gm) {
-  return gm == 3 ? (N <= 4 ? 4 : N == 5 ? 3 : 2)  // B^T D B records: 16 packed coefficients in registers
+  return gm == 4 ? (N <= 5 ? 4 : 2) : gm == 3 ? (N <= 4 ? 4 : N == 5 ? 3 : 2)  // B^T D B records: 16 packed coefficients in registers
          : N == 2 ? 6
          : N == 3 ? (mass ? (gm ? 5 : 4) : (gm ? 6 : 5))
          : N == 4 ? (mass ? (gm ? 5 : 4) : 5)
@@ -440,7 +440,9 @@ __device__ __forceinline__ void pair_backward(int pl, int pa, int pk, bool activ
 // element (8 floats: G and the mass coefficient), 3 = the generic B^T D B form
 // with one 16-float record per affine element (the reference-coordinate 4x4
 // matrix Mh of bdb.cu, row = test component (v, d/dxi, d/deta, d/dzeta), column =
-// trial component; MASS = true), the rule weight applied in the kernel.
+// trial component; MASS = true), the rule weight applied in the kernel; 4 = the
+// generic form with a 16-float record per rule point (weights included; rows of
+// N^3 values per element, loaded directly after a bulk L2 prefetch).
 template <int N, bool MASS, int GM>
 __global__ void __launch_bounds__(PairCfg<N>::BLOCK, pair_min_blocks(N, MASS, GM))
 hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const float* __restrict__ Gq, int gstride,
@@ -541,7 +543,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     if (lane == 0) {
       issue_t(ch, 0);
       if (GM == 0) issue_g(ch);
-      else if (GM == 1) bulk_prefetch_l2(Gq + (size_t)ch * E * gstride, (uint32_t)(rows_of(ch) * rowg * sizeof(float)));
+      else if (GM == 1 || GM == 4) bulk_prefetch_l2(Gq + (size_t)ch * E * gstride, (uint32_t)(rows_of(ch) * rowg * sizeof(float)));
     }
     t_issued = 1;
     g_issued = GM == 0 ? 1 : 0;
@@ -563,7 +565,7 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
       fence_proxy_async();
       issue_t(ch + stride, b ^ 1);
       // G mode 1 reads the next chunk's G rows with plain loads: stage them in L2 now
-      if (GM == 1) bulk_prefetch_l2(Gq + (size_t)(ch + stride) * E * gstride, (uint32_t)(rows_of(ch + stride) * rowg * sizeof(float)));
+      if (GM == 1 || GM == 4) bulk_prefetch_l2(Gq + (size_t)(ch + stride) * E * gstride, (uint32_t)(rows_of(ch + stride) * rowg * sizeof(float)));
     }
     if (has_next) t_issued++;
     group_sync<G>(gid);
@@ -586,7 +588,23 @@ hex_apply_pair_kernel(int ne, const int* __restrict__ tdof, int tstride, const f
     const float* Ga = GM == 0 ? gbuf + (size_t)r0 * rowg : Gq + ((size_t)ch * E + r0) * gstride;
     const float* Gb = GM == 0 ? gbuf + (size_t)r1 * rowg : Gq + ((size_t)ch * E + r1) * gstride;
     f2 vx[N], vy[N], vz[N], vm[N];
-    if (GM == 3 && active) {
+    if (GM == 4 && active) {
+      // (vm, vx, vy, vz) = Mh_q (uq, gx, gy, gz) with a record per point (weights
+      // included): 16 rows of N^3 values per element, loaded directly
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        const int o = i * N2 + pl;
+        f2 mq[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) mq[c] = pack2(__ldcs(Ga + c * N3 + o), __ldcs(Gb + c * N3 + o));
+        const f2 a0 = uq[i], a1 = gx[i], a2 = gy[i], a3 = gz[i];
+        vm[i] = fma2(mq[3], a3, fma2(mq[2], a2, fma2(mq[1], a1, mul2(mq[0], a0))));
+        vx[i] = fma2(mq[7], a3, fma2(mq[6], a2, fma2(mq[5], a1, mul2(mq[4], a0))));
+        vy[i] = fma2(mq[11], a3, fma2(mq[10], a2, fma2(mq[9], a1, mul2(mq[8], a0))));
+        vz[i] = fma2(mq[15], a3, fma2(mq[14], a2, fma2(mq[13], a1, mul2(mq[12], a0))));
+        if (want_e) acc = add2(acc, fma2(a0, vm[i], fma2(a3, vz[i], fma2(a2, vy[i], mul2(a1, vx[i])))));
+      }
+    } else if (GM == 3 && active) {
       // (vm, vx, vy, vz) = w_i w_j w_k Mh (uq, gx, gy, gz) with one Mh per element
       constexpr int WO = N * (N - 1) / 2 - 1;
       f2 em[16];
@@ -1351,7 +1369,8 @@ int hex_pair_occupancy(gh1_op* op, int gm) {
                                : pair_occupancy<NN, false, 1>(PairCfg<NN>::total(gs, ts, 1));                 \
     else if (gm == 2) v = mass ? pair_occupancy<NN, true, 2>(PairCfg<NN>::total(8, ts, 2))                    \
                                : pair_occupancy<NN, false, 2>(PairCfg<NN>::total(8, ts, 2));                  \
-    else v = pair_occupancy<NN, true, 3>(PairCfg<NN>::total(16, ts, 3));                                      \
+    else if (gm == 3) v = pair_occupancy<NN, true, 3>(PairCfg<NN>::total(16, ts, 3));                         \
+    else v = pair_occupancy<NN, true, 4>(PairCfg<NN>::total(gs, ts, 4));                                      \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_OCC)
 #undef GH1_PAIR_OCC
@@ -1372,8 +1391,10 @@ void hex_pair_apply(gh1_op* op, int gm, const float* x, float* y, double* partia
     } else if (gm == 2) {                                                                       \
       if (mass) pair_launch<NN, true, 2>(op, x, y, partial, counter, energy, skip);             \
       else pair_launch<NN, false, 2>(op, x, y, partial, counter, energy, skip);                 \
-    } else {                                                                                    \
+    } else if (gm == 3) {                                                                       \
       pair_launch<NN, true, 3>(op, x, y, partial, counter, energy, skip);                       \
+    } else {                                                                                    \
+      pair_launch<NN, true, 4>(op, x, y, partial, counter, energy, skip);                       \
     }                                                                                           \
     break;
   GH1_PAIR_SWITCH(op->sp->p + 1, GH1_PAIR_CASE)
