@@ -268,6 +268,39 @@ def workload_c1(args):
     lf = ng.LinearForm(fes)
     lf += ng.CoefficientFunction(f) * v * ng.dx
     lf.Assemble()
+    # FP64 SpMV on the assembled matrix: nnz x 12 B + row pointers + x and y,
+    # about 181 MB against the 129 MB L2, so both states are timed with CUDA
+    # events: back to back (steady state, part of the matrix still in L2) and
+    # after writing a 256 MB buffer before every call (first touch)
+    N, nnz = fes.ndof, a.mat.nze
+    xs_dev = ng.BaseVector(data=torch.rand(N, dtype=torch.float64, device="cuda"))
+    ys_dev = ng.BaseVector(N)
+    for _ in range(5):
+        a.mat.Mult(xs_dev, ys_dev)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(50):
+        a.mat.Mult(xs_dev, ys_dev)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_steady = e0.elapsed_time(e1) / 1e3 / 50
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    t_first = 0.0
+    for i in range(20):
+        flush.fill_(i + 1)
+        e0.record(stream)
+        a.mat.Mult(xs_dev, ys_dev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_first += e0.elapsed_time(e1) / 1e3 / 20
+    del flush
+    B = nnz * 12 + 8 * (N + 1) + 2 * N * 8
+    peak = load_peaks()[0]
+    spmv = {"bytes": B, "steady_ms": t_steady * 1e3, "steady_gbs": B / t_steady / 1e9,
+            "steady_frac": B / t_steady / 1e9 / peak, "first_touch_ms": t_first * 1e3,
+            "first_touch_gbs": B / t_first / 1e9, "first_touch_frac": B / t_first / 1e9 / peak}
     pre = a.mat.CreateSmoother(fes.FreeDofs())
     def solve():
         return ng.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=10000, printrates=False)
@@ -322,8 +355,9 @@ def workload_c1(args):
                "cg_s": c_cg, "cg_iterations": its,
                "err_gpu_vs_cpu_solution": float(np.abs(xg - xo).max() / np.abs(xo).max())}
     return {"workload": "C1: 16^3 hex p=3 FP64 assemble + Jacobi-PCG to 1e-10", "ndof": fes.ndof, "nnz": a.mat.nze,
-            "space_s": t_space, "assemble_first_s": t_graph, "assemble_s": t_asm, "cg_s": t_cg,
-            "cg_iterations": r.iterations, "true_relres": r.true_relres, "schwarz_pcg": schwarz, "cpu_oracle": cpu}
+            "space_s": t_space, "assemble_first_s": t_graph, "assemble_s": t_asm, "spmv_fp64": spmv, "cg_s": t_cg,
+            "cg_iterations": r.iterations, "cg_ms_per_iteration": t_cg / max(r.iterations, 1) * 1e3,
+            "true_relres": r.true_relres, "schwarz_pcg": schwarz, "cpu_oracle": cpu}
 
 
 def workload_c2(args):
