@@ -287,14 +287,18 @@ template <int P>
 static int tet_tc_occupancy_p() {
   auto kern = tet_tc_kernel<P>;
   GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TetTcCfg<P>::smem));
-  int dev = 0, smem_sm = 0;
+  // resident CTAs by shared memory and by registers (a grid above both would run
+  // a second, partly empty wave: p = 2 holds 4 CTAs by registers, 10 by shared
+  // memory), and by TMEM: at most 512 columns per SM
+  int dev = 0, smem_sm = 0, regs_sm = 0;
   GH1_CUDA(cudaGetDevice(&dev));
   GH1_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
   cudaFuncAttributes fa;
   GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
-  const int v = smem_sm / (int)(TetTcCfg<P>::smem + fa.sharedSizeBytes + 1024);
-  // TMEM: at most 512 columns per SM across the resident CTAs
-  return std::min(v, 512 / TetTcCfg<P>::TCOLS);
+  const int by_smem = smem_sm / (int)(TetTcCfg<P>::smem + fa.sharedSizeBytes + 1024);
+  const int by_regs = regs_sm / (TT_THREADS * ((fa.numRegs + 7) / 8 * 8));
+  return std::min(std::min(by_smem, by_regs), 512 / TetTcCfg<P>::TCOLS);
 }
 
 // per class: the table D_c as the B operand of both products, split into TF32
