@@ -719,8 +719,12 @@ static int tet_bdb_tc_prepare_p(gh1_op* op, const double* t64) {
   GH1_CUDA(cudaFuncGetAttributes(&fa, kern));
   if ((size_t)optin < C::smem + fa.sharedSizeBytes) return 0;
   GH1_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem));
-  int v = 0;
-  GH1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, TT_THREADS, C::smem));
+  // resident CTAs by shared memory and by registers (TMEM below)
+  int smem_sm = 0, regs_sm = 0;
+  GH1_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  GH1_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+  const int v = std::min(smem_sm / (int)(C::smem + fa.sharedSizeBytes + 1024),
+                         regs_sm / (TT_THREADS * ((fa.numRegs + 7) / 8 * 8)));
   if (v <= 0) return 0;
   op->d_tet_bdb_tab.alloc((size_t)N_TET_CLASSES * C::TAB);
   const int64_t tot = (int64_t)N_TET_CLASSES * ((int64_t)C::N1 * C::K1 + (int64_t)C::N2 * C::N1);
