@@ -118,8 +118,10 @@ __device__ __forceinline__ void tt_put4(float* A, int r, int k, const float* v) 
 // tiles: [ntiles][4] = class, first position in perm, element count (<= 128), 0
 constexpr int TT_THREADS = 256;
 
+// resident CTAs the register allocation must allow: 3 at p = 3 (shared memory
+// and TMEM hold 4), 2 at p = 4 (shared memory holds 2); p = 2 fits 4 as compiled
 template <int P>
-__global__ void __launch_bounds__(TT_THREADS, 2)
+__global__ void __launch_bounds__(TT_THREADS, P == 3 ? 3 : 2)
 tet_tc_kernel(int ntiles, const int* __restrict__ tiles, const int* __restrict__ tdofs, const float* __restrict__ Gt,
               const float* __restrict__ tab, const double* __restrict__ W64,
               const float* __restrict__ x, float* __restrict__ y, double* partial, unsigned int* counter,
