@@ -139,7 +139,11 @@ def test_tensor_cg_and_adjoint(gpu):
     inv = np.where(S.freedofs().astype(bool), 1.0 / d, 0.0)
     xo, its, hist = S.cg(S.rhs(f), inv, tol=1e-10, maxit=5000, csr=(orp, oci, ova))
     assert abs(solver.iterations - its) <= 1
-    assert_cg_history_close(solver.residuals, hist)
+    # the anisotropic tensor amplifies rounding earlier than the isotropic
+    # problems: on the oracle alone, random last-bit changes of the matrix
+    # entries move this history by up to 2.4e-6 while the residual is above 1e-4
+    # of the first (2 of 8 trials above 1e-6), and by ~1e-14 above 1e-3
+    assert_cg_history_close(solver.residuals, hist, knee=1e-3)
     assert np.abs(sol.NumPy() - xo).max() <= 1e-9 * np.abs(xo).max()
     gpu.solvers.CG(mat=a.mat, rhs=lf.vec, pre=pre, tol=1e-10, maxsteps=20000, printrates=False,
                    mode="mixed", stop_rule="true")
